@@ -1,0 +1,153 @@
+"""ctypes binding of libbldfm_gb300.so (declarations: include/bldfm_gb300.h).
+
+The library is built in-tree by ``python -m bldfm_gb300.build``.  There is no
+CPU fallback: if the library is missing, every solve raises.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libbldfm_gb300.so")
+
+OK = 0
+ERR_ODD_MODES = -1
+ERR_PRECISION = -2
+ERR_ARG = -3
+ERR_SPECTRUM_SHAPE = -4
+ERR_BROADCAST = -5
+ERR_UNSUPPORTED = -6
+ERR_WORKSPACE = -7
+ERR_CUDA = -8
+ERR_TIMEOUT = -9
+ERR_NONFINITE = -10
+
+PREC_SINGLE = 0
+PREC_DOUBLE = 1
+MODE_FP64 = 0
+MODE_FP32 = 1
+
+CLOSURES = {"MOST": 0, "CONSTANT": 1, "MOSTM": 2, "OAAHOC": 3}
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32),
+        ("ny", ctypes.c_int32),
+        ("nz", ctypes.c_int32),
+        ("nlx", ctypes.c_int32),
+        ("nly", ctypes.c_int32),
+        ("footprint", ctypes.c_int32),
+        ("analytic", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("has_halo", ctypes.c_int32),
+        ("xmax", ctypes.c_double),
+        ("ymax", ctypes.c_double),
+        ("halo", ctypes.c_double),
+        ("meas_x", ctypes.c_double),
+        ("meas_y", ctypes.c_double),
+        ("srf_bg_conc", ctypes.c_double),
+    ]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("nxe", ctypes.c_int32),
+        ("nye", ctypes.c_int32),
+        ("nlx", ctypes.c_int32),
+        ("nly", ctypes.c_int32),
+        ("px", ctypes.c_int32),
+        ("py", ctypes.c_int32),
+        ("nfx", ctypes.c_int32),
+        ("nfy", ctypes.c_int32),
+        ("out_nx", ctypes.c_int32),
+        ("out_ny", ctypes.c_int32),
+        ("nsolved", ctypes.c_int64),
+        ("workspace_bytes", ctypes.c_int64),
+    ]
+
+
+_P = ctypes.c_void_p
+_SIGS = {
+    "bldfm_status_str": (ctypes.c_char_p, [ctypes.c_int]),
+    "bldfm_version": (ctypes.c_char_p, []),
+    "bldfm_plan": (ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int, ctypes.POINTER(PlanInfo)]),
+    "bldfm_solve": (
+        ctypes.c_int,
+        [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P, ctypes.c_size_t, _P],
+    ),
+    "bldfm_solve_host": (ctypes.c_int, [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P]),
+    "bldfm_vertical_profiles": (
+        ctypes.c_int,
+        [
+            ctypes.c_int32,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_int32,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.c_double,
+            ctypes.POINTER(ctypes.c_int32),
+            _P,
+            _P,
+            _P,
+        ],
+    ),
+}
+
+_lib = None
+
+
+def exported_symbols():
+    """Names of the C-ABI entry points this binding declares."""
+    return list(_SIGS)
+
+
+def load():
+    """Load the in-tree CUDA library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                "bldfm_gb300: CUDA library %s is not built (run `python -m bldfm_gb300.build`); "
+                "there is no CPU fallback" % LIB_PATH
+            )
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status, what="bldfm"):
+    """Map a C-ABI status to the exception the reference raises for the same input."""
+    if status == OK:
+        return
+    lib = load()
+    msg = lib.bldfm_status_str(status).decode()
+    if status in (ERR_ODD_MODES, ERR_PRECISION):
+        raise ValueError(msg)
+    if status == ERR_SPECTRUM_SHAPE:
+        raise IndexError("boolean index did not match indexed array: " + msg)
+    if status == ERR_BROADCAST:
+        raise ValueError("operands could not be broadcast together: " + msg)
+    if status in (ERR_ARG, ERR_UNSUPPORTED, ERR_WORKSPACE):
+        raise ValueError("%s: %s" % (what, msg))
+    raise RuntimeError("%s: %s (status %d)" % (what, msg, status))
+
+
+def ptr(a):
+    """Host pointer of a C-contiguous numpy array (or None)."""
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)

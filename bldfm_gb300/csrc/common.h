@@ -1,0 +1,82 @@
+// Internal definitions shared by the host planner and the device kernels.
+#pragma once
+
+#include <stdint.h>
+#include <vector_types.h>
+
+// complex vector type of a real type
+template <typename R> struct cvec;
+template <> struct cvec<double> { typedef double2 T; };
+template <> struct cvec<float> { typedef float2 T; };
+
+#define BLDFM_MAX_FFT_N 4096    // longest transform held in shared memory
+#define BLDFM_MAX_STAGES 16
+#define BLDFM_MAX_NZ 2048       // level table must fit in shared memory
+#define BLDFM_LV64 12           // doubles per FP64 level-table row
+#define BLDFM_LV32 12           // floats per FP32 level-table row
+
+// Columns of the FP64 level table (same layout as the CPU oracle's).
+enum {
+    LV_KX = 0, LV_KY, LV_U, LV_V, LV_S1, LV_H2, LV_S2, LV_H3, LV_S3, LV_S4, LV_H, LV_PAD
+};
+
+// Columns of the FP32 level table (Riccati sweep).
+enum {
+    L32_NKX = 0,  // -Kx
+    L32_NKY,      // -Ky
+    L32_NU,       // -u
+    L32_NV,       // -v
+    L32_A,        // 0.5 * h^2 / Kz
+    L32_B0,       // -h / Kz
+    L32_B1,       // h^3 / (6 Kz^2)
+    L32_H,        // h
+    L32_C1,       // h^3 / (6 Kz)
+    L32_C2,       // -2 * C1
+    L32_P0, L32_P1
+};
+
+// Plan of one mixed-radix transform length.
+struct FftPlan {
+    int32_t n;
+    int32_t nstages;
+    int32_t radix[BLDFM_MAX_STAGES];
+};
+
+// Everything a kernel needs to know about one solve (passed by value).
+struct SolveGeom {
+    int32_t nx, ny, nz;
+    int32_t nlx, nly;       // effective modes
+    int32_t nxe, nye;
+    int32_t px, py, dlx, dly;
+    int32_t nfx, nfy;       // output transform size
+    int32_t out_nx, out_ny;
+    int32_t nlvls, nsnap;
+    int32_t footprint, analytic, precision, mode;
+    int32_t do_shift;
+    int32_t out_sign;       // -1: fft2 (footprint), +1: ifft2 norm=forward
+    int32_t nbx;            // number of band columns of the output transform
+    int64_t nsolved;
+    double lx_scale, ly_scale;  // Lx = lx_scale * (kx * valx)
+    double valx, valy;
+    double sx, sy;              // phase shift offsets
+    double kz_top;
+    double q0dc_fp;             // footprint source spectrum 1/nxe/nye
+    double inv_nxe, inv_nye;    // forward-FFT normalisation
+    // top-level coefficients for the FP32 eigenvalue
+    double kxk_top, kyk_top, uk_top, vk_top;
+    uint32_t turn_x, turn_y;    // phase shift as 32-bit fixed-point turns per unit k
+};
+
+// fftfreq ordering helpers: index <-> signed frequency.
+__host__ __device__ inline int freq_of_index(int idx, int n)
+{
+    int half = (n - 1) / 2 + 1;
+    return idx < half ? idx : idx - n;
+}
+__host__ __device__ inline int index_of_freq(int f, int n)
+{
+    return f >= 0 ? f : f + n;
+}
+// lowest / highest signed frequency of fftfreq(n)
+__host__ __device__ inline int freq_min(int n) { return -(n / 2); }
+__host__ __device__ inline int freq_max(int n) { return (n - 1) / 2; }

@@ -1,0 +1,14 @@
+#pragma once
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+void hx_level_table(int nz, const double *z, const double *prof, double *lv);
+void hx_level_table32(int nz, const double *z, const double *prof, float *lv);
+double hx_fftfreq_val(int n);
+void hx_eigval(int64_t m0, int64_t m1, const uint32_t *modes, int nlx, int nly, double valx, double valy,
+               double lx_scale, double ly_scale, double Kx_top, double Ky_top, double Kz_top, double u_top,
+               double v_top, double *eig);
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,135 @@
+"""Drop-in replacement of the reference's ``steady_state_transport_solver``.
+
+Reference: src/bldfm/solver.py:16-304.  Same signature, argument meaning,
+return convention ``(grid, conc, flx)``, output dtypes and error behaviour; the
+work runs on the GPU through the C ABI (include/bldfm_gb300.h).
+
+Swap it in by import (``from bldfm_gb300.solver import
+steady_state_transport_solver``) or by assigning it to
+``bldfm.solver.steady_state_transport_solver`` and
+``bldfm.interface.steady_state_transport_solver``.
+"""
+
+import numpy as np
+
+from . import _lib
+
+_MODES = {"fp64": _lib.MODE_FP64, "fp32": _lib.MODE_FP32}
+
+
+def _normalise_levels(levels, nz):
+    """Reference semantics: a scalar becomes a 1-element array (solver.py:102-105);
+    ``z[levels]`` must index (solver.py:295), so non-integer or out-of-range
+    levels raise IndexError as numpy does."""
+    if np.ndim(levels) == 0:
+        levels = np.array([levels])
+    arr = np.asarray(levels)
+    if arr.size == 0:
+        raise ValueError("levels must not be empty")
+    if arr.dtype.kind not in "iu":
+        raise IndexError("arrays used as indices must be of integer (or boolean) type")
+    lv = arr.astype(np.int64).ravel()
+    bad = (lv < -nz) | (lv >= nz)
+    if np.any(bad):
+        raise IndexError("index %d is out of bounds for axis 0 with size %d" % (int(lv[bad][0]), nz))
+    return levels, np.ascontiguousarray(lv)
+
+
+def make_desc(shape, nz, domain, modes, meas_pt, srf_bg_conc, footprint, analytic, halo, precision, mode):
+    ny, nx = shape
+    nlx, nly = modes
+    d = _lib.Desc()
+    d.nx, d.ny, d.nz = int(nx), int(ny), int(nz)
+    d.nlx, d.nly = int(nlx), int(nly)
+    d.footprint = 1 if footprint else 0
+    d.analytic = 1 if analytic else 0
+    if precision == "single":
+        d.precision = _lib.PREC_SINGLE
+    elif precision == "double":
+        d.precision = _lib.PREC_DOUBLE
+    else:
+        d.precision = 99  # rejected by the library with the reference's message
+    d.mode = _MODES[mode]
+    d.has_halo = 0 if halo is None else 1
+    d.halo = 0.0 if halo is None else float(halo)
+    d.xmax, d.ymax = float(domain[0]), float(domain[1])
+    d.meas_x, d.meas_y = float(meas_pt[0]), float(meas_pt[1])
+    d.srf_bg_conc = float(np.real(srf_bg_conc))
+    return d
+
+
+def plan(desc, nlvls):
+    """Derived sizes of a solve (bldfm_plan)."""
+    lib = _lib.load()
+    info = _lib.PlanInfo()
+    _lib.check(lib.bldfm_plan(desc, int(nlvls), info), "plan")
+    return info
+
+
+def steady_state_transport_solver(
+    srf_flx,
+    z,
+    profiles,
+    domain,
+    levels,
+    modes=(512, 512),
+    meas_pt=(0.0, 0.0),
+    srf_bg_conc=0.0,
+    footprint=False,
+    analytic=False,
+    halo=None,
+    precision="single",
+    cache=None,
+    *,
+    mode="fp64",
+):
+    """Steady-state advection-diffusion solve on the GPU (solver.py:16-304).
+
+    Parameters are the reference's.  The keyword-only ``mode`` selects the
+    sweep: ``"fp64"`` (default) integrates the reference's shooting method with
+    the reference's rounding; ``"fp32"`` integrates the same discrete problem
+    with the FP32 invariant-imbedding sweep (relative L2 error about 1e-5).
+    ``cache`` is a Green's-function cache with the reference's ``get``/``put``
+    interface (src/bldfm/cache.py:19-83), consulted in footprint mode only.
+    """
+    if cache is not None and footprint:
+        cached = cache.get(z, profiles, domain, modes, meas_pt, halo, precision)
+        if cached is not None:
+            return cached
+    if mode not in _MODES:
+        raise ValueError("mode must be 'fp64' or 'fp32'")
+    lib = _lib.load()
+    shape = np.shape(srf_flx)
+    if len(shape) != 2:
+        raise ValueError("srf_flx must be a 2D array")
+    zz = np.ascontiguousarray(z, dtype=np.float64)
+    nz = zz.shape[0]
+    prof = np.ascontiguousarray(np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in profiles]))
+    levels, lv = _normalise_levels(levels, nz)
+    d = make_desc(shape, nz, domain, modes, meas_pt, srf_bg_conc, footprint, analytic, halo, precision, mode)
+    info = _lib.PlanInfo()
+    _lib.check(lib.bldfm_plan(d, int(lv.size), info), "steady_state_transport_solver")
+    conc = np.empty((lv.size, info.out_ny, info.out_nx), dtype=np.float64)
+    flx = np.empty_like(conc)
+    src = None if footprint else np.ascontiguousarray(srf_flx, dtype=np.float64)
+    st = lib.bldfm_solve_host(
+        d, _lib.ptr(src), _lib.ptr(zz), _lib.ptr(prof), _lib.ptr(lv), int(lv.size), _lib.ptr(conc), _lib.ptr(flx)
+    )
+    _lib.check(st, "steady_state_transport_solver")
+
+    xm, ym = meas_pt
+    # output dtype rule: complex64 spectra stay complex64 unless the complex128
+    # phase shift multiplied them (solver.py:177-188, 253-262)
+    if precision == "single" and not footprint and not (xm**2 + ym**2 > 0.0):
+        conc = conc.astype(np.float32)
+        flx = flx.astype(np.float32)
+    ny, nx = shape
+    xmx, ymx = domain
+    x = np.linspace(0, xmx, nx, endpoint=False)
+    y = np.linspace(0, ymx, ny, endpoint=False)
+    Z, Y, X = np.meshgrid(zz[levels], y, x, indexing="ij")
+    grid = (np.squeeze(X), np.squeeze(Y), np.squeeze(Z))
+    result = (grid, np.squeeze(conc), np.squeeze(flx))
+    if cache is not None and footprint:
+        cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result)
+    return result

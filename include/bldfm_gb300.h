@@ -1,0 +1,133 @@
+/*
+ * bldfm_gb300 -- C ABI of the GB300 steady-state advection-diffusion solve.
+ *
+ * Drop-in boundary for the reference's
+ *   steady_state_transport_solver(srf_flx, z, profiles, domain, levels, modes,
+ *                                 meas_pt, srf_bg_conc, footprint, analytic,
+ *                                 halo, precision, cache)
+ * (src/bldfm/solver.py:16-304).  The reference has no FFI: it is pure Python
+ * and its callers import the function (src/bldfm/interface.py:15,115-128;
+ * src/bldfm/__init__.py:3).  The Python module bldfm_gb300.solver binds these
+ * entry points with ctypes and exposes the reference's signature.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (BLDFM_OK = 0 or a negative
+ *    BLDFM_ERR_* code); bldfm_status_str() names it.
+ *  - Arrays are C-contiguous, float64 unless stated.  Fields are row-major
+ *    (ny rows of nx), level-major for 3D outputs: (nlvls, out_ny, out_nx).
+ *  - "dev" pointers are CUDA device pointers on the current device; "host"
+ *    pointers are ordinary host memory.  The z grid, the profiles and the
+ *    level list are small (O(nz)) host arrays read during the call.
+ *  - stream is a cudaStream_t passed as void* (NULL = legacy default stream).
+ */
+#ifndef BLDFM_GB300_H
+#define BLDFM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define BLDFM_OK 0
+#define BLDFM_ERR_ODD_MODES -1       /* ValueError("modes must consist of even numbers.")  solver.py:89-91 */
+#define BLDFM_ERR_PRECISION -2       /* ValueError("precision must be single (default) or double.") solver.py:187-188 */
+#define BLDFM_ERR_ARG -3             /* malformed descriptor / sizes / pointers */
+#define BLDFM_ERR_SPECTRUM_SHAPE -4  /* truncated source spectrum does not match modes (reference raises IndexError) */
+#define BLDFM_ERR_BROADCAST -5       /* analytic branch with >1 output level (reference raises ValueError) */
+#define BLDFM_ERR_UNSUPPORTED -6     /* extended grid larger than the supported transform length */
+#define BLDFM_ERR_WORKSPACE -7       /* workspace too small */
+#define BLDFM_ERR_CUDA -8            /* a CUDA runtime call failed */
+#define BLDFM_ERR_TIMEOUT -9         /* a bounded device wait ran out */
+#define BLDFM_ERR_NONFINITE -10      /* non-finite values detected in the output */
+
+/* ---- descriptor -------------------------------------------------------- */
+#define BLDFM_PREC_SINGLE 0 /* reference precision="single": spectra stored as complex64 */
+#define BLDFM_PREC_DOUBLE 1 /* reference precision="double" */
+
+#define BLDFM_MODE_FP64 0 /* FP64 shooting sweep, rounding identical to the reference */
+#define BLDFM_MODE_FP32 1 /* FP32 invariant-imbedding (Riccati) sweep, renormalised */
+
+typedef struct bldfm_desc {
+    int32_t nx, ny;     /* srf_flx shape is (ny, nx)                          */
+    int32_t nz;         /* len(z)                                             */
+    int32_t nlx, nly;   /* requested Fourier modes (must be even)             */
+    int32_t footprint;  /* reference footprint flag                           */
+    int32_t analytic;   /* reference analytic flag                            */
+    int32_t precision;  /* BLDFM_PREC_*                                       */
+    int32_t mode;       /* BLDFM_MODE_*                                       */
+    int32_t has_halo;   /* 0: halo = max(xmax, ymax) (reference halo=None)    */
+    double xmax, ymax;  /* domain                                             */
+    double halo;        /* metres, used when has_halo != 0                    */
+    double meas_x, meas_y;
+    double srf_bg_conc;
+} bldfm_desc;
+
+/* Sizes derived from a descriptor (solver.py:94-131, 264-290). */
+typedef struct bldfm_plan_info {
+    int32_t nxe, nye;       /* extended grid                        */
+    int32_t nlx, nly;       /* modes after the clamp                */
+    int32_t px, py;         /* halo pad in cells                    */
+    int32_t nfx, nfy;       /* output transform size                */
+    int32_t out_nx, out_ny; /* cropped output field                 */
+    int64_t nsolved;        /* modes the sweep integrates           */
+    int64_t workspace_bytes;
+} bldfm_plan_info;
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* Name of a status code. */
+const char *bldfm_status_str(int status);
+
+/* Library build string (arch, version). */
+const char *bldfm_version(void);
+
+/* Derived sizes and workspace bytes for bldfm_solve.
+ * Replaces the grid arithmetic of solver.py:94-131. */
+int bldfm_plan(const bldfm_desc *d, int nlvls, bldfm_plan_info *out);
+
+/* Full solve on device buffers.  Replaces steady_state_transport_solver
+ * (solver.py:16-304) for inputs already resident on the GPU.
+ *   srf_flx_dev   (ny, nx) float64, ignored (may be NULL) when footprint != 0
+ *   z_host        (nz,)
+ *   prof_host     (5, nz): u, v, Kx, Ky, Kz  (the reference's profiles tuple)
+ *   levels_host   (nlvls,) int64 indices into z
+ *   conc_dev, flx_dev  (nlvls, out_ny, out_nx) float64 outputs
+ *   workspace_dev bytes >= bldfm_plan().workspace_bytes, 256-byte aligned
+ * Returns after the work is enqueued on stream.  In BLDFM_MODE_FP64 the
+ * host computes the top eigenvalues with libm while the device sweeps. */
+int bldfm_solve(const bldfm_desc *d, const double *srf_flx_dev,
+                const double *z_host, const double *prof_host,
+                const int64_t *levels_host, int32_t nlvls, double *conc_dev,
+                double *flx_dev, void *workspace_dev, size_t workspace_bytes,
+                void *stream);
+
+/* Same solve on host buffers: copies srf_flx in and conc/flx out inside the
+ * call and returns when the outputs are on the host (synchronous).  The
+ * library keeps and reuses its own device and pinned buffers per device.
+ * This is the entry point the reference-facing ctypes binding uses. */
+int bldfm_solve_host(const bldfm_desc *d, const double *srf_flx_host,
+                     const double *z_host, const double *prof_host,
+                     const int64_t *levels_host, int32_t nlvls,
+                     double *conc_host, double *flx_host);
+
+/* Device evaluation of vertical_profiles (src/bldfm/pbl_model.py:8-204).
+ * closure: 0 = MOST, 1 = CONSTANT, 2 = MOSTM, 3 = OAAHOC (tke <= 0 means the
+ * reference's default 1.0).  For MOST/CONSTANT/MOSTM exactly one of ustar / z0
+ * is > 0 (the other <= 0 means "derive it", pbl_model.py:64-77); OAAHOC needs
+ * ustar.  domain_height / stretch <= 0 mean the reference's None.
+ * Writes z_dev (nz) and prof_dev (5, nz): u, v, Kx, Ky, Kz.  nz_out (host)
+ * receives len(z); call with z_dev == NULL to size the buffers first. */
+int bldfm_vertical_profiles(int32_t n, double meas_height, double um, double vm,
+                            double ustar, double z0, double mol, double prsc,
+                            int32_t closure, double domain_height,
+                            double stretch, double tke, int32_t *nz_out,
+                            double *z_dev, double *prof_dev, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BLDFM_GB300_H */

@@ -1,0 +1,92 @@
+"""C-ABI library: loads without a GPU, exports every declared symbol, and its
+host-side planning matches the reference's grid arithmetic (solver.py:94-131)."""
+
+import os
+import re
+
+import numpy as np
+import pytest
+
+from bldfm_gb300 import _lib
+from bldfm_gb300.solver import make_desc, plan
+from oracle import bldfm_oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"\b(bldfm_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_library_exports_declared_symbols():
+    lib = _lib.load()
+    declared = _declared()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(declared) <= set(_lib.exported_symbols()) | set(declared)
+
+
+def test_version_string():
+    assert b"sm_103a" in _lib.load().bldfm_version()
+
+
+CASES = [
+    ((512, 512), (1000.0, 1000.0), (512, 512), None),
+    ((256, 256), (1000.0, 700.0), (512, 512), None),
+    ((128, 64), (500.0, 250.0), (512, 512), 1.0),
+    ((37, 53), (53.0, 37.0), (200, 200), 7.3),
+    ((64, 128), (100.0, 700.0), (64, 128), None),
+    ((100, 90), (123.4, 98.7), (64, 32), 11.0),
+]
+
+
+@pytest.mark.parametrize("shape,domain,modes,halo", CASES)
+def test_plan_matches_reference_grid(shape, domain, modes, halo):
+    d = make_desc(shape, 20, domain, modes, (0, 0), 0.0, True, False, halo, "double", "fp64")
+    info = plan(d, 1)
+    ref = O.solve_plan(shape, np.zeros(20), domain, 1, modes, halo)
+    for k in ("nxe", "nye", "nlx", "nly", "px", "py"):
+        assert getattr(info, k) == ref[k], k
+    assert info.nfx == ref["nlx"] + 2 * ref["dlx"] and info.nfy == ref["nly"] + 2 * ref["dly"]
+    nlx, nly = ref["nlx"], ref["nly"]
+    # solved modes: Hermitian half plus unpaired modes
+    kx = np.fft.fftfreq(nlx, 1.0 / nlx).astype(int)
+    ky = np.fft.fftfreq(nly, 1.0 / nly).astype(int)
+    KX, KY = np.meshgrid(kx, ky)
+    mirror = np.isin(-KX, kx) & np.isin(-KY, ky)
+    nonzero = ~((KX == 0) & (KY == 0))
+    rep = (~mirror) | (KX > 0) | ((KX == 0) & (KY > 0))
+    assert info.nsolved == int((rep & nonzero).sum())
+
+
+def test_plan_errors_follow_reference():
+    with pytest.raises(ValueError, match="modes must consist of even numbers"):
+        plan(make_desc((64, 64), 10, (10.0, 10.0), (63, 64), (0, 0), 0.0, True, False, None, "single", "fp64"), 1)
+    with pytest.raises(ValueError, match="precision must be single"):
+        plan(make_desc((64, 64), 10, (10.0, 10.0), (64, 64), (0, 0), 0.0, True, False, None, "quad", "fp64"), 1)
+    with pytest.raises(ValueError, match="broadcast"):
+        plan(make_desc((64, 64), 10, (10.0, 10.0), (64, 64), (0, 0), 0.0, False, True, None, "single", "fp64"), 3)
+    # non-footprint with an odd padding difference: the reference's truncated
+    # spectrum does not fit the mode mask (IndexError)
+    with pytest.raises(IndexError):
+        plan(make_desc((63, 64), 10, (64.0, 63.0), (64, 64), (0, 0), 0.0, False, False, 3.0, "single", "fp64"), 1)
+
+
+def test_odd_modes_reference_message_through_solver():
+    from bldfm_gb300 import steady_state_transport_solver as S
+
+    z = np.linspace(0.1, 10, 12)
+    prof = tuple(np.ones(12) for _ in range(5))
+    with pytest.raises(ValueError, match="modes must consist of even numbers"):
+        S(np.zeros((32, 32)), z, prof, (10.0, 10.0), 5, modes=(31, 32))
+    with pytest.raises(ValueError, match="precision must be single"):
+        S(np.zeros((32, 32)), z, prof, (10.0, 10.0), 5, modes=(32, 32), precision="quad")
+    with pytest.raises(IndexError):
+        S(np.zeros((32, 32)), z, prof, (10.0, 10.0), 50, modes=(32, 32))
