@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""Benchmark: footprints/s of the steady-state transport solve on one GB300.
+
+Workload (the reference's headline configuration, synthetic met timeseries):
+footprint mode, 512 x 512 physical grid on a 1000 m x 1000 m domain with the
+default halo (1536 x 1536 extended grid), 512 x 512 Fourier modes,
+vertical_profiles(n=128, z_m=20 m) -> 207 levels, unstable MOST profiles
+(L = -50 m, u* ~ 0.3 m/s, 4 m/s wind around 225 deg), tower at (500, 500) m.
+One step = one batch of B footprints for B met cases (seeded).
+
+Reported:
+  value          FP32 invariant-imbedding path, device-resident buffers
+                 (bldfm_solve), footprints/s over K timed steps
+  fp64           the FP64 path (reference rounding) on the same batches
+  e2e            the reference-facing drop-in steady_state_transport_solver
+                 (numpy in, numpy out, host<->device copies inside)
+  roofline       the sweep kernel against the measured FP32 FMA peak
+  cpu_baseline   the CPU oracle port (reference arithmetic, OpenMP on all
+                 host cores) on a bounded sample
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 512
+DOMAIN = (1000.0, 1000.0)
+N_LEVELS = 128
+ZM = 20.0
+MODES = (512, 512)
+MEAS = (500.0, 500.0)
+# algorithmic flops per (mode, sweep step), FMA counted as 2
+F32_FLOPS_PER_MODE_STEP = 63  # Riccati update (bldfm_gb300/csrc/kernels.cu riccati32_kernel)
+F64_FLOPS_PER_MODE_STEP = 88  # reference shooting step, both IVPs (src/bldfm/solver.py:357-368)
+WORKLOAD_NAME = "footprint 512x512 (ext 1536x1536), modes 512x512, n=128 (207 levels), unstable MOST"
+
+
+def met_cases(batch, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(batch):
+        out.append(
+            dict(
+                ustar=float(rng.uniform(0.25, 0.35)),
+                mol=-50.0,
+                wind_speed=4.0,
+                wind_dir=float(225.0 + rng.uniform(-30.0, 30.0)),
+            )
+        )
+    return out
+
+
+def profiles_for(case, device_profiles):
+    from bldfm_gb300.utils import compute_wind_fields
+
+    wind = compute_wind_fields(case["wind_speed"], case["wind_dir"])
+    if device_profiles:
+        from bldfm_gb300 import vertical_profiles
+    else:
+        from oracle.bldfm_oracle import vertical_profiles
+    return vertical_profiles(N_LEVELS, ZM, wind, ustar=case["ustar"], mol=case["mol"])
+
+
+def solver_kwargs(z, profs, precision="double"):
+    return dict(
+        srf_flx=np.zeros((NY, NX)), z=z, profiles=profs, domain=DOMAIN, levels=N_LEVELS, modes=MODES,
+        meas_pt=MEAS, footprint=True, precision=precision,
+    )
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": smax,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def cpu_port_time(kw, reps=2):
+    """Oracle C port (reference arithmetic) on all host cores: seconds/footprint."""
+    from oracle import bldfm_oracle as O
+    from oracle import build_oracle
+
+    build_oracle()
+    O.steady_state_transport_solver(**kw)  # warm (thread pool, pages)
+    best = 1e30
+    for _ in range(reps):
+        t = time.perf_counter()
+        O.steady_state_transport_solver(**kw)
+        best = min(best, time.perf_counter() - t)
+    return best
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation of the path (the
+    oracle port: the reference's arithmetic, OpenMP over modes on all cores,
+    numpy FFT) on the same workload; one footprint per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cases = met_cases(max(args.steps + args.warmup, 1), seed=1)
+    kws = []
+    for c in cases:
+        z, p = profiles_for(c, device_profiles=False)
+        kws.append(solver_kwargs(z, p))
+    from oracle import bldfm_oracle as O
+    from oracle import build_oracle
+
+    build_oracle()
+    for i in range(args.warmup):
+        O.steady_state_transport_solver(**kws[i % len(kws)])
+    t = time.perf_counter()
+    for i in range(args.steps):
+        O.steady_state_transport_solver(**kws[(args.warmup + i) % len(kws)])
+    dt = time.perf_counter() - t
+    fps = args.steps / dt
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference",
+        "metric": "footprints/s",
+        "value": fps,
+        "unit": "footprints/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "footprints_per_step": 1, "path": "CPU oracle port"},
+        "cpu_baseline": {
+            "value": fps, "unit": "footprints/s", "cores": cores, "kind": "port",
+            "sample": "1 footprint per step: C port of the reference sweep (OpenMP, %d threads) + numpy FFT" % cores,
+        },
+        "e2e": {"value": fps, "unit": "footprints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import ctypes
+
+    import torch
+
+    from bldfm_gb300 import _lib
+    from bldfm_gb300 import steady_state_transport_solver
+    from bldfm_gb300.solver import make_desc, plan
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    B = args.batch
+    cases = met_cases(B, seed=1000 + rank)
+    inputs = []
+    for c in cases:
+        z, p = profiles_for(c, device_profiles=True)
+        inputs.append((z, p))
+
+    def make_solves(mode):
+        solves = []
+        for z, p in inputs:
+            d = make_desc((NY, NX), len(z), DOMAIN, MODES, MEAS, 0.0, True, False, None, "double", mode)
+            info = plan(d, 1)
+            ws = torch.empty(int(info.workspace_bytes), dtype=torch.uint8, device=dev)
+            conc = torch.empty((info.out_ny, info.out_nx), dtype=torch.float64, device=dev)
+            flx = torch.empty_like(conc)
+            zz = np.ascontiguousarray(z, dtype=np.float64)
+            prof = np.ascontiguousarray(np.stack(p))
+            lv = np.array([N_LEVELS], dtype=np.int64)
+            solves.append((d, info, ws, conc, flx, zz, prof, lv))
+        return solves
+
+    def run_batch(solves):
+        for d, info, ws, conc, flx, zz, prof, lv in solves:
+            st = lib.bldfm_solve(
+                d, None, _lib.ptr(zz), _lib.ptr(prof), _lib.ptr(lv), 1, ctypes.c_void_p(conc.data_ptr()),
+                ctypes.c_void_p(flx.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ctypes.c_size_t(ws.numel()), sptr,
+            )
+            _lib.check(st, "bench")
+
+    def timed(solves, steps, warmup, stage_timing=False):
+        for _ in range(warmup):
+            run_batch(solves)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        if stage_timing:
+            lib.bldfm_set_stage_timing(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            run_batch(solves)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        stages = None
+        if stage_timing:
+            arr = (ctypes.c_float * 8)()
+            n = lib.bldfm_stage_times(arr, 8)
+            stages = [float(arr[i]) for i in range(max(n, 0))]
+            lib.bldfm_set_stage_timing(0)
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, stages
+
+    # --- FP32 path (headline) ---
+    s32 = make_solves("fp32")
+    with ClockSampler(local) as clk:
+        ms32, stages32 = timed(s32, args.steps, args.warmup, stage_timing=True)
+    fps32 = world * B * args.steps / (ms32 * 1e-3)
+
+    # --- FP64 path (reference rounding) ---
+    s64 = make_solves("fp64")
+    ms64, stages64 = timed(s64, args.fp64_steps, 1, stage_timing=True)
+    fps64 = world * B * args.fp64_steps / (ms64 * 1e-3)
+
+    # accuracy of the FP32 path against the FP64 path on this batch
+    errs = []
+    for a, b in zip(s32, s64):
+        ca, fa = a[3].cpu().numpy(), a[4].cpu().numpy()
+        cb, fb = b[3].cpu().numpy(), b[4].cpu().numpy()
+        errs.append(max(np.linalg.norm(ca - cb) / np.linalg.norm(cb), np.linalg.norm(fa - fb) / np.linalg.norm(fb)))
+    rel32 = max(errs)
+
+    # --- e2e through the reference-facing drop-in (numpy in / numpy out) ---
+    kws = [solver_kwargs(z, p) for z, p in inputs]
+    e2e_steps = max(2, args.steps // 2)
+    for kw in kws[: min(B, 4)]:
+        steady_state_transport_solver(**kw, mode="fp32")
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        for kw in kws:
+            steady_state_transport_solver(**kw, mode="fp32")
+    e2e_dt = time.perf_counter() - t
+    e2e_fps = world * B * e2e_steps / e2e_dt
+    nz = len(inputs[0][0])
+    h2d = B * ((nz - 1) * (12 * 8 + 12 * 4) + nz * 4)
+    d2h = B * 2 * NY * NX * 8
+
+    # --- roofline of the FP32 sweep kernel ---
+    peak = ctypes.c_double(0)
+    _lib.check(lib.bldfm_fma_peak(0, ctypes.byref(peak), sptr), "fma_peak")
+    peak64 = ctypes.c_double(0)
+    _lib.check(lib.bldfm_fma_peak(1, ctypes.byref(peak64), sptr), "fma_peak")
+    nsolved = int(s32[0][1].nsolved)
+    steps_z = nz - 1
+    flops_launch = F32_FLOPS_PER_MODE_STEP * nsolved * steps_z
+    sweep_ms = stages32[1] if stages32 and len(stages32) > 1 else None
+    achieved = flops_launch / (sweep_ms * 1e-3) / 1e12 if sweep_ms else None
+    flops64 = F64_FLOPS_PER_MODE_STEP * nsolved * steps_z
+    sweep64_ms = stages64[1] if stages64 and len(stages64) > 1 else None
+    achieved64 = flops64 / (sweep64_ms * 1e-3) / 1e12 if sweep64_ms else None
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sec = cpu_port_time(kws[0])
+        cpu = {
+            "value": 1.0 / sec, "unit": "footprints/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "1 footprint of the workload: C port of the reference sweep (OpenMP, all cores) + numpy FFT",
+        }
+
+    if rank == 0:
+        line = {
+            "metric": "footprints/s",
+            "value": fps32,
+            "unit": "footprints/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms32 / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": WORKLOAD_NAME,
+                "footprints_per_step": B,
+                "path": "fp32 invariant-imbedding sweep + fp32 FFT, device-resident",
+                "l2": "inputs larger than L2: each footprint of a step has its own ~10 MB workspace and outputs",
+                "parallelism": "replicas" if world > 1 else "single",
+            },
+            "relL2_fp32_vs_fp64": rel32,
+            "fp64": {"value": fps64, "unit": "footprints/s", "ms_per_footprint": ms64 / (args.fp64_steps * B),
+                     "stage_ms": stages64, "sweep_tflops": achieved64,
+                     "fp64_peak_tflops": peak64.value / 1e12,
+                     "frac": (achieved64 / (peak64.value / 1e12)) if achieved64 else None},
+            "fp32_stage_ms": stages32,
+            "e2e": {"value": e2e_fps, "unit": "footprints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "api": "bldfm_gb300.steady_state_transport_solver(mode='fp32')"},
+            "roofline": {
+                "bound": "fp32-pipe",
+                "kernel": "riccati32_kernel",
+                "achieved": achieved,
+                "peak": peak.value / 1e12,
+                "unit": "TFLOP/s",
+                "frac": (achieved / (peak.value / 1e12)) if achieved else None,
+                "peak_source": "measured FFMA throughput (bldfm_fma_peak); not in MEASURED_PEAKS.json",
+                "traffic": None,
+                "flops_per_launch": flops_launch,
+            },
+            "cpu_baseline": cpu,
+            "gpu_launches": 4 * B * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

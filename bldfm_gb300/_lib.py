@@ -101,6 +101,9 @@ _SIGS = {
             _P,
         ],
     ),
+    "bldfm_set_stage_timing": (ctypes.c_int, [ctypes.c_int]),
+    "bldfm_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "bldfm_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), _P]),
 }
 
 _lib = None

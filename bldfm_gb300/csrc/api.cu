@@ -56,6 +56,20 @@ void factorize(int n, FftPlan &p)
     if (m > 1) p.radix[p.nstages++] = m;
 }
 
+int64_t count_and_fill_modes(int nlx, int nly, std::vector<uint32_t> *out);
+
+// number of solved modes per (nlx, nly), memoised (called under g_mutex)
+int64_t solved_count(int nlx, int nly)
+{
+    static std::map<std::pair<int, int>, int64_t> memo;
+    auto key = std::make_pair(nlx, nly);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    const int64_t n = count_and_fill_modes(nlx, nly, nullptr);
+    memo[key] = n;
+    return n;
+}
+
 int64_t count_and_fill_modes(int nlx, int nly, std::vector<uint32_t> *out)
 {
     const int fx0 = freq_min(nlx), fx1 = freq_max(nlx), fy0 = freq_min(nly), fy1 = freq_max(nly);
@@ -134,7 +148,9 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
     g.ly_scale = 2.0 * M_PI / dy / g.nye;
     g.inv_nxe = 1.0 / g.nxe;
     g.inv_nye = 1.0 / g.nye;
-    g.q0dc_fp = 1.0 / g.nxe / g.nye;
+    // numpy evaluates ones(complex128) / nxe / nye with Smith's reciprocal-scale
+    // division, i.e. (1/nxe) * (1/nye) (solver.py:134)
+    g.q0dc_fp = (1.0 / g.nxe) * (1.0 / g.nye);
     if (d->footprint) {
         g.do_shift = 1;
         g.sx = d->meas_x + halo;
@@ -178,18 +194,17 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
             if (levels[k] < -(int64_t)nz || levels[k] >= nz) return BLDFM_ERR_ARG;
     }
     g.nsnap = ns;
-    g.nsolved = count_and_fill_modes(nlx, nly, nullptr);
+    g.nsolved = solved_count(nlx, nly);
     // output band columns: positions of frequencies [-h, h] mod nfx
     hp.xband.clear();
     {
         const int f0 = freq_min(nlx), f1 = freq_max(nlx);
         const int hmax = std::max(-f0, f1);
+        std::vector<char> seen(g.nfx, 0);
         for (int f = -hmax; f <= hmax; ++f) {
             const int pos = ((f % g.nfx) + g.nfx) % g.nfx;
-            bool dup = false;
-            for (auto &e : hp.xband)
-                if (e.x == pos) dup = true;
-            if (dup) continue;
+            if (seen[pos]) continue;
+            seen[pos] = 1;
             auto colof = [&](int p) -> int {
                 if (p <= f1) return p;  // non-negative frequencies
                 if (p >= g.nfx + f0) return p - g.nfx + nlx;
@@ -275,18 +290,30 @@ struct HostBuffers {
     size_t out_bytes = 0;
     cudaStream_t stream = nullptr;
 };
+// A pinned upload buffer; its event marks the last copy out of it.
+struct StageSlot {
+    void *buf = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t ev = nullptr;
+};
+enum { NSTAGE = 8, NTIMER = 8, NTSETS = 1024 };
+// CUDA events of one solve's stage boundaries
+struct TimerSet {
+    cudaEvent_t ev[NTIMER + 1] = {};
+    int used = 0;
+};
 struct DeviceCache {
     int nsm = 0;
     std::map<int, TwTable> tw;
     std::map<std::pair<int, int>, ModeList> modes;
     std::map<std::vector<int>, int4 *> xband;
-    // pinned staging for per-call uploads
-    void *stage = nullptr;
-    size_t stage_bytes = 0;
-    cudaEvent_t stage_ev = nullptr;
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_sweep = nullptr;
+    StageSlot stage[NSTAGE];  // ring of pinned staging buffers
+    int stage_next = 0;
     HostBuffers hb;
+    bool timing = false;       // per-stage CUDA-event timers
+    std::vector<TimerSet> tsets;
+    TimerSet *cur = nullptr;   // timers of the solve being enqueued
+    int tnext = 0, tpending = 0;
 };
 
 std::map<int, DeviceCache> g_cache;
@@ -299,10 +326,9 @@ DeviceCache &cache_for_current(int *status)
     if (dc.nsm == 0) {
         cudaDeviceGetAttribute(&dc.nsm, cudaDevAttrMultiProcessorCount, dev);
         if (dc.nsm <= 0) dc.nsm = 1;
-        if (cudaEventCreateWithFlags(&dc.stage_ev, cudaEventDisableTiming) != cudaSuccess) *status = BLDFM_ERR_CUDA;
-        if (cudaEventCreateWithFlags(&dc.ev_sweep, cudaEventDisableTiming) != cudaSuccess) *status = BLDFM_ERR_CUDA;
-        if (cudaStreamCreateWithFlags(&dc.side, cudaStreamNonBlocking) != cudaSuccess) *status = BLDFM_ERR_CUDA;
-        cudaEventRecord(dc.stage_ev, 0);
+        for (int i = 0; i < NSTAGE; ++i)
+            if (cudaEventCreateWithFlags(&dc.stage[i].ev, cudaEventDisableTiming) != cudaSuccess)
+                *status = BLDFM_ERR_CUDA;
     }
     return dc;
 }
@@ -372,18 +398,46 @@ int get_xband(DeviceCache &dc, const HostPlan &hp, int4 **out)
     return BLDFM_OK;
 }
 
-int ensure_stage(DeviceCache &dc, size_t bytes)
+// Next slot of the staging ring, grown to `bytes`; waits only for the copies
+// that last read this slot (NSTAGE solves ago), not for whole solves.
+int acquire_stage(DeviceCache &dc, size_t bytes, StageSlot **out)
 {
-    // previous call's uploads must have left the staging buffer
-    if (cudaEventSynchronize(dc.stage_ev) != cudaSuccess) return BLDFM_ERR_CUDA;
-    if (bytes <= dc.stage_bytes) return BLDFM_OK;
-    if (dc.stage) cudaFreeHost(dc.stage);
-    dc.stage = nullptr;
-    dc.stage_bytes = 0;
-    size_t want = std::max(bytes, (size_t)1 << 20);
-    if (cudaHostAlloc(&dc.stage, want, cudaHostAllocDefault) != cudaSuccess) return BLDFM_ERR_CUDA;
-    dc.stage_bytes = want;
+    StageSlot &sl = dc.stage[dc.stage_next];
+    dc.stage_next = (dc.stage_next + 1) % NSTAGE;
+    if (cudaEventSynchronize(sl.ev) != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (bytes > sl.bytes) {
+        if (sl.buf) cudaFreeHost(sl.buf);
+        sl.buf = nullptr;
+        sl.bytes = 0;
+        size_t want = std::max(bytes, (size_t)1 << 20);
+        if (cudaHostAlloc(&sl.buf, want, cudaHostAllocDefault) != cudaSuccess) return BLDFM_ERR_CUDA;
+        sl.bytes = want;
+    }
+    *out = &sl;
     return BLDFM_OK;
+}
+
+// stage timers: event k is recorded before stage k
+inline void tmark(DeviceCache &dc, cudaStream_t st)
+{
+    if (!dc.timing || !dc.cur || dc.cur->used > NTIMER) return;
+    cudaEventRecord(dc.cur->ev[dc.cur->used++], st);
+}
+
+inline void timers_begin(DeviceCache &dc)
+{
+    dc.cur = nullptr;
+    if (!dc.timing) return;
+    if (dc.tsets.empty()) {
+        dc.tsets.resize(NTSETS);
+        for (auto &t : dc.tsets)
+            for (int i = 0; i <= NTIMER; ++i) cudaEventCreate(&t.ev[i]);
+    }
+    if (dc.tpending >= NTSETS) return;  // full: further solves are not timed
+    dc.cur = &dc.tsets[dc.tnext];
+    dc.tnext = (dc.tnext + 1) % NTSETS;
+    dc.tpending++;
+    dc.cur->used = 0;
 }
 
 void eigval_parallel(const ModeList &ml, const SolveGeom &g, const double *prof, int nz, double *eig)
@@ -456,8 +510,10 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
     const size_t slotb = (size_t)nz * 4;
     const size_t eigb = f64 ? (size_t)g.nsolved * 16 : 0;
     const size_t off_lv32 = al(lv64b), off_slot = off_lv32 + al(lv32b), off_eig = off_slot + al(slotb);
-    if ((rc = ensure_stage(dc, off_eig + al(eigb) + 256)) != BLDFM_OK) return rc;
-    char *sg = (char *)dc.stage;
+    StageSlot *slt = nullptr;
+    if ((rc = acquire_stage(dc, off_eig + al(eigb) + 256, &slt)) != BLDFM_OK) return rc;
+    char *sg = (char *)slt->buf;
+    timers_begin(dc);
     hx_level_table(nz, z, prof, (double *)sg);
     if (!f64) hx_level_table32(nz, z, prof, (float *)(sg + off_lv32));
     memcpy(sg + off_slot, hp.slot.data(), slotb);
@@ -466,9 +522,14 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
     if (lv64b) CK(cudaMemcpyAsync(lv64, sg, lv64b, cudaMemcpyHostToDevice, st));
     if (!f64 && lv32b) CK(cudaMemcpyAsync(lv32, sg + off_lv32, lv32b, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(slot, sg + off_slot, slotb, cudaMemcpyHostToDevice, st));
+    // every spectrum entry is written unless some output slot stays empty
+    // (duplicate levels) or the analytic branch runs
     const size_t specb = (size_t)g.nlvls * g.nlx * g.nly * (f64 ? 16 : 8);
-    CK(cudaMemsetAsync(w + L.Xp, 0, specb, st));
-    CK(cudaMemsetAsync(w + L.Xq, 0, specb, st));
+    if (g.nsnap < g.nlvls || g.analytic) {
+        CK(cudaMemsetAsync(w + L.Xp, 0, specb, st));
+        CK(cudaMemsetAsync(w + L.Xq, 0, specb, st));
+    }
+    tmark(dc, st);  // 0: before the forward transform
 
     const double p000 = d->srf_bg_conc;
     if (f64) {
@@ -476,6 +537,7 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         if (!g.footprint)
             CK(launch_forward_fft<double>(g, hp.plx_fwd, hp.ply_fwd, twxf->d64, twyf->d64, srf_dev,
                                           (double2 *)(w + L.A), q0, st));
+        tmark(dc, st);  // 1: before the sweep
         double2 *eig = (double2 *)(w + L.eig);
         double2 *Xp = (double2 *)(w + L.Xp), *Xq = (double2 *)(w + L.Xq);
         if (g.analytic) {
@@ -488,13 +550,15 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         } else {
             double2 *snap = (double2 *)(w + L.snap), *top = (double2 *)(w + L.top);
             if (g.nsolved > 0) CK(launch_sweep64(g, lv64, slot, ml->dev, q0, snap, top, err, dc.nsm, st));
+            tmark(dc, st);  // 2: after the sweep
             // the host evaluates libm csqrt for every mode while the device sweeps
-            CK(cudaEventRecord(dc.ev_sweep, st));
             eigval_parallel(*ml, g, prof, nz, (double *)(sg + off_eig));
             if (eigb) CK(cudaMemcpyAsync(eig, sg + off_eig, eigb, cudaMemcpyHostToDevice, st));
+            CK(cudaEventRecord(slt->ev, st));
             CK(launch_combine64(g, ml->dev, eig, snap, top, Xp, Xq, st));
             CK(launch_trapezoid64(g, lv64, slot, q0, p000, Xp, Xq, st));
         }
+        tmark(dc, st);  // 3: before the output transform
         CK(launch_output_fft<double>(g, hp.plx_out, hp.ply_out, twxo->d64, twyo->d64, xband, Xp, Xq,
                                      (double2 *)(w + L.Cb), conc, flx, st));
     } else {
@@ -502,16 +566,21 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         if (!g.footprint)
             CK(launch_forward_fft<float>(g, hp.plx_fwd, hp.ply_fwd, twxf->d32, twyf->d32, srf_dev,
                                          (float2 *)(w + L.A), q0, st));
+        CK(cudaEventRecord(slt->ev, st));
+        tmark(dc, st);  // 1: before the sweep
         float2 *Xp = (float2 *)(w + L.Xp), *Xq = (float2 *)(w + L.Xq);
         const float ax = (float)(g.lx_scale * g.valx), ay = (float)(g.ly_scale * g.valy);
         if (g.nsolved > 0)
             CK(launch_riccati32(g, lv32, slot, ml->dev, q0, (float *)(w + L.scratch), Xp, Xq, ax, ay, err, dc.nsm,
                                 256, st));
+        tmark(dc, st);  // 2: after the sweep
         CK(launch_trapezoid32(g, lv64, slot, q0, p000, Xp, Xq, st));
+        tmark(dc, st);  // 3: before the output transform
         CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq,
                                     (float2 *)(w + L.Cb), conc, flx, st));
     }
-    CK(cudaEventRecord(dc.stage_ev, st));
+    tmark(dc, st);  // 4: end
+    if (f64 && g.analytic) CK(cudaEventRecord(slt->ev, st));
     return BLDFM_OK;
 }
 
@@ -541,6 +610,61 @@ const char *bldfm_status_str(int s)
 }
 
 const char *bldfm_version(void) { return BLDFM_VERSION_STR; }
+
+int bldfm_set_stage_timing(int enable)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    int status = BLDFM_OK;
+    DeviceCache &dc = cache_for_current(&status);
+    if (status != BLDFM_OK) return status;
+    dc.timing = enable != 0;
+    dc.tpending = 0;
+    dc.tnext = 0;
+    return BLDFM_OK;
+}
+
+int bldfm_stage_times(float *ms, int n)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    int status = BLDFM_OK;
+    DeviceCache &dc = cache_for_current(&status);
+    if (status != BLDFM_OK) return status;
+    if (!ms || n < 1) return BLDFM_ERR_ARG;
+    for (int k = 0; k < n; ++k) ms[k] = 0.f;
+    if (!dc.timing || dc.tpending == 0) return 0;
+    // average over every solve timed since the last call
+    std::vector<double> acc(NTIMER, 0.0);
+    int nst = 0, cnt = 0;
+    const int first = (dc.tnext - dc.tpending + NTSETS) % NTSETS;
+    for (int j = 0; j < dc.tpending; ++j) {
+        TimerSet &t = dc.tsets[(first + j) % NTSETS];
+        if (t.used < 2) continue;
+        CK(cudaEventSynchronize(t.ev[t.used - 1]));
+        for (int k = 0; k + 1 < t.used && k < NTIMER; ++k) {
+            float e = 0.f;
+            CK(cudaEventElapsedTime(&e, t.ev[k], t.ev[k + 1]));
+            acc[k] += e;
+        }
+        nst = std::max(nst, t.used - 1);
+        ++cnt;
+    }
+    dc.tpending = 0;
+    for (int k = 0; k < nst && k < n; ++k) ms[k] = (float)(acc[k] / std::max(cnt, 1));
+    return std::min(nst, n);
+}
+
+int bldfm_fma_peak(int fp64, double *flops_per_s, void *stream)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (!flops_per_s) return BLDFM_ERR_ARG;
+    int status = BLDFM_OK;
+    DeviceCache &dc = cache_for_current(&status);
+    if (status != BLDFM_OK) return status;
+    double v = 0;
+    if (run_fma_peak(fp64 != 0, dc.nsm, (cudaStream_t)stream, &v) != cudaSuccess) return BLDFM_ERR_CUDA;
+    *flops_per_s = v;
+    return BLDFM_OK;
+}
 
 int bldfm_plan(const bldfm_desc *d, int nlvls, bldfm_plan_info *out)
 {

@@ -893,3 +893,54 @@ cudaError_t launch_nonfinite(const double *a, const double *b, int64_t n, int *f
     nonfinite_kernel<<<(unsigned)blocks, 256, 0, st>>>(a, b, n, flag);
     return LAUNCH_CHECK();
 }
+
+// ---------------------------------------------------------------------------
+// FMA throughput probe: independent FMA chains per thread, CUDA-event timed.
+// Measures the FP32 / FP64 pipe peaks that bound the sweep kernels.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) fma_peak_kernel(T *out, int iters, T b, T c)
+{
+    T a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = (T)(threadIdx.x + k) * (T)1e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == (T)-12345.678) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_s)
+{
+    const int threads = 256, blocks = nsm * 8;
+    const int iters = fp64 ? 2048 : 65536;
+    void *out = nullptr;
+    cudaError_t e = cudaMalloc(&out, (size_t)threads * blocks * 8);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(a, st);
+        if (fp64)
+            fma_peak_kernel<double><<<blocks, threads, 0, st>>>((double *)out, iters, 0.999999, 1e-7);
+        else
+            fma_peak_kernel<float><<<blocks, threads, 0, st>>>((float *)out, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    *flops_per_s = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3);
+    return e;
+}

@@ -34,3 +34,4 @@ cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftP
 cudaError_t launch_tw_to_float(const double2 *src, float2 *dst, int n, cudaStream_t st);
 cudaError_t launch_spec_to_float(const double2 *src, float2 *dst, int64_t n, cudaStream_t st);
 cudaError_t launch_nonfinite(const double *a, const double *b, int64_t n, int *flag, int nsm, cudaStream_t st);
+cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_s);

@@ -126,6 +126,21 @@ int bldfm_vertical_profiles(int32_t n, double meas_height, double um, double vm,
                             double stretch, double tke, int32_t *nz_out,
                             double *z_dev, double *prof_dev, void *stream);
 
+/* Per-stage CUDA-event timers of bldfm_solve on the current device (no
+ * counterpart in the reference, which only times whole runs with time.time,
+ * runs/manuscript/low_level/comparison_analytic.py:43-49).  When enabled,
+ * bldfm_stage_times() returns the mean milliseconds per stage over the
+ * solves enqueued since the previous call (up to 1024): [0] forward transform,
+ * [1] sweep, [2] k=0 mode / combination, [3] output transform.  It returns the
+ * number of stages written and restarts the average. */
+int bldfm_set_stage_timing(int enable);
+int bldfm_stage_times(float *ms, int n);
+
+/* Measured FMA throughput of this GPU (flops/s, an FMA counted as 2), FP32 or
+ * FP64: the pipe peak the sweep kernels are held against (no reference
+ * counterpart). */
+int bldfm_fma_peak(int fp64, double *flops_per_s, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
