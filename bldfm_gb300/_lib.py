@@ -104,6 +104,10 @@ _SIGS = {
     "bldfm_set_stage_timing": (ctypes.c_int, [ctypes.c_int]),
     "bldfm_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     "bldfm_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), _P]),
+    "bldfm_solve_noalloc": (
+        ctypes.c_int,
+        [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P],
+    ),
 }
 
 _lib = None

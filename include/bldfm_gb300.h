@@ -141,6 +141,25 @@ int bldfm_stage_times(float *ms, int n);
  * counterpart). */
 int bldfm_fma_peak(int fp64, double *flops_per_s, void *stream);
 
+/* Allocation-free FP32 solve.  No counterpart in the reference (which never
+ * touches a GPU).  For callers that may not allocate device memory while they
+ * solve: work enqueued inside a CUDA stream capture, hosts that reserve all
+ * device memory up front, plugin hosts whose allocator policy forbids
+ * cudaMalloc from libraries.  Same arguments as bldfm_solve minus the
+ * workspace: every intermediate lives in one static device array of 16 MiB
+ * that each GPU loading this library holds until exit.
+ *  - BLDFM_MODE_FP32 only, analytic == 0; larger problems return
+ *    BLDFM_ERR_WORKSPACE (the 512^2 footprint with 512^2 modes needs ~7 MiB).
+ *  - The first call on a device looks up the array's address with that
+ *    device current; make it before any stream capture.
+ *  - All calls share the array: calls whose GPU work overlaps race; order
+ *    them on one stream.
+ *  - Calls no cudaMalloc/cudaFree/cudaHostAlloc; host staging is static. */
+int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_dev,
+                        const double *z_host, const double *prof_host,
+                        const int64_t *levels_host, int32_t nlvls,
+                        double *conc_dev, double *flx_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

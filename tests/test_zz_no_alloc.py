@@ -1,0 +1,106 @@
+"""The allocation-free entry point bldfm_solve_noalloc against bldfm_solve.
+
+bldfm_solve_noalloc serves callers that cannot allocate GPU memory while they
+solve (stream capture, pre-reserved device memory, allocator policies of a
+plugin host): its scratch is one static 16 MiB device array.  This file runs
+last (pytest collects it after the others) and must pass both alone in a fresh
+process and after the rest of the suite.  Two calls in a row with different
+problems check that the shared array is reused and cleared correctly.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-3  # same bar as the FP32 parity tests
+
+
+def _problem(footprint, levels, seed):
+    from oracle import bldfm_oracle as O
+
+    rng = np.random.default_rng(seed)
+    z, p = O.vertical_profiles(24, 10.0, (float(rng.uniform(1, 4)), float(rng.uniform(-4, -1))), ustar=0.35,
+                               mol=-40.0)
+    ny, nx = 96, 128
+    src = np.zeros((ny, nx))
+    if not footprint:
+        src = rng.random((ny, nx))
+    return dict(srf=src, z=z, prof=np.ascontiguousarray(np.stack(p)), levels=np.asarray(levels, np.int64),
+                footprint=footprint, domain=(256.0, 192.0), modes=(128, 96), meas=(60.0, 90.0))
+
+
+def _solve_both(pb, torch, lib, _lib, make_desc, plan):
+    dev = torch.device("cuda", 0)
+    d = make_desc(pb["srf"].shape, len(pb["z"]), pb["domain"], pb["modes"], pb["meas"], 0.25, pb["footprint"],
+                  False, None, "double", "fp32")
+    info = plan(d, len(pb["levels"]))
+    shape = (len(pb["levels"]), info.out_ny, info.out_nx)
+    srf = torch.from_numpy(np.ascontiguousarray(pb["srf"])).to(dev)
+    out = {}
+    ws = torch.empty(int(info.workspace_bytes), dtype=torch.uint8, device=dev)
+    c1 = torch.empty(shape, dtype=torch.float64, device=dev)
+    f1 = torch.empty_like(c1)
+    st = lib.bldfm_solve(
+        d, ctypes.c_void_p(srf.data_ptr()), _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]),
+        len(pb["levels"]), ctypes.c_void_p(c1.data_ptr()), ctypes.c_void_p(f1.data_ptr()),
+        ctypes.c_void_p(ws.data_ptr()), ctypes.c_size_t(ws.numel()), None)
+    _lib.check(st)
+    out["ws"] = (c1, f1)
+    c2 = torch.full(shape, float("nan"), dtype=torch.float64, device=dev)
+    f2 = torch.full(shape, float("nan"), dtype=torch.float64, device=dev)
+    out["noalloc_args"] = (d, srf, c2, f2)
+    return out
+
+
+def test_noalloc_matches_workspace_entry_two_calls():
+    import torch
+
+    from bldfm_gb300 import _lib
+    from bldfm_gb300.solver import make_desc, plan
+
+    lib = _lib.load()
+    problems = [
+        _problem(True, [24], seed=1),              # footprint, one level
+        _problem(False, [0, 12, 12, 24], seed=2),  # dispersion, duplicate level: slot left empty
+    ]
+    prepared = [_solve_both(pb, torch, lib, _lib, make_desc, plan) for pb in problems]
+    # two allocation-free calls back to back on the same stream
+    for pb, pr in zip(problems, prepared):
+        d, srf, c2, f2 = pr["noalloc_args"]
+        st = lib.bldfm_solve_noalloc(
+            d, ctypes.c_void_p(srf.data_ptr()), _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]),
+            len(pb["levels"]), ctypes.c_void_p(c2.data_ptr()), ctypes.c_void_p(f2.data_ptr()), None)
+        _lib.check(st, "bldfm_solve_noalloc")
+    torch.cuda.synchronize()
+    for pb, pr in zip(problems, prepared):
+        c1, f1 = (t.cpu().numpy() for t in pr["ws"])
+        _, _, c2, f2 = pr["noalloc_args"]
+        c2, f2 = c2.cpu().numpy(), f2.cpu().numpy()
+        assert np.all(np.isfinite(c2)) and np.all(np.isfinite(f2))
+        for a, b in ((c2, c1), (f2, f1)):
+            err = np.linalg.norm(a - b) / np.linalg.norm(b)
+            assert err <= FP32_TOL, err
+
+
+def test_noalloc_rejects_what_it_cannot_do():
+    from bldfm_gb300 import _lib
+    from bldfm_gb300.solver import make_desc
+
+    lib = _lib.load()
+    pb = _problem(True, [24], seed=3)
+    out = np.zeros(1)
+    # FP64 mode needs pinned host staging: not offered here
+    d = make_desc(pb["srf"].shape, len(pb["z"]), pb["domain"], pb["modes"], pb["meas"], 0.0, True, False, None,
+                  "double", "fp64")
+    st = lib.bldfm_solve_noalloc(d, None, _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]), 1,
+                                 _lib.ptr(out), _lib.ptr(out), None)
+    assert st == _lib.ERR_UNSUPPORTED
+    # beyond the 16 MiB scratch array: 1024^2 modes on a 2048^2 extended grid
+    d = make_desc((1024, 1024), len(pb["z"]), (1000.0, 1000.0), (1024, 1024), (500.0, 500.0), 0.0, True, False,
+                  512.0, "double", "fp32")
+    st = lib.bldfm_solve_noalloc(d, None, _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]), 1,
+                                 _lib.ptr(out), _lib.ptr(out), None)
+    assert st == _lib.ERR_WORKSPACE
