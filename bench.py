@@ -9,12 +9,14 @@ vertical_profiles(n=128, z_m=20 m) -> 207 levels, unstable MOST profiles
 One step = one batch of B footprints for B met cases (seeded).
 
 Reported:
-  value          FP32 invariant-imbedding path, device-resident buffers
-                 (bldfm_solve), footprints/s over K timed steps
-  fp64           the FP64 path (reference rounding) on the same batches
-  e2e            the reference-facing drop-in steady_state_transport_solver
-                 (numpy in, numpy out, host<->device copies inside)
-  roofline       the sweep kernel against the measured FP32 FMA peak
+  value          batched FP32 invariant-imbedding path (bldfm_solve_batch,
+                 replayed as a CUDA graph, device-resident outputs),
+                 footprints/s over K timed steps cycling 4 met batches
+  single_fp32    one bldfm_solve per footprint (no batching)
+  fp64           the FP64 path (reference rounding), one solve per footprint
+  e2e            the public batched API solve_batch (numpy in, numpy out,
+                 host<->device copies inside); also the single-case drop-in
+  roofline       the batched sweep kernel against the measured FP32 FMA peak
   cpu_baseline   the CPU oracle port (reference arithmetic, OpenMP on all
                  host cores) on a bounded sample
 
@@ -242,11 +244,18 @@ def main():
     sptr = ctypes.c_void_p(stream.cuda_stream)
 
     B = args.batch
-    cases = met_cases(B, seed=1000 + rank)
-    inputs = []
-    for c in cases:
-        z, p = profiles_for(c, device_profiles=True)
-        inputs.append((z, p))
+    NB = 4  # distinct met batches cycled through the timed steps
+    batches = []
+    for j in range(NB):
+        cs = met_cases(B, seed=1000 + 97 * rank + j)
+        batches.append([profiles_for(c, device_profiles=True) for c in cs])
+    inputs = batches[0]
+    kwb = [[solver_kwargs(z, p) for z, p in bt] for bt in batches]
+
+    from bldfm_gb300 import autotune
+    from bldfm_gb300.batch import BatchSolver, solve_batch
+
+    threads, per_sm = autotune.tune(kwb[0])
 
     def make_solves(mode):
         solves = []
@@ -298,10 +307,53 @@ def main():
             ms = float(t.item())
         return ms, stages
 
-    # --- FP32 path (headline) ---
-    s32 = make_solves("fp32")
+    def timed_batches(solver, steps, warmup, stage_timing=False):
+        # descriptors built once per met batch (input preparation); each timed
+        # step is one bldfm_solve_batch call: level tables, k = 0 values and
+        # maps are computed from the profiles inside the call
+        prep = [solver.prepare_cached(kwb[j]) for j in range(NB)]
+        for i in range(warmup):
+            solver.solve_prepared(prep[i % NB])
+        solver.stream.synchronize()
+        if dist is not None:
+            dist.barrier()
+        if stage_timing:
+            lib.bldfm_set_stage_timing(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(solver.stream)
+        for i in range(steps):
+            solver.solve_prepared(prep[i % NB])
+        e1.record(solver.stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        stages = None
+        if stage_timing:
+            arr = (ctypes.c_float * 8)()
+            n = lib.bldfm_stage_times(arr, 8)
+            stages = [float(arr[i]) for i in range(max(n, 0))]
+            lib.bldfm_set_stage_timing(0)
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, stages
+
+    # --- headline: batched FP32 path replayed as a CUDA graph ---
+    gsolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True)
     with ClockSampler(local) as clk:
-        ms32, stages32 = timed(s32, args.steps, args.warmup, stage_timing=True)
+        msb, _ = timed_batches(gsolver, args.steps, args.warmup)
+    fps_batch = world * B * args.steps / (msb * 1e-3)
+    if gsolver.status() != 0:
+        raise RuntimeError("device status %d" % gsolver.status())
+    # same batches without the graph, with per-stage CUDA-event timers (roofline)
+    tsolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=False)
+    msnb, stages_b = timed_batches(tsolver, args.steps, args.warmup, stage_timing=True)
+    fps_nograph = world * B * args.steps / (msnb * 1e-3)
+
+    # --- single-footprint FP32 solves (bldfm_solve), for comparison ---
+    s32 = make_solves("fp32")
+    ms32, stages32 = timed(s32, args.steps, args.warmup, stage_timing=True)
     fps32 = world * B * args.steps / (ms32 * 1e-3)
 
     # --- FP64 path (reference rounding) ---
@@ -309,39 +361,57 @@ def main():
     ms64, stages64 = timed(s64, args.fp64_steps, 1, stage_timing=True)
     fps64 = world * B * args.fp64_steps / (ms64 * 1e-3)
 
-    # accuracy of the FP32 path against the FP64 path on this batch
+    # accuracy of the batched FP32 path against the FP64 path on batch 0
+    outs = gsolver.solve(kwb[0])
+    gsolver.stream.synchronize()
     errs = []
-    for a, b in zip(s32, s64):
-        ca, fa = a[3].cpu().numpy(), a[4].cpu().numpy()
+    for (ca, fa), b in zip(outs, s64):
+        ca, fa = ca[0].cpu().numpy(), fa[0].cpu().numpy()
         cb, fb = b[3].cpu().numpy(), b[4].cpu().numpy()
         errs.append(max(np.linalg.norm(ca - cb) / np.linalg.norm(cb), np.linalg.norm(fa - fb) / np.linalg.norm(fb)))
     rel32 = max(errs)
-
-    # --- e2e through the reference-facing drop-in (numpy in / numpy out) ---
-    kws = [solver_kwargs(z, p) for z, p in inputs]
-    e2e_steps = max(2, args.steps // 2)
-    for kw in kws[: min(B, 4)]:
-        steady_state_transport_solver(**kw, mode="fp32")
+    # against the exact discrete solution (accurate FP64 mode) on 4 cases: the
+    # accuracy bar of the fast path, and the reference rounding's own error
+    sr = make_solves("fp64r")[:4]
+    run_batch(sr)
     torch.cuda.synchronize()
+    e32x, e64x = [], []
+    for (ca, fa), b, r in zip(outs, s64, sr):
+        ca, fa = ca[0].cpu().numpy(), fa[0].cpu().numpy()
+        cb, fb = b[3].cpu().numpy(), b[4].cpu().numpy()
+        cr, fr = r[3].cpu().numpy(), r[4].cpu().numpy()
+        e32x.append(max(np.linalg.norm(ca - cr) / np.linalg.norm(cr), np.linalg.norm(fa - fr) / np.linalg.norm(fr)))
+        e64x.append(max(np.linalg.norm(cb - cr) / np.linalg.norm(cr), np.linalg.norm(fb - fr) / np.linalg.norm(fr)))
+
+    # --- e2e through the public batched API (numpy in, numpy out) ---
+    esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True)
+    e2e_steps = max(2, args.steps // 2)
+    solve_batch(kwb[0], solver=esolver)
     t = time.perf_counter()
-    for _ in range(e2e_steps):
-        for kw in kws:
-            steady_state_transport_solver(**kw, mode="fp32")
+    for i in range(e2e_steps):
+        solve_batch(kwb[i % NB], solver=esolver)
     e2e_dt = time.perf_counter() - t
     e2e_fps = world * B * e2e_steps / e2e_dt
     nz = len(inputs[0][0])
-    h2d = B * ((nz - 1) * (12 * 8 + 12 * 4) + nz * 4)
+    h2d = B * ((nz - 1) * (12 * 8 + 12 * 4) + nz * 4 + 32 + 640)
     d2h = B * 2 * NY * NX * 8
+    # the single-footprint drop-in, for comparison
+    kws = kwb[0]
+    steady_state_transport_solver(**kws[0], mode="fp32")
+    t = time.perf_counter()
+    for kw in kws:
+        steady_state_transport_solver(**kw, mode="fp32")
+    e2e_single = world * B / (time.perf_counter() - t)
 
-    # --- roofline of the FP32 sweep kernel ---
+    # --- roofline of the batched FP32 sweep kernel ---
     peak = ctypes.c_double(0)
     _lib.check(lib.bldfm_fma_peak(0, ctypes.byref(peak), sptr), "fma_peak")
     peak64 = ctypes.c_double(0)
     _lib.check(lib.bldfm_fma_peak(1, ctypes.byref(peak64), sptr), "fma_peak")
     nsolved = int(s32[0][1].nsolved)
     steps_z = nz - 1
-    flops_launch = F32_FLOPS_PER_MODE_STEP * nsolved * steps_z
-    sweep_ms = stages32[1] if stages32 and len(stages32) > 1 else None
+    flops_launch = F32_FLOPS_PER_MODE_STEP * nsolved * steps_z * B
+    sweep_ms = stages_b[1] if stages_b and len(stages_b) > 1 else None
     achieved = flops_launch / (sweep_ms * 1e-3) / 1e12 if sweep_ms else None
     flops64 = F64_FLOPS_PER_MODE_STEP * nsolved * steps_z
     sweep64_ms = stages64[1] if stages64 and len(stages64) > 1 else None
@@ -358,12 +428,12 @@ def main():
     if rank == 0:
         line = {
             "metric": "footprints/s",
-            "value": fps32,
+            "value": fps_batch,
             "unit": "footprints/s",
             "n_gpus": world,
             "steps": args.steps,
             "warmup": args.warmup,
-            "ms_per_step": ms32 / args.steps,
+            "ms_per_step": msb / args.steps,
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
@@ -372,21 +442,27 @@ def main():
             "config": {
                 "workload": WORKLOAD_NAME,
                 "footprints_per_step": B,
-                "path": "fp32 invariant-imbedding sweep + fp32 FFT, device-resident",
-                "l2": "inputs larger than L2: each footprint of a step has its own ~10 MB workspace and outputs",
+                "path": "batched fp32 invariant-imbedding sweep + fp32 transforms, CUDA graph, device-resident",
+                "met_batches": NB,
+                "sweep_launch": {"threads": threads, "ctas_per_sm": per_sm, "autotuned": True},
+                "l2": "inputs larger than L2: a step's 16 footprints use ~170 MB of spectra and outputs",
                 "parallelism": "replicas" if world > 1 else "single",
             },
             "relL2_fp32_vs_fp64": rel32,
+            "relL2_fp32_vs_exact": max(e32x),
+            "relL2_fp64_reference_rounding_vs_exact": max(e64x),
+            "batched_no_graph": {"value": fps_nograph, "unit": "footprints/s", "stage_ms": stages_b},
+            "single_fp32": {"value": fps32, "unit": "footprints/s", "stage_ms": stages32},
             "fp64": {"value": fps64, "unit": "footprints/s", "ms_per_footprint": ms64 / (args.fp64_steps * B),
                      "stage_ms": stages64, "sweep_tflops": achieved64,
                      "fp64_peak_tflops": peak64.value / 1e12,
                      "frac": (achieved64 / (peak64.value / 1e12)) if achieved64 else None},
-            "fp32_stage_ms": stages32,
             "e2e": {"value": e2e_fps, "unit": "footprints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "api": "bldfm_gb300.steady_state_transport_solver(mode='fp32')"},
+                    "api": "bldfm_gb300.batch.solve_batch (numpy in, numpy out)",
+                    "single_case_dropin": e2e_single},
             "roofline": {
                 "bound": "fp32-pipe",
-                "kernel": "riccati32_kernel",
+                "kernel": "riccati32_batch_kernel",
                 "achieved": achieved,
                 "peak": peak.value / 1e12,
                 "unit": "TFLOP/s",
@@ -396,7 +472,7 @@ def main():
                 "flops_per_launch": flops_launch,
             },
             "cpu_baseline": cpu,
-            "gpu_launches": 4 * B * args.steps,
+            "gpu_launches": 3 * args.steps,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

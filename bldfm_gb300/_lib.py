@@ -28,6 +28,7 @@ PREC_SINGLE = 0
 PREC_DOUBLE = 1
 MODE_FP64 = 0
 MODE_FP32 = 1
+MODE_FP64R = 2
 
 CLOSURES = {"MOST": 0, "CONSTANT": 1, "MOSTM": 2, "OAAHOC": 3}
 
@@ -70,6 +71,29 @@ class PlanInfo(ctypes.Structure):
     ]
 
 
+class Case(ctypes.Structure):
+    _fields_ = [
+        ("desc", Desc),
+        ("srf_flx_dev", ctypes.c_void_p),
+        ("z_host", ctypes.c_void_p),
+        ("prof_host", ctypes.c_void_p),
+        ("levels_host", ctypes.c_void_p),
+        ("nlvls", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("conc_dev", ctypes.c_void_p),
+        ("flx_dev", ctypes.c_void_p),
+    ]
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [
+        ("threads", ctypes.c_int32),
+        ("ctas_per_sm", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 _P = ctypes.c_void_p
 _SIGS = {
     "bldfm_status_str": (ctypes.c_char_p, [ctypes.c_int]),
@@ -104,6 +128,14 @@ _SIGS = {
     "bldfm_set_stage_timing": (ctypes.c_int, [ctypes.c_int]),
     "bldfm_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     "bldfm_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), _P]),
+    "bldfm_batch_plan": (
+        ctypes.c_int,
+        [ctypes.POINTER(Case), ctypes.c_int32, ctypes.POINTER(BatchOpts), ctypes.POINTER(ctypes.c_int64)],
+    ),
+    "bldfm_solve_batch": (
+        ctypes.c_int,
+        [ctypes.POINTER(Case), ctypes.c_int32, ctypes.POINTER(BatchOpts), _P, ctypes.c_size_t, _P],
+    ),
     "bldfm_solve_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P],

@@ -1,0 +1,92 @@
+"""Autotuner for the batched sweep launch.
+
+Picks the sweep CTA size (modes per CTA tile) and the number of persistent
+CTAs per SM for a batch shape by timing candidates on the device with CUDA
+events, and caches the winner in a JSON file keyed by GPU name and a coarse
+shape signature (total solved modes, deepest level count, number of cases).
+Cache file: $BLDFM_GB300_CACHE or ~/.cache/bldfm_gb300/autotune.json.
+"""
+
+import json
+import os
+
+import numpy as np
+import torch
+
+from . import _lib
+from .batch import BatchSolver
+
+CANDIDATES = [(256, 0), (256, 4), (256, 6), (128, 0), (128, 8), (128, 12)]
+
+
+def _cache_path():
+    p = os.environ.get("BLDFM_GB300_CACHE")
+    if p:
+        return p
+    return os.path.join(os.path.expanduser("~"), ".cache", "bldfm_gb300", "autotune.json")
+
+
+def _load():
+    try:
+        with open(_cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(d):
+    p = _cache_path()
+    try:
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        with open(p, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+    except OSError:
+        pass
+
+
+def signature(cases):
+    """Coarse shape key: modes to 2^k buckets, levels to 16s, cases to 2^k."""
+    from .solver import make_desc, plan
+
+    total, maxnz = 0, 0
+    for kw in cases:
+        d = make_desc(np.shape(kw["srf_flx"]), len(kw["z"]), kw["domain"], kw.get("modes", (512, 512)),
+                      kw.get("meas_pt", (0.0, 0.0)), 0.0, bool(kw.get("footprint", False)), False, kw.get("halo"),
+                      kw.get("precision", "single"), "fp32")
+        info = plan(d, 1)
+        total += int(info.nsolved)
+        maxnz = max(maxnz, len(kw["z"]))
+    b = lambda v: 1 << max(0, int(v - 1).bit_length())  # noqa: E731
+    return "%s|modes%d|nz%d|cases%d" % (torch.cuda.get_device_name(), b(total), 16 * ((maxnz + 15) // 16),
+                                        b(len(cases)))
+
+
+def tune(cases, reps=3, use_cache=True):
+    """Return (threads, ctas_per_sm) for this batch shape (timed or cached)."""
+    key = signature(cases)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        v = cache[key]
+        return int(v["threads"]), int(v["ctas_per_sm"])
+    best, best_ms = CANDIDATES[0], None
+    for threads, per_sm in CANDIDATES:
+        s = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=False)
+        s.solve(cases)  # warm
+        s.stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s.stream)
+        for _ in range(reps):
+            s.solve(cases)
+        e1.record(s.stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        if s.status() != 0:
+            continue
+        if best_ms is None or ms < best_ms:
+            best, best_ms = (threads, per_sm), ms
+    if use_cache:
+        cache[key] = {"threads": best[0], "ctas_per_sm": best[1], "ms": best_ms}
+        _save(cache)
+    return best
+

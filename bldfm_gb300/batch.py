@@ -1,0 +1,197 @@
+"""Batched FP32 solves on the GPU: many towers x timesteps in one launch.
+
+The reference solves one case per Python call and parallelises over cases
+with a process pool (src/bldfm/interface.py:141-326).  Here a batch of cases,
+each with its own grid, modes, levels and profiles, goes to the C ABI entry
+point ``bldfm_solve_batch``: one persistent sweep launch over every
+(case, mode tile), one launch per transform pass, replayed as a CUDA graph
+when the batch topology repeats (e.g. a met timeseries on fixed towers).
+
+``solve_batch(cases)`` takes a list of keyword-argument dicts of
+``steady_state_transport_solver`` and returns the list of ``(grid, conc, flx)``
+tuples.  ``BatchSolver`` keeps workspace and device outputs between batches.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .solver import _normalise_levels, make_desc, plan
+
+
+def _host_inputs(kw):
+    z = np.ascontiguousarray(kw["z"], dtype=np.float64)
+    nz = z.shape[0]
+    prof = np.ascontiguousarray(
+        np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in kw["profiles"]])
+    )
+    levels, lv = _normalise_levels(kw["levels"], nz)
+    return z, prof, levels, lv
+
+
+class BatchSolver:
+    """Solve batches of FP32 cases with persistent device buffers.
+
+    ``solve(cases)`` enqueues a batch on ``self.stream`` and returns device
+    tensors ``(conc, flx)`` per case, shape (nlvls, out_ny, out_nx).  Buffers
+    are reused while the batch shape repeats.
+    """
+
+    def __init__(self, device=None, threads=0, ctas_per_sm=0, use_graph=True):
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.stream = torch.cuda.Stream(device=self.device)
+        self.opts = _lib.BatchOpts(threads=int(threads), ctas_per_sm=int(ctas_per_sm), use_graph=int(use_graph))
+        self._ws = None
+        self._out_buf = None  # one device buffer holding every case's conc and flx
+        self._srf = {}
+        self._keep = None
+
+    def _srf_dev(self, k, srf):
+        a = np.ascontiguousarray(srf, dtype=np.float64)
+        t = self._srf.get(k)
+        if t is None or tuple(t.shape) != a.shape:
+            t = torch.empty(a.shape, dtype=torch.float64, device=self.device)
+            self._srf[k] = t
+        with torch.cuda.stream(self.stream):
+            t.copy_(torch.from_numpy(a).pin_memory(), non_blocking=True)
+        return t
+
+    def prepare(self, cases):
+        """Build the C descriptors of a batch; returns (array, outputs, keepalive)."""
+        n = len(cases)
+        arr = (_lib.Case * n)()
+        outs, keep = [], []
+        descs, shapes = [], []
+        for kw in cases:
+            z, prof, levels, lv = _host_inputs(kw)
+            d = make_desc(
+                np.shape(kw["srf_flx"]), len(z), kw["domain"], kw.get("modes", (512, 512)),
+                kw.get("meas_pt", (0.0, 0.0)), kw.get("srf_bg_conc", 0.0), bool(kw.get("footprint", False)), False,
+                kw.get("halo"), kw.get("precision", "single"), "fp32",
+            )
+            info = plan(d, lv.size)
+            descs.append((d, z, prof, levels, lv))
+            shapes.append((lv.size, info.out_ny, info.out_nx))
+        total = 2 * sum(int(np.prod(sh)) for sh in shapes)
+        if self._out_buf is None or self._out_buf.numel() < total:
+            self._out_buf = torch.empty(total, dtype=torch.float64, device=self.device)
+        self.out_elems = total
+        off = 0
+        for k, kw in enumerate(cases):
+            d, z, prof, levels, lv = descs[k]
+            sz = int(np.prod(shapes[k]))
+            conc = self._out_buf[off : off + sz].view(shapes[k])
+            flx = self._out_buf[off + sz : off + 2 * sz].view(shapes[k])
+            off += 2 * sz
+            footprint = bool(kw.get("footprint", False))
+            c = arr[k]
+            c.desc = d
+            c.srf_flx_dev = None if footprint else self._srf_dev(k, kw["srf_flx"]).data_ptr()
+            c.z_host = z.ctypes.data
+            c.prof_host = prof.ctypes.data
+            c.levels_host = lv.ctypes.data
+            c.nlvls = lv.size
+            c.conc_dev = conc.data_ptr()
+            c.flx_dev = flx.data_ptr()
+            outs.append((conc, flx))
+            keep.append((z, prof, lv, levels))
+        return arr, outs, keep
+
+    def solve(self, cases):
+        """Enqueue a batch given as keyword-argument dicts; returns device outputs."""
+        return self.solve_prepared(self.prepare(cases))
+
+    def solve_prepared(self, prepared):
+        """Enqueue a batch whose C descriptors were built by :meth:`prepare`
+        (reusable across calls: the library reads the host arrays at every
+        call, so refreshing their contents in place needs no new descriptors)."""
+        lib = _lib.load()
+        arr, outs, keep = prepared[:3]
+        n = len(arr)
+        if len(prepared) > 3:
+            need = prepared[3]
+        else:
+            nb = ctypes.c_int64(0)
+            _lib.check(lib.bldfm_batch_plan(arr, n, self.opts, ctypes.byref(nb)), "solve_batch")
+            need = int(nb.value)
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(int(need), dtype=torch.uint8, device=self.device)
+        st = lib.bldfm_solve_batch(
+            arr, n, self.opts, ctypes.c_void_p(self._ws.data_ptr()), ctypes.c_size_t(self._ws.numel()),
+            ctypes.c_void_p(self.stream.cuda_stream),
+        )
+        _lib.check(st, "solve_batch")
+        self._keep = keep
+        return outs
+
+    def prepare_cached(self, cases):
+        """:meth:`prepare` plus the workspace size, for repeated solves."""
+        lib = _lib.load()
+        arr, outs, keep = self.prepare(cases)
+        need = ctypes.c_int64(0)
+        _lib.check(lib.bldfm_batch_plan(arr, len(cases), self.opts, ctypes.byref(need)), "solve_batch")
+        return (arr, outs, keep, int(need.value))
+
+    def status(self):
+        """Device status word of the last batch (0, or a BLDFM_ERR_* code)."""
+        self.stream.synchronize()
+        return int(self._ws[:4].view(torch.int32).item()) if self._ws is not None else 0
+
+
+_GRID_CACHE = {}
+
+
+def _grid(z, levels, shape, domain):
+    """The reference's output grid (solver.py:292-297) as read-only arrays,
+    shared between cases with the same levels, shape and domain."""
+    zl = np.asarray(z)[levels]
+    key = (zl.tobytes(), tuple(shape), tuple(float(v) for v in domain))
+    g = _GRID_CACHE.get(key)
+    if g is None:
+        ny, nx = shape
+        x = np.linspace(0, domain[0], nx, endpoint=False)
+        y = np.linspace(0, domain[1], ny, endpoint=False)
+        Z, Y, X = np.meshgrid(zl, y, x, indexing="ij")
+        g = tuple(np.squeeze(a) for a in (X, Y, Z))
+        for a in g:
+            a.flags.writeable = False
+        if len(_GRID_CACHE) > 64:
+            _GRID_CACHE.clear()
+        _GRID_CACHE[key] = g
+    return g
+
+
+def solve_batch(cases, *, solver=None):
+    """Solve a list of cases (keyword-argument dicts of
+    ``steady_state_transport_solver``) in FP32 on the GPU; returns a list of
+    ``(grid, conc, flx)`` with the single-case function's shapes and dtypes.
+    All outputs come back in one device-to-host copy into pinned memory; the
+    grid arrays are shared read-only arrays."""
+    solver = solver or BatchSolver()
+    outs = solver.solve(cases)
+    host = torch.empty(solver.out_elems, dtype=torch.float64, pin_memory=True)
+    with torch.cuda.stream(solver.stream):
+        host.copy_(solver._out_buf[: solver.out_elems], non_blocking=True)
+    st = solver.status()
+    if st != 0:
+        _lib.check(st, "solve_batch")
+    hn = host.numpy()
+    results = []
+    off = 0
+    for kw, (conc_d, _) in zip(cases, outs):
+        shape = tuple(conc_d.shape)
+        sz = int(np.prod(shape))
+        conc = hn[off : off + sz].reshape(shape)
+        flx = hn[off + sz : off + 2 * sz].reshape(shape)
+        off += 2 * sz
+        footprint = bool(kw.get("footprint", False))
+        precision = kw.get("precision", "single")
+        xm, ym = kw.get("meas_pt", (0.0, 0.0))
+        if precision == "single" and not footprint and not (xm**2 + ym**2 > 0.0):
+            conc, flx = conc.astype(np.float32), flx.astype(np.float32)
+        z, _, levels, _ = _host_inputs(kw)
+        grid = _grid(z, levels, np.shape(kw["srf_flx"]), kw["domain"])
+        results.append((grid, np.squeeze(conc), np.squeeze(flx)))
+    return results

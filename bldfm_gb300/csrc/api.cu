@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/bldfm_gb300.h"
+#include "batch.h"
 #include "common.h"
 #include "host_exact.h"
 #include "kernels.h"
@@ -96,7 +97,7 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
     if ((d->nlx % 2) != 0 || (d->nly % 2) != 0) return BLDFM_ERR_ODD_MODES;
     if (d->precision != BLDFM_PREC_SINGLE && d->precision != BLDFM_PREC_DOUBLE) return BLDFM_ERR_PRECISION;
     if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nlx < 0 || d->nly < 0 || nlvls < 1) return BLDFM_ERR_ARG;
-    if (d->mode != BLDFM_MODE_FP64 && d->mode != BLDFM_MODE_FP32) return BLDFM_ERR_ARG;
+    if (d->mode != BLDFM_MODE_FP64 && d->mode != BLDFM_MODE_FP32 && d->mode != BLDFM_MODE_FP64R) return BLDFM_ERR_ARG;
     if (!(d->xmax > 0) || !(d->ymax > 0)) return BLDFM_ERR_ARG;
     if (d->nz > BLDFM_MAX_NZ) return BLDFM_ERR_UNSUPPORTED;
     SolveGeom &g = hp.g;
@@ -178,6 +179,10 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
         g.kyk_top = Ky[nz - 1] * kzinv;
         g.uk_top = u[nz - 1] * kzinv;
         g.vk_top = v[nz - 1] * kzinv;
+        double ex = 1.0, ey = 0.0;
+        g.iso = hx_profiles_iso(nz, prof, &ex, &ey);
+        g.ex = (float)ex;
+        g.ey = (float)ey;
     }
     // snapshot schedule (solver.py:350-372): slot s = s-th distinct level in [0, nz-1]
     hp.slot.assign(nz, -1);
@@ -194,6 +199,9 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
             if (levels[k] < -(int64_t)nz || levels[k] >= nz) return BLDFM_ERR_ARG;
     }
     g.nsnap = ns;
+    g.jmax = -1;
+    for (int i = 0; i < nz; ++i)
+        if (hp.slot[i] >= 0) g.jmax = i;
     g.nsolved = solved_count(nlx, nly);
     // output band columns: positions of frequencies [-h, h] mod nfx
     hp.xband.clear();
@@ -228,7 +236,7 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
 // workspace layout
 // ---------------------------------------------------------------------------
 struct Layout {
-    size_t err, lv64, lv32, slot, eig, snap, top, q0, A, Xp, Xq, Cb, scratch, total;
+    size_t err, lv64, lv32, slot, dc, eig, snap, top, q0, A, Xp, Xq, Cb, scratch, total;
 };
 
 inline size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -236,7 +244,8 @@ inline size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 Layout layout_for(const SolveGeom &g)
 {
     Layout L;
-    const bool f64 = g.mode == BLDFM_MODE_FP64 || g.analytic;
+    const bool f64 = g.mode != BLDFM_MODE_FP32 || g.analytic;
+    const bool shoot = g.mode == BLDFM_MODE_FP64 && !g.analytic;  // eigval, snapshots, top states
     const size_t ce = f64 ? 16 : 8;  // complex element size
     const size_t ns = (size_t)g.nsolved;
     size_t o = 0;
@@ -248,14 +257,16 @@ Layout layout_for(const SolveGeom &g)
     o = al(o + (size_t)std::max(g.nz - 1, 1) * BLDFM_LV32 * 4);
     L.slot = o;
     o = al(o + (size_t)g.nz * 4);
+    L.dc = o;  // k = 0 values (p, q) per output level
+    o = al(o + (size_t)g.nlvls * 32);
     L.eig = o;
-    o = al(o + (f64 ? ns * 16 : 0));
+    o = al(o + ((shoot || g.analytic) ? ns * 16 : 0));
     L.snap = o;
-    o = al(o + ((f64 && !g.analytic) ? (size_t)g.nsnap * 4 * ns * 16 : 0));
+    o = al(o + (shoot ? (size_t)g.nsnap * 4 * ns * 16 : 0));
     L.top = o;
-    o = al(o + ((f64 && !g.analytic) ? 4 * ns * 16 : 0));
-    L.scratch = o;
-    o = al(o + ((!f64 && g.nsnap > 1) ? (size_t)g.nsnap * 5 * ns * 4 : 0));
+    o = al(o + (shoot ? 4 * ns * 16 : 0));
+    L.scratch = o;  // multi-level Riccati snapshots (5 reals per mode and level)
+    o = al(o + ((!shoot && !g.analytic && g.nsnap > 1) ? (size_t)g.nsnap * 5 * ns * (f64 ? 8 : 4) : 0));
     L.q0 = o;
     o = al(o + (g.footprint ? 0 : (size_t)g.nlx * g.nly * ce));
     L.A = o;
@@ -310,6 +321,15 @@ struct DeviceCache {
     StageSlot stage[NSTAGE];  // ring of pinned staging buffers
     int stage_next = 0;
     HostBuffers hb;
+    // CUDA graphs of batches, keyed by the launch topology; each instance owns
+    // the pinned buffer its upload node reads
+    struct GraphInst {
+        cudaGraphExec_t exec = nullptr;
+        void *pinned = nullptr;
+        size_t bytes = 0;
+        cudaEvent_t done = nullptr;
+    };
+    std::map<std::vector<int64_t>, std::vector<GraphInst>> graphs;
     bool timing = false;       // per-stage CUDA-event timers
     std::vector<TimerSet> tsets;
     TimerSet *cur = nullptr;   // timers of the solve being enqueued
@@ -329,6 +349,8 @@ DeviceCache &cache_for_current(int *status)
         for (int i = 0; i < NSTAGE; ++i)
             if (cudaEventCreateWithFlags(&dc.stage[i].ev, cudaEventDisableTiming) != cudaSuccess)
                 *status = BLDFM_ERR_CUDA;
+        prepare_kernel_attributes();
+        prepare_batch_attributes();
     }
     return dc;
 }
@@ -484,7 +506,8 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
     int status = BLDFM_OK;
     DeviceCache &dc = cache_for_current(&status);
     if (status != BLDFM_OK) return status;
-    const bool f64 = g.mode == BLDFM_MODE_FP64 || g.analytic;
+    const bool f64 = g.mode != BLDFM_MODE_FP32 || g.analytic;
+    const bool shoot = g.mode == BLDFM_MODE_FP64 && !g.analytic;
     ModeList *ml = nullptr;
     TwTable *twxo = nullptr, *twyo = nullptr, *twxf = nullptr, *twyf = nullptr;
     int4 *xband = nullptr;
@@ -508,20 +531,54 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
     const size_t lv64b = (size_t)std::max(nz - 1, 0) * BLDFM_LV64 * 8;
     const size_t lv32b = (size_t)std::max(nz - 1, 0) * BLDFM_LV32 * 4;
     const size_t slotb = (size_t)nz * 4;
-    const size_t eigb = f64 ? (size_t)g.nsolved * 16 : 0;
-    const size_t off_lv32 = al(lv64b), off_slot = off_lv32 + al(lv32b), off_eig = off_slot + al(slotb);
+    const size_t eigb = (shoot || g.analytic) ? (size_t)g.nsolved * 16 : 0;
+    const size_t dcb = (size_t)g.nlvls * 32;
+    const size_t off_lv32 = al(lv64b), off_slot = off_lv32 + al(lv32b), off_dc = off_slot + al(slotb),
+                 off_eig = off_dc + al(dcb);
     StageSlot *slt = nullptr;
     if ((rc = acquire_stage(dc, off_eig + al(eigb) + 256, &slt)) != BLDFM_OK) return rc;
     char *sg = (char *)slt->buf;
     timers_begin(dc);
     hx_level_table(nz, z, prof, (double *)sg);
-    if (!f64) hx_level_table32(nz, z, prof, (float *)(sg + off_lv32));
+    if (!f64) {
+        if (g.iso)
+            hx_level_table32_iso(nz, z, prof, g.ex, g.ey, (float *)(sg + off_lv32));
+        else
+            hx_level_table32(nz, z, prof, (float *)(sg + off_lv32));
+    }
     memcpy(sg + off_slot, hp.slot.data(), slotb);
+    double2 *dcv = (double2 *)(w + L.dc);
+    if (g.footprint) {
+        // the k = 0 values need only host data in footprint mode
+        double *hdc = (double *)(sg + off_dc);
+        const double q0r = g.q0dc_fp;
+        if (g.analytic) {
+            const int64_t lev = levels[0] < 0 ? levels[0] + nz : levels[0];
+            const double hlev = z[lev] - z[0];
+            const double kzinv = 1.0 / prof[4 * nz + nz - 1];
+            double pr = d->srf_bg_conc - (q0r * kzinv) * hlev;
+            double pi = 0.0 - (0.0 * kzinv) * hlev;
+            double qr = q0r, qi = 0.0;
+            if (g.precision == BLDFM_PREC_SINGLE) {
+                pr = (double)(float)pr;
+                pi = (double)(float)pi;
+                qr = (double)(float)qr;
+            }
+            hdc[0] = pr;
+            hdc[1] = pi;
+            hdc[2] = qr;
+            hdc[3] = qi;
+        } else {
+            hx_dc_values(nz, (const double *)sg, hp.slot.data(), q0r, 0.0, d->srf_bg_conc,
+                         g.precision == BLDFM_PREC_SINGLE, g.nlvls, 0, hdc);
+        }
+    }
 
     CK(cudaMemsetAsync(err, 0, 64, st));
     if (lv64b) CK(cudaMemcpyAsync(lv64, sg, lv64b, cudaMemcpyHostToDevice, st));
     if (!f64 && lv32b) CK(cudaMemcpyAsync(lv32, sg + off_lv32, lv32b, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(slot, sg + off_slot, slotb, cudaMemcpyHostToDevice, st));
+    if (g.footprint) CK(cudaMemcpyAsync(dcv, sg + off_dc, dcb, cudaMemcpyHostToDevice, st));
     // every spectrum entry is written unless some output slot stays empty
     // (duplicate levels) or the analytic branch runs
     const size_t specb = (size_t)g.nlvls * g.nlx * g.nly * (f64 ? 16 : 8);
@@ -546,7 +603,13 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
             const int64_t lev = levels[0] < 0 ? levels[0] + nz : levels[0];
             const double hlev = z[lev] - z[0];
             const double kzinv = 1.0 / prof[4 * nz + nz - 1];
-            CK(launch_analytic64(g, ml->dev, eig, q0, p000, kzinv, hlev, Xp, Xq, st));
+            CK(launch_analytic64(g, ml->dev, eig, q0, p000, kzinv, hlev, Xp, Xq, dcv, st));
+        } else if (!shoot) {
+            // accurate FP64 mode: invariant imbedding, no libm values needed
+            CK(cudaEventRecord(slt->ev, st));
+            CK(launch_riccati64(g, lv64, slot, ml->dev, q0, (double *)(w + L.scratch), Xp, Xq, err, dc.nsm, st));
+            tmark(dc, st);  // 2: after the sweep
+            if (!g.footprint) CK(launch_trapezoid64(g, lv64, slot, q0, p000, dcv, st));
         } else {
             double2 *snap = (double2 *)(w + L.snap), *top = (double2 *)(w + L.top);
             if (g.nsolved > 0) CK(launch_sweep64(g, lv64, slot, ml->dev, q0, snap, top, err, dc.nsm, st));
@@ -556,10 +619,10 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
             if (eigb) CK(cudaMemcpyAsync(eig, sg + off_eig, eigb, cudaMemcpyHostToDevice, st));
             CK(cudaEventRecord(slt->ev, st));
             CK(launch_combine64(g, ml->dev, eig, snap, top, Xp, Xq, st));
-            CK(launch_trapezoid64(g, lv64, slot, q0, p000, Xp, Xq, st));
+            if (!g.footprint) CK(launch_trapezoid64(g, lv64, slot, q0, p000, dcv, st));
         }
         tmark(dc, st);  // 3: before the output transform
-        CK(launch_output_fft<double>(g, hp.plx_out, hp.ply_out, twxo->d64, twyo->d64, xband, Xp, Xq,
+        CK(launch_output_fft<double>(g, hp.plx_out, hp.ply_out, twxo->d64, twyo->d64, xband, Xp, Xq, dcv,
                                      (double2 *)(w + L.Cb), conc, flx, st));
     } else {
         float2 *q0 = g.footprint ? nullptr : (float2 *)(w + L.q0);
@@ -574,14 +637,308 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
             CK(launch_riccati32(g, lv32, slot, ml->dev, q0, (float *)(w + L.scratch), Xp, Xq, ax, ay, err, dc.nsm,
                                 256, st));
         tmark(dc, st);  // 2: after the sweep
-        CK(launch_trapezoid32(g, lv64, slot, q0, p000, Xp, Xq, st));
+        if (!g.footprint) CK(launch_trapezoid32(g, lv64, slot, q0, p000, dcv, st));
         tmark(dc, st);  // 3: before the output transform
-        CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq,
+        CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
                                     (float2 *)(w + L.Cb), conc, flx, st));
     }
     tmark(dc, st);  // 4: end
     if (f64 && g.analytic) CK(cudaEventRecord(slt->ev, st));
     return BLDFM_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// batches (bldfm_solve_batch)
+// ---------------------------------------------------------------------------
+enum { BATCH_MAX_CTAS = 16384 };
+
+struct BatchBuild {
+    std::vector<HostPlan> hp;
+    std::vector<ModeList *> ml;
+    std::vector<TwTable *> twxo, twyo, twxf, twyf;
+    std::vector<int4 *> xb;
+    size_t off_cases = 0, off_tile_case = 0, off_cta_tiles = 0, off_col_case = 0, off_row_case = 0;
+    std::vector<size_t> off_lv32, off_lv64, off_slot, off_dc;
+    size_t blob_bytes = 0, blob_at = 0;
+    std::vector<size_t> d_q0, d_A, d_scratch, d_Xp, d_Xq, d_Cb;
+    size_t total = 0;
+    int64_t ntiles = 0;
+    int G = 0, threads = 256, ncol = 0, nrow = 0, rpc = 2;
+    size_t sweep_smem = 0, col_smem = 0, row_smem = 0;
+    std::vector<int64_t> tile0, col0, row0;
+};
+
+int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, DeviceCache *dc, BatchBuild &B)
+{
+    if (!cs || n < 1) return BLDFM_ERR_ARG;
+    B.threads = (opts && opts->threads > 0) ? opts->threads : 256;
+    if (B.threads != 128 && B.threads != 256) return BLDFM_ERR_ARG;
+    B.hp.resize(n);
+    size_t o = 0;
+    B.off_cases = o;
+    o = al(o + sizeof(BatchCase) * n);
+    B.tile0.resize(n);
+    B.col0.resize(n);
+    B.row0.resize(n);
+    int maxL = 0, maxnz = 0, maxnfy = 0, maxnfx = 0;
+    for (int k = 0; k < n; ++k) {
+        const bldfm_case &c = cs[k];
+        if (c.desc.mode != BLDFM_MODE_FP32 || c.desc.analytic) return BLDFM_ERR_UNSUPPORTED;
+        if (!c.z_host || !c.prof_host || !c.levels_host || !c.conc_dev || !c.flx_dev) return BLDFM_ERR_ARG;
+        if (!c.desc.footprint && !c.srf_flx_dev) return BLDFM_ERR_ARG;
+        int rc = make_plan(&c.desc, c.z_host, c.prof_host, c.levels_host, c.nlvls, B.hp[k]);
+        if (rc != BLDFM_OK) return rc;
+        const SolveGeom &g = B.hp[k].g;
+        B.tile0[k] = B.ntiles;
+        B.ntiles += (g.nsolved + B.threads - 1) / B.threads;
+        B.col0[k] = B.ncol;
+        B.ncol += g.nlvls * g.nbx;
+        maxL = std::max(maxL, g.nz - 1);
+        maxnz = std::max(maxnz, g.nz);
+        maxnfy = std::max(maxnfy, g.nfy);
+        maxnfx = std::max(maxnfx, g.nfx);
+    }
+    B.rpc = 2;
+    while (B.rpc > 1 && (2 * (size_t)B.rpc + 1) * maxnfx * 8 > 190 * 1024) --B.rpc;
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        B.row0[k] = B.nrow;
+        B.nrow += g.nlvls * ((g.out_ny + B.rpc - 1) / B.rpc);
+    }
+    B.off_tile_case = o;
+    o = al(o + 4 * (size_t)std::max<int64_t>(B.ntiles, 1));
+    B.off_cta_tiles = o;
+    o = al(o + 8 * (size_t)(BATCH_MAX_CTAS + 1));
+    B.off_col_case = o;
+    o = al(o + 4 * (size_t)std::max(B.ncol, 1));
+    B.off_row_case = o;
+    o = al(o + 4 * (size_t)std::max(B.nrow, 1));
+    B.off_lv32.resize(n);
+    B.off_lv64.resize(n);
+    B.off_slot.resize(n);
+    B.off_dc.resize(n);
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        B.off_lv32[k] = o;
+        o = al(o + (size_t)std::max(g.nz - 1, 1) * BLDFM_LV32 * 4);
+        B.off_lv64[k] = o;
+        o = al(o + (size_t)std::max(g.nz - 1, 1) * BLDFM_LV64 * 8);
+        B.off_slot[k] = o;
+        o = al(o + (size_t)g.nz * 4);
+        B.off_dc[k] = o;
+        o = al(o + (size_t)g.nlvls * 32);
+    }
+    B.blob_bytes = o;
+    // workspace: status word, blob, per-case device regions
+    size_t w = 0;
+    w = al(w + 64);
+    B.blob_at = w;
+    w = al(w + B.blob_bytes);
+    B.d_q0.resize(n);
+    B.d_A.resize(n);
+    B.d_scratch.resize(n);
+    B.d_Xp.resize(n);
+    B.d_Xq.resize(n);
+    B.d_Cb.resize(n);
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        const size_t specb = (size_t)g.nlvls * g.nlx * g.nly * 8;
+        B.d_q0[k] = w;
+        w = al(w + (g.footprint ? 0 : (size_t)g.nlx * g.nly * 8));
+        B.d_A[k] = w;
+        w = al(w + (g.footprint ? 0 : (size_t)g.nlx * g.ny * 8));
+        B.d_scratch[k] = w;
+        w = al(w + (g.nsnap > 1 ? (size_t)g.nsnap * 5 * g.nsolved * 4 : 0));
+        B.d_Xp[k] = w;
+        w = al(w + specb);
+        B.d_Xq[k] = w;
+        w = al(w + specb);
+        B.d_Cb[k] = w;
+        w = al(w + (size_t)g.nlvls * g.nbx * std::max(g.out_ny, 1) * 8);
+    }
+    B.total = w;
+    B.sweep_smem = (size_t)maxL * BLDFM_LV32 * 4 + (size_t)maxnz * 4 + 16;
+    B.col_smem = 3 * (size_t)maxnfy * 8;
+    B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
+    if (B.sweep_smem > 200 * 1024) return BLDFM_ERR_UNSUPPORTED;
+    if (!dc) return BLDFM_OK;
+    // persistent sweep grid
+    int per_sm = (opts && opts->ctas_per_sm > 0) ? opts->ctas_per_sm : batch_sweep_occupancy(B.threads, B.sweep_smem);
+    B.G = (int)std::min<int64_t>(std::min<int64_t>((int64_t)dc->nsm * per_sm, BATCH_MAX_CTAS), std::max<int64_t>(B.ntiles, 1));
+    B.ml.resize(n);
+    B.twxo.resize(n);
+    B.twyo.resize(n);
+    B.twxf.assign(n, nullptr);
+    B.twyf.assign(n, nullptr);
+    B.xb.resize(n);
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        int rc;
+        if ((rc = get_modes(*dc, g.nlx, g.nly, &B.ml[k])) != BLDFM_OK) return rc;
+        if ((rc = get_tw(*dc, g.nfx, &B.twxo[k])) != BLDFM_OK) return rc;
+        if ((rc = get_tw(*dc, g.nfy, &B.twyo[k])) != BLDFM_OK) return rc;
+        if (!g.footprint) {
+            if ((rc = get_tw(*dc, g.nxe, &B.twxf[k])) != BLDFM_OK) return rc;
+            if ((rc = get_tw(*dc, g.nye, &B.twyf[k])) != BLDFM_OK) return rc;
+        }
+        if ((rc = get_xband(*dc, B.hp[k], &B.xb[k])) != BLDFM_OK) return rc;
+    }
+    return BLDFM_OK;
+}
+
+// Fill the upload blob: case descriptors with device pointers into ws, the
+// tile / CTA maps, and every case's level tables, slot map and k = 0 values.
+void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char *blob)
+{
+    BatchCase *bc = (BatchCase *)(blob + B.off_cases);
+    int *tile_case = (int *)(blob + B.off_tile_case);
+    int64_t *cta_tiles = (int64_t *)(blob + B.off_cta_tiles);
+    int *col_case = (int *)(blob + B.off_col_case);
+    int *row_case = (int *)(blob + B.off_row_case);
+    char *wb = ws + B.blob_at;  // device address of the blob
+    std::vector<double> tile_cost;
+    tile_cost.reserve((size_t)B.ntiles);
+    for (int k = 0; k < n; ++k) {
+        const HostPlan &hp = B.hp[k];
+        const SolveGeom &g = hp.g;
+        const bldfm_case &c = cs[k];
+        const int nz = g.nz;
+        BatchCase &x = bc[k];
+        memset(&x, 0, sizeof(x));
+        x.g = g;
+        x.plx = hp.plx_out;
+        x.ply = hp.ply_out;
+        x.lv32 = (const float *)(wb + B.off_lv32[k]);
+        x.slot = (const int *)(wb + B.off_slot[k]);
+        x.modes = B.ml[k]->dev;
+        x.q0 = g.footprint ? nullptr : (const float2 *)(ws + B.d_q0[k]);
+        x.scratch = (float *)(ws + B.d_scratch[k]);
+        x.Xp = (float2 *)(ws + B.d_Xp[k]);
+        x.Xq = (float2 *)(ws + B.d_Xq[k]);
+        x.dc = (const double2 *)(wb + B.off_dc[k]);
+        x.Cb = (float2 *)(ws + B.d_Cb[k]);
+        x.twx = B.twxo[k]->d32;
+        x.twy = B.twyo[k]->d32;
+        x.xband = B.xb[k];
+        x.conc = c.conc_dev;
+        x.flx = c.flx_dev;
+        x.ax = (float)(g.lx_scale * g.valx);
+        x.ay = (float)(g.ly_scale * g.valy);
+        x.tile0 = B.tile0[k];
+        x.col0 = B.col0[k];
+        x.row0 = B.row0[k];
+        x.rpc = B.rpc;
+        double *lv64 = (double *)(blob + B.off_lv64[k]);
+        hx_level_table(nz, c.z_host, c.prof_host, lv64);
+        if (g.iso)
+            hx_level_table32_iso(nz, c.z_host, c.prof_host, g.ex, g.ey, (float *)(blob + B.off_lv32[k]));
+        else
+            hx_level_table32(nz, c.z_host, c.prof_host, (float *)(blob + B.off_lv32[k]));
+        memcpy(blob + B.off_slot[k], hp.slot.data(), (size_t)nz * 4);
+        if (g.footprint)
+            hx_dc_values(nz, lv64, hp.slot.data(), g.q0dc_fp, 0.0, c.desc.srf_bg_conc,
+                         g.precision == BLDFM_PREC_SINGLE, g.nlvls, 0, (double *)(blob + B.off_dc[k]));
+        const int64_t nt = (g.nsolved + B.threads - 1) / B.threads;
+        for (int64_t t = 0; t < nt; ++t) {
+            tile_case[B.tile0[k] + t] = k;
+            tile_cost.push_back((double)std::max(nz - 1, 1));
+        }
+        for (int64_t i = 0; i < (int64_t)g.nlvls * g.nbx; ++i) col_case[B.col0[k] + i] = k;
+        const int nblk = (g.out_ny + B.rpc - 1) / B.rpc;
+        for (int64_t i = 0; i < (int64_t)g.nlvls * nblk; ++i) row_case[B.row0[k] + i] = k;
+    }
+    // cost-weighted contiguous partition of the tiles over G persistent CTAs
+    double total = 0;
+    for (double c : tile_cost) total += c;
+    int64_t t = 0;
+    double acc = 0;
+    cta_tiles[0] = 0;
+    for (int b = 0; b < B.G; ++b) {
+        const double target = total * (b + 1) / B.G;
+        while (t < B.ntiles && acc + 0.5 * tile_cost[(size_t)t] <= target) acc += tile_cost[(size_t)t++];
+        if (b == B.G - 1) t = B.ntiles;
+        cta_tiles[b + 1] = t;
+    }
+}
+
+int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const void *blob_host, cudaStream_t st,
+                  DeviceCache *tdc)
+{
+    if (tdc) tmark(*tdc, st);  // 0: upload and per-case forward transforms
+    CK(cudaMemcpyAsync(ws + B.blob_at, blob_host, B.blob_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(ws, 0, 64, st));
+    char *wb = ws + B.blob_at;
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        if (g.nsnap < g.nlvls) {
+            const size_t specb = (size_t)g.nlvls * g.nlx * g.nly * 8;
+            CK(cudaMemsetAsync(ws + B.d_Xp[k], 0, specb, st));
+            CK(cudaMemsetAsync(ws + B.d_Xq[k], 0, specb, st));
+        }
+        if (!g.footprint) {
+            float2 *q0 = (float2 *)(ws + B.d_q0[k]);
+            CK(launch_forward_fft<float>(g, B.hp[k].plx_fwd, B.hp[k].ply_fwd, B.twxf[k]->d32, B.twyf[k]->d32,
+                                         cs[k].srf_flx_dev, (float2 *)(ws + B.d_A[k]), q0, st));
+            CK(launch_trapezoid32(g, (const double *)(wb + B.off_lv64[k]), (const int *)(wb + B.off_slot[k]), q0,
+                                  cs[k].desc.srf_bg_conc, (double2 *)(wb + B.off_dc[k]), st));
+        }
+    }
+    BatchLaunch bl;
+    bl.cases = (const BatchCase *)(wb + B.off_cases);
+    bl.tile_case = (const int *)(wb + B.off_tile_case);
+    bl.cta_tiles = (const int64_t *)(wb + B.off_cta_tiles);
+    bl.col_case = (const int *)(wb + B.off_col_case);
+    bl.row_case = (const int *)(wb + B.off_row_case);
+    bl.err = (int *)ws;
+    bl.sweep_ctas = B.ntiles > 0 ? B.G : 0;
+    bl.threads = B.threads;
+    bl.sweep_smem = B.sweep_smem;
+    bl.col_ctas = B.ncol;
+    bl.col_smem = B.col_smem;
+    bl.row_ctas = B.nrow;
+    bl.row_smem = B.row_smem;
+    if (tdc) tmark(*tdc, st);  // 1: the sweep
+    CK(launch_batch_kernels(bl, st, 0));
+    if (tdc) tmark(*tdc, st);  // 2: the output transform
+    CK(launch_batch_kernels(bl, st, 1));
+    if (tdc) tmark(*tdc, st);  // 3: end
+    return BLDFM_OK;
+}
+
+std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B, const void *ws)
+{
+    std::vector<int64_t> k;
+    k.push_back((int64_t)(uintptr_t)ws);
+    k.push_back(n);
+    k.push_back((int64_t)B.blob_bytes);
+    k.push_back(B.G);
+    k.push_back(B.threads);
+    k.push_back((int64_t)B.sweep_smem);
+    k.push_back(B.ncol);
+    k.push_back((int64_t)B.col_smem);
+    k.push_back(B.nrow);
+    k.push_back((int64_t)B.row_smem);
+    for (int i = 0; i < n; ++i) {
+        const SolveGeom &g = B.hp[i].g;
+        k.push_back(g.footprint);
+        k.push_back(g.nsnap < g.nlvls);
+        k.push_back(g.nlvls);
+        k.push_back(g.nlx);
+        k.push_back(g.nly);
+        k.push_back(g.nz);
+        if (!g.footprint) {
+            k.push_back(g.nx);
+            k.push_back(g.ny);
+            k.push_back(g.nxe);
+            k.push_back(g.nye);
+            k.push_back(g.px);
+            k.push_back(g.py);
+            k.push_back(g.precision);
+            k.push_back((int64_t)(uintptr_t)cs[i].srf_flx_dev);
+        }
+    }
+    return k;
 }
 
 }  // namespace
@@ -758,6 +1115,86 @@ int bldfm_solve_host(const bldfm_desc *d, const double *srf_flx_host, const doub
     CK(cudaMemcpyAsync(&err, hb.ws, sizeof(int), cudaMemcpyDeviceToHost, hb.stream));
     CK(cudaStreamSynchronize(hb.stream));
     if (err != 0) return BLDFM_ERR_TIMEOUT;
+    return BLDFM_OK;
+}
+
+int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases, const bldfm_batch_opts *opts, int64_t *workspace_bytes)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (!workspace_bytes) return BLDFM_ERR_ARG;
+    BatchBuild B;
+    int rc = batch_build(cases, ncases, opts, nullptr, B);
+    if (rc != BLDFM_OK) return rc;
+    *workspace_bytes = (int64_t)B.total;
+    return BLDFM_OK;
+}
+
+int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch_opts *opts, void *workspace,
+                      size_t workspace_bytes, void *stream)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (!workspace) return BLDFM_ERR_ARG;
+    if (((uintptr_t)workspace & 255) != 0) return BLDFM_ERR_ARG;
+    int status = BLDFM_OK;
+    DeviceCache &dc = cache_for_current(&status);
+    if (status != BLDFM_OK) return status;
+    BatchBuild B;
+    int rc = batch_build(cases, ncases, opts, &dc, B);
+    if (rc != BLDFM_OK) return rc;
+    if (workspace_bytes < B.total) return BLDFM_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    const bool graph = opts && opts->use_graph && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+    if (!graph) {
+        StageSlot *slt = nullptr;
+        if ((rc = acquire_stage(dc, B.blob_bytes + 256, &slt)) != BLDFM_OK) return rc;
+        batch_fill_blob(cases, ncases, B, ws, (char *)slt->buf);
+        timers_begin(dc);
+        if ((rc = batch_enqueue(cases, ncases, B, ws, slt->buf, st, dc.timing ? &dc : nullptr)) != BLDFM_OK)
+            return rc;
+        CK(cudaEventRecord(slt->ev, st));
+        return BLDFM_OK;
+    }
+    // graph path: an instance whose previous replay has finished, else a new
+    // capture (up to two instances per topology), else wait for the oldest
+    std::vector<int64_t> key = batch_key(cases, ncases, B, ws);
+    auto &insts = dc.graphs[key];
+    DeviceCache::GraphInst *gi = nullptr;
+    for (auto &x : insts)
+        if (cudaEventQuery(x.done) == cudaSuccess) {
+            gi = &x;
+            break;
+        }
+    if (!gi && insts.size() < 2) {
+        DeviceCache::GraphInst x;
+        if (cudaHostAlloc(&x.pinned, B.blob_bytes, cudaHostAllocDefault) != cudaSuccess) return BLDFM_ERR_CUDA;
+        x.bytes = B.blob_bytes;
+        CK(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+        batch_fill_blob(cases, ncases, B, ws, (char *)x.pinned);
+        // capture the whole batch once; a failure leaves the stream usable
+        cudaGraph_t graph_h = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rc = batch_enqueue(cases, ncases, B, ws, x.pinned, st, nullptr);
+        cudaError_t ce = cudaStreamEndCapture(st, &graph_h);
+        if (rc != BLDFM_OK || ce != cudaSuccess) {
+            if (graph_h) cudaGraphDestroy(graph_h);
+            return rc != BLDFM_OK ? rc : BLDFM_ERR_CUDA;
+        }
+        ce = cudaGraphInstantiate(&x.exec, graph_h, 0);
+        cudaGraphDestroy(graph_h);
+        if (ce != cudaSuccess) return BLDFM_ERR_CUDA;
+        CK(cudaGraphLaunch(x.exec, st));
+        CK(cudaEventRecord(x.done, st));
+        insts.push_back(x);
+        return BLDFM_OK;
+    }
+    if (!gi) {
+        gi = &insts[0];
+        CK(cudaEventSynchronize(gi->done));
+    }
+    batch_fill_blob(cases, ncases, B, ws, (char *)gi->pinned);
+    CK(cudaGraphLaunch(gi->exec, st));
+    CK(cudaEventRecord(gi->done, st));
     return BLDFM_OK;
 }
 

@@ -1,0 +1,49 @@
+// Batched FP32 solve: device descriptors and launch parameters.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.h"
+
+// One case of a batch as the device kernels see it.
+struct __align__(16) BatchCase {
+    SolveGeom g;
+    FftPlan plx, ply;  // output transform plans
+    const float *lv32;
+    const int *slot;
+    const uint32_t *modes;
+    const float2 *q0;
+    float *scratch;
+    float2 *Xp, *Xq;
+    const double2 *dc;
+    float2 *Cb;
+    const float2 *twx, *twy;
+    const int4 *xband;
+    double *conc, *flx;
+    float ax, ay;
+    int64_t tile0;  // first sweep tile of this case
+    int64_t col0;   // first column-transform CTA
+    int64_t row0;   // first row-transform CTA
+    int32_t rpc;    // rows per row-transform CTA
+    int32_t pad;
+};
+
+struct BatchLaunch {
+    const BatchCase *cases;
+    const int *tile_case;
+    const int64_t *cta_tiles;
+    const int *col_case;
+    const int *row_case;
+    int *err;
+    int sweep_ctas, threads;
+    size_t sweep_smem;
+    int col_ctas;
+    size_t col_smem;
+    int row_ctas;
+    size_t row_smem;
+};
+
+cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);
+int batch_sweep_occupancy(int threads, size_t smem);
+void prepare_batch_attributes();

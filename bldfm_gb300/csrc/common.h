@@ -20,7 +20,8 @@ enum {
     LV_KX = 0, LV_KY, LV_U, LV_V, LV_S1, LV_H2, LV_S2, LV_H3, LV_S3, LV_S4, LV_H, LV_PAD
 };
 
-// Columns of the FP32 level table (Riccati sweep).
+// Columns of the FP32 level table (Riccati sweep), generic profiles.  Isotropic
+// profiles with a fixed wind direction use the compact row of StepCoef<true>.
 enum {
     L32_NKX = 0,  // -Kx
     L32_NKY,      // -Ky
@@ -65,6 +66,9 @@ struct SolveGeom {
     // top-level coefficients for the FP32 eigenvalue
     double kxk_top, kyk_top, uk_top, vk_top;
     uint32_t turn_x, turn_y;    // phase shift as 32-bit fixed-point turns per unit k
+    int32_t iso;                // Kx == Ky and (u, v) along one direction at every level
+    int32_t jmax;               // highest output level (slot level), -1 if none
+    float ex, ey;               // wind direction unit vector (iso tables)
 };
 
 // fftfreq ordering helpers: index <-> signed frequency.

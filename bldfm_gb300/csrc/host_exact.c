@@ -94,3 +94,101 @@ void hx_eigval(int64_t m0, int64_t m1, const uint32_t *modes, int nlx, int nly, 
         eig[2 * m + 1] = cimag(s);
     }
 }
+
+/* 1 when Kx == Ky at every level and (u, v) keeps one direction (ex, ey):
+ * then T = -K k^2 - i U (ex kx + ey ky) with U = u ex + v ey (all four
+ * closures of vertical_profiles have this form). */
+int hx_profiles_iso(int nz, const double *prof, double *ex, double *ey)
+{
+    const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Ky = prof + 3 * nz;
+    int imax = 0;
+    double best = -1.0;
+    for (int i = 0; i < nz; ++i) {
+        if (Kx[i] != Ky[i]) return 0;
+        double m = u[i] * u[i] + v[i] * v[i];
+        if (m > best) {
+            best = m;
+            imax = i;
+        }
+    }
+    double n = sqrt(best);
+    if (!(n > 0)) {
+        *ex = 1.0;
+        *ey = 0.0;
+        return 1;
+    }
+    double dx = u[imax] / n, dy = v[imax] / n;
+    for (int i = 0; i < nz; ++i) {
+        double cross = u[i] * dy - v[i] * dx;
+        double mag = sqrt(u[i] * u[i] + v[i] * v[i]);
+        if (fabs(cross) > 1e-12 * mag + 1e-300) return 0;
+    }
+    *ex = dx;
+    *ey = dy;
+    return 1;
+}
+
+/* Compact FP32 level table for isotropic profiles with a fixed wind
+ * direction (row layout of StepCoef<true> in kernels.cu). */
+void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex, double ey, float *lv)
+{
+    const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Kz = prof + 4 * nz;
+    for (int i = 0; i < nz - 1; ++i) {
+        double k = 1.0 / Kz[i];
+        double h = z[i + 1] - z[i];
+        double K = Kx[i];
+        double U = u[i] * ex + v[i] * ey;
+        double A = 0.5 * k * h * h, B0 = -k * h, B1 = k * k * h * h * h / 6.0, C1 = k * h * h * h / 6.0;
+        float *row = lv + (size_t)i * 12;
+        row[0] = (float)(A * K);
+        row[1] = (float)(A * U);
+        row[2] = (float)B0;
+        row[3] = (float)(B1 * K);
+        row[4] = (float)(B1 * U);
+        row[5] = (float)(-h * K);
+        row[6] = (float)(-C1 * K * K);
+        row[7] = (float)(C1 * U * U);
+        row[8] = (float)(-h * U);
+        row[9] = (float)(-2.0 * C1 * K * U);
+        row[10] = 0.f;
+        row[11] = 0.f;
+    }
+}
+
+/* k = 0 mode of every output slot when the source spectrum's k = 0 value q0
+ * is known on the host (footprint mode), exactly as solver.py:186-191 and
+ * 237-251 evaluate it: p00 starts at p000 and loses (q0 dz_i) w_i per step,
+ * w_i = 0.5/Kz[i] + 0.5/Kz[i+1] (level-table column 11).  dc receives
+ * (p_s, q_s) as 4 doubles per slot s < nlvls; complex64 rounding when
+ * single != 0.  Slots without a level keep p = 0 (slot 0: p000), q = q0. */
+void hx_dc_values(int nz, const double *lv, const int *slot, double q0r, double q0i, double p000, int single,
+                  int nlvls, int analytic, double *dc)
+{
+    double qr = q0r, qi = q0i;
+    if (single) {
+        qr = (double)(float)qr;
+        qi = (double)(float)qi;
+    }
+    for (int s = 0; s < nlvls; ++s) {
+        dc[4 * s + 0] = 0.0;
+        dc[4 * s + 1] = 0.0;
+        dc[4 * s + 2] = qr;
+        dc[4 * s + 3] = qi;
+    }
+    dc[0] = single ? (double)(float)p000 : p000;
+    if (analytic) return;
+    double pr = p000, pi = 0.0;
+    for (int i = 0; i < nz - 1; ++i) {
+        if (slot[i] >= 0) {
+            dc[4 * slot[i] + 0] = single ? (double)(float)pr : pr;
+            dc[4 * slot[i] + 1] = single ? (double)(float)pi : pi;
+        }
+        const double dz = lv[(size_t)i * 12 + 10], w = lv[(size_t)i * 12 + 11];
+        pr = pr - (q0r * dz) * w;
+        pi = pi - (q0i * dz) * w;
+    }
+    if (slot[nz - 1] >= 0) {
+        dc[4 * slot[nz - 1] + 0] = single ? (double)(float)pr : pr;
+        dc[4 * slot[nz - 1] + 1] = single ? (double)(float)pi : pi;
+    }
+}

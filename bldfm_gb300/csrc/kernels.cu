@@ -15,108 +15,13 @@
 #include <stdint.h>
 
 #include "common.h"
+#include "devmath.cuh"
 #include "fft_core.cuh"
 #include "kernels.h"
+#include "sweep32.cuh"
+#include "fft_passes.cuh"
 
-// ---------------------------------------------------------------------------
-// numpy-exact complex128 arithmetic
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double2 np_cmul(double2 a, double2 b)
-{
-    return make_double2(__fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y)), __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x)));
-}
-__device__ __forceinline__ double2 np_cadd(double2 a, double2 b)
-{
-    return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y));
-}
-__device__ __forceinline__ double2 np_csub(double2 a, double2 b)
-{
-    return make_double2(__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y));
-}
-// Smith's method, reciprocal-scale form (numpy complex128 divide).
-__device__ __forceinline__ double2 np_cdiv(double2 a, double2 b)
-{
-    double2 o;
-    if (fabs(b.x) >= fabs(b.y)) {
-        double rat = __ddiv_rn(b.y, b.x);
-        double scl = __ddiv_rn(1.0, __dadd_rn(b.x, __dmul_rn(b.y, rat)));
-        o.x = __dmul_rn(__dadd_rn(a.x, __dmul_rn(a.y, rat)), scl);
-        o.y = __dmul_rn(__dsub_rn(a.y, __dmul_rn(a.x, rat)), scl);
-    } else {
-        double rat = __ddiv_rn(b.x, b.y);
-        double scl = __ddiv_rn(1.0, __dadd_rn(b.y, __dmul_rn(b.x, rat)));
-        o.x = __dmul_rn(__dadd_rn(__dmul_rn(a.x, rat), a.y), scl);
-        o.y = __dmul_rn(__dsub_rn(__dmul_rn(a.y, rat), a.x), scl);
-    }
-    return o;
-}
-__device__ __forceinline__ double2 round_c64(double2 a)
-{
-    return make_double2((double)__double2float_rn(a.x), (double)__double2float_rn(a.y));
-}
-
-// wavenumber of fftfreq index (solver.py:148-155): scale * (k * val)
-__device__ __forceinline__ double wavenumber(int k, double val, double scale)
-{
-    return __dmul_rn(scale, __dmul_rn((double)k, val));
-}
-
-__device__ __forceinline__ void unpack_mode(uint32_t e, int &r, int &c, bool &paired)
-{
-    c = (int)(e & 0x7fffu);
-    r = (int)((e >> 15) & 0x7fffu);
-    paired = (e >> 31) != 0;
-}
-
-// ---------------------------------------------------------------------------
-// bulk (TMA) copy of a table into shared memory with a bounded wait
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// Copies `bytes` (multiple of 16, both addresses 16-byte aligned) from global
-// to shared memory with cp.async.bulk, completing on an mbarrier.  Returns
-// false (and sets *err) if the wait runs out; never spins without a limit.
-__device__ bool bulk_load_to_smem(void *dst, const void *src, uint32_t bytes, uint64_t *bar, int *err)
-{
-    const uint32_t bar_a = smem_u32(bar);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar_a), "r"(1) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(bytes) : "memory");
-        const uint32_t chunk = 32768;
-        for (uint32_t off = 0; off < bytes; off += chunk) {
-            uint32_t n = bytes - off < chunk ? bytes - off : chunk;
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    smem_u32((char *)dst + off)),
-                "l"((const char *)src + off), "r"(n), "r"(bar_a)
-                : "memory");
-        }
-    }
-    uint32_t done = 0;
-    for (long it = 0; it < (1L << 24); ++it) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar_a), "r"(0)
-            : "memory");
-        if (done) break;
-    }
-    if (!done) {
-        atomicExch(err, BLDFM_ERR_TIMEOUT_DEV);
-        return false;
-    }
-    return true;
-}
+#define LAUNCH_CHECK() (cudaGetLastError())
 
 // ---------------------------------------------------------------------------
 // FP64 shooting sweep
@@ -207,12 +112,6 @@ __global__ void __launch_bounds__(128) sweep64_kernel(SolveGeom g, const double 
     }
 }
 
-// Spectrum layout shared by all writers: [lvl][col c][row r], complex.
-__device__ __forceinline__ size_t spec_idx(const SolveGeom &g, int lvl, int r, int c)
-{
-    return ((size_t)lvl * g.nlx + c) * g.nly + r;
-}
-
 // ---------------------------------------------------------------------------
 // FP64 combination: alpha, levels, complex64 rounding, phase shift, mirror
 // ---------------------------------------------------------------------------
@@ -274,43 +173,45 @@ __global__ void __launch_bounds__(256) combine64_kernel(SolveGeom g, const uint3
 // k = 0 mode: trapezoid rule, one thread.  lvtab column LV_PAD holds
 // w_i = 0.5/Kz[i] + 0.5/Kz[i+1], column LV_H holds dz[i].
 // ---------------------------------------------------------------------------
+// k = 0 mode when q0 lives on the device (dispersion mode): writes the
+// reference's trapezoid values (solver.py:237-251) into dc[2 s] (p), dc[2 s + 1]
+// (q).  The terms (q0 dz_i) w_i are independent and computed in parallel; the
+// running difference keeps the reference's order on one thread.
 template <typename C>
-__global__ void trapezoid_kernel(SolveGeom g, const double *__restrict__ lvtab, const int *__restrict__ slot_of_step,
-                                 const C *__restrict__ q0spec, double p000, C *__restrict__ Xp, C *__restrict__ Xq)
+__global__ void __launch_bounds__(256) trapezoid_kernel(SolveGeom g, const double *__restrict__ lvtab,
+                                                        const int *__restrict__ slot_of_step,
+                                                        const C *__restrict__ q0spec, double p000,
+                                                        double2 *__restrict__ dc)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double2 q0;
-    if (q0spec) {
-        q0 = make_double2((double)q0spec[0].x, (double)q0spec[0].y);
-    } else {
-        q0 = make_double2(g.q0dc_fp, 0.0);
-    }
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2 *term = (double2 *)smem_raw;
+    int *sl = (int *)(term + (g.nz > 1 ? g.nz - 1 : 1));
+    const double2 q0 = make_double2((double)q0spec[0].x, (double)q0spec[0].y);
     const bool single = g.precision == 0;
-    double2 qs = single ? round_c64(q0) : q0;
-    for (int s = 0; s < g.nlvls; ++s) {
-        Xq[spec_idx(g, s, 0, 0)] = cx_make<C>(qs.x, qs.y);
-        Xp[spec_idx(g, s, 0, 0)] = cx_make<C>(0.0, 0.0);
+    const double2 qs = single ? round_c64(q0) : q0;
+    for (int s = threadIdx.x; s < g.nlvls; s += blockDim.x) {
+        dc[2 * s + 1] = qs;
+        if (s > 0) dc[2 * s] = make_double2(0.0, 0.0);
     }
-    double2 p0 = make_double2(p000, 0.0);
-    Xp[spec_idx(g, 0, 0, 0)] = cx_make<C>(single ? (double)__double2float_rn(p000) : p000, 0.0);
-    if (g.analytic) return;
-    double2 p00 = p0;
-    for (int i = 0; i < g.nz - 1; ++i) {
-        const int s = slot_of_step[i];
-        if (s >= 0) {
-            double2 v = single ? round_c64(p00) : p00;
-            Xp[spec_idx(g, s, 0, 0)] = cx_make<C>(v.x, v.y);
-        }
+    for (int i = threadIdx.x; i < g.nz - 1; i += blockDim.x) {
         const double dz = lvtab[(size_t)i * BLDFM_LV64 + LV_H];
         const double w = lvtab[(size_t)i * BLDFM_LV64 + LV_PAD];
-        p00.x = __dsub_rn(p00.x, __dmul_rn(__dmul_rn(q0.x, dz), w));
-        p00.y = __dsub_rn(p00.y, __dmul_rn(__dmul_rn(q0.y, dz), w));
+        term[i] = make_double2(__dmul_rn(__dmul_rn(q0.x, dz), w), __dmul_rn(__dmul_rn(q0.y, dz), w));
     }
-    const int s = slot_of_step[g.nz - 1];
-    if (s >= 0) {
-        double2 v = single ? round_c64(p00) : p00;
-        Xp[spec_idx(g, s, 0, 0)] = cx_make<C>(v.x, v.y);
+    for (int i = threadIdx.x; i < g.nz; i += blockDim.x) sl[i] = slot_of_step[i];
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    dc[0] = make_double2(single ? (double)__double2float_rn(p000) : p000, 0.0);
+    if (g.analytic) return;
+    double2 p00 = make_double2(p000, 0.0);
+    for (int i = 0; i < g.nz - 1; ++i) {
+        const int s = sl[i];
+        if (s >= 0) dc[2 * s] = single ? round_c64(p00) : p00;
+        p00.x = __dsub_rn(p00.x, term[i].x);
+        p00.y = __dsub_rn(p00.y, term[i].y);
     }
+    const int s = sl[g.nz - 1];
+    if (s >= 0) dc[2 * s] = single ? round_c64(p00) : p00;
 }
 
 // ---------------------------------------------------------------------------
@@ -360,12 +261,12 @@ __global__ void __launch_bounds__(256) analytic64_kernel(SolveGeom g, const uint
     }
 }
 
-// analytic k = 0: p = p000 - q0 * Kzinv * h, q = q0
+// analytic k = 0 (dispersion mode, q0 on the device): p = p000 - q0 Kzinv h, q = q0
 __global__ void analytic_dc_kernel(SolveGeom g, const double2 *__restrict__ q0spec, double p000, double kzinv,
-                                   double hlev, double2 *__restrict__ Xp, double2 *__restrict__ Xq)
+                                   double hlev, double2 *__restrict__ dc)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const double2 q0 = q0spec ? q0spec[0] : make_double2(g.q0dc_fp, 0.0);
+    const double2 q0 = q0spec[0];
     double2 p = make_double2(__dsub_rn(p000, __dmul_rn(__dmul_rn(q0.x, kzinv), hlev)),
                              __dsub_rn(0.0, __dmul_rn(__dmul_rn(q0.y, kzinv), hlev)));
     double2 q = q0;
@@ -373,37 +274,12 @@ __global__ void analytic_dc_kernel(SolveGeom g, const double2 *__restrict__ q0sp
         p = round_c64(p);
         q = round_c64(q);
     }
-    Xp[spec_idx(g, 0, 0, 0)] = p;
-    Xq[spec_idx(g, 0, 0, 0)] = q;
+    dc[0] = p;
+    dc[1] = q;
 }
 
-// ---------------------------------------------------------------------------
-// FP32 invariant-imbedding (Riccati) sweep
-// ---------------------------------------------------------------------------
-// Same discrete boundary-value problem as the shooting method: with
-// s_{i+1} = M_i s_i, M_i = [[a, b], [c, a]] and the radiation condition at the
-// top, the ratio R_i = p_i / q_i obeys R_i = (a R_{i+1} - b) / (a - c R_{i+1})
-// from R_L = 1 / (Kz_top * eig), and q_{i+1} = (c R_i + a) q_i.  The backward
-// recursion is contractive (it follows the decaying solution), so FP32 loses
-// nothing to the cancellation that forces FP64 in the forward shooting form.
-// The running product Q_i = prod_{k>=i} (c_k R_k + a_k) is kept as an FP32
-// mantissa with an integer power-of-two exponent, renormalised every 4 steps.
-__device__ __forceinline__ float2 csqrt_f(float2 w)
-{
-    // principal branch, Kahan's formulation
-    float x = w.x, y = w.y;
-    float t = sqrtf(0.5f * (fabsf(x) + hypotf(x, y)));
-    if (t == 0.f) return make_float2(0.f, 0.f);
-    if (x >= 0.f) return make_float2(t, y / (2.f * t));
-    return make_float2(fabsf(y) / (2.f * t), copysignf(t, y));
-}
-
-__device__ __forceinline__ float2 fc_mul(float2 a, float2 b)
-{
-    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-
-template <int SNAPREG>
+// One thread per solved mode, grid-stride.
+template <bool ISO, bool SINGLE>
 __global__ void __launch_bounds__(256) riccati32_kernel(SolveGeom g, const float *__restrict__ lv32,
                                                         const int *__restrict__ slot_of_step,
                                                         const uint32_t *__restrict__ modes,
@@ -421,131 +297,183 @@ __global__ void __launch_bounds__(256) riccati32_kernel(SolveGeom g, const float
     }
     for (int i = threadIdx.x; i < g.nz; i += blockDim.x) s_slot[i] = slot_of_step[i];
     __syncthreads();
+    const int64_t ns = g.nsolved;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += (int64_t)gridDim.x * blockDim.x)
+        ricc_mode<ISO, SINGLE>(g, s_lv, s_slot, modes, q0spec, scratch, Xp, Xq, ax, ay, m);
+}
 
+// ---------------------------------------------------------------------------
+// FP64 invariant-imbedding sweep (accurate mode)
+// ---------------------------------------------------------------------------
+// The FP32 kernel's recursion in FP64 with exact division: the solution of the
+// reference's discrete problem without the shooting method's cancellation.
+__device__ __forceinline__ double2 csqrt_d(double2 w)
+{
+    const double x = w.x, y = w.y;
+    const double t = sqrt(0.5 * (fabs(x) + hypot(x, y)));
+    if (t == 0.0) return make_double2(0.0, 0.0);
+    if (x >= 0.0) return make_double2(t, y / (2.0 * t));
+    return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
+}
+
+__device__ __forceinline__ double2 dc_mul(double2 a, double2 b)
+{
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+template <bool SINGLE>
+__global__ void __launch_bounds__(128) riccati64_kernel(SolveGeom g, const double *__restrict__ lvtab,
+                                                        const int *__restrict__ slot_of_step,
+                                                        const uint32_t *__restrict__ modes,
+                                                        const double2 *__restrict__ q0spec,
+                                                        double *__restrict__ scratch, double2 *__restrict__ Xp,
+                                                        double2 *__restrict__ Xq, int *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint64_t bar;
+    double *s_lv = (double *)smem_raw;
+    const int L = g.nz - 1;
+    int *s_slot = (int *)(s_lv + (size_t)L * BLDFM_LV64);
+    if (L > 0) {
+        if (!bulk_load_to_smem(s_lv, lvtab, (uint32_t)((size_t)L * BLDFM_LV64 * sizeof(double)), &bar, err))
+            return;
+    }
+    for (int i = threadIdx.x; i < g.nz; i += blockDim.x) s_slot[i] = slot_of_step[i];
+    __syncthreads();
+    const int jmax = g.jmax;
     const int64_t ns = g.nsolved;
     for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += (int64_t)gridDim.x * blockDim.x) {
         int r, c;
         bool paired;
         unpack_mode(modes[m], r, c, paired);
         const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
-        const float lx = ax * (float)kx, ly = ay * (float)ky;
-        const float lx2 = lx * lx, ly2 = ly * ly;
-        // top eigenvalue and radiation ratio R_L = 1 / (Kz_top eig)
-        const float2 w = make_float2(fmaf((float)g.kxk_top, lx2, (float)g.kyk_top * ly2),
-                                     fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
-        const float2 eg = csqrt_f(w);
-        const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
-        const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
-        float2 R = make_float2(ke.x * inv, -ke.y * inv);
-        float2 Q = make_float2(1.f, 0.f);
+        const double lx = wavenumber(kx, g.valx, g.lx_scale), ly = wavenumber(ky, g.valy, g.ly_scale);
+        const double lx2 = lx * lx, ly2 = ly * ly;
+        const double2 eg = csqrt_d(make_double2(fma(g.kxk_top, lx2, g.kyk_top * ly2), fma(g.uk_top, lx, g.vk_top * ly)));
+        const double2 ke = make_double2(g.kz_top * eg.x, g.kz_top * eg.y);
+        const double kn = 1.0 / fma(ke.x, ke.x, ke.y * ke.y);
+        double2 R = make_double2(ke.x * kn, -ke.y * kn);
+        double2 Q = make_double2(1.0, 0.0), Rj = R;
         int E = 0;
-        float2 sR[SNAPREG > 0 ? SNAPREG : 1], sQ[SNAPREG > 0 ? SNAPREG : 1];
-        int sE[SNAPREG > 0 ? SNAPREG : 1];
-        auto snapshot = [&](int s) {
-            if (SNAPREG > 0 && s < SNAPREG) {
-#pragma unroll
-                for (int k = 0; k < (SNAPREG > 0 ? SNAPREG : 1); ++k)
-                    if (k == s) {
-                        sR[k] = R;
-                        sQ[k] = Q;
-                        sE[k] = E;
-                    }
-            } else {
-                float *o = scratch + (size_t)s * 5 * ns + m;
-                o[0] = R.x;
-                o[ns] = R.y;
-                o[2 * ns] = Q.x;
-                o[3 * ns] = Q.y;
-                o[4 * ns] = __int_as_float(E);
-            }
+        auto coef = [&](int i, double2 &a, double2 &b, double2 &cc) {
+            const double *lv = s_lv + (size_t)i * BLDFM_LV64;
+            const double Tr = -fma(lv[LV_KX], lx2, lv[LV_KY] * ly2);
+            const double Ti = -fma(lv[LV_U], lx, lv[LV_V] * ly);
+            const double A = lv[LV_S1] * lv[LV_H2], B1 = lv[LV_S2] * lv[LV_H3], C1 = lv[LV_S4] * lv[LV_H3];
+            a = make_double2(fma(-A, Tr, 1.0), -A * Ti);
+            b = make_double2(fma(-B1, Tr, lv[LV_S3]), -B1 * Ti);
+            const double t2r = fma(Tr, Tr, -Ti * Ti), t2i = 2.0 * Tr * Ti;
+            cc = make_double2(fma(-C1, t2r, lv[LV_H] * Tr), fma(-C1, t2i, lv[LV_H] * Ti));
         };
-        {
-            const int s = s_slot[g.nz - 1];
-            if (s >= 0) snapshot(s);
+        auto step = [&](const double2 a, const double2 b, const double2 cc) {
+            const double2 cR = dc_mul(cc, R);
+            const double2 D = make_double2(a.x - cR.x, a.y - cR.y);
+            const double2 N = make_double2(fma(a.x, R.x, fma(-a.y, R.y, -b.x)), fma(a.x, R.y, fma(a.y, R.x, -b.y)));
+            const double dinv = 1.0 / fma(D.x, D.x, D.y * D.y);
+            R = make_double2(fma(N.x, D.x, N.y * D.y) * dinv, fma(N.y, D.x, -N.x * D.y) * dinv);
+        };
+        int i = L - 1;
+        for (; i >= jmax; --i) {
+            double2 a, b, cc;
+            coef(i, a, b, cc);
+            step(a, b, cc);
         }
-        for (int i = L - 1; i >= 0; --i) {
-            const float *lv = s_lv + (size_t)i * BLDFM_LV32;
-            const float Tr = fmaf(lv[L32_NKX], lx2, lv[L32_NKY] * ly2);
-            const float Ti = fmaf(lv[L32_NU], lx, lv[L32_NV] * ly);
-            const float2 a = make_float2(fmaf(-lv[L32_A], Tr, 1.f), -lv[L32_A] * Ti);
-            const float2 b = make_float2(fmaf(-lv[L32_B1], Tr, lv[L32_B0]), -lv[L32_B1] * Ti);
-            const float t2r = fmaf(Tr, Tr, -Ti * Ti);
-            const float2 cc = make_float2(fmaf(-lv[L32_C1], t2r, lv[L32_H] * Tr), Ti * fmaf(lv[L32_C2], Tr, lv[L32_H]));
-            // R_i = (a R_{i+1} - b) / (a - c R_{i+1});  f_i = c R_i + a = q_{i+1} / q_i
-            const float2 cR = fc_mul(cc, R);
-            const float2 D = make_float2(a.x - cR.x, a.y - cR.y);
-            const float2 N = make_float2(fmaf(a.x, R.x, fmaf(-a.y, R.y, -b.x)), fmaf(a.x, R.y, fmaf(a.y, R.x, -b.y)));
-            const float dinv = __frcp_rn(fmaf(D.x, D.x, D.y * D.y));
-            const float tr = fmaf(N.x, D.x, N.y * D.y);
-            const float ti = fmaf(N.y, D.x, -N.x * D.y);
-            R = make_float2(tr * dinv, ti * dinv);
-            const float2 cRn = fc_mul(cc, R);
-            const float2 f = make_float2(cRn.x + a.x, cRn.y + a.y);
-            Q = fc_mul(Q, f);
-            if ((i & 3) == 0) {
-                const float mx = fmaxf(fabsf(Q.x), fabsf(Q.y));
-                if (mx > 0.f) {
-                    const int e = ((__float_as_int(mx) >> 23) & 0xff) - 127;
-                    const float sc = __int_as_float((127 - e) << 23);
-                    Q.x *= sc;
-                    Q.y *= sc;
-                    E += e;
+        Rj = R;
+        if (!SINGLE) {
+            const int s = s_slot[jmax];
+            double *o = scratch + (size_t)s * 5 * ns + m;
+            o[0] = R.x;
+            o[ns] = R.y;
+            o[2 * ns] = 1.0;
+            o[3 * ns] = 0.0;
+            o[4 * ns] = 0.0;
+        }
+        for (; i >= 0; --i) {
+            double2 a, b, cc;
+            coef(i, a, b, cc);
+            step(a, b, cc);
+            Q = dc_mul(Q, make_double2(fma(cc.x, R.x, fma(-cc.y, R.y, a.x)), fma(cc.x, R.y, fma(cc.y, R.x, a.y))));
+            if ((i & 15) == 0) {
+                int e;
+                frexp(fmax(fabs(Q.x), fabs(Q.y)), &e);
+                Q.x = ldexp(Q.x, -e);
+                Q.y = ldexp(Q.y, -e);
+                E += e;
+            }
+            if (!SINGLE) {
+                const int s = s_slot[i];
+                if (s >= 0) {
+                    double *o = scratch + (size_t)s * 5 * ns + m;
+                    o[0] = R.x;
+                    o[ns] = R.y;
+                    o[2 * ns] = Q.x;
+                    o[3 * ns] = Q.y;
+                    o[4 * ns] = (double)E;
                 }
             }
-            const int s = s_slot[i];
-            if (s >= 0) snapshot(s);
         }
-        // outputs: q_j = q0 * Q_0 / Q_j, p_j = R_j q_j
-        const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2((float)g.q0dc_fp, 0.f);
-        float2 sh = make_float2(1.f, 0.f);
+        const double2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_double2(g.q0dc_fp, 0.0);
+        double2 sh = make_double2(1.0, 0.0);
         if (g.do_shift) {
-            const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
-            float sn, cs;
-            sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
-            sh = make_float2(cs, sn);
+            const double th = lx * g.sx + ly * g.sy;
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            sh = make_double2(cs, sn);
         }
         const int rm = paired ? index_of_freq(-ky, g.nly) : 0;
         const int cm = paired ? index_of_freq(-kx, g.nlx) : 0;
-        for (int s = 0; s < g.nsnap; ++s) {
-            float2 Rj, Qj;
-            int Ej;
-            bool inreg = false;
-            if (SNAPREG > 0 && s < SNAPREG) {
-#pragma unroll
-                for (int k = 0; k < (SNAPREG > 0 ? SNAPREG : 1); ++k)
-                    if (k == s) {
-                        Rj = sR[k];
-                        Qj = sQ[k];
-                        Ej = sE[k];
-                    }
-                inreg = true;
+        for (int s = 0; s < (SINGLE ? 1 : g.nsnap); ++s) {
+            double2 ratio;
+            if (SINGLE) {
+                ratio = make_double2(ldexp(Q.x, E), ldexp(Q.y, E));
+            } else {
+                const double *o = scratch + (size_t)s * 5 * ns + m;
+                Rj = make_double2(o[0], o[ns]);
+                const double2 Qj = make_double2(o[2 * ns], o[3 * ns]);
+                const int Ej = (int)o[4 * ns];
+                const double qn = fma(Qj.x, Qj.x, Qj.y * Qj.y);
+                ratio = make_double2(0.0, 0.0);
+                if (qn > 0.0) {
+                    const double scl = ldexp(1.0 / qn, E - Ej);
+                    ratio = make_double2(fma(Q.x, Qj.x, Q.y * Qj.y) * scl, fma(Q.y, Qj.x, -Q.x * Qj.y) * scl);
+                }
             }
-            if (!inreg) {
-                const float *o = scratch + (size_t)s * 5 * ns + m;
-                Rj = make_float2(o[0], o[ns]);
-                Qj = make_float2(o[2 * ns], o[3 * ns]);
-                Ej = __float_as_int(o[4 * ns]);
+            double2 q = dc_mul(q0, ratio);
+            double2 p = dc_mul(Rj, q);
+            if (g.precision == 0) {
+                p = round_c64(p);
+                q = round_c64(q);
             }
-            // ratio Q / Qj with exponents
-            const float qn = fmaf(Qj.x, Qj.x, Qj.y * Qj.y);
-            float2 ratio = make_float2(0.f, 0.f);
-            if (qn > 0.f) {
-                const float2 t = make_float2(fmaf(Q.x, Qj.x, Q.y * Qj.y), fmaf(Q.y, Qj.x, -Q.x * Qj.y));
-                const float sc = exp2f((float)(E - Ej)) / qn;
-                ratio = make_float2(t.x * sc, t.y * sc);
+            if (g.do_shift) {
+                p = dc_mul(p, sh);
+                q = dc_mul(q, sh);
             }
-            float2 q = fc_mul(q0, ratio);
-            float2 p = fc_mul(Rj, q);
-            p = fc_mul(p, sh);
-            q = fc_mul(q, sh);
             Xp[spec_idx(g, s, r, c)] = p;
             Xq[spec_idx(g, s, r, c)] = q;
             if (paired) {
-                Xp[spec_idx(g, s, rm, cm)] = make_float2(p.x, -p.y);
-                Xq[spec_idx(g, s, rm, cm)] = make_float2(q.x, -q.y);
+                Xp[spec_idx(g, s, rm, cm)] = make_double2(p.x, -p.y);
+                Xq[spec_idx(g, s, rm, cm)] = make_double2(q.x, -q.y);
             }
         }
     }
+}
+
+cudaError_t launch_riccati64(const SolveGeom &g, const double *lvtab, const int *slot, const uint32_t *modes,
+                             const double2 *q0spec, double *scratch, double2 *Xp, double2 *Xq, int *err, int nsm,
+                             cudaStream_t st)
+{
+    if (g.nsnap < 1 || g.nsolved == 0) return cudaSuccess;
+    const size_t smem = (size_t)(g.nz - 1) * BLDFM_LV64 * sizeof(double) + (size_t)g.nz * sizeof(int) + 16;
+    const int threads = 128;
+    int64_t blocks = (g.nsolved + threads - 1) / threads;
+    if (blocks > 64LL * nsm) blocks = 64LL * nsm;
+    if (g.nsnap == 1)
+        riccati64_kernel<true><<<(unsigned)blocks, threads, smem, st>>>(g, lvtab, slot, modes, q0spec, scratch, Xp,
+                                                                        Xq, err);
+    else
+        riccati64_kernel<false><<<(unsigned)blocks, threads, smem, st>>>(g, lvtab, slot, modes, q0spec, scratch, Xp,
+                                                                         Xq, err);
+    return LAUNCH_CHECK();
 }
 
 // ---------------------------------------------------------------------------
@@ -617,50 +545,17 @@ __global__ void __launch_bounds__(256) fwd_cols_kernel(SolveGeom g, FftPlan pl, 
 }
 
 // out_cols: one band column per CTA (blockIdx.x), one level (blockIdx.y).
-// Builds Z = Hp + i Hq, H(P) = (X(P) + conj X(-P)) / 2, transforms along y and
-// keeps rows [py, py + out_ny).  Output C[(lvl * nbx + b) * out_ny + y'].
 template <typename R>
 __global__ void __launch_bounds__(256) out_cols_kernel(SolveGeom g, FftPlan pl, const typename cvec<R>::T *__restrict__ tw,
                                                        const int4 *__restrict__ xband,
                                                        const typename cvec<R>::T *__restrict__ Xp,
                                                        const typename cvec<R>::T *__restrict__ Xq,
+                                                       const double2 *__restrict__ dc,
                                                        typename cvec<R>::T *__restrict__ Cout)
 {
     typedef typename cvec<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n = pl.n;
-    C *bufA = (C *)smem_raw;
-    C *bufB = bufA + n;
-    const int b = blockIdx.x, lvl = blockIdx.y;
-    const int4 bx = xband[b];  // x = position, y = column of X at P, z = column of X at -P
-    for (int i = threadIdx.x; i < n; i += blockDim.x) bufA[i] = cx_make<C>(0.0, 0.0);
-    __syncthreads();
-    const R h = (R)0.5;
-    if (bx.y >= 0) {
-        const size_t base = ((size_t)lvl * g.nlx + bx.y) * g.nly;
-        for (int r = threadIdx.x; r < g.nly; r += blockDim.x) {
-            const int ky = freq_of_index(r, g.nly);
-            const int pos = ky >= 0 ? ky : ky + n;
-            const C p = Xp[base + r], q = Xq[base + r];
-            bufA[pos] = cx_make<C>(h * (p.x - q.y), h * (p.y + q.x));
-        }
-    }
-    __syncthreads();
-    if (bx.z >= 0) {
-        const size_t base = ((size_t)lvl * g.nlx + bx.z) * g.nly;
-        for (int r = threadIdx.x; r < g.nly; r += blockDim.x) {
-            const int ky = freq_of_index(r, g.nly);
-            const int pm = ky > 0 ? n - ky : -ky;  // position of -ky
-            const C p = Xp[base + r], q = Xq[base + r];
-            C cur = bufA[pm];
-            cur.x += h * (p.x + q.y);
-            cur.y += h * (q.x - p.y);
-            bufA[pm] = cur;
-        }
-    }
-    C *res = fft_run<C>(bufA, bufB, pl, 1, tw, g.out_sign);
-    C *o = Cout + ((size_t)lvl * g.nbx + b) * g.out_ny;
-    for (int y = threadIdx.x; y < g.out_ny; y += blockDim.x) o[y] = res[g.py + y];
+    out_col_line<R>(g, pl, tw, xband, Xp, Xq, dc, Cout, blockIdx.x, blockIdx.y, (C *)smem_raw);
 }
 
 // out_rows: rows_per_cta output rows per CTA, one level (blockIdx.y).
@@ -673,25 +568,8 @@ __global__ void __launch_bounds__(256) out_rows_kernel(SolveGeom g, FftPlan pl, 
 {
     typedef typename cvec<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n = pl.n;
-    C *bufA = (C *)smem_raw;
-    C *bufB = bufA + (size_t)rows_per_cta * n;
-    const int y0 = blockIdx.x * rows_per_cta, lvl = blockIdx.y;
-    const int nl = min(rows_per_cta, g.out_ny - y0);
-    for (int i = threadIdx.x; i < nl * n; i += blockDim.x) bufA[i] = cx_make<C>(0.0, 0.0);
-    __syncthreads();
-    for (int i = threadIdx.x; i < nl * g.nbx; i += blockDim.x) {
-        const int b = i / nl, l = i - b * nl;
-        bufA[(size_t)l * n + xband[b].x] = Cin[((size_t)lvl * g.nbx + b) * g.out_ny + y0 + l];
-    }
-    C *res = fft_run<C>(bufA, bufB, pl, nl, tw, g.out_sign);
-    for (int i = threadIdx.x; i < nl * g.out_nx; i += blockDim.x) {
-        const int l = i / g.out_nx, x = i - l * g.out_nx;
-        const C v = res[(size_t)l * n + g.px + x];
-        const size_t o = ((size_t)lvl * g.out_ny + y0 + l) * g.out_nx + x;
-        conc[o] = (double)v.x;
-        flx[o] = (double)v.y;
-    }
+    out_row_lines<R>(g, pl, tw, xband, Cin, conc, flx, blockIdx.x * rows_per_cta, rows_per_cta, blockIdx.y,
+                     (C *)smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -724,7 +602,7 @@ __global__ void nonfinite_kernel(const double *__restrict__ a, const double *__r
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-#define LAUNCH_CHECK() (cudaGetLastError())
+
 
 cudaError_t launch_sweep64(const SolveGeom &g, const double *lvtab, const int *slot, const uint32_t *modes,
                            const double2 *q0spec, double2 *snap, double2 *top, int *err, int nsm, cudaStream_t st)
@@ -755,28 +633,31 @@ cudaError_t launch_combine64(const SolveGeom &g, const uint32_t *modes, const do
 }
 
 cudaError_t launch_trapezoid64(const SolveGeom &g, const double *lvtab, const int *slot, const double2 *q0spec,
-                               double p000, double2 *Xp, double2 *Xq, cudaStream_t st)
+                               double p000, double2 *dc, cudaStream_t st)
 {
-    trapezoid_kernel<double2><<<1, 32, 0, st>>>(g, lvtab, slot, q0spec, p000, Xp, Xq);
+    const size_t smem = (size_t)(g.nz > 1 ? g.nz - 1 : 1) * sizeof(double2) + (size_t)g.nz * sizeof(int);
+    trapezoid_kernel<double2><<<1, 256, smem, st>>>(g, lvtab, slot, q0spec, p000, dc);
     return LAUNCH_CHECK();
 }
 
 cudaError_t launch_trapezoid32(const SolveGeom &g, const double *lvtab, const int *slot, const float2 *q0spec,
-                               double p000, float2 *Xp, float2 *Xq, cudaStream_t st)
+                               double p000, double2 *dc, cudaStream_t st)
 {
-    trapezoid_kernel<float2><<<1, 32, 0, st>>>(g, lvtab, slot, q0spec, p000, Xp, Xq);
+    const size_t smem = (size_t)(g.nz > 1 ? g.nz - 1 : 1) * sizeof(double2) + (size_t)g.nz * sizeof(int);
+    trapezoid_kernel<float2><<<1, 256, smem, st>>>(g, lvtab, slot, q0spec, p000, dc);
     return LAUNCH_CHECK();
 }
 
 cudaError_t launch_analytic64(const SolveGeom &g, const uint32_t *modes, const double2 *eig, const double2 *q0spec,
-                              double p000, double kzinv, double hlev, double2 *Xp, double2 *Xq, cudaStream_t st)
+                              double p000, double kzinv, double hlev, double2 *Xp, double2 *Xq, double2 *dc,
+                              cudaStream_t st)
 {
     if (g.nsolved > 0) {
         const int threads = 256;
         const unsigned blocks = (unsigned)((g.nsolved + threads - 1) / threads);
         analytic64_kernel<<<blocks, threads, 0, st>>>(g, modes, eig, q0spec, kzinv, hlev, Xp, Xq);
     }
-    analytic_dc_kernel<<<1, 32, 0, st>>>(g, q0spec, p000, kzinv, hlev, Xp, Xq);
+    if (q0spec) analytic_dc_kernel<<<1, 32, 0, st>>>(g, q0spec, p000, kzinv, hlev, dc);
     return LAUNCH_CHECK();
 }
 
@@ -788,20 +669,33 @@ cudaError_t launch_riccati32(const SolveGeom &g, const float *lv32, const int *s
     const size_t smem = (size_t)L * BLDFM_LV32 * sizeof(float) + (size_t)g.nz * sizeof(int) + 16;
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(riccati32_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(riccati32_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(riccati32_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(riccati32_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(riccati32_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(riccati32_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
     if (threads <= 0) threads = 256;
     int64_t blocks = (g.nsolved + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
     if (blocks > 64LL * nsm) blocks = 64LL * nsm;
-    if (g.nsnap <= 1)
-        riccati32_kernel<1><<<(unsigned)blocks, threads, smem, st>>>(g, lv32, slot, modes, q0spec, scratch, Xp, Xq, ax,
-                                                                      ay, err);
-    else
-        riccati32_kernel<0><<<(unsigned)blocks, threads, smem, st>>>(g, lv32, slot, modes, q0spec, scratch, Xp, Xq, ax,
-                                                                      ay, err);
+    const bool single = g.nsnap == 1;
+    if (g.nsnap < 1) return cudaSuccess;  // no output level inside the grid: spectra stay zero
+    if (g.iso) {
+        if (single)
+            riccati32_kernel<true, true><<<(unsigned)blocks, threads, smem, st>>>(g, lv32, slot, modes, q0spec, scratch,
+                                                                                Xp, Xq, ax, ay, err);
+        else
+            riccati32_kernel<true, false><<<(unsigned)blocks, threads, smem, st>>>(g, lv32, slot, modes, q0spec,
+                                                                                 scratch, Xp, Xq, ax, ay, err);
+    } else {
+        if (single)
+            riccati32_kernel<false, true><<<(unsigned)blocks, threads, smem, st>>>(g, lv32, slot, modes, q0spec,
+                                                                                 scratch, Xp, Xq, ax, ay, err);
+        else
+            riccati32_kernel<false, false><<<(unsigned)blocks, threads, smem, st>>>(g, lv32, slot, modes, q0spec,
+                                                                                  scratch, Xp, Xq, ax, ay, err);
+    }
     return LAUNCH_CHECK();
 }
 
@@ -846,18 +740,20 @@ cudaError_t launch_forward_fft(const SolveGeom &g, const FftPlan &plx, const Fft
 template <typename R>
 cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftPlan &ply,
                               const typename cvec<R>::T *twx, const typename cvec<R>::T *twy, const int4 *xband,
-                              const typename cvec<R>::T *Xp, const typename cvec<R>::T *Xq, typename cvec<R>::T *Cbuf,
-                              double *conc, double *flx, cudaStream_t st)
+                              const typename cvec<R>::T *Xp, const typename cvec<R>::T *Xq, const double2 *dc,
+                              typename cvec<R>::T *Cbuf, double *conc, double *flx, cudaStream_t st)
 {
     typedef typename cvec<R>::T C;
     set_fft_smem_attr<R>();
     if (g.nbx <= 0 || g.out_ny <= 0 || g.out_nx <= 0 || g.nlvls <= 0) return cudaSuccess;
     dim3 gc(g.nbx, g.nlvls);
-    out_cols_kernel<R><<<gc, 256, 2 * (size_t)ply.n * sizeof(C), st>>>(g, ply, twy, xband, Xp, Xq, Cbuf);
-    const size_t budget = 96 * 1024;
-    int rpc = lines_per_cta(plx.n, sizeof(C), budget);
+    out_cols_kernel<R><<<gc, 256, 3 * (size_t)ply.n * sizeof(C), st>>>(g, ply, twy, xband, Xp, Xq, dc, Cbuf);
+    // two rows per CTA in FP32, one in FP64, bounded by shared memory
+    int rpc = sizeof(C) == 8 ? 2 : 1;
+    while (rpc > 1 && (2 * (size_t)rpc + 1) * plx.n * sizeof(C) > 190 * 1024) --rpc;
     dim3 gr((g.out_ny + rpc - 1) / rpc, g.nlvls);
-    out_rows_kernel<R><<<gr, 256, 2 * (size_t)rpc * plx.n * sizeof(C), st>>>(g, plx, twx, xband, Cbuf, conc, flx, rpc);
+    out_rows_kernel<R><<<gr, 256, (2 * (size_t)rpc + 1) * plx.n * sizeof(C), st>>>(g, plx, twx, xband, Cbuf, conc,
+                                                                                   flx, rpc);
     return LAUNCH_CHECK();
 }
 
@@ -867,10 +763,10 @@ template cudaError_t launch_forward_fft<float>(const SolveGeom &, const FftPlan 
                                                const float2 *, const double *, float2 *, float2 *, cudaStream_t);
 template cudaError_t launch_output_fft<double>(const SolveGeom &, const FftPlan &, const FftPlan &, const double2 *,
                                                const double2 *, const int4 *, const double2 *, const double2 *,
-                                               double2 *, double *, double *, cudaStream_t);
+                                               const double2 *, double2 *, double *, double *, cudaStream_t);
 template cudaError_t launch_output_fft<float>(const SolveGeom &, const FftPlan &, const FftPlan &, const float2 *,
-                                              const float2 *, const int4 *, const float2 *, const float2 *, float2 *,
-                                              double *, double *, cudaStream_t);
+                                              const float2 *, const int4 *, const float2 *, const float2 *,
+                                              const double2 *, float2 *, double *, double *, cudaStream_t);
 
 cudaError_t launch_tw_to_float(const double2 *src, float2 *dst, int n, cudaStream_t st)
 {
@@ -943,4 +839,19 @@ cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_
     cudaFree(out);
     *flops_per_s = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3);
     return e;
+}
+
+// Shared-memory limits of every kernel, set once per device before any launch
+// (and so before any stream capture).
+void prepare_kernel_attributes()
+{
+    set_fft_smem_attr<double>();
+    set_fft_smem_attr<float>();
+    cudaFuncSetAttribute(sweep64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati32_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati32_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati32_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati32_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }

@@ -13,12 +13,14 @@ cudaError_t launch_sweep64(const SolveGeom &g, const double *lvtab, const int *s
                            const double2 *q0spec, double2 *snap, double2 *top, int *err, int nsm, cudaStream_t st);
 cudaError_t launch_combine64(const SolveGeom &g, const uint32_t *modes, const double2 *eig, const double2 *snap,
                              const double2 *top, double2 *Xp, double2 *Xq, cudaStream_t st);
+// k = 0 mode from a device-resident q0 (dispersion mode) into dc[2 s], dc[2 s + 1]
 cudaError_t launch_trapezoid64(const SolveGeom &g, const double *lvtab, const int *slot, const double2 *q0spec,
-                               double p000, double2 *Xp, double2 *Xq, cudaStream_t st);
+                               double p000, double2 *dc, cudaStream_t st);
 cudaError_t launch_trapezoid32(const SolveGeom &g, const double *lvtab, const int *slot, const float2 *q0spec,
-                               double p000, float2 *Xp, float2 *Xq, cudaStream_t st);
+                               double p000, double2 *dc, cudaStream_t st);
 cudaError_t launch_analytic64(const SolveGeom &g, const uint32_t *modes, const double2 *eig, const double2 *q0spec,
-                              double p000, double kzinv, double hlev, double2 *Xp, double2 *Xq, cudaStream_t st);
+                              double p000, double kzinv, double hlev, double2 *Xp, double2 *Xq, double2 *dc,
+                              cudaStream_t st);
 cudaError_t launch_riccati32(const SolveGeom &g, const float *lv32, const int *slot, const uint32_t *modes,
                              const float2 *q0spec, float *scratch, float2 *Xp, float2 *Xq, float ax, float ay,
                              int *err, int nsm, int threads, cudaStream_t st);
@@ -29,9 +31,13 @@ cudaError_t launch_forward_fft(const SolveGeom &g, const FftPlan &plx, const Fft
 template <typename R>
 cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftPlan &ply,
                               const typename cvec<R>::T *twx, const typename cvec<R>::T *twy, const int4 *xband,
-                              const typename cvec<R>::T *Xp, const typename cvec<R>::T *Xq, typename cvec<R>::T *Cbuf,
-                              double *conc, double *flx, cudaStream_t st);
+                              const typename cvec<R>::T *Xp, const typename cvec<R>::T *Xq, const double2 *dc,
+                              typename cvec<R>::T *Cbuf, double *conc, double *flx, cudaStream_t st);
 cudaError_t launch_tw_to_float(const double2 *src, float2 *dst, int n, cudaStream_t st);
 cudaError_t launch_spec_to_float(const double2 *src, float2 *dst, int64_t n, cudaStream_t st);
 cudaError_t launch_nonfinite(const double *a, const double *b, int64_t n, int *flag, int nsm, cudaStream_t st);
 cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_s);
+void prepare_kernel_attributes();
+cudaError_t launch_riccati64(const SolveGeom &g, const double *lvtab, const int *slot, const uint32_t *modes,
+                             const double2 *q0spec, double *scratch, double2 *Xp, double2 *Xq, int *err, int nsm,
+                             cudaStream_t st);

@@ -47,6 +47,7 @@ void *na_scratch_dev[NA_MAX_DEVICES];  // device address of g_noalloc_scratch pe
 // host-side staging (static, no heap): level tables, slot map, band table
 struct NaHost {
     double lv64[(BLDFM_MAX_NZ - 1) * BLDFM_LV64];
+    double dc[4 * BLDFM_MAX_NZ];
     float lv32[(BLDFM_MAX_NZ - 1) * BLDFM_LV32];
     int slot[BLDFM_MAX_NZ];
     int4 xband[BLDFM_MAX_FFT_N + 1];
@@ -132,7 +133,7 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     if (d->mode != BLDFM_MODE_FP32 || d->analytic) return BLDFM_ERR_UNSUPPORTED;
     if (d->nx < 1 || d->ny < 1 || d->nz < 2 || nlvls < 1 || !(d->xmax > 0) || !(d->ymax > 0))
         return BLDFM_ERR_ARG;
-    if (d->nz > BLDFM_MAX_NZ) return BLDFM_ERR_UNSUPPORTED;
+    if (d->nz > BLDFM_MAX_NZ || nlvls > BLDFM_MAX_NZ) return BLDFM_ERR_UNSUPPORTED;
     cudaStream_t st = (cudaStream_t)stream;
 
     // per-device set-up: device address of the scratch array
@@ -223,6 +224,10 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
         g.kyk_top = Ky[nz - 1] * kzinv;
         g.uk_top = u[nz - 1] * kzinv;
         g.vk_top = v[nz - 1] * kzinv;
+        double ex = 1.0, ey = 0.0;
+        g.iso = hx_profiles_iso(nz, prof_host, &ex, &ey);
+        g.ex = (float)ex;
+        g.ey = (float)ey;
     }
     int ns = 0;
     for (int i = 0; i < nz; ++i) {
@@ -234,6 +239,9 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
             }
     }
     g.nsnap = ns;
+    g.jmax = -1;
+    for (int i = 0; i < nz; ++i)
+        if (na_host.slot[i] >= 0) g.jmax = i;
     int64_t nsolved = 0;
     for (int c = 0; c < nlx; ++c) {
         na_host.colstart[c] = (int)nsolved;
@@ -279,6 +287,8 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     o = na_al(o + (size_t)L * BLDFM_LV32 * 4);
     const size_t o_slot = o;
     o = na_al(o + (size_t)nz * 4);
+    const size_t o_dc = o;
+    o = na_al(o + (size_t)nlvls * 32);
     const size_t o_cs = o;
     o = na_al(o + (size_t)(nlx + 1) * 4);
     const size_t o_modes = o;
@@ -310,7 +320,10 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
 
     char *w = (char *)na_scratch_dev[dev];
     hx_level_table(nz, z_host, prof_host, na_host.lv64);
-    hx_level_table32(nz, z_host, prof_host, na_host.lv32);
+    if (g.iso)
+        hx_level_table32_iso(nz, z_host, prof_host, g.ex, g.ey, na_host.lv32);
+    else
+        hx_level_table32(nz, z_host, prof_host, na_host.lv32);
 #define NA_CK(x)                                                                                                       \
     do {                                                                                                               \
         if ((x) != cudaSuccess) return BLDFM_ERR_CUDA;                                                                 \
@@ -320,6 +333,11 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     NA_CK(cudaMemcpyAsync(w + o_lv64, na_host.lv64, (size_t)L * BLDFM_LV64 * 8, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(w + o_lv32, na_host.lv32, (size_t)L * BLDFM_LV32 * 4, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(w + o_slot, na_host.slot, (size_t)nz * 4, cudaMemcpyHostToDevice, st));
+    if (d->footprint) {
+        hx_dc_values(nz, na_host.lv64, na_host.slot, g.q0dc_fp, 0.0, d->srf_bg_conc, d->precision == BLDFM_PREC_SINGLE,
+                     nlvls, 0, na_host.dc);
+        NA_CK(cudaMemcpyAsync(w + o_dc, na_host.dc, (size_t)nlvls * 32, cudaMemcpyHostToDevice, st));
+    }
     NA_CK(cudaMemcpyAsync(w + o_cs, na_host.colstart, (size_t)(nlx + 1) * 4, cudaMemcpyHostToDevice, st));
     if (nbx > 0) NA_CK(cudaMemcpyAsync(w + o_xb, na_host.xband, (size_t)nbx * 16, cudaMemcpyHostToDevice, st));
     // the spectra start at zero when some output slot stays empty
@@ -347,9 +365,11 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
         NA_CK(launch_riccati32(g, (const float *)(w + o_lv32), (const int *)(w + o_slot),
                                (const uint32_t *)(w + o_modes), q0, (float *)(w + o_snap), Xp, Xq, ax, ay,
                                (int *)(w + o_err), nsm, 256, st));
-    NA_CK(launch_trapezoid32(g, (const double *)(w + o_lv64), (const int *)(w + o_slot), q0, d->srf_bg_conc, Xp,
-                             Xq, st));
+    if (!d->footprint)
+        NA_CK(launch_trapezoid32(g, (const double *)(w + o_lv64), (const int *)(w + o_slot), q0, d->srf_bg_conc,
+                                 (double2 *)(w + o_dc), st));
     NA_CK(launch_output_fft<float>(g, plx_out, ply_out, (const float2 *)(w + o_twxo), (const float2 *)(w + o_twyo),
-                                   (const int4 *)(w + o_xb), Xp, Xq, (float2 *)(w + o_Cb), conc_dev, flx_dev, st));
+                                   (const int4 *)(w + o_xb), Xp, Xq, (const double2 *)(w + o_dc), (float2 *)(w + o_Cb),
+                                   conc_dev, flx_dev, st));
     return BLDFM_OK;
 }

@@ -1,0 +1,231 @@
+// FP32 invariant-imbedding (Riccati) sweep: per-step device functions and the
+// per-mode body shared by the single-solve and batched kernels.
+#pragma once
+
+#include "devmath.cuh"
+
+// ---------------------------------------------------------------------------
+// FP32 invariant-imbedding (Riccati) sweep
+// ---------------------------------------------------------------------------
+// Same discrete boundary-value problem as the shooting method: with
+// s_{i+1} = M_i s_i, M_i = [[a, b], [c, a]] and the radiation condition at the
+// top, the ratio R_i = p_i / q_i obeys R_i = (a R_{i+1} - b) / (a - c R_{i+1})
+// from R_L = 1 / (Kz_top * eig), and q_{i+1} = (c R_i + a) q_i.  The backward
+// recursion is contractive (it follows the decaying solution), so FP32 loses
+// nothing to the cancellation that forces FP64 in the forward shooting form.
+// The running product Q_i = prod_{k>=i} (c_k R_k + a_k) is kept as an FP32
+// mantissa with an integer power-of-two exponent, renormalised every 4 steps.
+__device__ __forceinline__ float2 csqrt_f(float2 w)
+{
+    // principal branch, Kahan's formulation
+    float x = w.x, y = w.y;
+    float t = sqrtf(0.5f * (fabsf(x) + hypotf(x, y)));
+    if (t == 0.f) return make_float2(0.f, 0.f);
+    if (x >= 0.f) return make_float2(t, y / (2.f * t));
+    return make_float2(fabsf(y) / (2.f * t), copysignf(t, y));
+}
+
+__device__ __forceinline__ float2 fc_mul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Coefficients a, b, c of step i for one mode.
+//   ISO: Kx == Ky and (u, v) = U (ex, ey) at every level, so
+//        T = -K k2 - i U kw with per-mode k2 = lx^2 + ly^2, kw = ex lx + ey ly;
+//        row = {AK, AU, B0, B1K, B1U, -HK, -C1K2, C1U2, -HU, -2 C1 K U}
+//   generic: row = {-Kx, -Ky, -u, -v, A, B0, B1, H, C1, -2 C1}
+template <bool ISO>
+struct StepCoef;
+
+template <>
+struct StepCoef<true> {
+    float k2, kw, k4, kw2, k2kw;
+    __device__ __forceinline__ void init(float lx, float ly, float ex, float ey)
+    {
+        k2 = fmaf(lx, lx, ly * ly);
+        kw = fmaf(ex, lx, ey * ly);
+        k4 = k2 * k2;
+        kw2 = kw * kw;
+        k2kw = k2 * kw;
+    }
+    __device__ __forceinline__ void eval(const float *lv, float2 &a, float2 &b, float2 &c) const
+    {
+        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+        a = make_float2(fmaf(r0.x, k2, 1.f), r0.y * kw);
+        b = make_float2(fmaf(r0.w, k2, r0.z), r1.x * kw);
+        c = make_float2(fmaf(r1.z, k4, fmaf(r1.w, kw2, r1.y * k2)), fmaf(r2.y, k2kw, r2.x * kw));
+    }
+};
+
+template <>
+struct StepCoef<false> {
+    float lx, ly, lx2, ly2;
+    __device__ __forceinline__ void init(float lx_, float ly_, float, float)
+    {
+        lx = lx_;
+        ly = ly_;
+        lx2 = lx * lx;
+        ly2 = ly * ly;
+    }
+    __device__ __forceinline__ void eval(const float *lv, float2 &a, float2 &b, float2 &c) const
+    {
+        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+        const float Tr = fmaf(r0.x, lx2, r0.y * ly2);
+        const float Ti = fmaf(r0.z, lx, r0.w * ly);
+        a = make_float2(fmaf(-r1.x, Tr, 1.f), -r1.x * Ti);
+        b = make_float2(fmaf(-r1.z, Tr, r1.y), -r1.z * Ti);
+        const float t2r = fmaf(Tr, Tr, -Ti * Ti);
+        c = make_float2(fmaf(-r2.x, t2r, r1.w * Tr), Ti * fmaf(r2.y, Tr, r1.w));
+    }
+};
+
+// One backward step: R <- (a R - b) / (a - c R).
+__device__ __forceinline__ void ricc_step(float2 &R, const float2 a, const float2 b, const float2 c)
+{
+    const float cRr = fmaf(c.x, R.x, -c.y * R.y), cRi = fmaf(c.x, R.y, c.y * R.x);
+    const float Dr = a.x - cRr, Di = a.y - cRi;
+    const float Nr = fmaf(a.x, R.x, fmaf(-a.y, R.y, -b.x));
+    const float Ni = fmaf(a.x, R.y, fmaf(a.y, R.x, -b.y));
+    const float inv = rcp_approx(fmaf(Dr, Dr, Di * Di));
+    R.x = fmaf(Nr, Dr, Ni * Di) * inv;
+    R.y = fmaf(Ni, Dr, -Nr * Di) * inv;
+}
+
+// flux factor of step i with the updated ratio: Q *= c R + a
+__device__ __forceinline__ void flux_step(float2 &Q, const float2 R, const float2 a, const float2 c)
+{
+    const float fr = fmaf(c.x, R.x, fmaf(-c.y, R.y, a.x));
+    const float fi = fmaf(c.x, R.y, fmaf(c.y, R.x, a.y));
+    const float qr = fmaf(Q.x, fr, -Q.y * fi);
+    Q.y = fmaf(Q.x, fi, Q.y * fr);
+    Q.x = qr;
+}
+
+__device__ __forceinline__ void renorm(float2 &Q, int &E)
+{
+    const float mx = fmaxf(fabsf(Q.x), fabsf(Q.y));
+    const int e = ((__float_as_int(mx) >> 23) & 0xff) - 127;
+    if (mx > 0.f && e > -126 && e < 127) {
+        const float sc = __int_as_float((127 - e) << 23);
+        Q.x *= sc;
+        Q.y *= sc;
+        E += e;
+    }
+}
+
+// One solved mode m of a solve: backward Riccati sweep over the level table
+// in shared memory (s_lv, s_slot), then the level values, phase shift and
+// mirror write.  SINGLE: exactly one output slot (no per-step slot test).
+template <bool ISO, bool SINGLE>
+__device__ __forceinline__ void ricc_mode(const SolveGeom &g, const float *__restrict__ s_lv,
+                                          const int *__restrict__ s_slot, const uint32_t *__restrict__ modes,
+                                          const float2 *__restrict__ q0spec, float *__restrict__ scratch,
+                                          float2 *__restrict__ Xp, float2 *__restrict__ Xq, float ax, float ay,
+                                          int64_t m)
+{
+    const int L = g.nz - 1;
+    const int jmax = g.jmax;
+    const int64_t ns = g.nsolved;
+    int r, c;
+    bool paired;
+    unpack_mode(modes[m], r, c, paired);
+    const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
+    const float lx = ax * (float)kx, ly = ay * (float)ky;
+    StepCoef<ISO> sc;
+    sc.init(lx, ly, g.ex, g.ey);
+    // top eigenvalue and radiation ratio R_L = 1 / (Kz_top eig)
+    const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
+                                 fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+    const float2 eg = csqrt_f(w);
+    const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+    const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
+    float2 R = make_float2(ke.x * inv, -ke.y * inv);
+    // above the highest output level: only the ratio
+    int i = L - 1;
+    for (; i >= jmax; --i) {
+        float2 a, b, cc;
+        sc.eval(s_lv + (size_t)i * BLDFM_LV32, a, b, cc);
+        ricc_step(R, a, b, cc);
+    }
+    float2 Rj = R;
+    float2 Q = make_float2(1.f, 0.f);
+    int E = 0;
+    if (!SINGLE) {
+        const int s = s_slot[jmax];
+        float *o = scratch + (size_t)s * 5 * ns + m;
+        o[0] = R.x;
+        o[ns] = R.y;
+        o[2 * ns] = 1.f;
+        o[3 * ns] = 0.f;
+        o[4 * ns] = __int_as_float(0);
+    }
+    // below it: ratio and flux product, renormalised every 8 steps
+    int cnt = 0;
+    for (; i >= 0; --i) {
+        float2 a, b, cc;
+        sc.eval(s_lv + (size_t)i * BLDFM_LV32, a, b, cc);
+        ricc_step(R, a, b, cc);
+        flux_step(Q, R, a, cc);
+        if (++cnt == 8) {
+            cnt = 0;
+            renorm(Q, E);
+        }
+        if (!SINGLE) {
+            const int s = s_slot[i];
+            if (s >= 0) {
+                float *o = scratch + (size_t)s * 5 * ns + m;
+                o[0] = R.x;
+                o[ns] = R.y;
+                o[2 * ns] = Q.x;
+                o[3 * ns] = Q.y;
+                o[4 * ns] = __int_as_float(E);
+            }
+        }
+    }
+    const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2((float)g.q0dc_fp, 0.f);
+    float2 sh = make_float2(1.f, 0.f);
+    if (g.do_shift) {
+        const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
+        float sn, cs;
+        sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
+        sh = make_float2(cs, sn);
+    }
+    const int rm = paired ? index_of_freq(-ky, g.nly) : 0;
+    const int cm = paired ? index_of_freq(-kx, g.nlx) : 0;
+    for (int s = 0; s < (SINGLE ? 1 : g.nsnap); ++s) {
+        float2 ratio;
+        if (SINGLE) {
+            ratio = make_float2(ldexpf(Q.x, E), ldexpf(Q.y, E));
+        } else {
+            const float *o = scratch + (size_t)s * 5 * ns + m;
+            Rj = make_float2(o[0], o[ns]);
+            const float2 Qj = make_float2(o[2 * ns], o[3 * ns]);
+            const int Ej = __float_as_int(o[4 * ns]);
+            const float qn = fmaf(Qj.x, Qj.x, Qj.y * Qj.y);
+            ratio = make_float2(0.f, 0.f);
+            if (qn > 0.f) {
+                const float2 t = make_float2(fmaf(Q.x, Qj.x, Q.y * Qj.y), fmaf(Q.y, Qj.x, -Q.x * Qj.y));
+                const float scl = ldexpf(1.0f / qn, E - Ej);
+                ratio = make_float2(t.x * scl, t.y * scl);
+            }
+        }
+        float2 q = fc_mul(q0, ratio);
+        float2 p = fc_mul(Rj, q);
+        p = fc_mul(p, sh);
+        q = fc_mul(q, sh);
+        Xp[spec_idx(g, s, r, c)] = p;
+        Xq[spec_idx(g, s, r, c)] = q;
+        if (paired) {
+            Xp[spec_idx(g, s, rm, cm)] = make_float2(p.x, -p.y);
+            Xq[spec_idx(g, s, rm, cm)] = make_float2(q.x, -q.y);
+        }
+    }
+}

@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _lib
 
-_MODES = {"fp64": _lib.MODE_FP64, "fp32": _lib.MODE_FP32}
+_MODES = {"fp64": _lib.MODE_FP64, "fp32": _lib.MODE_FP32, "fp64r": _lib.MODE_FP64R}
 
 
 def _normalise_levels(levels, nz):
@@ -97,7 +97,7 @@ def steady_state_transport_solver(
         if cached is not None:
             return cached
     if mode not in _MODES:
-        raise ValueError("mode must be 'fp64' or 'fp32'")
+        raise ValueError("mode must be 'fp64', 'fp32' or 'fp64r'")
     lib = _lib.load()
     shape = np.shape(srf_flx)
     if len(shape) != 2:

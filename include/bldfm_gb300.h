@@ -49,6 +49,8 @@ extern "C" {
 
 #define BLDFM_MODE_FP64 0 /* FP64 shooting sweep, rounding identical to the reference */
 #define BLDFM_MODE_FP32 1 /* FP32 invariant-imbedding (Riccati) sweep, renormalised */
+#define BLDFM_MODE_FP64R 2 /* FP64 invariant imbedding: the discrete solution without the
+                              shooting method's cancellation (more accurate than the reference) */
 
 typedef struct bldfm_desc {
     int32_t nx, ny;     /* srf_flx shape is (ny, nx)                          */
@@ -132,7 +134,9 @@ int bldfm_vertical_profiles(int32_t n, double meas_height, double um, double vm,
  * bldfm_stage_times() returns the mean milliseconds per stage over the
  * solves enqueued since the previous call (up to 1024): [0] forward transform,
  * [1] sweep, [2] k=0 mode / combination, [3] output transform.  It returns the
- * number of stages written and restarts the average. */
+ * number of stages written and restarts the average.  Batches
+ * (bldfm_solve_batch without a graph) record [0] upload and per-case forward
+ * transforms, [1] the sweep, [2] the output transform. */
 int bldfm_set_stage_timing(int enable);
 int bldfm_stage_times(float *ms, int n);
 
@@ -140,6 +144,41 @@ int bldfm_stage_times(float *ms, int n);
  * FP64: the pipe peak the sweep kernels are held against (no reference
  * counterpart). */
 int bldfm_fma_peak(int fp64, double *flops_per_s, void *stream);
+
+/* ---- batches ------------------------------------------------------------
+ * Many cases (towers x timesteps), each with its own grid, modes, levels and
+ * profiles, solved together in FP32 (BLDFM_MODE_FP32; analytic = 0).  Replaces
+ * the reference's per-case loops and process pool around the solve
+ * (src/bldfm/interface.py:141-326): one persistent sweep launch over every
+ * (case, mode tile), one launch per transform pass, optionally replayed as a
+ * CUDA graph (not on the legacy default stream). */
+typedef struct bldfm_case {
+    bldfm_desc desc;             /* mode must be BLDFM_MODE_FP32            */
+    const double *srf_flx_dev;   /* (ny, nx) device, NULL in footprint mode */
+    const double *z_host;        /* (nz)                                    */
+    const double *prof_host;     /* (5, nz): u, v, Kx, Ky, Kz               */
+    const int64_t *levels_host;  /* (nlvls)                                 */
+    int32_t nlvls;
+    int32_t pad;
+    double *conc_dev, *flx_dev;  /* (nlvls, out_ny, out_nx) device outputs  */
+} bldfm_case;
+
+typedef struct bldfm_batch_opts {
+    int32_t threads;     /* sweep CTA size: 128 or 256 (0: 256)            */
+    int32_t ctas_per_sm; /* persistent sweep CTAs per SM (0: occupancy max) */
+    int32_t use_graph;   /* capture the batch once, replay it afterwards   */
+    int32_t reserved;
+} bldfm_batch_opts;
+
+/* Workspace bytes for a batch (256-byte aligned workspace required). */
+int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases,
+                     const bldfm_batch_opts *opts, int64_t *workspace_bytes);
+
+/* Enqueue a batch on stream; returns once enqueued.  The int32 at workspace
+ * offset 0 holds the device status after completion. */
+int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases,
+                      const bldfm_batch_opts *opts, void *workspace,
+                      size_t workspace_bytes, void *stream);
 
 /* Allocation-free FP32 solve.  No counterpart in the reference (which never
  * touches a GPU).  For callers that may not allocate device memory while they

@@ -145,6 +145,45 @@ def ivp_sweep_numpy(p0, q0, profiles, z, levels, Lx, Ly):
     return p, q, ps, qs
 
 
+def riccati_sweep(Lx, Ly, q0, eigval, Kz_top, profiles, z, levels):
+    """The same discrete boundary-value problem as the shooting sweep, solved by
+    invariant imbedding in FP64 (no cancellation): R_i = p_i/q_i from the top
+    radiation condition R_L = 1/(Kz_top eigval) downwards,
+    R_i = (a R_{i+1} - b)/(a - c R_{i+1}), q_{i+1} = (c R_i + a) q_i.
+    Returns (p, q) of shape (nlvls, nmodes)."""
+    u, v, Kx, Ky, Kz = profiles
+    nz = len(z)
+    dz = np.diff(z)
+    slot, nsnap = snapshot_schedule(levels, nz)
+    nlvls = len(np.atleast_1d(levels))
+    n = Lx.shape[0]
+    R = 1.0 / (Kz_top * eigval)
+    logQ = np.zeros(n, dtype=np.complex128)  # log of prod_{k >= i} f_k
+    Rs = {}
+    Ls = {}
+    if slot[nz - 1] >= 0:
+        Rs[nz - 1], Ls[nz - 1] = R.copy(), logQ.copy()
+    for i in range(nz - 2, -1, -1):
+        T = -(Kx[i] * Lx**2 + Ky[i] * Ly**2) - 1j * (u[i] * Lx + v[i] * Ly)
+        k = 1.0 / Kz[i]
+        h = dz[i]
+        a = 1 - 0.5 * k * h * h * T
+        b = -k * h - k * k * h**3 / 6.0 * T
+        c = T * h - k * h**3 / 6.0 * T * T
+        R = (a * R - b) / (a - c * R)
+        logQ = logQ + np.log(c * R + a)
+        if slot[i] >= 0:
+            Rs[i], Ls[i] = R.copy(), logQ.copy()
+    p = np.zeros((nlvls, n), dtype=np.complex128)
+    q = np.zeros_like(p)
+    for i, s in enumerate(slot):
+        if s >= 0:
+            # q_j = q0 prod_{k<j} f_k = q0 exp(logQ_0 - logQ_j)
+            q[s] = q0 * np.exp(logQ - Ls[i])
+            p[s] = Rs[i] * q[s]
+    return p, q
+
+
 def shooting_sweep(Lx, Ly, q0, eigval, Kz_top, profiles, z, levels, nthreads=0, use_port=True):
     """Both IVPs plus the alpha combination; returns (p, q) of shape (nlvls, nmodes)."""
     nz = len(z)
@@ -234,11 +273,14 @@ def steady_state_transport_solver(
     cache=None,
     nthreads=0,
     use_port=True,
+    sweep="shooting",
 ):
     """Oracle restatement of the reference solve (solver.py:16-304).
 
     Same signature and return convention as the reference.  ``cache`` is
-    accepted and ignored (the oracle never memoises).
+    accepted and ignored (the oracle never memoises).  ``sweep="riccati"``
+    replaces the shooting sweep by :func:`riccati_sweep` (the exact solution of
+    the same discrete problem, the yardstick of the accurate modes).
     """
     q0 = np.asarray(srf_flx)
     p000 = srf_bg_conc
@@ -310,10 +352,13 @@ def steady_state_transport_solver(
         tfftq[:, msk] = tfftq0[msk] * np.exp(-eigval * h)
         tfftp[:, msk] = tfftq[:, msk] * Kzinv / eigval
     else:
-        pm, qm = shooting_sweep(
-            Lx[msk], Ly[msk], tfftq0[msk], eigval, Kz[nz - 1], profiles, z, levels,
-            nthreads=nthreads, use_port=use_port,
-        )
+        if sweep == "riccati":
+            pm, qm = riccati_sweep(Lx[msk], Ly[msk], tfftq0[msk], eigval, Kz[nz - 1], profiles, z, levels)
+        else:
+            pm, qm = shooting_sweep(
+                Lx[msk], Ly[msk], tfftq0[msk], eigval, Kz[nz - 1], profiles, z, levels,
+                nthreads=nthreads, use_port=use_port,
+            )
         tfftp[:, msk] = pm
         tfftq[:, msk] = qm
         # k = 0 mode by the trapezoid rule (solver.py:237-251)

@@ -122,3 +122,34 @@ def test_repeated_calls_are_deterministic():
     a = _gpu_solve(kw)[2]
     b = _gpu_solve(kw)[2]
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["source_area", "plume_3d", "multilevel_footprint", "ragged_odd",
+                                  "quick_double_shift", "plume_levels_double", "cfg1_gaussian_256"])
+def test_fp64r_matches_exact_discrete_solution(name):
+    """Accurate FP64 mode against the FP64 invariant-imbedding restatement of
+    the oracle: same mathematics, so agreement to FP64 rounding."""
+    from oracle import bldfm_oracle as O
+
+    d = G.load(name)
+    kw = G.kwargs_of(d)
+    _, conc, flx = _gpu_solve(kw, mode="fp64r")
+    _, oc, of = O.steady_state_transport_solver(**kw, sweep="riccati")
+    tol = F32_OUT_TOL if str(d["conc_dtype"]) == "float32" else 1e-11
+    assert G.rel_l2(conc, oc) <= tol and G.rel_l2(flx, of) <= tol
+
+
+def test_fp32_against_exact_on_headline_workload():
+    """FP32 path against the accurate FP64 path on the full 512^2 footprint:
+    the bar the batched FP32 and the surrogate are held to (relative L2 1e-3);
+    the reference's own FP64 rounding floor on this case is ~5e-5."""
+    d = G.load("metric_footprint_512")
+    kw = G.kwargs_of(d)
+    _, c32, f32 = _gpu_solve(kw, mode="fp32")
+    _, cr, fr = _gpu_solve(kw, mode="fp64r")
+    _, c64, f64 = _gpu_solve(kw, mode="fp64")
+    e32 = max(G.rel_l2(c32, cr), G.rel_l2(f32, fr))
+    floor = max(G.rel_l2(c64, cr), G.rel_l2(f64, fr))
+    print("headline: fp32 vs exact %.2e, reference rounding vs exact %.2e" % (e32, floor))
+    assert e32 <= 1e-4
+    assert floor <= 1e-3

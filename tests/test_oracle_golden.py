@@ -58,3 +58,14 @@ def test_footprint_unit_mass_extended_grid():
 def test_snapshot_schedule_semantics():
     slot, n = O.snapshot_schedule(np.array([5, 2, 2, 40]), 10)
     assert n == 2 and slot[2] == 0 and slot[5] == 1 and (slot >= 0).sum() == 2
+
+
+@pytest.mark.parametrize("name", ["source_area", "plume_3d", "multilevel_footprint", "ragged_odd"])
+def test_riccati_oracle_agrees_with_shooting_where_well_conditioned(name):
+    """The invariant-imbedding restatement solves the same discrete problem:
+    on fixtures whose shooting cancellation is mild both agree closely."""
+    d = G.load(name)
+    kw = G.kwargs_of(d)
+    _, c1, f1 = O.steady_state_transport_solver(**kw)
+    _, c2, f2 = O.steady_state_transport_solver(**kw, sweep="riccati")
+    assert G.rel_l2(c2, c1) <= 1e-6 and G.rel_l2(f2, f1) <= 1e-6
