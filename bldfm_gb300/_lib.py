@@ -136,6 +136,14 @@ _SIGS = {
         ctypes.c_int,
         [ctypes.POINTER(Case), ctypes.c_int32, ctypes.POINTER(BatchOpts), _P, ctypes.c_size_t, _P],
     ),
+    "bldfm_tc_gemm_check": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int32]),
+    "bldfm_surrogate_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    "bldfm_surrogate_destroy": (ctypes.c_int, [_P]),
+    "bldfm_surrogate_nparams": (ctypes.c_int, []),
+    "bldfm_surrogate_params": (ctypes.c_int, [_P, _P, _P]),
+    "bldfm_surrogate_grads": (ctypes.c_int, [_P, _P, _P]),
+    "bldfm_surrogate_train_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_float, _P]),
+    "bldfm_surrogate_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
     "bldfm_solve_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P],

@@ -1,0 +1,624 @@
+// Learned surrogate of the per-mode transfer function: a BF16 MLP whose hidden
+// 256 x 256 layers run on the tcgen05 tensor cores (tcgemm.cuh).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/bldfm_gb300.h"
+#include "tcgemm.cuh"
+
+namespace {
+
+// row-major R x K bf16 -> blocks [R / rows_per_block][K / KC] in core-matrix order
+void host_block(const uint16_t *src, int R, int K, int rows_per_block, int KC, std::vector<uint16_t> &dst)
+{
+    dst.assign((size_t)R * K, 0);
+    const int nb = R / rows_per_block, nc = K / KC;
+    for (int b = 0; b < nb; ++b)
+        for (int c = 0; c < nc; ++c) {
+            uint16_t *blk = dst.data() + ((size_t)b * nc + c) * rows_per_block * KC;
+            for (int r = 0; r < rows_per_block; ++r)
+                for (int k = 0; k < KC; ++k)
+                    blk[tc_core_offset(r, k, KC) / 2] = src[(size_t)(b * rows_per_block + r) * K + c * KC + k];
+        }
+}
+
+struct StoreF32 {
+    float *D;
+    int ld;
+    __device__ void row(int r, int col0, const float *v, uint16_t *) const
+    {
+        float *o = D + (size_t)r * ld + col0;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) o[i] = v[i];
+    }
+    __device__ void finish(int, uint16_t *) const {}
+};
+
+}  // namespace
+
+// D (M x 256, fp32) = A (M x K) * B (256 x K)^T, bf16 operands given row-major
+// on the host; M a multiple of 128, K a multiple of 16.  Validates the tensor
+// core path against a reference GEMM; allocates its own device buffers.
+extern "C" int bldfm_tc_gemm_check(const uint16_t *A, const uint16_t *B, float *D, int32_t M, int32_t K)
+{
+    if (!A || !B || !D || M <= 0 || K <= 0 || M % 128 != 0 || K % 16 != 0) return BLDFM_ERR_ARG;
+    int KC = K <= 256 ? K : 256;
+    if (K % KC != 0) return BLDFM_ERR_ARG;
+    std::vector<uint16_t> Ab, Bb;
+    host_block(A, M, K, 128, KC, Ab);
+    host_block(B, 256, K, 256, KC, Bb);
+    uint16_t *dA = nullptr, *dB = nullptr;
+    float *dD = nullptr;
+    int *derr = nullptr;
+    int rc = BLDFM_OK;
+    if (cudaMalloc(&dA, Ab.size() * 2) != cudaSuccess || cudaMalloc(&dB, Bb.size() * 2) != cudaSuccess ||
+        cudaMalloc(&dD, (size_t)M * 256 * 4) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess)
+        rc = BLDFM_ERR_CUDA;
+    if (rc == BLDFM_OK) {
+        cudaMemcpy(dA, Ab.data(), Ab.size() * 2, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, Bb.data(), Bb.size() * 2, cudaMemcpyHostToDevice);
+        cudaMemset(derr, 0, 4);
+        const size_t smem = tc_gemm_smem(KC);
+        cudaFuncSetAttribute(tc_gemm_kernel<StoreF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        StoreF32 epi{dD, 256};
+        tc_gemm_kernel<StoreF32><<<M / 128, 128, smem>>>(dA, dB, K, KC, epi, derr);
+        int herr = 0;
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = BLDFM_ERR_CUDA;
+        if (rc == BLDFM_OK && cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = BLDFM_ERR_CUDA;
+        if (rc == BLDFM_OK && herr != 0) rc = BLDFM_ERR_TIMEOUT;
+        if (rc == BLDFM_OK) cudaMemcpy(D, dD, (size_t)M * 256 * 4, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dD);
+    cudaFree(derr);
+    return rc;
+}
+
+// ===========================================================================
+// The MLP: 5 -> 256 -> 256 -> 256 -> 256 -> 4, GELU after each hidden layer.
+// Hidden 256 x 256 layers on tensor cores (BF16 operands, FP32 accumulation),
+// input and output layers on CUDA cores (FP32).  Parameters are FP32 masters
+// updated by Adam; the tensor-core layers read BF16 copies.
+//
+// Flat parameter vector: W0 [5][256] (in, out), b0 [256], then for j = 1..3
+// Wt_j [256][256] (out, in) and b_j [256], then W4 [256][4] (in, out), b4 [4].
+// ===========================================================================
+#define MLP_IN 5
+#define MLP_XS 8  // stride of the input rows
+#define MLP_H 256
+#define MLP_OUT 4
+#define MLP_OFF_W0 0
+#define MLP_OFF_B0 (MLP_IN * MLP_H)
+#define MLP_OFF_WT(j) (MLP_OFF_B0 + MLP_H + ((j)-1) * (MLP_H * MLP_H + MLP_H))
+#define MLP_OFF_B(j) (MLP_OFF_WT(j) + MLP_H * MLP_H)
+#define MLP_OFF_W4 (MLP_OFF_WT(4))
+#define MLP_OFF_B4 (MLP_OFF_W4 + MLP_H * MLP_OUT)
+#define MLP_NPARAM (MLP_OFF_B4 + MLP_OUT)
+
+namespace {
+
+__device__ __forceinline__ uint16_t f2bf(float f)
+{
+    return __bfloat16_as_ushort(__float2bfloat16_rn(f));
+}
+__device__ __forceinline__ float bf2f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+
+__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float z)
+{
+    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+// A CTA's 128 x 256 bf16 tile in core-matrix order (tc_core_offset) is copied
+// to the row blocks of its tile (contiguous 64 KB), and scattered into the
+// transposed layouts used as operands of the weight-gradient GEMM:
+//   mode 0 (B operand, H^T): blocks [chunk = sample / 256] of 256 x 256,
+//          element (feature, sample % 256)
+//   mode 1 (A operand, dZ^T): blocks [feature / 128][chunk] of 128 x 256,
+//          element (feature % 128, sample % 256)
+__device__ void emit_tile(int tile, const uint16_t *st, uint16_t *rows_dst, uint16_t *T_dst, int mode, int nchunks)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (rows_dst) {
+        const uint4 *s = (const uint4 *)st;
+        uint4 *d = (uint4 *)(rows_dst + (size_t)tile * 128 * MLP_H);
+        for (int i = tid; i < 128 * MLP_H / 8; i += nt) d[i] = s[i];
+    }
+    if (!T_dst) return;
+    const int chunk = tile >> 1, half = tile & 1;
+    // one 16-byte store per (feature, group of 8 samples): 256 x 16 per tile
+    for (int i = tid; i < MLP_H * 16; i += nt) {
+        const int f = i & (MLP_H - 1), g = i >> 8;  // consecutive threads: consecutive features
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int s0 = g * 8 + 2 * q;
+            const uint32_t lo = st[tc_core_offset(s0, f, MLP_H) / 2];
+            const uint32_t hi = st[tc_core_offset(s0 + 1, f, MLP_H) / 2];
+            w[q] = lo | (hi << 16);
+        }
+        const int s256 = half * 128 + g * 8;
+        size_t off;
+        if (mode == 0)
+            off = (size_t)chunk * MLP_H * 256 + tc_core_offset(f, s256, 256) / 2;
+        else
+            off = ((size_t)(f >> 7) * nchunks + chunk) * 128 * 256 + tc_core_offset(f & 127, s256, 256) / 2;
+        *(uint4 *)(T_dst + off) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// 8 consecutive values of one row into the smem tile (one 16-byte store)
+__device__ __forceinline__ void put8(uint16_t *st, int r, int c, const float *v)
+{
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q] = (uint32_t)f2bf(v[2 * q]) | ((uint32_t)f2bf(v[2 * q + 1]) << 16);
+    *(uint4 *)(st + tc_core_offset(r, c, MLP_H) / 2) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// forward hidden layer: Z = acc + b, H = gelu(Z) (bf16), G = gelu'(Z) (bf16)
+struct EpiFwd {
+    const float *bias;
+    uint16_t *rows_dst, *T_dst, *G_dst, *rowmajor_dst;
+    int nchunks;
+    __device__ void row(int r, int c0, const float *v, uint16_t *st) const
+    {
+        float h[32], gd[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            const float z = v[i] + bias[c0 + i];
+            h[i] = gelu_f(z);
+            gd[i] = gelu_d(z);
+        }
+        const int rl = r & 127;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) put8(st, rl, c0 + 8 * q, h + 8 * q);
+        uint32_t w[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = (uint32_t)f2bf(gd[2 * i]) | ((uint32_t)f2bf(gd[2 * i + 1]) << 16);
+        uint4 *g = (uint4 *)(G_dst + (size_t)r * MLP_H + c0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) g[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+        if (rowmajor_dst) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) w[i] = (uint32_t)f2bf(h[2 * i]) | ((uint32_t)f2bf(h[2 * i + 1]) << 16);
+            uint4 *o = (uint4 *)(rowmajor_dst + (size_t)r * MLP_H + c0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) o[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+        }
+    }
+    __device__ void finish(int tile, uint16_t *st) const { emit_tile(tile, st, rows_dst, T_dst, 0, nchunks); }
+};
+
+// backward data: dZ = bf16(acc * G); db += sum over rows of dZ
+struct EpiBwd {
+    const uint16_t *G;
+    uint16_t *rows_dst, *T_dst;
+    float *rowmajor_f32;  // dZ1 for the input layer's gradient
+    float *dbias;
+    int nchunks;
+    __device__ void row(int r, int c0, const float *v, uint16_t *st) const
+    {
+        float dz[32];
+        const uint4 *g4 = (const uint4 *)(G + (size_t)r * MLP_H + c0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 u = g4[q];
+            const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                dz[8 * q + 2 * k] = bf2f(f2bf(v[8 * q + 2 * k] * bf2f((uint16_t)(w[k] & 0xFFFF))));
+                dz[8 * q + 2 * k + 1] = bf2f(f2bf(v[8 * q + 2 * k + 1] * bf2f((uint16_t)(w[k] >> 16))));
+            }
+        }
+        if (rows_dst || T_dst) {
+            const int rl = r & 127;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) put8(st, rl, c0 + 8 * q, dz + 8 * q);
+        }
+        if (rowmajor_f32) {
+            float4 *o = (float4 *)(rowmajor_f32 + (size_t)r * MLP_H + c0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) o[q] = make_float4(dz[4 * q], dz[4 * q + 1], dz[4 * q + 2], dz[4 * q + 3]);
+        }
+        // bias gradient: sum the warp's 32 rows per column, one atomic per column
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            float s = dz[i];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+            if ((threadIdx.x & 31) == 0) atomicAdd(dbias + c0 + i, s);
+        }
+    }
+    __device__ void finish(int tile, uint16_t *st) const
+    {
+        if (rows_dst || T_dst) emit_tile(tile, st, rows_dst, T_dst, 1, nchunks);
+    }
+};
+
+// weight gradient partial sums: grad[out][in] += acc
+struct EpiGrad {
+    float *grad;
+    __device__ void row(int r, int c0, const float *v, uint16_t *) const
+    {
+        float *o = grad + (size_t)r * MLP_H + c0;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) atomicAdd(o + i, v[i]);
+    }
+    __device__ void finish(int, uint16_t *) const {}
+};
+
+// input layer forward: one CTA per 128-sample tile, thread = feature
+__global__ void __launch_bounds__(256) mlp_in_fwd_kernel(const float *__restrict__ X, const float *__restrict__ P,
+                                                         uint16_t *rows_dst, uint16_t *T_dst, uint16_t *G_dst,
+                                                         int nchunks)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint16_t *st = (uint16_t *)smem_raw;
+    const int f = threadIdx.x, tile = blockIdx.x;
+    float w[MLP_IN];
+#pragma unroll
+    for (int i = 0; i < MLP_IN; ++i) w[i] = P[MLP_OFF_W0 + i * MLP_H + f];
+    const float b = P[MLP_OFF_B0 + f];
+    for (int s = 0; s < 128; ++s) {
+        const int r = tile * 128 + s;
+        const float *x = X + (size_t)r * MLP_XS;
+        float z = b;
+#pragma unroll
+        for (int i = 0; i < MLP_IN; ++i) z = fmaf(x[i], w[i], z);
+        st[tc_core_offset(s, f, MLP_H) / 2] = f2bf(gelu_f(z));
+        G_dst[(size_t)r * MLP_H + f] = f2bf(gelu_d(z));
+    }
+    __syncthreads();
+    emit_tile(tile, st, rows_dst, T_dst, 0, nchunks);
+}
+
+// output layer forward (+ loss and the start of the backward pass when T is
+// given): one CTA per 128-sample tile, thread = sample
+__global__ void __launch_bounds__(128) mlp_out_kernel(const uint16_t *__restrict__ H4, const uint16_t *__restrict__ G4,
+                                                      const float *__restrict__ P, const float *__restrict__ T,
+                                                      const float *__restrict__ wts, float inv_n, float *Y,
+                                                      float *grad, float *loss, uint16_t *rows_dst, uint16_t *T_dst,
+                                                      int nchunks, int n)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint16_t *st = (uint16_t *)smem_raw;                          // dZ4 tile (64 KB)
+    float *sW = (float *)(smem_raw + 128 * MLP_H * 2);            // W4 [256][4]
+    float *sG = sW + MLP_H * MLP_OUT;                             // dW4 partial [256][4]
+    float *sdb = sG + MLP_H * MLP_OUT;                            // db3 partial [256]
+    __shared__ float sdb4[MLP_OUT], sloss;
+    const int t = threadIdx.x, tile = blockIdx.x;
+    for (int i = t; i < MLP_H * MLP_OUT; i += blockDim.x) {
+        sW[i] = P[MLP_OFF_W4 + i];
+        sG[i] = 0.f;
+    }
+    for (int i = t; i < MLP_H; i += blockDim.x) sdb[i] = 0.f;
+    if (t < MLP_OUT) sdb4[t] = 0.f;
+    if (t == 0) sloss = 0.f;
+    __syncthreads();
+    const int r = tile * 128 + t;
+    const bool live = r < n;
+    const uint4 *h4 = (const uint4 *)(H4 + (size_t)r * MLP_H);
+    float y[MLP_OUT];
+#pragma unroll
+    for (int o = 0; o < MLP_OUT; ++o) y[o] = P[MLP_OFF_B4 + o];
+    for (int q = 0; q < MLP_H / 8; ++q) {
+        const uint4 u = h4[q];
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float hv = bf2f((uint16_t)(k & 1 ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xFFFF)));
+            const int f = q * 8 + k;
+#pragma unroll
+            for (int o = 0; o < MLP_OUT; ++o) y[o] = fmaf(hv, sW[f * MLP_OUT + o], y[o]);
+        }
+    }
+    if (Y && live)
+        for (int o = 0; o < MLP_OUT; ++o) Y[(size_t)r * MLP_OUT + o] = y[o];
+    if (!T) return;
+    float dy[MLP_OUT];
+    float l = 0.f;
+    const float wb = live ? wts[r] : 0.f;
+#pragma unroll
+    for (int o = 0; o < MLP_OUT; ++o) {
+        const float e = live ? (y[o] - T[(size_t)r * MLP_OUT + o]) : 0.f;
+        l = fmaf(wb * e, e, l);
+        dy[o] = 2.f * wb * e * inv_n;
+    }
+    atomicAdd(&sloss, l * inv_n);
+#pragma unroll
+    for (int o = 0; o < MLP_OUT; ++o) atomicAdd(&sdb4[o], dy[o]);
+    for (int q = 0; q < MLP_H / 8; ++q) {
+        const uint4 u = h4[q];
+        const uint4 g = ((const uint4 *)(G4 + (size_t)r * MLP_H))[q];
+        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+        const uint32_t gw[4] = {g.x, g.y, g.z, g.w};
+        float dz[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int f = q * 8 + k;
+            const float hv = bf2f((uint16_t)(k & 1 ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xFFFF)));
+            const float gv = bf2f((uint16_t)(k & 1 ? (gw[k >> 1] >> 16) : (gw[k >> 1] & 0xFFFF)));
+            float dh = 0.f;
+#pragma unroll
+            for (int o = 0; o < MLP_OUT; ++o) {
+                dh = fmaf(dy[o], sW[f * MLP_OUT + o], dh);
+                atomicAdd(&sG[f * MLP_OUT + o], hv * dy[o]);
+            }
+            dz[k] = bf2f(f2bf(dh * gv));
+            atomicAdd(&sdb[f], dz[k]);
+        }
+        put8(st, t, q * 8, dz);
+    }
+    __syncthreads();
+    for (int i = t; i < MLP_H * MLP_OUT; i += blockDim.x) atomicAdd(grad + MLP_OFF_W4 + i, sG[i]);
+    for (int i = t; i < MLP_H; i += blockDim.x) atomicAdd(grad + MLP_OFF_B(3) + i, sdb[i]);
+    if (t < MLP_OUT) atomicAdd(grad + MLP_OFF_B4 + t, sdb4[t]);
+    if (t == 0) atomicAdd(loss, sloss);
+    emit_tile(tile, st, rows_dst, T_dst, 1, nchunks);
+}
+
+// input layer weight gradient: dW0[i][f] += sum_b X[b][i] dZ1[b][f]
+__global__ void __launch_bounds__(256) mlp_in_grad_kernel(const float *__restrict__ X, const float *__restrict__ dZ1,
+                                                          float *grad, int n)
+{
+    const int f = threadIdx.x;
+    float acc[MLP_IN] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int r0 = blockIdx.x * 128, r1 = min(n, r0 + 128);
+    for (int r = r0; r < r1; ++r) {
+        const float d = dZ1[(size_t)r * MLP_H + f];
+#pragma unroll
+        for (int i = 0; i < MLP_IN; ++i) acc[i] = fmaf(X[(size_t)r * MLP_XS + i], d, acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < MLP_IN; ++i) atomicAdd(grad + MLP_OFF_W0 + i * MLP_H + f, acc[i]);
+}
+
+__global__ void adam_kernel(float *P, const float *G, float *m, float *v, int n, float lr, float b1, float b2,
+                            float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float g = G[i];
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    P[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+// BF16 operand blocks of the hidden weights: Wt_j (rows out, K in) for the
+// forward GEMM, W_j (rows in, K out) for the backward-data GEMM
+__global__ void weights_to_blocks_kernel(const float *__restrict__ P, uint16_t *Wt1, uint16_t *Wt2, uint16_t *Wt3,
+                                         uint16_t *W1, uint16_t *W2, uint16_t *W3)
+{
+    const int j = blockIdx.y + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;  // out * 256 + in
+    if (e >= MLP_H * MLP_H) return;
+    const int out = e >> 8, in = e & 255;
+    const uint16_t b = f2bf(P[MLP_OFF_WT(j) + e]);
+    uint16_t *wt = j == 1 ? Wt1 : (j == 2 ? Wt2 : Wt3);
+    uint16_t *w = j == 1 ? W1 : (j == 2 ? W2 : W3);
+    wt[tc_core_offset(out, in, MLP_H) / 2] = b;
+    w[tc_core_offset(in, out, MLP_H) / 2] = b;
+}
+
+struct Mlp {
+    int B = 0;  // batch capacity, multiple of 256
+    int step = 0;
+    float *P = nullptr, *G = nullptr, *m = nullptr, *v = nullptr;
+    uint16_t *Wt[3] = {}, *W[3] = {};
+    uint16_t *Hrows[3] = {}, *HT[3] = {}, *H4 = nullptr;
+    uint16_t *Gz[4] = {};
+    uint16_t *dZrows[3] = {}, *dZT[3] = {};  // index j-2 for dZ_j, j = 2..4
+    float *dZ1 = nullptr, *Y = nullptr, *loss = nullptr;
+    int *err = nullptr;
+    std::vector<void *> allocs;
+};
+
+template <typename T>
+bool mlp_alloc(Mlp &M, T **p, size_t count)
+{
+    void *q = nullptr;
+    if (cudaMalloc(&q, count * sizeof(T)) != cudaSuccess) return false;
+    M.allocs.push_back(q);
+    *p = (T *)q;
+    return true;
+}
+
+void mlp_free(Mlp *M)
+{
+    for (void *p : M->allocs) cudaFree(p);
+    delete M;
+}
+
+template <class Epi>
+cudaError_t gemm(const uint16_t *A, const uint16_t *Bop, int tiles, int K, int splits, Epi epi, int *err,
+                 cudaStream_t st)
+{
+    const size_t smem = tc_gemm_smem(256);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(tc_gemm_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    tc_gemm_kernel<Epi><<<dim3(tiles, splits), 128, smem, st>>>(A, Bop, K, 256, epi, err);
+    return cudaGetLastError();
+}
+
+// forward pass through the hidden layers; H4 / G4 left for the output layer
+cudaError_t mlp_forward_hidden(Mlp &M, const float *X, int n, cudaStream_t st)
+{
+    const int tiles = n / 128, nchunks = n / 256;
+    cudaFuncSetAttribute(mlp_in_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * MLP_H * 2);
+    mlp_in_fwd_kernel<<<tiles, 256, 128 * MLP_H * 2, st>>>(X, M.P, M.Hrows[0], M.HT[0], M.Gz[0], nchunks);
+    for (int j = 1; j <= 3; ++j) {
+        EpiFwd e;
+        e.bias = M.P + MLP_OFF_B(j);
+        e.rows_dst = j < 3 ? M.Hrows[j] : nullptr;
+        e.T_dst = j < 3 ? M.HT[j] : nullptr;
+        e.G_dst = M.Gz[j];
+        e.rowmajor_dst = j == 3 ? M.H4 : nullptr;
+        e.nchunks = nchunks;
+        cudaError_t c = gemm(M.Hrows[j - 1], M.Wt[j - 1], tiles, MLP_H, 1, e, M.err, st);
+        if (c != cudaSuccess) return c;
+    }
+    return cudaGetLastError();
+}
+
+const size_t OUT_SMEM = 128 * MLP_H * 2 + (2 * MLP_H * MLP_OUT + MLP_H) * 4;
+
+}  // namespace
+
+extern "C" {
+
+int bldfm_surrogate_create(int32_t batch, uint64_t seed, void **handle)
+{
+    if (!handle || batch < 256 || batch % 256 != 0) return BLDFM_ERR_ARG;
+    Mlp *M = new Mlp();
+    M->B = batch;
+    const size_t B = (size_t)batch;
+    bool ok = mlp_alloc(*M, &M->P, MLP_NPARAM) && mlp_alloc(*M, &M->G, MLP_NPARAM) &&
+              mlp_alloc(*M, &M->m, MLP_NPARAM) && mlp_alloc(*M, &M->v, MLP_NPARAM) &&
+              mlp_alloc(*M, &M->H4, B * MLP_H) && mlp_alloc(*M, &M->dZ1, B * MLP_H) &&
+              mlp_alloc(*M, &M->Y, B * MLP_OUT) && mlp_alloc(*M, &M->loss, 1) && mlp_alloc(*M, &M->err, 1);
+    for (int j = 0; j < 3 && ok; ++j)
+        ok = mlp_alloc(*M, &M->Wt[j], (size_t)MLP_H * MLP_H) && mlp_alloc(*M, &M->W[j], (size_t)MLP_H * MLP_H) &&
+             mlp_alloc(*M, &M->Hrows[j], B * MLP_H) && mlp_alloc(*M, &M->HT[j], B * MLP_H) &&
+             mlp_alloc(*M, &M->dZrows[j], B * MLP_H) && mlp_alloc(*M, &M->dZT[j], B * MLP_H);
+    for (int j = 0; j < 4 && ok; ++j) ok = mlp_alloc(*M, &M->Gz[j], B * MLP_H);
+    if (!ok) {
+        mlp_free(M);
+        return BLDFM_ERR_CUDA;
+    }
+    // He-scaled normal weights (Box-Muller on a 64-bit LCG), zero biases
+    std::vector<float> p(MLP_NPARAM, 0.f);
+    uint64_t s = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto unif = [&]() {
+        s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+        return ((s >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    auto normal = [&]() { return sqrt(-2.0 * log(unif())) * cos(6.283185307179586 * unif()); };
+    for (int i = 0; i < MLP_IN * MLP_H; ++i) p[MLP_OFF_W0 + i] = (float)(normal() * sqrt(2.0 / MLP_IN));
+    for (int j = 1; j <= 3; ++j)
+        for (int i = 0; i < MLP_H * MLP_H; ++i) p[MLP_OFF_WT(j) + i] = (float)(normal() * sqrt(2.0 / MLP_H));
+    for (int i = 0; i < MLP_H * MLP_OUT; ++i) p[MLP_OFF_W4 + i] = (float)(normal() * sqrt(1.0 / MLP_H));
+    cudaMemcpy(M->P, p.data(), MLP_NPARAM * 4, cudaMemcpyHostToDevice);
+    cudaMemset(M->m, 0, MLP_NPARAM * 4);
+    cudaMemset(M->v, 0, MLP_NPARAM * 4);
+    cudaMemset(M->G, 0, MLP_NPARAM * 4);
+    cudaMemset(M->err, 0, 4);
+    weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, M->Wt[0], M->Wt[1], M->Wt[2], M->W[0],
+                                                                  M->W[1], M->W[2]);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        mlp_free(M);
+        return BLDFM_ERR_CUDA;
+    }
+    *handle = M;
+    return BLDFM_OK;
+}
+
+int bldfm_surrogate_destroy(void *handle)
+{
+    if (!handle) return BLDFM_ERR_ARG;
+    cudaDeviceSynchronize();
+    mlp_free((Mlp *)handle);
+    return BLDFM_OK;
+}
+
+int bldfm_surrogate_nparams(void) { return MLP_NPARAM; }
+
+// get (host_out != NULL) and/or set (host_in != NULL) the FP32 parameters
+int bldfm_surrogate_params(void *handle, float *host_out, const float *host_in)
+{
+    Mlp *M = (Mlp *)handle;
+    if (!M) return BLDFM_ERR_ARG;
+    if (cudaDeviceSynchronize() != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (host_out && cudaMemcpy(host_out, M->P, MLP_NPARAM * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return BLDFM_ERR_CUDA;
+    if (host_in) {
+        if (cudaMemcpy(M->P, host_in, MLP_NPARAM * 4, cudaMemcpyHostToDevice) != cudaSuccess) return BLDFM_ERR_CUDA;
+        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, M->Wt[0], M->Wt[1], M->Wt[2], M->W[0],
+                                                                      M->W[1], M->W[2]);
+        if (cudaDeviceSynchronize() != cudaSuccess) return BLDFM_ERR_CUDA;
+    }
+    return BLDFM_OK;
+}
+
+// gradients of the last training step and its loss
+int bldfm_surrogate_grads(void *handle, float *host_grads, float *host_loss)
+{
+    Mlp *M = (Mlp *)handle;
+    if (!M) return BLDFM_ERR_ARG;
+    if (cudaDeviceSynchronize() != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (host_grads && cudaMemcpy(host_grads, M->G, MLP_NPARAM * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return BLDFM_ERR_CUDA;
+    if (host_loss && cudaMemcpy(host_loss, M->loss, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BLDFM_ERR_CUDA;
+    int e = 0;
+    if (cudaMemcpy(&e, M->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BLDFM_ERR_CUDA;
+    return e != 0 ? BLDFM_ERR_TIMEOUT : BLDFM_OK;
+}
+
+// One Adam step on n samples (n <= batch, n % 256 == 0): X [n][8] inputs
+// (5 used), T [n][4] targets, w [n] loss weights, all device pointers.
+// loss = sum_b w_b |y_b - t_b|^2 / n.  lr = 0 computes gradients only.
+int bldfm_surrogate_train_step(void *handle, const float *X, const float *T, const float *w, int32_t n, float lr,
+                               void *stream)
+{
+    Mlp *M = (Mlp *)handle;
+    if (!M || !X || !T || !w || n < 256 || n > M->B || n % 256 != 0) return BLDFM_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int tiles = n / 128, nchunks = n / 256;
+    if (cudaMemsetAsync(M->G, 0, MLP_NPARAM * 4, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (cudaMemsetAsync(M->loss, 0, 4, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (mlp_forward_hidden(*M, X, n, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    cudaFuncSetAttribute(mlp_out_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM);
+    mlp_out_kernel<<<tiles, 128, OUT_SMEM, st>>>(M->H4, M->Gz[3], M->P, T, w, 1.0f / n, M->Y, M->G, M->loss,
+                                                 M->dZrows[2], M->dZT[2], nchunks, n);
+    // hidden layers, last to first: dW_j from dZ_{j+1}^T and H_j^T, dH_j from dZ_{j+1} and W_j
+    for (int j = 3; j >= 1; --j) {
+        EpiGrad eg;
+        eg.grad = M->G + MLP_OFF_WT(j);
+        const int splits = nchunks < 64 ? nchunks : 64;
+        if (gemm(M->dZT[j - 1], M->HT[j - 1], 2, n, splits, eg, M->err, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+        EpiBwd eb;
+        eb.G = M->Gz[j - 1];
+        eb.rows_dst = j > 1 ? M->dZrows[j - 2] : nullptr;
+        eb.T_dst = j > 1 ? M->dZT[j - 2] : nullptr;
+        eb.rowmajor_f32 = j == 1 ? M->dZ1 : nullptr;
+        eb.dbias = M->G + (j > 1 ? MLP_OFF_B(j - 1) : MLP_OFF_B0);
+        eb.nchunks = nchunks;
+        if (gemm(M->dZrows[j - 1], M->W[j - 1], tiles, MLP_H, 1, eb, M->err, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    }
+    mlp_in_grad_kernel<<<tiles, 256, 0, st>>>(X, M->dZ1, M->G, n);
+    if (lr != 0.f) {
+        M->step += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f / (1.f - powf(b1, (float)M->step)), c2 = 1.f / (1.f - powf(b2, (float)M->step));
+        adam_kernel<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(M->P, M->G, M->m, M->v, MLP_NPARAM, lr, b1, b2, 1e-8f,
+                                                              c1, c2);
+        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256, 0, st>>>(M->P, M->Wt[0], M->Wt[1], M->Wt[2],
+                                                                             M->W[0], M->W[1], M->W[2]);
+    }
+    return cudaGetLastError() == cudaSuccess ? BLDFM_OK : BLDFM_ERR_CUDA;
+}
+
+// Y [n][4] = MLP(X [n][8]), n % 256 == 0, device pointers
+int bldfm_surrogate_forward(void *handle, const float *X, float *Y, int32_t n, void *stream)
+{
+    Mlp *M = (Mlp *)handle;
+    if (!M || !X || !Y || n < 256 || n > M->B || n % 256 != 0) return BLDFM_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (mlp_forward_hidden(*M, X, n, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    cudaFuncSetAttribute(mlp_out_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM);
+    mlp_out_kernel<<<n / 128, 128, OUT_SMEM, st>>>(M->H4, M->Gz[3], M->P, nullptr, nullptr, 0.f, Y, nullptr, nullptr,
+                                                   nullptr, nullptr, n / 256, n);
+    return cudaGetLastError() == cudaSuccess ? BLDFM_OK : BLDFM_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -180,6 +180,35 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases,
                       const bldfm_batch_opts *opts, void *workspace,
                       size_t workspace_bytes, void *stream);
 
+/* ---- surrogate building blocks ----------------------------------------- */
+
+/* Check of the tcgen05 BF16 tensor-core GEMM the surrogate MLP runs on (no
+ * reference counterpart): D (M x 256, FP32) = A (M x K) * B (256 x K)^T with
+ * A, B row-major BF16 bit patterns on the host, M % 128 == 0, K % 16 == 0. */
+int bldfm_tc_gemm_check(const uint16_t *A, const uint16_t *B, float *D,
+                        int32_t M, int32_t K);
+
+/* The surrogate MLP (no reference counterpart): inputs (5 features, rows of
+ * 8 floats) -> 4 x 256 GELU hidden layers -> 4 outputs.  The three 256 x 256
+ * layers run forward and backward on the tcgen05 tensor cores (BF16 operands,
+ * FP32 accumulation in tensor memory); FP32 master weights, Adam.  The handle
+ * owns device buffers for up to `batch` samples (multiple of 256). */
+int bldfm_surrogate_create(int32_t batch, uint64_t seed, void **handle);
+int bldfm_surrogate_destroy(void *handle);
+int bldfm_surrogate_nparams(void);
+/* get (host_out) and/or set (host_in) the FP32 parameter vector */
+int bldfm_surrogate_params(void *handle, float *host_out, const float *host_in);
+/* gradients and loss of the last training step */
+int bldfm_surrogate_grads(void *handle, float *host_grads, float *host_loss);
+/* one Adam step on n samples (device X [n][8], T [n][4], w [n]); lr = 0
+ * computes the gradients only */
+int bldfm_surrogate_train_step(void *handle, const float *X, const float *T,
+                               const float *w, int32_t n, float lr,
+                               void *stream);
+/* Y [n][4] = MLP(X [n][8]), device pointers, n % 256 == 0 */
+int bldfm_surrogate_forward(void *handle, const float *X, float *Y, int32_t n,
+                            void *stream);
+
 /* Allocation-free FP32 solve.  No counterpart in the reference (which never
  * touches a GPU).  For callers that may not allocate device memory while they
  * solve: work enqueued inside a CUDA stream capture, hosts that reserve all
