@@ -17,6 +17,8 @@ Reported:
   e2e            the public batched API solve_batch (numpy in, numpy out,
                  host<->device copies inside); also the single-case drop-in
   roofline       the batched sweep kernel against the measured FP32 FMA peak
+  surrogate      the learned surrogate (trained weights in
+                 bldfm_gb300/weights): footprints/s and relL2 against FP64
   cpu_baseline   the CPU oracle port (reference arithmetic, OpenMP on all
                  host cores) on a bounded sample
 
@@ -205,6 +207,80 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world):
+    """Footprints/s of the surrogate on batch 0's met cases (device-resident
+    outputs, descriptors prepared once), its relL2 against the FP64 path, and
+    the training throughput of the tensor-core MLP kernels."""
+    import torch
+
+    from bldfm_gb300 import surrogate as S
+    from bldfm_gb300.mlp import MLP
+
+    if not os.path.exists(S.WEIGHTS):
+        return {"unavailable": "no trained weights at bldfm_gb300/weights (python -m bldfm_gb300.surrogate train)"}
+    net, box, meta = S.load(S.WEIGHTS)
+    sur = S.Surrogate(net, spot_every=0)
+    preps, in_box = [], []
+    for (z, p), c in zip(inputs, met_cases(B, seed=1000 + 97 * int(os.environ.get("RANK", "0")))):
+        wd = np.deg2rad(c["wind_dir"])
+        wind = (-c["wind_speed"] * np.sin(wd), -c["wind_speed"] * np.cos(wd))
+        kw = dict(n=N_LEVELS, zm=ZM, wind=wind, srf_shape=(NY, NX), domain=DOMAIN, modes=MODES, meas_pt=MEAS,
+                  ustar=c["ustar"], mol=c["mol"])
+        pr = sur.prepare(**kw)
+        preps.append(pr)
+        s1, s2, _ = pr["s"]
+        in_box.append(sur.in_box(N_LEVELS, ZM, s1, s2, S.mode_kmax((NY, NX), DOMAIN, MODES)))
+    outs = [(torch.empty((NY, NX), dtype=torch.float64, device=dev), torch.empty((NY, NX), dtype=torch.float64,
+                                                                                 device=dev)) for _ in preps]
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        for pr, (c, f) in zip(preps, outs):
+            sur.solve_prepared(pr, c, f)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        for pr, (c, f) in zip(preps, outs):
+            sur.solve_prepared(pr, c, f)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    errs = []
+    for (c, f), b in zip(outs, s64):
+        cb, fb = b[3].cpu().numpy(), b[4].cpu().numpy()
+        ca, fa = c.cpu().numpy(), f.cpu().numpy()
+        errs.append(max(np.linalg.norm(ca - cb) / np.linalg.norm(cb), np.linalg.norm(fa - fb) / np.linalg.norm(fb)))
+    # training throughput of the project's forward/backward kernels (batch 65536)
+    pool = S.TransferPool(ncases=1024, seed=5)
+    tnet = MLP(batch=65536, seed=9)
+    S.train(tnet, pool, 3, batch=65536, log_every=1000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nsteps = 20
+    S.train(tnet, pool, nsteps, batch=65536, log_every=1000)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    return {
+        "value": world * B * args.steps / (ms * 1e-3),
+        "unit": "footprints/s",
+        "ms_per_footprint": ms / (args.steps * B),
+        "relL2_vs_fp64_max": max(errs),
+        "relL2_vs_fp64_median": float(np.median(errs)),
+        "in_box": int(sum(in_box)),
+        "kernel": "sur_serve_kernel (features -> 8x256 -> 3x tcgen05 256x256 BF16 -> 256x4 -> spectra) + output FFT",
+        "weights": {"box": box, **{k: meta[k] for k in meta if k in ("steps", "batch", "val_loss", "train_s")}},
+        "training": {"ms_per_step": train_s / nsteps * 1e3, "samples_per_s": 65536 * nsteps / train_s,
+                     "batch": 65536},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,6 +459,9 @@ def main():
         e32x.append(max(np.linalg.norm(ca - cr) / np.linalg.norm(cr), np.linalg.norm(fa - fr) / np.linalg.norm(fr)))
         e64x.append(max(np.linalg.norm(cb - cr) / np.linalg.norm(cr), np.linalg.norm(fb - fr) / np.linalg.norm(fr)))
 
+    # --- learned surrogate: fused features -> tcgen05 MLP -> spectra, trained weights ---
+    sur_line = surrogate_section(kwb, inputs, s64, B, args, dev, dist, world)
+
     # --- e2e through the public batched API (numpy in, numpy out) ---
     esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True)
     e2e_steps = max(2, args.steps // 2)
@@ -471,6 +550,7 @@ def main():
                 "traffic": None,
                 "flops_per_launch": flops_launch,
             },
+            "surrogate": sur_line,
             "cpu_baseline": cpu,
             "gpu_launches": 3 * args.steps,
             "clocks": clk.summary(),

@@ -94,6 +94,20 @@ class BatchOpts(ctypes.Structure):
     ]
 
 
+class SurrogateCase(ctypes.Structure):
+    """bldfm_surrogate_case: the met scalars of one surrogate footprint."""
+
+    _fields_ = [
+        ("zm", ctypes.c_double),
+        ("wind", ctypes.c_double),
+        ("s1", ctypes.c_double),
+        ("s2", ctypes.c_double),
+        ("s3", ctypes.c_double),
+        ("variant", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 _P = ctypes.c_void_p
 _SIGS = {
     "bldfm_status_str": (ctypes.c_char_p, [ctypes.c_int]),
@@ -144,6 +158,29 @@ _SIGS = {
     "bldfm_surrogate_grads": (ctypes.c_int, [_P, _P, _P]),
     "bldfm_surrogate_train_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, ctypes.c_float, _P]),
     "bldfm_surrogate_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
+    "bldfm_surrogate_batch": (ctypes.c_int, [_P]),
+    "bldfm_transfer_pool_create": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_P)]),
+    "bldfm_transfer_pool_destroy": (ctypes.c_int, [_P]),
+    "bldfm_transfer_pool_case": (
+        ctypes.c_int,
+        [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)],
+    ),
+    "bldfm_transfer_samples": (
+        ctypes.c_int,
+        [_P, ctypes.c_uint64, ctypes.c_int32, ctypes.c_float, ctypes.c_float, _P, ctypes.c_float, _P, _P, _P, _P, _P],
+    ),
+    "bldfm_transfer_eval": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int32, _P]),
+    "bldfm_point_measurement_workspace": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int32]),
+    "bldfm_point_measurement": (
+        ctypes.c_int,
+        [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P],
+    ),
+    "bldfm_surrogate_plan": (ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
+    "bldfm_surrogate_solve": (
+        ctypes.c_int,
+        [_P, ctypes.POINTER(Desc), ctypes.POINTER(SurrogateCase), _P, _P, _P, ctypes.c_int32, _P, _P, _P,
+         ctypes.c_size_t, _P],
+    ),
     "bldfm_solve_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P],

@@ -1,0 +1,120 @@
+"""Green's-function cache in GPU memory (reference: GreensFunctionCache,
+src/bldfm/cache.py:19-83).
+
+In footprint mode the solver's output depends only on the vertical grid and
+profiles, the domain, modes, measurement point, halo and precision, never on
+the surface flux.  The reference keeps such results as ``<sha256>.npz`` files
+on disk.  Here entries live in HBM (least-recently-used eviction above
+``max_bytes``), so a footprint timeseries that revisits a met state reuses
+the device result without a solve or a host round trip (``get_device``).
+The key is the reference's (same hash inputs in the same order), and with
+``cache_dir`` set entries are also written to and read from disk in the
+reference's file format, so the two caches can share a directory.
+
+``get``/``put``/``clear`` keep the reference's signatures, so the object can
+be passed as ``cache=`` to ``steady_state_transport_solver``.
+"""
+
+import collections
+import hashlib
+from pathlib import Path
+
+import numpy as np
+import torch
+
+
+def cache_key(z, profiles, domain, modes, meas_pt, halo, precision):
+    """SHA-256 hex digest of the solver inputs (cache.py:34-45)."""
+    h = hashlib.sha256()
+    h.update(np.asarray(z).tobytes())
+    for arr in profiles:
+        h.update(np.asarray(arr).tobytes())
+    h.update(np.asarray(domain).tobytes())
+    h.update(np.asarray(modes).tobytes())
+    h.update(np.asarray(meas_pt).tobytes())
+    h.update(str(halo).encode())
+    h.update(precision.encode())
+    return h.hexdigest()
+
+
+class GreensFunctionCache:
+    def __init__(self, cache_dir=None, max_bytes=8 << 30, device=None):
+        self.cache_dir = None if cache_dir is None else Path(cache_dir)
+        if self.cache_dir is not None:
+            self.cache_dir.mkdir(parents=True, exist_ok=True)
+        self.max_bytes = int(max_bytes)
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        self._entries = collections.OrderedDict()  # key -> (grid, conc_dev, flx_dev, host dtype)
+        self._bytes = 0
+        self.hits = 0
+        self.misses = 0
+
+    def _compute_key(self, z, profiles, domain, modes, meas_pt, halo, precision):
+        return cache_key(z, profiles, domain, modes, meas_pt, halo, precision)
+
+    def _insert(self, key, grid, conc, flx):
+        if key in self._entries:
+            self._drop(key)
+        c = torch.as_tensor(np.ascontiguousarray(conc)).to(self.device, non_blocking=False)
+        f = torch.as_tensor(np.ascontiguousarray(flx)).to(self.device, non_blocking=False)
+        self._entries[key] = (grid, c, f, np.asarray(conc).dtype)
+        self._bytes += c.numel() * c.element_size() + f.numel() * f.element_size()
+        while self._bytes > self.max_bytes and len(self._entries) > 1:
+            self._drop(next(iter(self._entries)))
+
+    def _drop(self, key):
+        _, c, f, _ = self._entries.pop(key)
+        self._bytes -= c.numel() * c.element_size() + f.numel() * f.element_size()
+
+    def _lookup(self, key):
+        e = self._entries.get(key)
+        if e is not None:
+            self._entries.move_to_end(key)
+            return e
+        if self.cache_dir is not None:
+            path = self.cache_dir / f"{key}.npz"
+            if path.exists():
+                data = np.load(path)
+                self._insert(key, (data["X"], data["Y"], data["Z"]), data["conc"], data["flx"])
+                return self._entries[key]
+        return None
+
+    def get(self, z, profiles, domain, modes, meas_pt, halo, precision):
+        """(grid, conc, flx) as host arrays, or None on a miss."""
+        e = self._lookup(self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision))
+        if e is None:
+            self.misses += 1
+            return None
+        self.hits += 1
+        grid, c, f, dt = e
+        return grid, c.cpu().numpy().astype(dt, copy=False), f.cpu().numpy().astype(dt, copy=False)
+
+    def get_device(self, z, profiles, domain, modes, meas_pt, halo, precision):
+        """(conc, flx) as device tensors (shared with the cache: do not modify), or None."""
+        e = self._lookup(self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision))
+        if e is None:
+            self.misses += 1
+            return None
+        self.hits += 1
+        return e[1], e[2]
+
+    def put(self, z, profiles, domain, modes, meas_pt, halo, precision, grid, conc, flx):
+        """Store a result (in HBM, and on disk when cache_dir is set)."""
+        key = self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision)
+        self._insert(key, grid, conc, flx)
+        if self.cache_dir is not None:
+            X, Y, Z = grid
+            np.savez(self.cache_dir / f"{key}.npz", X=X, Y=Y, Z=Z, conc=conc, flx=flx)
+
+    def clear(self):
+        """Drop every entry (and the disk files, like the reference)."""
+        self._entries.clear()
+        self._bytes = 0
+        if self.cache_dir is not None:
+            for f in self.cache_dir.glob("*.npz"):
+                f.unlink()
+
+    def __len__(self):
+        return len(self._entries)

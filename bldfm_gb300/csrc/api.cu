@@ -16,6 +16,8 @@
 #include "common.h"
 #include "host_exact.h"
 #include "kernels.h"
+#include "serve.h"
+#include "surrogate_phys.cuh"
 
 #ifndef BLDFM_VERSION_STR
 #define BLDFM_VERSION_STR "bldfm_gb300 0.1 sm_103a"
@@ -941,6 +943,139 @@ std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B,
     return k;
 }
 
+
+// ---------------------------------------------------------------------------
+// surrogate serving (bldfm_surrogate_solve): FP32 footprint solve whose
+// per-mode sweep is replaced by the MLP's transfer at z_m
+// ---------------------------------------------------------------------------
+struct SurLayout {
+    Layout L;
+    size_t X, Y, steps, tcase, total;
+    int64_t npad;
+};
+
+SurLayout sur_layout(const SolveGeom &g)
+{
+    SurLayout S;
+    S.L = layout_for(g);
+    S.npad = std::max<int64_t>((g.nsolved + 255) / 256 * 256, 256);
+    size_t o = S.L.total;
+    S.X = o;
+    o = al(o + (size_t)S.npad * 32);
+    S.Y = o;
+    o = al(o + (size_t)S.npad * 16);
+    S.steps = o;
+    o = al(o + (size_t)std::max(g.nz - 1, 1) * 16);
+    S.tcase = o;
+    o = al(o + sizeof(TransferCase));
+    S.total = o;
+    return S;
+}
+
+int sur_check_desc(const bldfm_desc *d, int nlvls)
+{
+    if (!d) return BLDFM_ERR_ARG;
+    if (d->mode != BLDFM_MODE_FP32 || !d->footprint || d->analytic || nlvls != 1) return BLDFM_ERR_UNSUPPORTED;
+    return BLDFM_OK;
+}
+
+int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *met, const double *z,
+                   const double *prof, const int64_t *levels, int nlvls, double *conc, double *flx, void *ws,
+                   size_t ws_bytes, cudaStream_t st)
+{
+    if (!met || !z || !prof || !levels || !conc || !flx || !ws || (met->variant != 1 && !net) || met->variant < 0 ||
+        met->variant > 2)
+        return BLDFM_ERR_ARG;
+    int rc = sur_check_desc(d, nlvls);
+    if (rc != BLDFM_OK) return rc;
+    HostPlan hp;
+    if ((rc = make_plan(d, z, prof, levels, nlvls, hp)) != BLDFM_OK) return rc;
+    const SolveGeom g = hp.g;
+    if (!g.iso) return BLDFM_ERR_UNSUPPORTED;
+    const int nz = g.nz;
+    const int64_t lev = levels[0] < 0 ? levels[0] + nz : levels[0];
+    if (!(met->zm > 0) || !(met->wind > 0) || fabs(z[lev] - met->zm) > 1e-6 * met->zm) return BLDFM_ERR_ARG;
+    const SurLayout S = sur_layout(g);
+    if (ws_bytes < S.total) return BLDFM_ERR_WORKSPACE;
+    if (((uintptr_t)ws & 255) != 0) return BLDFM_ERR_ARG;
+    int status = BLDFM_OK;
+    DeviceCache &dc = cache_for_current(&status);
+    if (status != BLDFM_OK) return status;
+    ModeList *ml = nullptr;
+    TwTable *twxo = nullptr, *twyo = nullptr;
+    int4 *xband = nullptr;
+    if ((rc = get_modes(dc, g.nlx, g.nly, &ml)) != BLDFM_OK) return rc;
+    if ((rc = get_tw(dc, g.nfx, &twxo)) != BLDFM_OK) return rc;
+    if ((rc = get_tw(dc, g.nfy, &twyo)) != BLDFM_OK) return rc;
+    if ((rc = get_xband(dc, hp, &xband)) != BLDFM_OK) return rc;
+
+    char *w = (char *)ws;
+    // host data: FP64 level table (for the k = 0 values), k = 0 values, and
+    // in the check mode the nondimensional step table of this case
+    const size_t lv64b = (size_t)std::max(nz - 1, 0) * BLDFM_LV64 * 8;
+    const size_t dcb = 32, stb = (size_t)std::max(nz - 1, 1) * 16;
+    const size_t off_dc = al(lv64b), off_st = off_dc + al(dcb), off_tc = off_st + al(stb);
+    StageSlot *slt = nullptr;
+    if ((rc = acquire_stage(dc, off_tc + al(sizeof(TransferCase)) + 256, &slt)) != BLDFM_OK) return rc;
+    char *sg = (char *)slt->buf;
+    hx_level_table(nz, z, prof, (double *)sg);
+    hx_dc_values(nz, (const double *)sg, hp.slot.data(), g.q0dc_fp, 0.0, d->srf_bg_conc, 1, 1, 0,
+                 (double *)(sg + off_dc));
+    const float zm = (float)met->zm;
+    const double *u_ = prof, *v_ = prof + nz, *Kz_ = prof + 4 * nz;
+    const float ktop = (float)(Kz_[nz - 1] / (met->wind * met->zm));
+    const float utop = (float)((u_[nz - 1] * g.ex + v_[nz - 1] * g.ey) / met->wind);
+    const bool exact = met->variant == 1;
+    if (exact) {
+        surrogate_steps_from_profiles(nz, z, prof, met->zm, met->wind, g.ex, g.ey, (float4 *)(sg + off_st));
+        TransferCase *tc = (TransferCase *)(sg + off_tc);
+        tc->nz = nz;
+        tc->jm = (int)lev;
+        tc->ktop = ktop;
+        tc->utop = utop;
+        tc->s1 = (float)met->s1;
+        tc->s2 = (float)met->s2;
+        tc->s3 = (float)met->s3;
+        tc->pad = 0;
+    }
+    double2 *dcv = (double2 *)(w + S.L.dc);
+    CK(cudaMemsetAsync(w + S.L.err, 0, 64, st));
+    CK(cudaMemcpyAsync(dcv, sg + off_dc, dcb, cudaMemcpyHostToDevice, st));
+    if (exact) {
+        CK(cudaMemcpyAsync(w + S.steps, sg + off_st, stb, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(w + S.tcase, sg + off_tc, sizeof(TransferCase), cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaEventRecord(slt->ev, st));
+    const float ax = (float)(g.lx_scale * g.valx), ay = (float)(g.ly_scale * g.valy);
+    float *X = (float *)(w + S.X), *Y = (float *)(w + S.Y);
+    float2 *Xp = (float2 *)(w + S.L.Xp), *Xq = (float2 *)(w + S.L.Xq);
+    const float inv_wind = (float)(1.0 / met->wind);
+    if (met->variant == 0) {
+        MlpServing view;
+        if ((rc = mlp_serving_view(net, &view)) != BLDFM_OK) return rc;
+        CK(launch_sur_serve(g, ml->dev, ax, ay, zm, (float)met->s1, (float)met->s2, (float)met->s3, inv_wind, ktop,
+                            utop, view, Xp, Xq, (int *)(w + S.L.err), dc.nsm, st));
+    } else {
+        if (exact) {
+            CK(launch_sur_exact(g, ml->dev, ax, ay, zm, (const TransferCase *)(w + S.tcase),
+                                (const float4 *)(w + S.steps), Y, st));
+        } else {
+            CK(launch_sur_features(g, ml->dev, ax, ay, zm, (float)met->s1, (float)met->s2, (float)met->s3, X,
+                                   S.npad, st));
+            const int cap = bldfm_surrogate_batch(net);
+            if (cap < 256) return BLDFM_ERR_ARG;
+            for (int64_t off = 0; off < S.npad; off += cap) {
+                const int n = (int)std::min<int64_t>(cap, S.npad - off);
+                if ((rc = bldfm_surrogate_forward(net, X + off * 8, Y + off * 4, n, st)) != BLDFM_OK) return rc;
+            }
+        }
+        CK(launch_sur_spectra(g, ml->dev, Y, ax, ay, zm, inv_wind, ktop, utop, Xp, Xq, st));
+    }
+    CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
+                                (float2 *)(w + S.L.Cb), conc, flx, st));
+    return BLDFM_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1196,6 +1331,27 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch
     CK(cudaGraphLaunch(gi->exec, st));
     CK(cudaEventRecord(gi->done, st));
     return BLDFM_OK;
+}
+
+int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls, int64_t *workspace_bytes)
+{
+    if (!workspace_bytes) return BLDFM_ERR_ARG;
+    int rc = sur_check_desc(d, nlvls);
+    if (rc != BLDFM_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    HostPlan hp;
+    if ((rc = make_plan(d, nullptr, nullptr, nullptr, nlvls, hp)) != BLDFM_OK) return rc;
+    *workspace_bytes = (int64_t)sur_layout(hp.g).total;
+    return BLDFM_OK;
+}
+
+int bldfm_surrogate_solve(void *net, const bldfm_desc *d, const bldfm_surrogate_case *met, const double *z_host,
+                          const double *prof_host, const int64_t *levels_host, int32_t nlvls, double *conc_dev,
+                          double *flx_dev, void *workspace_dev, size_t workspace_bytes, void *stream)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    return sur_solve_impl(net, d, met, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
+                          workspace_bytes, (cudaStream_t)stream);
 }
 
 }  // extern "C"

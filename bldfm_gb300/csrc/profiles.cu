@@ -76,7 +76,7 @@ int profile_scalars(int n, double zm, double um, double vm, double ustar, double
     return BLDFM_OK;
 }
 
-__device__ void profile_level(const ProfileCase &pc, int i, double *z, double *prof, int stride)
+__host__ __device__ void profile_level(const ProfileCase &pc, int i, double *z, double *prof, int stride)
 {
     const double zeta = (double)i * pc.dzeta;
     const double zi = -pc.h * log(-(zeta - pc.aa) / pc.bb);
@@ -110,6 +110,12 @@ __device__ void profile_level(const ProfileCase &pc, int i, double *z, double *p
     prof[2 * stride + i] = Kx;
     prof[3 * stride + i] = Ky;
     prof[4 * stride + i] = K;
+}
+
+// host evaluation of every level (training data of the surrogate)
+void profile_levels_host(const ProfileCase &pc, double *z, double *prof)
+{
+    for (int i = 0; i < pc.nz; ++i) profile_level(pc, i, z, prof, pc.nz);
 }
 
 __global__ void profiles_kernel(ProfileCase pc, double *z, double *prof)

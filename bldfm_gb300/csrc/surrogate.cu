@@ -5,9 +5,14 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/bldfm_gb300.h"
+#include "common.h"
+#include "mlp_common.cuh"
+#include "profiles.h"
+#include "surrogate_phys.cuh"
 #include "tcgemm.cuh"
 
 namespace {
@@ -80,39 +85,19 @@ extern "C" int bldfm_tc_gemm_check(const uint16_t *A, const uint16_t *B, float *
 }
 
 // ===========================================================================
-// The MLP: 5 -> 256 -> 256 -> 256 -> 256 -> 4, GELU after each hidden layer.
+// The MLP: 8 -> 256 -> 256 -> 256 -> 256 -> 4, GELU after each hidden layer.
 // Hidden 256 x 256 layers on tensor cores (BF16 operands, FP32 accumulation),
-// input and output layers on CUDA cores (FP32).  Parameters are FP32 masters
-// updated by Adam; the tensor-core layers read BF16 copies.
+// input and output layers on CUDA cores (FP32); the last hidden layer is kept
+// in FP32 for the output layer (fused into the last GEMM's epilogue when only
+// the forward pass runs).  Parameters are FP32 masters updated by Adam; the
+// tensor-core layers read BF16 copies.
 //
-// Flat parameter vector: W0 [5][256] (in, out), b0 [256], then for j = 1..3
+// Flat parameter vector: W0 [8][256] (in, out), b0 [256], then for j = 1..3
 // Wt_j [256][256] (out, in) and b_j [256], then W4 [256][4] (in, out), b4 [4].
 // ===========================================================================
-#define MLP_IN 5
-#define MLP_XS 8  // stride of the input rows
-#define MLP_H 256
-#define MLP_OUT 4
-#define MLP_OFF_W0 0
-#define MLP_OFF_B0 (MLP_IN * MLP_H)
-#define MLP_OFF_WT(j) (MLP_OFF_B0 + MLP_H + ((j)-1) * (MLP_H * MLP_H + MLP_H))
-#define MLP_OFF_B(j) (MLP_OFF_WT(j) + MLP_H * MLP_H)
-#define MLP_OFF_W4 (MLP_OFF_WT(4))
-#define MLP_OFF_B4 (MLP_OFF_W4 + MLP_H * MLP_OUT)
-#define MLP_NPARAM (MLP_OFF_B4 + MLP_OUT)
+
 
 namespace {
-
-__device__ __forceinline__ uint16_t f2bf(float f)
-{
-    return __bfloat16_as_ushort(__float2bfloat16_rn(f));
-}
-__device__ __forceinline__ float bf2f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
-
-__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_d(float z)
-{
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
-}
 
 // A CTA's 128 x 256 bf16 tile in core-matrix order (tc_core_offset) is copied
 // to the row blocks of its tile (contiguous 64 KB), and scattered into the
@@ -161,10 +146,16 @@ __device__ __forceinline__ void put8(uint16_t *st, int r, int c, const float *v)
     *(uint4 *)(st + tc_core_offset(r, c, MLP_H) / 2) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-// forward hidden layer: Z = acc + b, H = gelu(Z) (bf16), G = gelu'(Z) (bf16)
+// forward hidden layer: Z = acc + b, H = gelu(Z); written as the bf16 rows
+// and transposed blocks of the next GEMM (rows_dst, T_dst), gelu'(Z) as bf16
+// (G_dst), H in FP32 row-major (h32_dst), or straight into the output layer:
+// Y[r] = b4 + sum_f H[r][f] W4[f] in FP32 (Y != null).  Null pointers skip.
 struct EpiFwd {
     const float *bias;
-    uint16_t *rows_dst, *T_dst, *G_dst, *rowmajor_dst;
+    uint16_t *rows_dst, *T_dst, *G_dst;
+    float *h32_dst;
+    const float *W4, *b4;
+    float *Y;
     int nchunks;
     __device__ void row(int r, int c0, const float *v, uint16_t *st) const
     {
@@ -173,26 +164,45 @@ struct EpiFwd {
         for (int i = 0; i < 32; ++i) {
             const float z = v[i] + bias[c0 + i];
             h[i] = gelu_f(z);
-            gd[i] = gelu_d(z);
+            gd[i] = G_dst ? gelu_d(z) : 0.f;
         }
-        const int rl = r & 127;
+        if (rows_dst || T_dst) {
+            const int rl = r & 127;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) put8(st, rl, c0 + 8 * q, h + 8 * q);
-        uint32_t w[16];
+            for (int q = 0; q < 4; ++q) put8(st, rl, c0 + 8 * q, h + 8 * q);
+        }
+        if (G_dst) {
+            uint32_t w[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) w[i] = (uint32_t)f2bf(gd[2 * i]) | ((uint32_t)f2bf(gd[2 * i + 1]) << 16);
-        uint4 *g = (uint4 *)(G_dst + (size_t)r * MLP_H + c0);
+            for (int i = 0; i < 16; ++i) w[i] = (uint32_t)f2bf(gd[2 * i]) | ((uint32_t)f2bf(gd[2 * i + 1]) << 16);
+            uint4 *g = (uint4 *)(G_dst + (size_t)r * MLP_H + c0);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) g[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
-        if (rowmajor_dst) {
+            for (int q = 0; q < 4; ++q) g[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+        }
+        if (h32_dst) {
+            float4 *o = (float4 *)(h32_dst + (size_t)r * MLP_H + c0);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) w[i] = (uint32_t)f2bf(h[2 * i]) | ((uint32_t)f2bf(h[2 * i + 1]) << 16);
-            uint4 *o = (uint4 *)(rowmajor_dst + (size_t)r * MLP_H + c0);
+            for (int q = 0; q < 8; ++q) o[q] = make_float4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+        }
+        if (Y) {
+            // this thread owns row r for every column slice, in order
+            float4 y = c0 == 0 ? make_float4(b4[0], b4[1], b4[2], b4[3]) : *(const float4 *)(Y + (size_t)r * 4);
+            const float4 *w4 = (const float4 *)(W4 + (size_t)c0 * MLP_OUT);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) o[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+            for (int i = 0; i < 32; ++i) {
+                const float4 wv = w4[i];
+                y.x = fmaf(h[i], wv.x, y.x);
+                y.y = fmaf(h[i], wv.y, y.y);
+                y.z = fmaf(h[i], wv.z, y.z);
+                y.w = fmaf(h[i], wv.w, y.w);
+            }
+            *(float4 *)(Y + (size_t)r * 4) = y;
         }
     }
-    __device__ void finish(int tile, uint16_t *st) const { emit_tile(tile, st, rows_dst, T_dst, 0, nchunks); }
+    __device__ void finish(int tile, uint16_t *st) const
+    {
+        if (rows_dst || T_dst) emit_tile(tile, st, rows_dst, T_dst, 0, nchunks);
+    }
 };
 
 // backward data: dZ = bf16(acc * G); db += sum over rows of dZ
@@ -272,50 +282,47 @@ __global__ void __launch_bounds__(256) mlp_in_fwd_kernel(const float *__restrict
 #pragma unroll
         for (int i = 0; i < MLP_IN; ++i) z = fmaf(x[i], w[i], z);
         st[tc_core_offset(s, f, MLP_H) / 2] = f2bf(gelu_f(z));
-        G_dst[(size_t)r * MLP_H + f] = f2bf(gelu_d(z));
+        if (G_dst) G_dst[(size_t)r * MLP_H + f] = f2bf(gelu_d(z));
     }
     __syncthreads();
     emit_tile(tile, st, rows_dst, T_dst, 0, nchunks);
 }
 
-// output layer forward (+ loss and the start of the backward pass when T is
-// given): one CTA per 128-sample tile, thread = sample
-__global__ void __launch_bounds__(128) mlp_out_kernel(const uint16_t *__restrict__ H4, const uint16_t *__restrict__ G4,
+// Output layer forward, loss and the start of the backward pass: one CTA per
+// 128-sample tile.  Phase 1, thread = sample: y = H4 W4 + b4, the weighted
+// error and dY (kept in shared memory).  Phase 2, thread = two features:
+// dW4 = H4^T dY and dZ4 = bf16(dY W4^T * gelu'), db3 = sum dZ4, reduced over
+// the tile's rows in registers (one global atomic per parameter and CTA).
+__global__ void __launch_bounds__(128) mlp_out_kernel(const float *__restrict__ H4, const uint16_t *__restrict__ G4,
                                                       const float *__restrict__ P, const float *__restrict__ T,
                                                       const float *__restrict__ wts, float inv_n, float *Y,
                                                       float *grad, float *loss, uint16_t *rows_dst, uint16_t *T_dst,
                                                       int nchunks, int n)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint16_t *st = (uint16_t *)smem_raw;                          // dZ4 tile (64 KB)
-    float *sW = (float *)(smem_raw + 128 * MLP_H * 2);            // W4 [256][4]
-    float *sG = sW + MLP_H * MLP_OUT;                             // dW4 partial [256][4]
-    float *sdb = sG + MLP_H * MLP_OUT;                            // db3 partial [256]
+    uint16_t *st = (uint16_t *)smem_raw;                // dZ4 tile (64 KB)
+    float *sW = (float *)(smem_raw + 128 * MLP_H * 2);  // W4 [256][4]
+    float4 *sDY = (float4 *)(sW + MLP_H * MLP_OUT);     // dY [128]
     __shared__ float sdb4[MLP_OUT], sloss;
     const int t = threadIdx.x, tile = blockIdx.x;
-    for (int i = t; i < MLP_H * MLP_OUT; i += blockDim.x) {
-        sW[i] = P[MLP_OFF_W4 + i];
-        sG[i] = 0.f;
-    }
-    for (int i = t; i < MLP_H; i += blockDim.x) sdb[i] = 0.f;
+    for (int i = t; i < MLP_H * MLP_OUT; i += blockDim.x) sW[i] = P[MLP_OFF_W4 + i];
     if (t < MLP_OUT) sdb4[t] = 0.f;
     if (t == 0) sloss = 0.f;
     __syncthreads();
     const int r = tile * 128 + t;
     const bool live = r < n;
-    const uint4 *h4 = (const uint4 *)(H4 + (size_t)r * MLP_H);
+    const float4 *h4 = (const float4 *)(H4 + (size_t)(live ? r : 0) * MLP_H);
     float y[MLP_OUT];
 #pragma unroll
     for (int o = 0; o < MLP_OUT; ++o) y[o] = P[MLP_OFF_B4 + o];
-    for (int q = 0; q < MLP_H / 8; ++q) {
-        const uint4 u = h4[q];
-        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+    for (int q = 0; q < MLP_H / 4; ++q) {
+        const float4 u = h4[q];
+        const float hq[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const float hv = bf2f((uint16_t)(k & 1 ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xFFFF)));
-            const int f = q * 8 + k;
+        for (int k = 0; k < 4; ++k) {
+            const int f = q * 4 + k;
 #pragma unroll
-            for (int o = 0; o < MLP_OUT; ++o) y[o] = fmaf(hv, sW[f * MLP_OUT + o], y[o]);
+            for (int o = 0; o < MLP_OUT; ++o) y[o] = fmaf(hq[k], sW[f * MLP_OUT + o], y[o]);
         }
     }
     if (Y && live)
@@ -323,43 +330,68 @@ __global__ void __launch_bounds__(128) mlp_out_kernel(const uint16_t *__restrict
     if (!T) return;
     float dy[MLP_OUT];
     float l = 0.f;
-    const float wb = live ? wts[r] : 0.f;
 #pragma unroll
     for (int o = 0; o < MLP_OUT; ++o) {
+        const float wb = live ? wts[(size_t)r * MLP_OUT + o] : 0.f;
         const float e = live ? (y[o] - T[(size_t)r * MLP_OUT + o]) : 0.f;
         l = fmaf(wb * e, e, l);
         dy[o] = 2.f * wb * e * inv_n;
     }
-    atomicAdd(&sloss, l * inv_n);
+    sDY[t] = make_float4(dy[0], dy[1], dy[2], dy[3]);
+    // tile sums of the loss and db4: warp reductions, one shared atomic per warp
 #pragma unroll
-    for (int o = 0; o < MLP_OUT; ++o) atomicAdd(&sdb4[o], dy[o]);
-    for (int q = 0; q < MLP_H / 8; ++q) {
-        const uint4 u = h4[q];
-        const uint4 g = ((const uint4 *)(G4 + (size_t)r * MLP_H))[q];
-        const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-        const uint32_t gw[4] = {g.x, g.y, g.z, g.w};
-        float dz[8];
+    for (int off = 16; off > 0; off >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, off);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int f = q * 8 + k;
-            const float hv = bf2f((uint16_t)(k & 1 ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xFFFF)));
-            const float gv = bf2f((uint16_t)(k & 1 ? (gw[k >> 1] >> 16) : (gw[k >> 1] & 0xFFFF)));
-            float dh = 0.f;
+        for (int o = 0; o < MLP_OUT; ++o) dy[o] += __shfl_xor_sync(0xffffffffu, dy[o], off);
+    }
+    if ((t & 31) == 0) {
+        atomicAdd(&sloss, l * inv_n);
 #pragma unroll
-            for (int o = 0; o < MLP_OUT; ++o) {
-                dh = fmaf(dy[o], sW[f * MLP_OUT + o], dh);
-                atomicAdd(&sG[f * MLP_OUT + o], hv * dy[o]);
-            }
-            dz[k] = bf2f(f2bf(dh * gv));
-            atomicAdd(&sdb[f], dz[k]);
-        }
-        put8(st, t, q * 8, dz);
+        for (int o = 0; o < MLP_OUT; ++o) atomicAdd(&sdb4[o], dy[o]);
     }
     __syncthreads();
-    for (int i = t; i < MLP_H * MLP_OUT; i += blockDim.x) atomicAdd(grad + MLP_OFF_W4 + i, sG[i]);
-    for (int i = t; i < MLP_H; i += blockDim.x) atomicAdd(grad + MLP_OFF_B(3) + i, sdb[i]);
+    // phase 2: features f0 = 2 t, f0 + 1
+    const int f0 = 2 * t;
+    float gW[2][MLP_OUT] = {};
+    float db[2] = {0.f, 0.f};
+    float w4[2][MLP_OUT];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int o = 0; o < MLP_OUT; ++o) w4[k][o] = sW[(f0 + k) * MLP_OUT + o];
+    const int rows = min(128, n - tile * 128);
+    for (int rr = 0; rr < rows; ++rr) {
+        const size_t gr = (size_t)(tile * 128 + rr) * MLP_H + f0;
+        const float2 h = *(const float2 *)(H4 + gr);
+        const uint32_t gw = *(const uint32_t *)(G4 + gr);
+        const float4 d = sDY[rr];
+        const float hk[2] = {h.x, h.y};
+        const float gk[2] = {bf2f((uint16_t)(gw & 0xFFFF)), bf2f((uint16_t)(gw >> 16))};
+        uint16_t zb[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            gW[k][0] = fmaf(hk[k], d.x, gW[k][0]);
+            gW[k][1] = fmaf(hk[k], d.y, gW[k][1]);
+            gW[k][2] = fmaf(hk[k], d.z, gW[k][2]);
+            gW[k][3] = fmaf(hk[k], d.w, gW[k][3]);
+            const float dh = fmaf(d.x, w4[k][0], fmaf(d.y, w4[k][1], fmaf(d.z, w4[k][2], d.w * w4[k][3])));
+            zb[k] = f2bf(dh * gk[k]);
+            db[k] += bf2f(zb[k]);
+        }
+        // f0 is even, so the pair is one aligned 32-bit word of the core-matrix row
+        *(uint32_t *)(st + tc_core_offset(rr, f0, MLP_H) / 2) = (uint32_t)zb[0] | ((uint32_t)zb[1] << 16);
+    }
+    for (int rr = rows; rr < 128; ++rr) *(uint32_t *)(st + tc_core_offset(rr, f0, MLP_H) / 2) = 0u;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+#pragma unroll
+        for (int o = 0; o < MLP_OUT; ++o) atomicAdd(grad + MLP_OFF_W4 + (f0 + k) * MLP_OUT + o, gW[k][o]);
+        atomicAdd(grad + MLP_OFF_B(3) + f0 + k, db[k]);
+    }
     if (t < MLP_OUT) atomicAdd(grad + MLP_OFF_B4 + t, sdb4[t]);
     if (t == 0) atomicAdd(loss, sloss);
+    __syncthreads();
     emit_tile(tile, st, rows_dst, T_dst, 1, nchunks);
 }
 
@@ -368,7 +400,9 @@ __global__ void __launch_bounds__(256) mlp_in_grad_kernel(const float *__restric
                                                           float *grad, int n)
 {
     const int f = threadIdx.x;
-    float acc[MLP_IN] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    float acc[MLP_IN];
+#pragma unroll
+    for (int i = 0; i < MLP_IN; ++i) acc[i] = 0.f;
     const int r0 = blockIdx.x * 128, r1 = min(n, r0 + 128);
     for (int r = r0; r < r1; ++r) {
         const float d = dZ1[(size_t)r * MLP_H + f];
@@ -413,7 +447,8 @@ struct Mlp {
     int step = 0;
     float *P = nullptr, *G = nullptr, *m = nullptr, *v = nullptr;
     uint16_t *Wt[3] = {}, *W[3] = {};
-    uint16_t *Hrows[3] = {}, *HT[3] = {}, *H4 = nullptr;
+    uint16_t *Hrows[3] = {}, *HT[3] = {};
+    float *H4 = nullptr;  // last hidden layer, FP32 row-major (training)
     uint16_t *Gz[4] = {};
     uint16_t *dZrows[3] = {}, *dZT[3] = {};  // index j-2 for dZ_j, j = 2..4
     float *dZ1 = nullptr, *Y = nullptr, *loss = nullptr;
@@ -451,19 +486,25 @@ cudaError_t gemm(const uint16_t *A, const uint16_t *Bop, int tiles, int K, int s
     return cudaGetLastError();
 }
 
-// forward pass through the hidden layers; H4 / G4 left for the output layer
-cudaError_t mlp_forward_hidden(Mlp &M, const float *X, int n, cudaStream_t st)
+// Forward pass.  train: keep what the backward pass reads (transposed blocks,
+// gelu'(Z), the FP32 last hidden layer H4) and leave the output layer to
+// mlp_out_kernel; otherwise the output layer runs in the last epilogue -> Y.
+cudaError_t mlp_forward(Mlp &M, const float *X, int n, bool train, float *Y, cudaStream_t st)
 {
     const int tiles = n / 128, nchunks = n / 256;
     cudaFuncSetAttribute(mlp_in_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * MLP_H * 2);
-    mlp_in_fwd_kernel<<<tiles, 256, 128 * MLP_H * 2, st>>>(X, M.P, M.Hrows[0], M.HT[0], M.Gz[0], nchunks);
+    mlp_in_fwd_kernel<<<tiles, 256, 128 * MLP_H * 2, st>>>(X, M.P, M.Hrows[0], train ? M.HT[0] : nullptr,
+                                                            train ? M.Gz[0] : nullptr, nchunks);
     for (int j = 1; j <= 3; ++j) {
         EpiFwd e;
         e.bias = M.P + MLP_OFF_B(j);
         e.rows_dst = j < 3 ? M.Hrows[j] : nullptr;
-        e.T_dst = j < 3 ? M.HT[j] : nullptr;
-        e.G_dst = M.Gz[j];
-        e.rowmajor_dst = j == 3 ? M.H4 : nullptr;
+        e.T_dst = train && j < 3 ? M.HT[j] : nullptr;
+        e.G_dst = train ? M.Gz[j] : nullptr;
+        e.h32_dst = train && j == 3 ? M.H4 : nullptr;
+        e.W4 = M.P + MLP_OFF_W4;
+        e.b4 = M.P + MLP_OFF_B4;
+        e.Y = !train && j == 3 ? Y : nullptr;
         e.nchunks = nchunks;
         cudaError_t c = gemm(M.Hrows[j - 1], M.Wt[j - 1], tiles, MLP_H, 1, e, M.err, st);
         if (c != cudaSuccess) return c;
@@ -471,7 +512,7 @@ cudaError_t mlp_forward_hidden(Mlp &M, const float *X, int n, cudaStream_t st)
     return cudaGetLastError();
 }
 
-const size_t OUT_SMEM = 128 * MLP_H * 2 + (2 * MLP_H * MLP_OUT + MLP_H) * 4;
+const size_t OUT_SMEM = 128 * MLP_H * 2 + MLP_H * MLP_OUT * 4 + 128 * 16;
 
 }  // namespace
 
@@ -533,6 +574,8 @@ int bldfm_surrogate_destroy(void *handle)
 
 int bldfm_surrogate_nparams(void) { return MLP_NPARAM; }
 
+int bldfm_surrogate_batch(void *handle) { return handle ? ((Mlp *)handle)->B : BLDFM_ERR_ARG; }
+
 // get (host_out != NULL) and/or set (host_in != NULL) the FP32 parameters
 int bldfm_surrogate_params(void *handle, float *host_out, const float *host_in)
 {
@@ -564,9 +607,9 @@ int bldfm_surrogate_grads(void *handle, float *host_grads, float *host_loss)
     return e != 0 ? BLDFM_ERR_TIMEOUT : BLDFM_OK;
 }
 
-// One Adam step on n samples (n <= batch, n % 256 == 0): X [n][8] inputs
-// (5 used), T [n][4] targets, w [n] loss weights, all device pointers.
-// loss = sum_b w_b |y_b - t_b|^2 / n.  lr = 0 computes gradients only.
+// One Adam step on n samples (n <= batch, n % 256 == 0): X [n][8] inputs,
+// T [n][4] targets, w [n][4] loss weights, all device pointers.
+// loss = sum_b sum_o w_bo (y_bo - t_bo)^2 / n.  lr = 0 computes gradients only.
 int bldfm_surrogate_train_step(void *handle, const float *X, const float *T, const float *w, int32_t n, float lr,
                                void *stream)
 {
@@ -576,7 +619,7 @@ int bldfm_surrogate_train_step(void *handle, const float *X, const float *T, con
     const int tiles = n / 128, nchunks = n / 256;
     if (cudaMemsetAsync(M->G, 0, MLP_NPARAM * 4, st) != cudaSuccess) return BLDFM_ERR_CUDA;
     if (cudaMemsetAsync(M->loss, 0, 4, st) != cudaSuccess) return BLDFM_ERR_CUDA;
-    if (mlp_forward_hidden(*M, X, n, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (mlp_forward(*M, X, n, true, nullptr, st) != cudaSuccess) return BLDFM_ERR_CUDA;
     cudaFuncSetAttribute(mlp_out_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM);
     mlp_out_kernel<<<tiles, 128, OUT_SMEM, st>>>(M->H4, M->Gz[3], M->P, T, w, 1.0f / n, M->Y, M->G, M->loss,
                                                  M->dZrows[2], M->dZT[2], nchunks, n);
@@ -608,16 +651,223 @@ int bldfm_surrogate_train_step(void *handle, const float *X, const float *T, con
     return cudaGetLastError() == cudaSuccess ? BLDFM_OK : BLDFM_ERR_CUDA;
 }
 
-// Y [n][4] = MLP(X [n][8]), n % 256 == 0, device pointers
+// Y [n][4] = MLP(X [n][8]), n % 256 == 0, device pointers (forward only: the
+// output layer is fused into the last tensor-core GEMM)
 int bldfm_surrogate_forward(void *handle, const float *X, float *Y, int32_t n, void *stream)
 {
     Mlp *M = (Mlp *)handle;
     if (!M || !X || !Y || n < 256 || n > M->B || n % 256 != 0) return BLDFM_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    if (mlp_forward_hidden(*M, X, n, st) != cudaSuccess) return BLDFM_ERR_CUDA;
-    cudaFuncSetAttribute(mlp_out_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM);
-    mlp_out_kernel<<<n / 128, 128, OUT_SMEM, st>>>(M->H4, M->Gz[3], M->P, nullptr, nullptr, 0.f, Y, nullptr, nullptr,
-                                                   nullptr, nullptr, n / 256, n);
+    if (mlp_forward(*M, X, n, false, Y, st) != cudaSuccess) return BLDFM_ERR_CUDA;
+    return BLDFM_OK;
+}
+
+}  // extern "C"
+
+int mlp_serving_view(void *handle, MlpServing *out)
+{
+    Mlp *M = (Mlp *)handle;
+    if (!M || !out) return BLDFM_ERR_ARG;
+    out->P = M->P;
+    for (int j = 0; j < 3; ++j) out->Wt[j] = M->Wt[j];
+    return BLDFM_OK;
+}
+
+// ===========================================================================
+// Training data: nondimensional transfer functions (surrogate_phys.cuh) of a
+// pool of MOST met cases, sampled on the device.
+// ===========================================================================
+namespace {
+
+struct TransferPool {
+    int ncases = 0, lmax = 0, n = 0;
+    TransferCase *cases = nullptr;  // device
+    float4 *steps = nullptr;        // device [case][lmax]: (h~, K~, U~, 0) of step i
+    std::vector<TransferCase> host_cases;
+};
+
+// counter-based uniform in (0, 1): splitmix64 of (seed, index, stream)
+__device__ __forceinline__ float hash_unif(uint64_t seed, uint64_t idx, uint32_t k)
+{
+    uint64_t z = seed + 0x9E3779B97F4A7C15ULL * (idx * 4 + k + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return ((float)(z >> 40) + 0.5f) * (1.0f / 16777216.0f);
+}
+
+// Random samples: case uniform over the pool, |k~| log-uniform in
+// [kmin, kmax], direction uniform in the first quadrant (k_par, k_perp >= 0).
+// W [m][4]: loss weights for the footprint's relative L2 error, with the
+// importance factor k^2 of the log-uniform draw: flux term
+// k^2 |Tq|^2 / Eq(case), concentration term k^2 |R~ Tq|^2 / Ep(case);
+// outputs 0, 1 weigh (1 + k)^2 (flux + conc), outputs 2, 3 weigh conc, each
+// plus `floor`.  norm == null: W = raw (k^2 |Tq|^2, -, k^2 |R~ Tq|^2, -)
+// for estimating the per-case energies.  cid_out (optional) gets the case ids.
+__global__ void transfer_samples_kernel(const TransferCase *__restrict__ cases, const float4 *__restrict__ steps,
+                                        int lmax, int ncases, uint64_t seed, float kmin, float lratio,
+                                        const float2 *__restrict__ norm, float floor_w, float *X, float *Tg,
+                                        float *W, int *cid_out, int m)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const int c = min((int)(hash_unif(seed, s, 0) * (float)ncases), ncases - 1);
+    // (|k|, direction) on the additive-recurrence sequence with plastic-number
+    // steps (a stratified 2D point set), shifted at random per call
+    // (fractional parts in 32-bit fixed point: frac(a s + r) = (A s + R) / 2^32)
+    const uint32_t r1 = (uint32_t)(hash_unif(seed, 0, 1) * 4294967296.0f);
+    const uint32_t r2 = (uint32_t)(hash_unif(seed, 0, 2) * 4294967296.0f);
+    const float u1 = ((uint32_t)s * 3242174890u + r1) * 2.3283064365386963e-10f;
+    const float u2 = ((uint32_t)s * 2447445414u + r2) * 2.3283064365386963e-10f;
+    const float k = kmin * expf(lratio * u1);
+    float sn, cs;
+    sincospif(0.5f * u2, &sn, &cs);
+    const float kpar = k * cs, kperp = k * sn;
+    const TransferCase tc = cases[c];
+    float out[4];
+    transfer_one(tc, steps + (size_t)c * lmax, kpar, kperp, out);
+    feature_row(X + (size_t)s * 8, kpar, kperp, tc.s1, tc.s2, tc.s3);
+#pragma unroll
+    for (int o = 0; o < 4; ++o) Tg[(size_t)s * 4 + o] = out[o];
+    if (cid_out) cid_out[s] = c;
+    const float kk = 1.f + k;
+    const float imp = k * k;
+    const float q2 = imp * expf(fmaxf(2.f * out[0] * kk, -80.f));
+    const float2 rt = top_ratio(tc.ktop, tc.utop, kpar, kperp);
+    const float p2 = q2 * expf(fminf(2.f * out[2], 80.f)) * fmaf(rt.x, rt.x, rt.y * rt.y);
+    float *w = W + (size_t)s * 4;
+    if (!norm) {
+        w[0] = q2;
+        w[1] = 0.f;
+        w[2] = p2;
+        w[3] = 0.f;
+        return;
+    }
+    const float2 nm = norm[c];
+    const float fq = q2 * nm.x, fp = p2 * nm.y;
+    w[0] = w[1] = kk * kk * (fq + fp) + floor_w;
+    w[2] = w[3] = fp + floor_w;
+}
+
+// targets of given samples (case ids and wavenumbers), for checks
+__global__ void transfer_eval_kernel(const TransferCase *__restrict__ cases, const float4 *__restrict__ steps,
+                                     int lmax, const int *__restrict__ cid, const float *__restrict__ kpar,
+                                     const float *__restrict__ kperp, float *Tg, int m)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    float out[4];
+    transfer_one(cases[cid[s]], steps + (size_t)cid[s] * lmax, kpar[s], kperp[s], out);
+#pragma unroll
+    for (int o = 0; o < 4; ++o) Tg[(size_t)s * 4 + o] = out[o];
+}
+
+}  // namespace
+
+// Nondimensional step table of a case given its dimensional grid and profiles
+// (u, v, Kx, Ky, Kz rows of nz): h~ = dz / zm, K~ = Kz / (U zm), U~ = u_par / U
+// with u_par the speed along (ex, ey).  Shared with the serving path.
+void surrogate_steps_from_profiles(int nz, const double *z, const double *prof, double zm, double wind, double ex,
+                                   double ey, float4 *st)
+{
+    const double *u = prof, *v = prof + nz, *Kz = prof + 4 * nz;
+    for (int i = 0; i < nz - 1; ++i)
+        st[i] = make_float4((float)((z[i + 1] - z[i]) / zm), (float)(Kz[i] / (wind * zm)),
+                            (float)((u[i] * ex + v[i] * ey) / wind), 0.f);
+}
+
+extern "C" {
+
+int bldfm_transfer_pool_create(const double *s1, const double *s2, int32_t ncases, int32_t n, void **pool)
+{
+    if (!s1 || !s2 || ncases < 1 || n < 2 || !pool) return BLDFM_ERR_ARG;
+    TransferPool *P = new TransferPool();
+    P->ncases = ncases;
+    P->n = n;
+    std::vector<std::vector<float4>> st(ncases);
+    P->host_cases.resize(ncases);
+    for (int c = 0; c < ncases; ++c) {
+        // z_m = 1 and unit wind at z_m: z0 = exp(-s2), L = 1 / s1, u* from the log-law
+        const double mol = fabs(s1[c]) < 1e-12 ? 1e12 : 1.0 / s1[c];
+        ProfileCase pc;
+        const int rc = profile_scalars(n, 1.0, 1.0, 0.0, -1.0, exp(-s2[c]), mol, 1.0, 0, -1.0, -1.0, -1.0, &pc);
+        if (rc != BLDFM_OK || pc.nz > BLDFM_MAX_NZ) {
+            delete P;
+            return rc != BLDFM_OK ? rc : BLDFM_ERR_UNSUPPORTED;
+        }
+        std::vector<double> z(pc.nz), prof(5 * (size_t)pc.nz);
+        profile_levels_host(pc, z.data(), prof.data());
+        TransferCase &tc = P->host_cases[c];
+        tc.nz = pc.nz;
+        tc.jm = n;
+        tc.ktop = (float)prof[4 * (size_t)pc.nz + pc.nz - 1];
+        tc.utop = (float)prof[pc.nz - 1];
+        tc.s1 = (float)s1[c];
+        tc.s2 = (float)s2[c];
+        tc.s3 = (float)pc.ustar;
+        tc.pad = 0;
+        st[c].resize(pc.nz - 1);
+        surrogate_steps_from_profiles(pc.nz, z.data(), prof.data(), 1.0, 1.0, 1.0, 0.0, st[c].data());
+        P->lmax = std::max(P->lmax, pc.nz - 1);
+    }
+    std::vector<float4> flat((size_t)ncases * P->lmax, make_float4(0.f, 1.f, 0.f, 0.f));
+    for (int c = 0; c < ncases; ++c) std::copy(st[c].begin(), st[c].end(), flat.begin() + (size_t)c * P->lmax);
+    if (cudaMalloc(&P->cases, sizeof(TransferCase) * ncases) != cudaSuccess ||
+        cudaMalloc(&P->steps, sizeof(float4) * flat.size()) != cudaSuccess) {
+        cudaFree(P->cases);
+        delete P;
+        return BLDFM_ERR_CUDA;
+    }
+    if (cudaMemcpy(P->cases, P->host_cases.data(), sizeof(TransferCase) * ncases, cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(P->steps, flat.data(), sizeof(float4) * flat.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(P->cases);
+        cudaFree(P->steps);
+        delete P;
+        return BLDFM_ERR_CUDA;
+    }
+    *pool = P;
+    return BLDFM_OK;
+}
+
+int bldfm_transfer_pool_destroy(void *pool)
+{
+    TransferPool *P = (TransferPool *)pool;
+    if (!P) return BLDFM_ERR_ARG;
+    cudaDeviceSynchronize();
+    cudaFree(P->cases);
+    cudaFree(P->steps);
+    delete P;
+    return BLDFM_OK;
+}
+
+int bldfm_transfer_pool_case(void *pool, int32_t c, double *s3, int32_t *nz)
+{
+    TransferPool *P = (TransferPool *)pool;
+    if (!P || c < 0 || c >= P->ncases) return BLDFM_ERR_ARG;
+    if (s3) *s3 = P->host_cases[c].s3;
+    if (nz) *nz = P->host_cases[c].nz;
+    return BLDFM_OK;
+}
+
+int bldfm_transfer_samples(void *pool, uint64_t seed, int32_t m, float kmin, float kmax, const float *norm,
+                           float floor_w, float *X, float *T, float *W, int32_t *cid, void *stream)
+{
+    TransferPool *P = (TransferPool *)pool;
+    if (!P || !X || !T || !W || m < 1 || !(kmin > 0.f) || !(kmax > kmin)) return BLDFM_ERR_ARG;
+    transfer_samples_kernel<<<(m + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+        P->cases, P->steps, P->lmax, P->ncases, seed, kmin, logf(kmax / kmin), (const float2 *)norm, floor_w, X, T,
+        W, cid, m);
+    return cudaGetLastError() == cudaSuccess ? BLDFM_OK : BLDFM_ERR_CUDA;
+}
+
+int bldfm_transfer_eval(void *pool, const int32_t *cid, const float *kpar, const float *kperp, float *T, int32_t m,
+                        void *stream)
+{
+    TransferPool *P = (TransferPool *)pool;
+    if (!P || !cid || !kpar || !kperp || !T || m < 1) return BLDFM_ERR_ARG;
+    transfer_eval_kernel<<<(m + 127) / 128, 128, 0, (cudaStream_t)stream>>>(P->cases, P->steps, P->lmax, cid, kpar,
+                                                                           kperp, T, m);
     return cudaGetLastError() == cudaSuccess ? BLDFM_OK : BLDFM_ERR_CUDA;
 }
 

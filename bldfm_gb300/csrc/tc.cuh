@@ -117,6 +117,13 @@ __device__ __forceinline__ void tc_commit(uint64_t *bar)
                  : "memory");
 }
 
+// make this thread's generic-proxy shared-memory writes visible to the async
+// proxy (tensor-core operand reads, bulk copies)
+__device__ __forceinline__ void tc_fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 

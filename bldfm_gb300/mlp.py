@@ -1,8 +1,10 @@
 """The surrogate's MLP on the tensor cores (C ABI bldfm_surrogate_*).
 
-5 input features -> four GELU hidden layers of 256 -> 4 outputs; the 256 x 256
+8 input features -> four GELU hidden layers of 256 -> 4 outputs; the 256 x 256
 layers run forward and backward as tcgen05 BF16 GEMMs with FP32 accumulation;
-FP32 master weights trained with Adam.  Tensors are torch CUDA tensors.
+the last hidden layer and the output layer stay FP32; FP32 master weights
+trained with Adam.  Tensors are torch CUDA tensors; loss weights are per
+sample and output, shape (n, 4).
 """
 
 import ctypes
@@ -12,7 +14,7 @@ import torch
 
 from . import _lib
 
-N_IN, N_HIDDEN, N_OUT, X_STRIDE = 5, 256, 4, 8
+N_IN, N_HIDDEN, N_OUT, X_STRIDE = 8, 256, 4, 8
 
 
 class MLP:

@@ -1,0 +1,340 @@
+"""Learned surrogate of the per-mode sweep, with the FP64 solver as fallback.
+
+Footprint mode with MOST profiles (reference: ``steady_state_transport_solver``,
+src/bldfm/solver.py:16-304, fed by ``vertical_profiles``,
+src/bldfm/pbl_model.py:8-204).  Per Fourier mode the solver's transfer from the
+surface to z_m depends only on the rotated, z_m-scaled wavenumbers and on
+s1 = z_m / L, s2 = ln(z_m / z0) (plus the level count n, default stretch and
+top).  A 8 -> 4 x 256 GELU -> 4 MLP (``mlp.MLP``, tcgen05 BF16 GEMMs with FP32
+accumulation) learns that transfer from data the FP32 invariant-imbedding
+sweep generates on the device (``TransferPool``), trained with Adam
+(``train``); ``Surrogate`` serves footprints through it inside the training
+box and through the FP64 solver outside it, and re-solves every
+``spot_every``-th case with the FP64 solver, returning the solver's result
+when the surrogate's relative L2 error exceeds ``tol``.
+"""
+
+import ctypes
+import json
+import math
+import os
+
+import numpy as np
+import torch
+
+from . import _lib
+from .mlp import MLP
+from .pbl_model import vertical_profiles
+from .solver import make_desc, steady_state_transport_solver
+
+KAPPA = 0.4
+# serving box: s1 = z_m / L, s2 = ln(z_m / z0), |k| z_m, levels below z_m;
+# the network is trained on TRAIN_BOX, which has a margin around it
+BOX = {"s1": (-1.0, 0.25), "s2": (4.5, 7.5), "kmin": 1e-3, "kmax": 40.0, "n": 128}
+TRAIN_BOX = {"s1": (-1.25, 0.35), "s2": (4.25, 7.75), "kmin": 1e-3, "kmax": 40.0, "n": 128}
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "surrogate_n128.npz")
+
+
+def psi(x):
+    """Businger-Dyer integrated stability function (pbl_model.py:207-230)."""
+    if x > 0:
+        return 5.0 * x
+    xi = (1.0 - 16.0 * x) ** 0.25
+    return -2.0 * math.log(0.5 * (1 + xi)) - math.log(0.5 * (1 + xi * xi)) + 2.0 * math.atan(xi) - 0.5 * math.pi
+
+
+def met_scalars(zm, wind, ustar=None, z0=None, mol=1e9):
+    """(U, s1, s2, s3): wind speed at z_m, z_m / L, ln(z_m / z0), u* / U, with
+    z0 or u* following from the other as in vertical_profiles (pbl_model.py:68-78)."""
+    U = math.hypot(float(wind[0]), float(wind[1]))
+    s1 = zm / mol
+    if z0 is None:
+        s2 = KAPPA * U / ustar - psi(zm / mol)
+    else:
+        s2 = math.log(zm / z0)
+    s3 = KAPPA / (s2 + psi(s1))
+    return U, s1, s2, s3
+
+
+def mode_kmax(srf_shape, domain, modes, halo=None):
+    """Largest |k| (1/m) of the solved modes (the solver's grid, solver.py:110-140)."""
+    ny, nx = srf_shape
+    dx, dy = domain[0] / nx, domain[1] / ny
+    h = max(domain) if halo is None else halo
+    nxe, nye = nx + 2 * int(h / dx), ny + 2 * int(h / dy)
+    nlx, nly = modes
+    if nlx > nxe or nly > nye:
+        nlx, nly = nxe, nye
+    return math.hypot(2 * math.pi / dx / nxe * (nlx // 2), 2 * math.pi / dy / nye * (nly // 2))
+
+
+class TransferPool:
+    """Nondimensional MOST met cases on the device (bldfm_transfer_pool_*)."""
+
+    def __init__(self, ncases=16384, seed=0, box=TRAIN_BOX, s1=None, s2=None):
+        self.lib = _lib.load()
+        self.box = dict(box)
+        rng = np.random.default_rng(seed)
+        self.s1 = np.ascontiguousarray(rng.uniform(*box["s1"], ncases) if s1 is None else s1, dtype=np.float64)
+        self.s2 = np.ascontiguousarray(rng.uniform(*box["s2"], ncases) if s2 is None else s2, dtype=np.float64)
+        self.ncases = self.s1.size
+        h = ctypes.c_void_p()
+        _lib.check(
+            self.lib.bldfm_transfer_pool_create(
+                _lib.ptr(self.s1), _lib.ptr(self.s2), self.ncases, int(box["n"]), ctypes.byref(h)
+            ),
+            "transfer_pool_create",
+        )
+        self.h = h
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        self.norm = None
+
+    def close(self):
+        if self.h:
+            self.lib.bldfm_transfer_pool_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def buffers(self, m):
+        f = dict(dtype=torch.float32, device=self.device)
+        return torch.empty((m, 8), **f), torch.empty((m, 4), **f), torch.empty((m, 4), **f)
+
+    def samples(self, seed, m, X, T, W, norm=None, floor=1e-3, cid=None, stream=None):
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        _lib.check(
+            self.lib.bldfm_transfer_samples(
+                self.h, int(seed) & (2**64 - 1), int(m), float(self.box["kmin"]), float(self.box["kmax"]),
+                ctypes.c_void_p(norm.data_ptr()) if norm is not None else None, float(floor),
+                ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(W.data_ptr()),
+                ctypes.c_void_p(cid.data_ptr()) if cid is not None else None, ctypes.c_void_p(s),
+            ),
+            "transfer_samples",
+        )
+
+    def eval(self, cid, kpar, kperp):
+        """Targets (m, 4) for device tensors of case ids and wavenumbers."""
+        m = cid.numel()
+        T = torch.empty((m, 4), dtype=torch.float32, device=self.device)
+        s = torch.cuda.current_stream().cuda_stream
+        _lib.check(
+            self.lib.bldfm_transfer_eval(
+                self.h, ctypes.c_void_p(cid.data_ptr()), ctypes.c_void_p(kpar.data_ptr()),
+                ctypes.c_void_p(kperp.data_ptr()), ctypes.c_void_p(T.data_ptr()), m, ctypes.c_void_p(s),
+            ),
+            "transfer_eval",
+        )
+        return T
+
+    def energies(self, per_case=2048, seed=12345):
+        """Per-case reciprocals (1/Eq, 1/Ep) of the flux and concentration
+        spectral energies, from per_case * ncases raw samples."""
+        m = per_case * self.ncases
+        chunk = 1 << 22
+        eq = torch.zeros(self.ncases, dtype=torch.float64, device=self.device)
+        ep = torch.zeros_like(eq)
+        cnt = torch.zeros_like(eq)
+        X, T, W = self.buffers(min(m, chunk))
+        cid = torch.empty(min(m, chunk), dtype=torch.int32, device=self.device)
+        for k, off in enumerate(range(0, m, chunk)):
+            n = min(chunk, m - off)
+            self.samples(seed + 7919 * k, n, X, T, W, cid=cid)
+            c = cid[:n].long()
+            eq.index_add_(0, c, W[:n, 0].double())
+            ep.index_add_(0, c, W[:n, 2].double())
+            cnt.index_add_(0, c, torch.ones(n, dtype=torch.float64, device=self.device))
+        eq = eq / cnt.clamp(min=1)
+        ep = ep / cnt.clamp(min=1)
+        self.norm = torch.stack([1.0 / eq, 1.0 / ep], 1).float().contiguous()
+        return self.norm
+
+
+def train(net, pool, steps, batch=65536, lr=1e-3, lr_final=1e-5, decay_from=0.3, seed=1, floor=1e-3,
+          log_every=100, callback=None):
+    """Adam on fresh device-generated samples every step; the learning rate
+    stays at ``lr`` for the first ``decay_from`` of the steps, then decays on a
+    cosine to ``lr_final``.  Returns [(step, loss)] every ``log_every`` steps."""
+    norm = pool.norm if pool.norm is not None else pool.energies()
+    X, T, W = pool.buffers(batch)
+    hist = []
+    for it in range(steps):
+        f = it / max(steps - 1, 1)
+        if f < decay_from:
+            lr_t = lr
+        else:
+            g = (f - decay_from) / max(1.0 - decay_from, 1e-9)
+            lr_t = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * g))
+        pool.samples(seed * 1000003 + it, batch, X, T, W, norm=norm, floor=floor)
+        net.train_step(X, T, W, lr_t)
+        if (it + 1) % log_every == 0 or it + 1 == steps:
+            _, loss = net.grads()
+            hist.append((it + 1, loss))
+            if callback:
+                callback(it + 1, loss)
+    return hist
+
+
+def validation_loss(net, pool, m=65536, seed=999, floor=1e-3):
+    """Weighted loss of the network on fresh samples (no update)."""
+    norm = pool.norm if pool.norm is not None else pool.energies()
+    X, T, W = pool.buffers(m)
+    pool.samples(seed, m, X, T, W, norm=norm, floor=floor)
+    net.train_step(X, T, W, 0.0)
+    return net.grads()[1]
+
+
+def save(net, path, meta=None):
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    np.savez(path, params=net.params(), box=json.dumps(BOX), meta=json.dumps(meta or {}))
+
+
+def load(path=WEIGHTS, batch=65536):
+    """MLP with saved parameters, and the box and metadata it was trained with."""
+    d = np.load(path)
+    net = MLP(batch=batch, seed=0)
+    net.set_params(d["params"])
+    return net, json.loads(str(d["box"])), json.loads(str(d["meta"]))
+
+
+def _rell2(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+class Surrogate:
+    """Footprints at z_m through the MLP, with the FP64 solver as fallback.
+
+    ``footprint(...)`` takes the met case as ``vertical_profiles`` does and the
+    footprint grid as ``steady_state_transport_solver`` does, and returns
+    ``(grid, conc, flx)`` like the solver.  ``stats`` counts the cases served
+    by the network, out-of-box fallbacks, spot checks and their failures.
+    """
+
+    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0):
+        self.lib = _lib.load()
+        self.net = net
+        self.box = dict(BOX if box is None else box)
+        self.spot_every = int(spot_every)
+        self.tol = float(tol)
+        self.variant = int(variant)  # 0 fused kernel, 1 exact transfer (check), 2 layer by layer
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        self._ws = None
+        self._out = None
+        self.count = 0
+        self.stats = {"surrogate": 0, "out_of_box": 0, "spot": 0, "spot_fail": 0, "errors": []}
+
+    def in_box(self, n, zm, s1, s2, kmax):
+        b = self.box
+        return (
+            n == b["n"]
+            and b["s1"][0] <= s1 <= b["s1"][1]
+            and b["s2"][0] <= s2 <= b["s2"][1]
+            and zm * kmax <= b["kmax"]
+        )
+
+    def prepare(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
+                ustar=None, z0=None, mol=1e9):
+        """Host inputs of one surrogate solve (reusable across calls)."""
+        z, prof = vertical_profiles(n, zm, wind, ustar=ustar, z0=z0, mol=mol)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        prof = np.ascontiguousarray(np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), z.shape) for p in prof]))
+        U, s1, s2, s3 = met_scalars(zm, wind, ustar, z0, mol)
+        d = make_desc(srf_shape, z.size, domain, modes, meas_pt, 0.0, True, False, halo, "single", "fp32")
+        info = _lib.PlanInfo()
+        _lib.check(self.lib.bldfm_plan(d, 1, info), "surrogate")
+        met = _lib.SurrogateCase(zm=float(z[n]), wind=U, s1=s1, s2=s2, s3=s3, variant=self.variant)
+        lv = np.array([n], dtype=np.int64)
+        need = ctypes.c_int64(0)
+        _lib.check(self.lib.bldfm_surrogate_plan(d, 1, ctypes.byref(need)), "surrogate")
+        return {"desc": d, "met": met, "z": z, "prof": prof, "lv": lv, "shape": (info.out_ny, info.out_nx),
+                "need": int(need.value), "s": (s1, s2, s3), "zm": zm,
+                "kw": dict(srf_flx=np.zeros(srf_shape), z=z, profiles=tuple(prof), domain=domain, levels=n,
+                           modes=modes, meas_pt=meas_pt, footprint=True, halo=halo)}
+
+    def solve_prepared(self, p, conc=None, flx=None, stream=None):
+        """Enqueue one surrogate solve; returns device (conc, flx) of shape (out_ny, out_nx)."""
+        if self._ws is None or self._ws.numel() < p["need"]:
+            self._ws = torch.empty(p["need"], dtype=torch.uint8, device=self.device)
+        if conc is None:
+            sz = p["shape"][0] * p["shape"][1]
+            if self._out is None or self._out.numel() < 2 * sz:
+                self._out = torch.empty(2 * sz, dtype=torch.float64, device=self.device)
+            conc = self._out[:sz].view(p["shape"])
+            flx = self._out[sz : 2 * sz].view(p["shape"])
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        st = self.lib.bldfm_surrogate_solve(
+            self.net.h if self.net is not None else None, p["desc"], p["met"], _lib.ptr(p["z"]), _lib.ptr(p["prof"]),
+            _lib.ptr(p["lv"]), 1, ctypes.c_void_p(conc.data_ptr()), ctypes.c_void_p(flx.data_ptr()),
+            ctypes.c_void_p(self._ws.data_ptr()), ctypes.c_size_t(self._ws.numel()), ctypes.c_void_p(s),
+        )
+        _lib.check(st, "surrogate_solve")
+        return conc, flx
+
+    def footprint(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
+                  ustar=None, z0=None, mol=1e9):
+        """One footprint at z_m: (grid, conc, flx) as the solver returns them,
+        and the path that produced it ("surrogate", "fp64-box", "fp64-spot")."""
+        p = self.prepare(n, zm, wind, srf_shape, domain, modes, meas_pt, halo, ustar, z0, mol)
+        s1, s2, _ = p["s"]
+        self.count += 1
+        if not (self.variant == 1 or self.in_box(n, zm, s1, s2, mode_kmax(srf_shape, domain, modes, halo))):
+            self.stats["out_of_box"] += 1
+            return steady_state_transport_solver(**p["kw"], mode="fp64"), "fp64-box"
+        conc_d, flx_d = self.solve_prepared(p)
+        conc, flx = conc_d.cpu().numpy(), flx_d.cpu().numpy()
+        grid = _grid(p["z"], n, srf_shape, domain)
+        self.stats["surrogate"] += 1
+        if self.spot_every > 0 and self.count % self.spot_every == 0:
+            ref = steady_state_transport_solver(**p["kw"], mode="fp64")
+            err = max(_rell2(conc, ref[1]), _rell2(flx, ref[2]))
+            self.stats["spot"] += 1
+            self.stats["errors"].append(err)
+            if err > self.tol:
+                self.stats["spot_fail"] += 1
+                return ref, "fp64-spot"
+        return (grid, conc, flx), "surrogate"
+
+
+def _grid(z, level, shape, domain):
+    ny, nx = shape
+    x = np.linspace(0, domain[0], nx, endpoint=False)
+    y = np.linspace(0, domain[1], ny, endpoint=False)
+    Z, Y, X = np.meshgrid(np.asarray(z)[[level]], y, x, indexing="ij")
+    return tuple(np.squeeze(a) for a in (X, Y, Z))
+
+
+def _main(argv=None):
+    """python -m bldfm_gb300.surrogate train [--steps N] [--out PATH]: train
+    the network on the GPU from solver-generated transfer functions and save
+    it (the shipped weights were made this way)."""
+    import argparse
+    import time
+
+    ap = argparse.ArgumentParser(prog="python -m bldfm_gb300.surrogate")
+    ap.add_argument("command", choices=["train"])
+    ap.add_argument("--steps", type=int, default=100000)
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--cases", type=int, default=16384)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", default=WEIGHTS)
+    a = ap.parse_args(argv)
+    pool = TransferPool(ncases=a.cases, seed=0)
+    net = MLP(batch=a.batch, seed=a.seed)
+    t0 = time.time()
+    hist = train(net, pool, a.steps, batch=a.batch, lr=a.lr, seed=a.seed, log_every=max(a.steps // 50, 1),
+                 callback=lambda i, l: print("step %d loss %.3e (%.0f s)" % (i, l, time.time() - t0), flush=True))
+    torch.cuda.synchronize()
+    dt = time.time() - t0
+    val = validation_loss(net, pool)
+    save(net, a.out, {"steps": a.steps, "batch": a.batch, "lr": a.lr, "cases": a.cases, "seed": a.seed,
+                      "train_s": dt, "val_loss": float(val), "train_box": TRAIN_BOX, "history": hist[-10:]})
+    print("saved %s: validation loss %.3e, %.1f s" % (a.out, val, dt))
+
+
+if __name__ == "__main__":
+    _main()

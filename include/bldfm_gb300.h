@@ -188,26 +188,92 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases,
 int bldfm_tc_gemm_check(const uint16_t *A, const uint16_t *B, float *D,
                         int32_t M, int32_t K);
 
-/* The surrogate MLP (no reference counterpart): inputs (5 features, rows of
+/* The surrogate MLP (no reference counterpart): inputs (8 features, rows of
  * 8 floats) -> 4 x 256 GELU hidden layers -> 4 outputs.  The three 256 x 256
  * layers run forward and backward on the tcgen05 tensor cores (BF16 operands,
- * FP32 accumulation in tensor memory); FP32 master weights, Adam.  The handle
- * owns device buffers for up to `batch` samples (multiple of 256). */
+ * FP32 accumulation in tensor memory); the last hidden layer and the output
+ * layer stay FP32; FP32 master weights, Adam.  The handle owns device buffers
+ * for up to `batch` samples (multiple of 256). */
 int bldfm_surrogate_create(int32_t batch, uint64_t seed, void **handle);
 int bldfm_surrogate_destroy(void *handle);
 int bldfm_surrogate_nparams(void);
+/* sample capacity of the handle */
+int bldfm_surrogate_batch(void *handle);
 /* get (host_out) and/or set (host_in) the FP32 parameter vector */
 int bldfm_surrogate_params(void *handle, float *host_out, const float *host_in);
 /* gradients and loss of the last training step */
 int bldfm_surrogate_grads(void *handle, float *host_grads, float *host_loss);
-/* one Adam step on n samples (device X [n][8], T [n][4], w [n]); lr = 0
- * computes the gradients only */
+/* one Adam step on n samples (device X [n][8], T [n][4], w [n][4]):
+ * loss = sum w (y - t)^2 / n; lr = 0 computes the gradients only */
 int bldfm_surrogate_train_step(void *handle, const float *X, const float *T,
                                const float *w, int32_t n, float lr,
                                void *stream);
 /* Y [n][4] = MLP(X [n][8]), device pointers, n % 256 == 0 */
 int bldfm_surrogate_forward(void *handle, const float *X, float *Y, int32_t n,
                             void *stream);
+
+/* Footprint-weighted point measurement, replaces point_measurement
+ * (src/bldfm/utils.py:80-92, np.sum(f * g)) for a batch: out[b] =
+ * sum_{i < n} f[b * stride + i] * g[b * stride + i] in FP64 (Kahan-compensated,
+ * deterministic order).  Device pointers; workspace of
+ * bldfm_point_measurement_workspace(n, nbatch) bytes, 8-byte aligned. */
+int64_t bldfm_point_measurement_workspace(int64_t n, int32_t nbatch);
+int bldfm_point_measurement(const double *f_dev, const double *g_dev,
+                            int64_t n, int64_t stride, int32_t nbatch,
+                            double *out_dev, void *workspace_dev,
+                            size_t workspace_bytes, void *stream);
+
+/* Training data of the surrogate (no reference counterpart): a pool of
+ * nondimensional MOST met cases (s1 = z_m / L, s2 = ln(z_m / z0)) on the
+ * n-level stretched grid of vertical_profiles (src/bldfm/pbl_model.py:8-204,
+ * default stretch and top), whose per-mode transfer at z_m the FP32
+ * invariant-imbedding sweep evaluates on the device.  Targets per sample:
+ * log|Tq| / (1 + k), arg Tq / (1 + k), log|R~|, arg R~ with Tq = q(z_m) / q(0),
+ * R~ = U p(z_m) / q(z_m), k = |k| z_m. */
+int bldfm_transfer_pool_create(const double *s1, const double *s2,
+                               int32_t ncases, int32_t n, void **pool);
+int bldfm_transfer_pool_destroy(void *pool);
+/* u* / U and the level count of pool case c */
+int bldfm_transfer_pool_case(void *pool, int32_t c, double *s3, int32_t *nz);
+/* m random samples (case uniform, |k| log-uniform in [kmin, kmax], first
+ * quadrant): X [m][8] features, T [m][4] targets, W [m][4] loss weights for
+ * the footprint's relative L2 error given per-case energy reciprocals
+ * norm [ncases][2] (flux, conc), or raw energies when norm is NULL;
+ * cid [m] (optional) the case ids.  Device pointers. */
+int bldfm_transfer_samples(void *pool, uint64_t seed, int32_t m, float kmin,
+                           float kmax, const float *norm, float floor_w,
+                           float *X, float *T, float *W, int32_t *cid,
+                           void *stream);
+/* targets of given samples (device cid [m], kpar [m], kperp [m] -> T [m][4]) */
+int bldfm_transfer_eval(void *pool, const int32_t *cid, const float *kpar,
+                        const float *kperp, float *T, int32_t m, void *stream);
+
+/* Surrogate footprint solve (no reference counterpart; stands in for
+ * steady_state_transport_solver, src/bldfm/solver.py:16-304, in footprint
+ * mode with MOST profiles): the FP32 path with the per-mode sweep replaced
+ * by the MLP's transfer at z_m, then the solver's own output transform.
+ * Requires desc->mode == BLDFM_MODE_FP32, footprint, one output level at
+ * z_m, Kx == Ky and one wind direction (else BLDFM_ERR_UNSUPPORTED).  The
+ * caller decides whether the case lies in the network's training box. */
+typedef struct bldfm_surrogate_case {
+    double zm;        /* measurement height, a level of z */
+    double wind;      /* wind speed at z_m */
+    double s1, s2, s3; /* z_m / L, ln(z_m / z0), u* / wind */
+    int32_t variant;  /* 0: fused features -> MLP -> spectra kernel;
+                       * 1: transfer from the nondimensional FP32 sweep of
+                       *    this case instead of the MLP (checks the serving
+                       *    path; net may be NULL);
+                       * 2: the MLP layer by layer (bldfm_surrogate_forward) */
+    int32_t reserved;
+} bldfm_surrogate_case;
+int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls,
+                         int64_t *workspace_bytes);
+int bldfm_surrogate_solve(void *net, const bldfm_desc *d,
+                          const bldfm_surrogate_case *met, const double *z_host,
+                          const double *prof_host, const int64_t *levels_host,
+                          int32_t nlvls, double *conc_dev, double *flx_dev,
+                          void *workspace_dev, size_t workspace_bytes,
+                          void *stream);
 
 /* Allocation-free FP32 solve.  No counterpart in the reference (which never
  * touches a GPU).  For callers that may not allocate device memory while they

@@ -1,17 +1,19 @@
 """CPU oracle of the surrogate MLP -- test infrastructure only.
 
-FP64 forward and backward of 5 -> 4 x 256 GELU -> 4 with BF16 rounding
+FP64 forward and backward of 8 -> 4 x 256 GELU (tanh form) -> 4 with BF16 rounding
 emulated at exactly the points where the GPU kernels round
-(bldfm_gb300/csrc/surrogate.cu): hidden weights as BF16, hidden activations
-H and GELU'(Z) stored as BF16, and every dZ rounded to BF16 before it enters a
-GEMM.  Accumulations are FP64 here and FP32 on the GPU.
+(bldfm_gb300/csrc/surrogate.cu): hidden weights as BF16, the activations of
+the first three hidden layers and every GELU'(Z) stored as BF16 (the last
+hidden layer stays FP32), and every dZ rounded to BF16 before it enters a
+GEMM.  Accumulations are FP64 here and FP32 on the GPU; tanh is exact here
+and the hardware tanh.approx there.
 """
 
 import math
 
 import numpy as np
 
-H, N_IN, N_OUT = 256, 5, 4
+H, N_IN, N_OUT = 256, 8, 4
 
 
 def bf16(x):
@@ -21,15 +23,17 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-_erf = np.vectorize(math.erf)
+GELU_C, GELU_A = math.sqrt(2.0 / math.pi), 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    """GELU in its tanh form (Hendrycks & Gimpel, 2016), as the kernels use it."""
+    return 0.5 * z * (1.0 + np.tanh(GELU_C * (z + GELU_A * z**3)))
 
 
 def gelu_d(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(GELU_C * (z + GELU_A * z**3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_C * (1.0 + 3.0 * GELU_A * z * z)
 
 
 def unpack(p):
@@ -52,7 +56,7 @@ def unpack(p):
 
 
 def forward_backward(p, X, T, w):
-    """Returns (Y, loss, grad flat) for inputs X [n][5+], targets T [n][4], weights w [n]."""
+    """Returns (Y, loss, grad flat) for inputs X [n][8], targets T [n][4], weights w [n][4]."""
     W0, b0, Wt, b, W4, b4 = unpack(p)
     X = np.asarray(X, dtype=np.float64)[:, :N_IN]
     n = X.shape[0]
@@ -62,12 +66,13 @@ def forward_backward(p, X, T, w):
     Gs = [bf16(gelu_d(z))]
     for j in range(3):
         z = Hs[-1] @ Wtb[j].T + b[j]
-        Hs.append(bf16(gelu(z)))
+        Hs.append(bf16(gelu(z)) if j < 2 else gelu(z))
         Gs.append(bf16(gelu_d(z)))
     Y = Hs[3] @ W4 + b4
     e = Y - T
-    loss = float(np.sum(w[:, None] * e * e) / n)
-    dY = 2.0 * w[:, None] * e / n
+    w = np.asarray(w, dtype=np.float64).reshape(n, N_OUT)
+    loss = float(np.sum(w * e * e) / n)
+    dY = 2.0 * w * e / n
     g = {}
     g["W4"] = Hs[3].T @ dY
     g["b4"] = dY.sum(0)

@@ -10,10 +10,12 @@ pytestmark = pytest.mark.gpu
 
 def _data(n, seed):
     rng = np.random.default_rng(seed)
-    X = np.zeros((n, 8), dtype=np.float32)
-    X[:, :5] = rng.uniform(-1, 1, (n, 5))
-    T = np.stack([np.sin(2 * X[:, 0]) * X[:, 1], np.cos(X[:, 2] + X[:, 3]), X[:, 4] ** 2, X[:, 0] * X[:, 3]], 1)
-    w = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    X = rng.uniform(-1, 1, (n, 8)).astype(np.float32)
+    T = np.stack(
+        [np.sin(2 * X[:, 0]) * X[:, 1], np.cos(X[:, 2] + X[:, 3]), X[:, 4] ** 2 + X[:, 5], X[:, 0] * X[:, 6] - X[:, 7]],
+        1,
+    )
+    w = rng.uniform(0.5, 1.5, (n, 4)).astype(np.float32)
     return X, T.astype(np.float32), w
 
 

@@ -1,0 +1,100 @@
+"""The learned surrogate on the GPU: its training data against the FP64 CPU
+oracle, its serving path against the solver, and what training gains."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def test_transfer_samples_match_oracle():
+    """FP32 device sweep of the nondimensional transfer vs the FP64 oracle."""
+    from bldfm_gb300.surrogate import TransferPool
+    from oracle.transfer_oracle import transfer
+
+    s1 = np.array([-1.5, -0.4, 0.0, 0.8])
+    s2 = np.array([2.5, 6.0, 4.6, 7.5])
+    pool = TransferPool(s1=s1, s2=s2)
+    rng = np.random.default_rng(0)
+    m = 512
+    cid = rng.integers(0, 4, m).astype(np.int32)
+    k = np.exp(rng.uniform(np.log(1e-3), np.log(40.0), m))
+    th = rng.uniform(0, np.pi / 2, m)
+    kpar, kperp = (k * np.cos(th)).astype(np.float32), (k * np.sin(th)).astype(np.float32)
+    dev = pool.device
+    T = pool.eval(*(torch.from_numpy(a).to(dev) for a in (cid, kpar, kperp))).cpu().numpy()
+    for c in range(4):
+        sel = cid == c
+        _, _, ref = transfer(s1[c], s2[c], 128, kpar[sel].astype(np.float64), kperp[sel].astype(np.float64))
+        err = np.abs(T[sel] - ref)
+        assert err.max() < 2e-4, (c, err.max(axis=0))
+
+
+def test_sample_weights_and_features():
+    from bldfm_gb300.surrogate import TransferPool
+
+    pool = TransferPool(ncases=64, seed=3)
+    norm = pool.energies(per_case=256)
+    assert torch.isfinite(norm).all() and (norm > 0).all()
+    X, T, W = pool.buffers(4096)
+    pool.samples(7, 4096, X, T, W, norm=norm)
+    for a in (X, T, W):
+        assert torch.isfinite(a).all()
+    assert (W > 0).all()
+    # the same seed gives the same samples
+    X2, T2, W2 = pool.buffers(4096)
+    pool.samples(7, 4096, X2, T2, W2, norm=norm)
+    assert torch.equal(X, X2) and torch.equal(T, T2)
+
+
+@pytest.mark.parametrize("wdir,mol", [(225.0, -50.0), (270.0, 1e9), (40.0, 80.0)])
+def test_exact_transfer_serving_matches_solver(wdir, mol):
+    """The serving path with the exact nondimensional transfer in place of the
+    network reproduces the solver's footprint (checks features, rotation,
+    conjugation, phase shift, k = 0 values and the output transform)."""
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import Surrogate
+
+    th = np.deg2rad(wdir)
+    wind = (-4.0 * np.sin(th), -4.0 * np.cos(th))
+    sur = Surrogate(variant=1, spot_every=0)
+    args = dict(n=32, zm=20.0, wind=wind, srf_shape=(128, 128), domain=(1000.0, 1000.0), modes=(128, 128),
+                meas_pt=(500.0, 500.0), ustar=0.3, mol=mol)
+    (grid, conc, flx), path = sur.footprint(**args)
+    assert path == "surrogate"
+    p = sur.prepare(**args)
+    _, c64, f64 = steady_state_transport_solver(**p["kw"], mode="fp64r")
+    assert conc.shape == c64.shape
+    assert _rel(flx, f64) < 2e-5
+    assert _rel(conc, c64) < 2e-5
+    assert abs(flx.sum() - f64.sum()) / abs(f64.sum()) < 1e-5
+
+
+def test_fused_serving_matches_layerwise():
+    """The fused features -> MLP -> spectra kernel computes what the
+    layer-by-layer tensor-core MLP and the spectra kernel compute."""
+    from bldfm_gb300.mlp import MLP
+    from bldfm_gb300.surrogate import Surrogate
+
+    net = MLP(batch=16384, seed=11)
+    p = net.params()
+    p *= 0.5  # keep the untrained outputs moderate
+    net.set_params(p)
+    args = dict(n=128, zm=20.0, wind=(2.83, 2.83), srf_shape=(256, 256), domain=(1000.0, 1000.0),
+                modes=(256, 256), meas_pt=(500.0, 500.0), ustar=0.3, mol=-50.0)
+    outs = []
+    for variant in (0, 2):
+        sur = Surrogate(net, variant=variant, spot_every=0)
+        c, f = sur.solve_prepared(sur.prepare(**args))
+        outs.append((c.cpu().numpy(), f.cpu().numpy()))
+    assert np.all(np.isfinite(outs[0][0])) and np.all(np.isfinite(outs[0][1]))
+    assert _rel(outs[0][0], outs[1][0]) < 1e-5
+    assert _rel(outs[0][1], outs[1][1]) < 1e-5
