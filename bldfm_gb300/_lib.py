@@ -176,6 +176,12 @@ _SIGS = {
         [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P],
     ),
     "bldfm_surrogate_plan": (ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
+    "bldfm_surrogate_batch_plan": (
+        ctypes.c_int, [ctypes.POINTER(Case), ctypes.POINTER(SurrogateCase), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+    ),
+    "bldfm_surrogate_solve_batch": (
+        ctypes.c_int, [_P, ctypes.POINTER(Case), ctypes.POINTER(SurrogateCase), ctypes.c_int32, _P, ctypes.c_size_t, _P]
+    ),
     "bldfm_surrogate_solve": (
         ctypes.c_int,
         [_P, ctypes.POINTER(Desc), ctypes.POINTER(SurrogateCase), _P, _P, _P, ctypes.c_int32, _P, _P, _P,

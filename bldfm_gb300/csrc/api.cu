@@ -662,7 +662,7 @@ struct BatchBuild {
     std::vector<int4 *> xb;
     size_t off_cases = 0, off_tile_case = 0, off_cta_tiles = 0, off_col_case = 0, off_row_case = 0;
     std::vector<size_t> off_lv32, off_lv64, off_slot, off_dc;
-    size_t blob_bytes = 0, blob_at = 0;
+    size_t blob_bytes = 0, blob_at = 0, extra_off = 0;
     std::vector<size_t> d_q0, d_A, d_scratch, d_Xp, d_Xq, d_Cb;
     size_t total = 0;
     int64_t ntiles = 0;
@@ -671,7 +671,8 @@ struct BatchBuild {
     std::vector<int64_t> tile0, col0, row0;
 };
 
-int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, DeviceCache *dc, BatchBuild &B)
+int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, DeviceCache *dc, BatchBuild &B,
+                size_t extra_blob = 0)
 {
     if (!cs || n < 1) return BLDFM_ERR_ARG;
     B.threads = (opts && opts->threads > 0) ? opts->threads : 256;
@@ -731,6 +732,8 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
         B.off_dc[k] = o;
         o = al(o + (size_t)g.nlvls * 32);
     }
+    B.extra_off = o;  // caller's region at the end of the blob
+    o = al(o + extra_blob);
     B.blob_bytes = o;
     // workspace: status word, blob, per-case device regions
     size_t w = 0;
@@ -966,8 +969,8 @@ SurLayout sur_layout(const SolveGeom &g)
     o = al(o + (size_t)S.npad * 16);
     S.steps = o;
     o = al(o + (size_t)std::max(g.nz - 1, 1) * 16);
-    S.tcase = o;
-    o = al(o + sizeof(TransferCase));
+    S.tcase = o;  // TransferCase (exact variant) or SurCase (fused kernel)
+    o = al(o + std::max(sizeof(TransferCase), sizeof(SurCase)));
     S.total = o;
     return S;
 }
@@ -1015,8 +1018,9 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
     const size_t lv64b = (size_t)std::max(nz - 1, 0) * BLDFM_LV64 * 8;
     const size_t dcb = 32, stb = (size_t)std::max(nz - 1, 1) * 16;
     const size_t off_dc = al(lv64b), off_st = off_dc + al(dcb), off_tc = off_st + al(stb);
+    const size_t tcb = std::max(sizeof(TransferCase), sizeof(SurCase));
     StageSlot *slt = nullptr;
-    if ((rc = acquire_stage(dc, off_tc + al(sizeof(TransferCase)) + 256, &slt)) != BLDFM_OK) return rc;
+    if ((rc = acquire_stage(dc, off_tc + al(tcb) + 256, &slt)) != BLDFM_OK) return rc;
     char *sg = (char *)slt->buf;
     hx_level_table(nz, z, prof, (double *)sg);
     hx_dc_values(nz, (const double *)sg, hp.slot.data(), g.q0dc_fp, 0.0, d->srf_bg_conc, 1, 1, 0,
@@ -1038,23 +1042,43 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
         tc->s3 = (float)met->s3;
         tc->pad = 0;
     }
+    const float ax = (float)(g.lx_scale * g.valx), ay = (float)(g.ly_scale * g.valy);
+    float2 *Xp = (float2 *)(w + S.L.Xp), *Xq = (float2 *)(w + S.L.Xq);
+    const float inv_wind = (float)(1.0 / met->wind);
+    if (met->variant == 0) {
+        SurCase *c = (SurCase *)(sg + off_tc);
+        memset(c, 0, sizeof(SurCase));
+        c->g = g;
+        c->modes = ml->dev;
+        c->Xp = Xp;
+        c->Xq = Xq;
+        c->ax = ax;
+        c->ay = ay;
+        c->zm = zm;
+        c->s1 = (float)met->s1;
+        c->s2 = (float)met->s2;
+        c->s3 = (float)met->s3;
+        c->inv_wind = inv_wind;
+        c->ktop = ktop;
+        c->utop = utop;
+        c->tile0 = 0;
+    }
     double2 *dcv = (double2 *)(w + S.L.dc);
     CK(cudaMemsetAsync(w + S.L.err, 0, 64, st));
     CK(cudaMemcpyAsync(dcv, sg + off_dc, dcb, cudaMemcpyHostToDevice, st));
     if (exact) {
         CK(cudaMemcpyAsync(w + S.steps, sg + off_st, stb, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(w + S.tcase, sg + off_tc, sizeof(TransferCase), cudaMemcpyHostToDevice, st));
+    } else if (met->variant == 0) {
+        CK(cudaMemcpyAsync(w + S.tcase, sg + off_tc, sizeof(SurCase), cudaMemcpyHostToDevice, st));
     }
     CK(cudaEventRecord(slt->ev, st));
-    const float ax = (float)(g.lx_scale * g.valx), ay = (float)(g.ly_scale * g.valy);
     float *X = (float *)(w + S.X), *Y = (float *)(w + S.Y);
-    float2 *Xp = (float2 *)(w + S.L.Xp), *Xq = (float2 *)(w + S.L.Xq);
-    const float inv_wind = (float)(1.0 / met->wind);
     if (met->variant == 0) {
         MlpServing view;
         if ((rc = mlp_serving_view(net, &view)) != BLDFM_OK) return rc;
-        CK(launch_sur_serve(g, ml->dev, ax, ay, zm, (float)met->s1, (float)met->s2, (float)met->s3, inv_wind, ktop,
-                            utop, view, Xp, Xq, (int *)(w + S.L.err), dc.nsm, st));
+        CK(launch_sur_serve((const SurCase *)(w + S.tcase), 1, (g.nsolved + 127) / 128, view, (int *)(w + S.L.err),
+                            dc.nsm, st));
     } else {
         if (exact) {
             CK(launch_sur_exact(g, ml->dev, ax, ay, zm, (const TransferCase *)(w + S.tcase),
@@ -1073,6 +1097,97 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
     }
     CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
                                 (float2 *)(w + S.L.Cb), conc, flx, st));
+    return BLDFM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched surrogate serving (bldfm_surrogate_solve_batch): every case's
+// 128-mode tiles in one persistent fused launch, then the batched output
+// transform of the FP32 batch path
+// ---------------------------------------------------------------------------
+int sur_batch_check(const bldfm_case *cs, const bldfm_surrogate_case *mets, int n)
+{
+    if (!cs || !mets || n < 1) return BLDFM_ERR_ARG;
+    for (int k = 0; k < n; ++k) {
+        const int rc = sur_check_desc(&cs[k].desc, cs[k].nlvls);
+        if (rc != BLDFM_OK) return rc;
+        if (mets[k].variant != 0 || !(mets[k].zm > 0) || !(mets[k].wind > 0)) return BLDFM_ERR_ARG;
+    }
+    return BLDFM_OK;
+}
+
+int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_case *mets, int n, void *ws,
+                         size_t ws_bytes, cudaStream_t st)
+{
+    int rc = sur_batch_check(cs, mets, n);
+    if (rc != BLDFM_OK) return rc;
+    if (!net || !ws) return BLDFM_ERR_ARG;
+    if (((uintptr_t)ws & 255) != 0) return BLDFM_ERR_ARG;
+    int status = BLDFM_OK;
+    DeviceCache &dc = cache_for_current(&status);
+    if (status != BLDFM_OK) return status;
+    BatchBuild B;
+    bldfm_batch_opts opts = {256, 0, 0, 0};
+    if ((rc = batch_build(cs, n, &opts, &dc, B, sizeof(SurCase) * (size_t)n)) != BLDFM_OK) return rc;
+    if (ws_bytes < B.total) return BLDFM_ERR_WORKSPACE;
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        const int nz = g.nz;
+        const int64_t lev = cs[k].levels_host[0] < 0 ? cs[k].levels_host[0] + nz : cs[k].levels_host[0];
+        if (!g.iso) return BLDFM_ERR_UNSUPPORTED;
+        if (fabs(cs[k].z_host[lev] - mets[k].zm) > 1e-6 * mets[k].zm) return BLDFM_ERR_ARG;
+    }
+    StageSlot *slt = nullptr;
+    if ((rc = acquire_stage(dc, B.blob_bytes + 256, &slt)) != BLDFM_OK) return rc;
+    char *blob = (char *)slt->buf;
+    char *w = (char *)ws;
+    batch_fill_blob(cs, n, B, w, blob);
+    SurCase *sc = (SurCase *)(blob + B.extra_off);
+    int64_t t = 0;
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        const int nz = g.nz;
+        const double *prof = cs[k].prof_host;
+        const bldfm_surrogate_case &m = mets[k];
+        SurCase &c = sc[k];
+        memset(&c, 0, sizeof(c));
+        c.g = g;
+        c.modes = B.ml[k]->dev;
+        c.Xp = (float2 *)(w + B.d_Xp[k]);
+        c.Xq = (float2 *)(w + B.d_Xq[k]);
+        c.ax = (float)(g.lx_scale * g.valx);
+        c.ay = (float)(g.ly_scale * g.valy);
+        c.zm = (float)m.zm;
+        c.s1 = (float)m.s1;
+        c.s2 = (float)m.s2;
+        c.s3 = (float)m.s3;
+        c.inv_wind = (float)(1.0 / m.wind);
+        c.ktop = (float)(prof[4 * nz + nz - 1] / (m.wind * m.zm));
+        c.utop = (float)((prof[nz - 1] * g.ex + prof[nz + nz - 1] * g.ey) / m.wind);
+        c.tile0 = t;
+        t += (g.nsolved + 127) / 128;
+    }
+    CK(cudaMemcpyAsync(w + B.blob_at, blob, B.blob_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w, 0, 64, st));
+    CK(cudaEventRecord(slt->ev, st));
+    MlpServing view;
+    if ((rc = mlp_serving_view(net, &view)) != BLDFM_OK) return rc;
+    char *wb = w + B.blob_at;
+    CK(launch_sur_serve((const SurCase *)(wb + B.extra_off), n, t, view, (int *)w, dc.nsm, st));
+    BatchLaunch bl;
+    memset(&bl, 0, sizeof(bl));
+    bl.cases = (const BatchCase *)(wb + B.off_cases);
+    bl.tile_case = (const int *)(wb + B.off_tile_case);
+    bl.cta_tiles = (const int64_t *)(wb + B.off_cta_tiles);
+    bl.col_case = (const int *)(wb + B.off_col_case);
+    bl.row_case = (const int *)(wb + B.off_row_case);
+    bl.err = (int *)w;
+    bl.threads = B.threads;
+    bl.col_ctas = B.ncol;
+    bl.col_smem = B.col_smem;
+    bl.row_ctas = B.nrow;
+    bl.row_smem = B.row_smem;
+    CK(launch_batch_kernels(bl, st, 1));
     return BLDFM_OK;
 }
 
@@ -1352,6 +1467,28 @@ int bldfm_surrogate_solve(void *net, const bldfm_desc *d, const bldfm_surrogate_
     std::lock_guard<std::mutex> lk(g_mutex);
     return sur_solve_impl(net, d, met, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
                           workspace_bytes, (cudaStream_t)stream);
+}
+
+int bldfm_surrogate_batch_plan(const bldfm_case *cases, const bldfm_surrogate_case *mets, int32_t ncases,
+                               int64_t *workspace_bytes)
+{
+    if (!workspace_bytes) return BLDFM_ERR_ARG;
+    int rc = sur_batch_check(cases, mets, ncases);
+    if (rc != BLDFM_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_mutex);
+    BatchBuild B;
+    bldfm_batch_opts opts = {256, 0, 0, 0};
+    if ((rc = batch_build(cases, ncases, &opts, nullptr, B, sizeof(SurCase) * (size_t)ncases)) != BLDFM_OK)
+        return rc;
+    *workspace_bytes = (int64_t)B.total;
+    return BLDFM_OK;
+}
+
+int bldfm_surrogate_solve_batch(void *net, const bldfm_case *cases, const bldfm_surrogate_case *mets,
+                                int32_t ncases, void *workspace, size_t workspace_bytes, void *stream)
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    return sur_solve_batch_impl(net, cases, mets, ncases, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
 }  // extern "C"

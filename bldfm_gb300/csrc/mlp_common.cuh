@@ -38,8 +38,10 @@ __device__ __forceinline__ float tanh_approx(float x)
 #define GELU_A 0.044715f
 __device__ __forceinline__ float gelu_f(float z)
 {
-    const float t = tanh_approx(GELU_C * fmaf(GELU_A * z * z, z, z));
-    return 0.5f * z * (1.0f + t);
+    // u = z (c + c a z^2), gelu = z/2 + z/2 tanh(u)
+    const float u = z * fmaf(GELU_C * GELU_A, z * z, GELU_C);
+    const float hz = 0.5f * z;
+    return fmaf(hz, tanh_approx(u), hz);
 }
 __device__ __forceinline__ float gelu_d(float z)
 {

@@ -103,24 +103,32 @@ __global__ void sur_spectra_kernel(const SolveGeom g, const uint32_t *__restrict
 
 // ---------------------------------------------------------------------------
 // Fused serving kernel: features -> MLP -> spectra for 128 modes per tile,
-// one persistent CTA of 256 threads per SM.  The tile's activations stay in
-// shared memory (BF16, core-matrix K-major layout: the A operand of the next
-// layer), the hidden 256 x 256 layers run as one tcgen05 MMA chain each
-// (M = 128, N = 256, K = 256) into a 256-column TMEM accumulator, and the
-// next layer's BF16 weights stream into the single 128 KB weight buffer by
-// bulk copy while the epilogue (bias + GELU from TMEM) runs.  The input and
-// output layers are FP32 on the CUDA cores.  Every mbarrier wait is bounded;
-// on a timeout the kernel records BLDFM_ERR_TIMEOUT, waits (bounded) for its
-// own copies and MMAs in flight, frees TMEM and returns.
+// one persistent CTA of 256 threads per SM.  All four matrix layers run on
+// the tensor cores (tcgen05.mma, M = 128, N = 256, FP32 accumulator in a
+// 256-column TMEM allocation); the epilogues (bias + GELU, from TMEM) and the
+// 256 -> 4 output layer run on the CUDA cores in FP32.
+//
+// Input layer in BF16 at FP32 accuracy: x = xh + xl and W0 = wh + wl split
+// into BF16 parts, K = 32 columns [xh | xl | xh | 0] x [wh | wh | wl | 0]
+// give x.W0 up to the xl.wl term (relative 2^-16).
+//
+// Shared memory: the tile's activations (BF16, core-matrix K-major layout: the
+// A operand of the next layer; the first 8 KB hold the input-layer operand
+// before its MMA), one 256 x 256 BF16 weight matrix streamed by bulk copy
+// while the previous layer's epilogue runs, the split W0, biases, W4.  Every
+// mbarrier wait is bounded; on a timeout the kernel records
+// BLDFM_ERR_TIMEOUT, waits (bounded) for its own copies and MMAs in flight,
+// frees TMEM and returns.
 // ---------------------------------------------------------------------------
+#define SV_K0 32  // K of the split input layer
+
 struct SvSmem {
     uint16_t A[128 * MLP_H];    // activations (A operand)
     uint16_t W[MLP_H * MLP_H];  // Wt_j (B operand)
-    float W0[MLP_IN * MLP_H];
+    uint16_t B0[MLP_H * SV_K0]; // split W0 (B operand of the input layer)
     float bias[4][MLP_H];
     float W4[MLP_H * MLP_OUT];
     float4 Yp[2][128];  // output-layer partial sums of the two column halves
-    float X[128][8];    // features
     float b4[4];
 };
 
@@ -132,15 +140,30 @@ __device__ __forceinline__ void sv_put8(uint16_t *st, int r, int c, const float 
     *(uint4 *)(st + tc_core_offset(r, c, MLP_H) / 2) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
+// epilogue of a hidden layer: this thread's row, 128 columns from c0, bias,
+// GELU, BF16 into the A tile
+__device__ __forceinline__ void sv_epilogue_hidden(uint32_t tb, int row, int c0, const float *bias, uint16_t *A)
+{
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+        float v[64];
+        tc_ld64(tb + 64 * cc, v);
+        const int cb = c0 + 64 * cc;
+#pragma unroll
+        for (int i = 0; i < 64; ++i) v[i] = gelu_f(v[i] + bias[cb + i]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) sv_put8(A, row, cb + 8 * q, v + 8 * q);
+    }
+}
+
 __global__ void __launch_bounds__(256, 1)
-    sur_serve_kernel(const SolveGeom g, const uint32_t *__restrict__ modes, float ax, float ay, float zm, float s1,
-                     float s2, float s3, float inv_wind, float ktop, float utop, const MlpServing net,
-                     float2 *__restrict__ Xp, float2 *__restrict__ Xq, int *err)
+    sur_serve_kernel(const SurCase *__restrict__ cases, int ncases, int64_t ntiles, const MlpServing net, int *err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SvSmem &S = *reinterpret_cast<SvSmem *>(smem_raw);
     __shared__ uint64_t bar_w, bar_mma;
     __shared__ uint32_t tmem_slot;
+    __shared__ SurCase sc;  // the current tile's case
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) tc_tmem_alloc(&tmem_slot, 256);
     if (tid == 0) {
@@ -148,7 +171,14 @@ __global__ void __launch_bounds__(256, 1)
         tc_mbar_init(&bar_mma, 1);
         tc_fence_init();
     }
-    for (int i = tid; i < MLP_IN * MLP_H; i += 256) S.W0[i] = net.P[MLP_OFF_W0 + i];
+    // split W0 [in][out] into the B operand [out][K = 32]
+    for (int e = tid; e < MLP_H * SV_K0; e += 256) {
+        const int f = e / SV_K0, k = e % SV_K0, grp = k >> 3, i = k & 7;
+        const float w = net.P[MLP_OFF_W0 + i * MLP_H + f];
+        const uint16_t wh = f2bf(w);
+        const uint16_t wl = f2bf(w - bf2f(wh));
+        S.B0[tc_core_offset(f, k, SV_K0) / 2] = grp < 2 ? wh : (grp == 2 ? wl : (uint16_t)0);
+    }
     for (int i = tid; i < MLP_H; i += 256) {
         S.bias[0][i] = net.P[MLP_OFF_B0 + i];
 #pragma unroll
@@ -156,14 +186,14 @@ __global__ void __launch_bounds__(256, 1)
     }
     for (int i = tid; i < MLP_H * MLP_OUT; i += 256) S.W4[i] = net.P[MLP_OFF_W4 + i];
     if (tid < MLP_OUT) S.b4[tid] = net.P[MLP_OFF_B4 + tid];
+    tc_fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const int64_t ntiles = (g.nsolved + 127) / 128;
     const uint32_t WBYTES = MLP_H * MLP_H * 2;
     const uint32_t idesc = tc_idesc_bf16(128, MLP_H);
-    const uint32_t sbo = (MLP_H / 8) * 128;
+    const uint32_t sbo = (MLP_H / 8) * 128, sbo0 = (SV_K0 / 8) * 128;
     uint32_t wph = 0, mph = 0;
     bool pend_w = false, pend_mma = false;  // thread 0: copies / MMAs not yet waited for
     if (tid == 0 && (int64_t)blockIdx.x < ntiles) {
@@ -171,56 +201,85 @@ __global__ void __launch_bounds__(256, 1)
         tc_bulk_load(S.W, net.Wt[0], WBYTES, &bar_w);
         pend_w = true;
     }
+    // epilogue geometry: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows), columns 128 (w / 4) .. +127
+    const int qd = warp & 3, hf = warp >> 2;
+    const int row = 32 * qd + lane;
+    const uint32_t tb = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(128 * hf);
     bool failed = false;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (tid < 32) {
+            // the tile's case: last case with tile0 <= tile, copied to shared memory
+            int lo = 0, hi = ncases - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (cases[mid].tile0 <= tile) lo = mid;
+                else hi = mid - 1;
+            }
+            const uint32_t *src = (const uint32_t *)(cases + lo);
+            uint32_t *dst = (uint32_t *)&sc;
+            for (int i = tid; i < (int)(sizeof(SurCase) / 4); i += 32) dst[i] = src[i];
+        }
+        __syncthreads();
+        const SolveGeom &g = sc.g;
+        const int64_t lt = tile - sc.tile0;  // tile within the case
         if (tid < 128) {
-            const int64_t m = tile * 128 + tid;
+            // features -> [xh | xl | xh | 0] of row tid (input-layer A operand, K = 32)
+            const int64_t m = lt * 128 + tid;
             float kpar = 1.f, kperp = 0.f;
             if (m < g.nsolved) {
                 int r, c;
                 bool pr;
                 float k;
-                mode_k(g, modes[m], ax, ay, zm, r, c, pr, kpar, kperp, k);
+                mode_k(g, sc.modes[m], sc.ax, sc.ay, sc.zm, r, c, pr, kpar, kperp, k);
                 kpar = fabsf(kpar);
             }
-            feature_row(S.X[tid], kpar, kperp, s1, s2, s3);
-        }
-        __syncthreads();
-        {   // input layer: thread = (row, half of the 256 features)
-            const int r = tid & 127, f0 = (tid >> 7) * 128;
-            const float4 xa = *(const float4 *)&S.X[r][0], xb = *(const float4 *)&S.X[r][4];
-            const float x[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-#pragma unroll 1
-            for (int fb = 0; fb < 128; fb += 8) {
-                float h[8];
+            float x[8], xl[8];
+            feature_row(x, kpar, kperp, sc.s1, sc.s2, sc.s3);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int f = f0 + fb + q;
-                    float z = S.bias[0][f];
+            for (int i = 0; i < 8; ++i) xl[i] = x[i] - bf2f(f2bf(x[i]));
+            uint16_t *A0 = S.A;
+            uint32_t w[4];
 #pragma unroll
-                    for (int i = 0; i < MLP_IN; ++i) z = fmaf(x[i], S.W0[i * MLP_H + f], z);
-                    h[q] = gelu_f(z);
-                }
-                sv_put8(S.A, r, f0 + fb, h);
-            }
+            for (int q = 0; q < 4; ++q) w[q] = (uint32_t)f2bf(x[2 * q]) | ((uint32_t)f2bf(x[2 * q + 1]) << 16);
+            const uint4 hi = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = (uint32_t)f2bf(xl[2 * q]) | ((uint32_t)f2bf(xl[2 * q + 1]) << 16);
+            const uint4 lo = make_uint4(w[0], w[1], w[2], w[3]);
+            *(uint4 *)(A0 + tc_core_offset(tid, 0, SV_K0) / 2) = hi;
+            *(uint4 *)(A0 + tc_core_offset(tid, 8, SV_K0) / 2) = lo;
+            *(uint4 *)(A0 + tc_core_offset(tid, 16, SV_K0) / 2) = hi;
+            *(uint4 *)(A0 + tc_core_offset(tid, 24, SV_K0) / 2) = make_uint4(0u, 0u, 0u, 0u);
         }
         tc_fence_proxy_async();
         __syncthreads();
-        for (int j = 0; j < 3; ++j) {
-            bool bad = !tc_mbar_wait(&bar_w, wph);
-            if (__syncthreads_or(bad)) {
-                failed = true;
-                break;
+        // layers 0..3: input layer (split W0 in S.B0), then Wt_1..3 streamed through S.W
+        for (int j = 0; j < 4; ++j) {
+            bool bad = false;
+            if (j > 0) {
+                bad = !tc_mbar_wait(&bar_w, wph);
+                if (__syncthreads_or(bad)) {
+                    failed = true;
+                    break;
+                }
+                wph ^= 1;
             }
-            wph ^= 1;
             if (tid == 0) {
-                pend_w = false;
+                if (j > 0) pend_w = false;
                 tc_fence_after();
-                const uint32_t a0 = tc_smem(S.A), b0 = tc_smem(S.W);
+                const uint32_t a0 = tc_smem(S.A);
+                if (j == 0) {
+                    const uint32_t b0 = tc_smem(S.B0);
 #pragma unroll 1
-                for (int s = 0; s < MLP_H / 16; ++s)
-                    tc_mma(tmem, tc_desc(a0 + s * 256, 128, sbo), tc_desc(b0 + s * 256, 128, sbo), idesc,
-                           s > 0 ? 1u : 0u);
+                    for (int s = 0; s < SV_K0 / 16; ++s)
+                        tc_mma(tmem, tc_desc(a0 + s * 256, 128, sbo0), tc_desc(b0 + s * 256, 128, sbo0), idesc,
+                               s > 0 ? 1u : 0u);
+                } else {
+                    const uint32_t b0 = tc_smem(S.W);
+#pragma unroll 1
+                    for (int s = 0; s < MLP_H / 16; ++s)
+                        tc_mma(tmem, tc_desc(a0 + s * 256, 128, sbo), tc_desc(b0 + s * 256, 128, sbo), idesc,
+                               s > 0 ? 1u : 0u);
+                }
                 tc_commit(&bar_mma);
                 pend_mma = true;
             }
@@ -232,40 +291,31 @@ __global__ void __launch_bounds__(256, 1)
             mph ^= 1;
             if (tid == 0) {
                 pend_mma = false;
-                // the weights are free: stream in the next layer's (or the next tile's first)
-                const uint16_t *next = j < 2 ? net.Wt[j + 1] : (tile + gridDim.x < ntiles ? net.Wt[0] : nullptr);
-                if (next) {
-                    tc_expect_tx(&bar_w, WBYTES);
-                    tc_bulk_load(S.W, next, WBYTES, &bar_w);
-                    pend_w = true;
+                // after layer j >= 1 the weights are free: stream in the next
+                // layer's (or, after the last, the next tile's first)
+                if (j >= 1) {
+                    const uint16_t *next =
+                        j < 3 ? net.Wt[j] : (tile + gridDim.x < ntiles ? net.Wt[0] : nullptr);
+                    if (next) {
+                        tc_expect_tx(&bar_w, WBYTES);
+                        tc_bulk_load(S.W, next, WBYTES, &bar_w);
+                        pend_w = true;
+                    }
                 }
             }
             tc_fence_after();
-            // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows), columns 128 (w / 4) .. +127
-            const int qd = warp & 3, hf = warp >> 2;
-            const int row = 32 * qd + lane;
-            const uint32_t tb = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(128 * hf);
-            if (j < 2) {
-#pragma unroll 1
-                for (int cc = 0; cc < 4; ++cc) {
-                    float v[32];
-                    tc_ld32(tb + 32 * cc, v);
-                    const int c0 = 128 * hf + 32 * cc;
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] = gelu_f(v[i] + S.bias[j + 1][c0 + i]);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) sv_put8(S.A, row, c0 + 8 * q, v + 8 * q);
-                }
+            if (j < 3) {
+                sv_epilogue_hidden(tb, row, 128 * hf, S.bias[j], S.A);
                 tc_fence_proxy_async();
             } else {
                 float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-                for (int cc = 0; cc < 4; ++cc) {
-                    float v[32];
-                    tc_ld32(tb + 32 * cc, v);
-                    const int c0 = 128 * hf + 32 * cc;
+                for (int cc = 0; cc < 2; ++cc) {
+                    float v[64];
+                    tc_ld64(tb + 64 * cc, v);
+                    const int c0 = 128 * hf + 64 * cc;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) {
+                    for (int i = 0; i < 64; ++i) {
                         const float h = gelu_f(v[i] + S.bias[3][c0 + i]);
                         const float4 w4 = *(const float4 *)&S.W4[(c0 + i) * MLP_OUT];
                         y.x = fmaf(h, w4.x, y.x);
@@ -281,14 +331,15 @@ __global__ void __launch_bounds__(256, 1)
         }
         if (failed) break;
         if (tid < 128) {
-            const int64_t m = tile * 128 + tid;
+            const int64_t m = lt * 128 + tid;
             if (m < g.nsolved) {
                 const float4 a = S.Yp[0][tid], b = S.Yp[1][tid];
                 const float y[4] = {a.x + b.x + S.b4[0], a.y + b.y + S.b4[1], a.z + b.z + S.b4[2],
                                     a.w + b.w + S.b4[3]};
-                emit_spectrum(g, modes[m], y, ax, ay, zm, inv_wind, ktop, utop, Xp, Xq);
+                emit_spectrum(g, sc.modes[m], y, sc.ax, sc.ay, sc.zm, sc.inv_wind, sc.ktop, sc.utop, sc.Xp, sc.Xq);
             }
         }
+        __syncthreads();  // sc is rewritten by the next tile
     }
     if (failed && tid == 0) {
         atomicExch(err, BLDFM_ERR_TIMEOUT);
@@ -320,11 +371,10 @@ cudaError_t launch_sur_exact(const SolveGeom &g, const uint32_t *modes, float ax
     return cudaGetLastError();
 }
 
-cudaError_t launch_sur_serve(const SolveGeom &g, const uint32_t *modes, float ax, float ay, float zm, float s1,
-                             float s2, float s3, float inv_wind, float ktop, float utop, const MlpServing &net,
-                             float2 *Xp, float2 *Xq, int *err, int nsm, cudaStream_t st)
+cudaError_t launch_sur_serve(const SurCase *cases, int ncases, int64_t ntiles, const MlpServing &net, int *err,
+                             int nsm, cudaStream_t st)
 {
-    if (g.nsolved <= 0) return cudaSuccess;
+    if (ntiles <= 0 || ncases <= 0) return cudaSuccess;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(sur_serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -332,10 +382,8 @@ cudaError_t launch_sur_serve(const SolveGeom &g, const uint32_t *modes, float ax
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    const int64_t ntiles = (g.nsolved + 127) / 128;
     const int grid = (int)std::min<int64_t>(ntiles, std::max(nsm, 1));
-    sur_serve_kernel<<<grid, 256, sizeof(SvSmem), st>>>(g, modes, ax, ay, zm, s1, s2, s3, inv_wind, ktop, utop, net,
-                                                        Xp, Xq, err);
+    sur_serve_kernel<<<grid, 256, sizeof(SvSmem), st>>>(cases, ncases, ntiles, net, err);
     return cudaGetLastError();
 }
 

@@ -12,6 +12,13 @@ sweep generates on the device (``TransferPool``), trained with Adam
 box and through the FP64 solver outside it, and re-solves every
 ``spot_every``-th case with the FP64 solver, returning the solver's result
 when the surrogate's relative L2 error exceeds ``tol``.
+
+The judge of a spot check is the accurate FP64 mode (``mode="fp64r"``: the
+same discrete problem solved without the shooting method's cancellation),
+because the reference-rounding FP64 result itself carries an error of order
+eps e^{2G} in high-|k| modes that exceeds 1e-3 for tall towers on fine grids;
+the fallback is the reference-rounding FP64 mode (``mode="fp64"``), which
+reproduces the reference's output.
 """
 
 import ctypes
@@ -214,13 +221,15 @@ class Surrogate:
     by the network, out-of-box fallbacks, spot checks and their failures.
     """
 
-    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0):
+    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0, judge="fp64r", fallback="fp64"):
         self.lib = _lib.load()
         self.net = net
         self.box = dict(BOX if box is None else box)
         self.spot_every = int(spot_every)
         self.tol = float(tol)
         self.variant = int(variant)  # 0 fused kernel, 1 exact transfer (check), 2 layer by layer
+        self.judge = judge
+        self.fallback = fallback
         self.device = torch.device("cuda", torch.cuda.current_device())
         self._ws = None
         self._out = None
@@ -274,6 +283,55 @@ class Surrogate:
         _lib.check(st, "surrogate_solve")
         return conc, flx
 
+    def prepare_batch(self, items):
+        """Descriptors of a batch of footprints (keyword dicts of ``prepare``),
+        reusable across calls; outputs are views of one device buffer."""
+        preps = [self.prepare(**kw) for kw in items]
+        n = len(preps)
+        arr = (_lib.Case * n)()
+        mets = (_lib.SurrogateCase * n)()
+        sizes = [p["shape"][0] * p["shape"][1] for p in preps]
+        out = torch.empty(2 * sum(sizes), dtype=torch.float64, device=self.device)
+        outs, off = [], 0
+        for k, p in enumerate(preps):
+            sz = sizes[k]
+            conc = out[off : off + sz].view(p["shape"])
+            flx = out[off + sz : off + 2 * sz].view(p["shape"])
+            off += 2 * sz
+            c = arr[k]
+            c.desc = p["desc"]
+            c.srf_flx_dev = None
+            c.z_host = p["z"].ctypes.data
+            c.prof_host = p["prof"].ctypes.data
+            c.levels_host = p["lv"].ctypes.data
+            c.nlvls = 1
+            c.conc_dev = conc.data_ptr()
+            c.flx_dev = flx.data_ptr()
+            mets[k] = p["met"]
+            mets[k].variant = 0
+            outs.append((conc, flx))
+        need = ctypes.c_int64(0)
+        _lib.check(self.lib.bldfm_surrogate_batch_plan(arr, mets, n, ctypes.byref(need)), "surrogate_batch")
+        return {"arr": arr, "mets": mets, "outs": outs, "out": out, "keep": preps, "need": int(need.value), "n": n}
+
+    def solve_batch_prepared(self, b, stream=None):
+        """Enqueue a prepared batch (one fused launch + the batched output
+        transform); returns the list of device (conc, flx)."""
+        if self._ws is None or self._ws.numel() < b["need"]:
+            self._ws = torch.empty(b["need"], dtype=torch.uint8, device=self.device)
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        st = self.lib.bldfm_surrogate_solve_batch(
+            self.net.h, b["arr"], b["mets"], b["n"], ctypes.c_void_p(self._ws.data_ptr()),
+            ctypes.c_size_t(self._ws.numel()), ctypes.c_void_p(s),
+        )
+        _lib.check(st, "surrogate_solve_batch")
+        return b["outs"]
+
+    def status(self):
+        """Device status word of the last launch (0, or a BLDFM_ERR_* code)."""
+        torch.cuda.synchronize(self.device)
+        return int(self._ws[:4].view(torch.int32).item()) if self._ws is not None else 0
+
     def footprint(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
                   ustar=None, z0=None, mol=1e9):
         """One footprint at z_m: (grid, conc, flx) as the solver returns them,
@@ -283,18 +341,20 @@ class Surrogate:
         self.count += 1
         if not (self.variant == 1 or self.in_box(n, zm, s1, s2, mode_kmax(srf_shape, domain, modes, halo))):
             self.stats["out_of_box"] += 1
-            return steady_state_transport_solver(**p["kw"], mode="fp64"), "fp64-box"
+            return steady_state_transport_solver(**p["kw"], mode=self.fallback), "fp64-box"
         conc_d, flx_d = self.solve_prepared(p)
         conc, flx = conc_d.cpu().numpy(), flx_d.cpu().numpy()
         grid = _grid(p["z"], n, srf_shape, domain)
         self.stats["surrogate"] += 1
         if self.spot_every > 0 and self.count % self.spot_every == 0:
-            ref = steady_state_transport_solver(**p["kw"], mode="fp64")
+            ref = steady_state_transport_solver(**p["kw"], mode=self.judge)
             err = max(_rell2(conc, ref[1]), _rell2(flx, ref[2]))
             self.stats["spot"] += 1
             self.stats["errors"].append(err)
             if err > self.tol:
                 self.stats["spot_fail"] += 1
+                if self.fallback != self.judge:
+                    ref = steady_state_transport_solver(**p["kw"], mode=self.fallback)
                 return ref, "fp64-spot"
         return (grid, conc, flx), "surrogate"
 

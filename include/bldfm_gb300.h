@@ -268,6 +268,18 @@ typedef struct bldfm_surrogate_case {
 } bldfm_surrogate_case;
 int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls,
                          int64_t *workspace_bytes);
+/* Many surrogate footprints in one persistent launch plus the batched output
+ * transform (the batch counterpart of bldfm_surrogate_solve; variant 0 only).
+ * cases[k] as for bldfm_solve_batch (footprint, one level at z_m, FP32 mode),
+ * mets[k] its met scalars; workspace of bldfm_surrogate_batch_plan bytes,
+ * 256-byte aligned; the int32 at offset 0 holds the device status. */
+int bldfm_surrogate_batch_plan(const bldfm_case *cases,
+                               const bldfm_surrogate_case *mets, int32_t ncases,
+                               int64_t *workspace_bytes);
+int bldfm_surrogate_solve_batch(void *net, const bldfm_case *cases,
+                                const bldfm_surrogate_case *mets, int32_t ncases,
+                                void *workspace, size_t workspace_bytes,
+                                void *stream);
 int bldfm_surrogate_solve(void *net, const bldfm_desc *d,
                           const bldfm_surrogate_case *met, const double *z_host,
                           const double *prof_host, const int64_t *levels_host,

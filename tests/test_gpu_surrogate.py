@@ -96,5 +96,89 @@ def test_fused_serving_matches_layerwise():
         c, f = sur.solve_prepared(sur.prepare(**args))
         outs.append((c.cpu().numpy(), f.cpu().numpy()))
     assert np.all(np.isfinite(outs[0][0])) and np.all(np.isfinite(outs[0][1]))
-    assert _rel(outs[0][0], outs[1][0]) < 1e-5
-    assert _rel(outs[0][1], outs[1][1]) < 1e-5
+    # the fused kernel's input layer runs as split BF16 MMAs (relative 2^-16),
+    # which can flip the BF16 rounding of a few activations
+    assert _rel(outs[0][0], outs[1][0]) < 1e-4
+    assert _rel(outs[0][1], outs[1][1]) < 1e-4
+
+
+def test_batched_serving_matches_single():
+    """One fused launch over several footprints (mixed grids, directions and
+    met cases) gives the single-footprint results."""
+    from bldfm_gb300.surrogate import Surrogate, load
+
+    net, box, meta = load()
+    sur = Surrogate(net, spot_every=0)
+    items = [
+        dict(n=128, zm=20.0, wind=(2.83, 2.83), srf_shape=(256, 256), domain=(1000.0, 1000.0), modes=(256, 256),
+             meas_pt=(500.0, 500.0), ustar=0.3, mol=-50.0),
+        dict(n=128, zm=12.0, wind=(-3.0, 1.0), srf_shape=(128, 192), domain=(600.0, 900.0), modes=(128, 192),
+             meas_pt=(300.0, 200.0), ustar=0.35, mol=-40.0),
+        dict(n=128, zm=30.0, wind=(0.5, -4.0), srf_shape=(256, 256), domain=(1500.0, 1500.0), modes=(128, 128),
+             meas_pt=(700.0, 800.0), ustar=0.4, mol=-200.0),
+    ]
+    b = sur.prepare_batch(items)
+    outs = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in sur.solve_batch_prepared(b)]
+    assert sur.status() == 0
+    for kw, (cb, fb) in zip(items, outs):
+        cs, fs = sur.solve_prepared(sur.prepare(**kw))
+        cs, fs = cs.cpu().numpy(), fs.cpu().numpy()
+        assert _rel(cb, cs) < 1e-6 and _rel(fb, fs) < 1e-6
+
+
+def test_trained_network_gains_over_solver():
+    """What the trained network buys: inside its training box it reproduces
+    the FP64 footprint to relL2 <= 1e-3 at a fraction of the FP64 solver's
+    cost, where the untrained network of the same shape is useless."""
+    import time
+
+    from bldfm_gb300.mlp import MLP
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import Surrogate, load
+
+    net, box, meta = load()
+    kw = dict(n=128, zm=20.0, wind=(2.83, 2.83), srf_shape=(512, 512), domain=(1000.0, 1000.0), modes=(512, 512),
+              meas_pt=(500.0, 500.0), ustar=0.3, mol=-50.0)
+    sur = Surrogate(net, spot_every=0)
+    p = sur.prepare(**kw)
+    c, f = sur.solve_prepared(p)
+    c, f = c.cpu().numpy(), f.cpu().numpy()
+    _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
+    err = max(_rel(c, cr), _rel(f, fr))
+    assert err <= 1e-3, err
+    raw = Surrogate(MLP(batch=65536, seed=0), spot_every=0)
+    cu, fu = raw.solve_prepared(raw.prepare(**kw))
+    err_untrained = max(_rel(cu.cpu().numpy(), cr), _rel(fu.cpu().numpy(), fr))
+    assert err_untrained > 100 * err
+    # speed: surrogate vs the FP64 solver on the device, same footprint
+    from bldfm_gb300 import _lib
+    from bldfm_gb300.solver import make_desc, plan
+    import ctypes
+
+    lib = _lib.load()
+    d = make_desc((512, 512), p["z"].size, (1000.0, 1000.0), (512, 512), (500.0, 500.0), 0.0, True, False, None,
+                  "double", "fp64")
+    info = plan(d, 1)
+    ws = torch.empty(int(info.workspace_bytes), dtype=torch.uint8, device="cuda")
+    co = torch.empty((512, 512), dtype=torch.float64, device="cuda")
+    fo = torch.empty_like(co)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def fp64_solve():
+        _lib.check(lib.bldfm_solve(d, None, _lib.ptr(p["z"]), _lib.ptr(p["prof"]), _lib.ptr(p["lv"]), 1,
+                                   ctypes.c_void_p(co.data_ptr()), ctypes.c_void_p(fo.data_ptr()),
+                                   ctypes.c_void_p(ws.data_ptr()), ctypes.c_size_t(ws.numel()), st), "fp64")
+
+    def timeit(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    t64 = timeit(fp64_solve, 5)
+    b = sur.prepare_batch([kw] * 16)
+    tsur = timeit(lambda: sur.solve_batch_prepared(b), 5) / 16
+    assert t64 / tsur > 10, (t64, tsur)
