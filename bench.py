@@ -19,6 +19,10 @@ Reported:
   roofline       the batched sweep kernel against the measured FP32 FMA peak
   surrogate      the learned surrogate (trained weights in
                  bldfm_gb300/weights): footprints/s and relL2 against FP64
+  timeseries     512 mixed-grid met cases (8 towers, 256^2..1024^2,
+                 n = 64..256) in one batched call per step
+  production     the 1024^2-extended, n = 256 footprint: FP64 / FP64
+                 accurate / FP32 on the GPU, the CPU port, analytic check
   cpu_baseline   the CPU oracle port (reference arithmetic, OpenMP on all
                  host cores) on a bounded sample
 
@@ -207,6 +211,173 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def measured_peaks():
+    """HBM GB/s and dense BF16 TFLOP/s measured on the GB300s
+    (MEASURED_PEAKS.json), else the fallback figures."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def transform_section(stages_b, B, dev):
+    """Achieved GB/s of the batched output transform (algorithmic bytes: the
+    two FP32 spectra read, conc and flx written) against the HBM peak, and a
+    cuFFT timing of the same transform size (torch.fft, comparison only)."""
+    import torch
+
+    peaks = measured_peaks()
+    bytes_fp = MODES[0] * MODES[1] * 8 * 2 + 2 * NY * NX * 8
+    ms = stages_b[2] if stages_b and len(stages_b) > 2 else None
+    achieved = B * bytes_fp / (ms * 1e-3) / 1e9 if ms else None
+    # cuFFT: the full 1536 x 1536 complex64 2D inverse transform of B spectra
+    n = 3 * NX
+    x = torch.randn(B, n, n, dtype=torch.complex64, device=dev)
+    torch.fft.ifft2(x)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        torch.fft.ifft2(x)
+    e1.record()
+    torch.cuda.synchronize()
+    cufft_ms = e0.elapsed_time(e1) / 5
+    del x
+    return {
+        "kernels": "out_cols_batch_kernel + out_rows_batch_kernel",
+        "ms_per_footprint": ms / B if ms else None,
+        "bytes_per_footprint": bytes_fp,
+        "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": achieved / peaks["hbm_gbs"] if achieved else None, "peak_source": peaks["source"],
+        "cufft_full_2d_ifft_1536x1536_c64_ms_per_footprint": cufft_ms / B,
+    }
+
+
+def timeseries_section(args, dev):
+    """The 512-case mixed-grid met timeseries (8 towers, 256^2 / 512^2 /
+    1024^2, n = 64..256) as one batched FP32 call per step: footprints/s with
+    device-resident outputs, and relL2 against the exact discrete solution on
+    one case per tower."""
+    import torch
+
+    from bldfm_gb300 import steady_state_transport_solver, vertical_profiles
+    from bldfm_gb300.batch import BatchSolver
+    from tests.timeseries_cases import met_cases
+
+    cases = met_cases(512, seed=0)
+    kws = []
+    for c in cases:
+        z, prof = vertical_profiles(c["n"], c["zm"], c["wind"], ustar=c["ustar"], mol=c["mol"])
+        kws.append(dict(srf_flx=np.zeros((c["grid"], c["grid"])), z=z, profiles=prof, domain=c["domain"],
+                        levels=c["n"], modes=(c["grid"], c["grid"]), meas_pt=c["meas_pt"], footprint=True,
+                        precision="double"))
+    solver = BatchSolver(use_graph=True)
+    prep = solver.prepare_cached(kws)
+    for _ in range(2):
+        solver.solve_prepared(prep)
+    solver.stream.synchronize()
+    steps = 3
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(solver.stream)
+    for _ in range(steps):
+        solver.solve_prepared(prep)
+    e1.record(solver.stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    if solver.status() != 0:
+        raise RuntimeError("timeseries device status %d" % solver.status())
+    outs = prep[1]
+    errs, seen = [], set()
+    for c, kw, (conc, flx) in zip(cases, kws, outs):
+        if c["tower"] in seen:
+            continue
+        seen.add(c["tower"])
+        _, cr, fr = steady_state_transport_solver(**kw, mode="fp64r")
+        ca, fa = conc[0].cpu().numpy(), flx[0].cpu().numpy()
+        errs.append(max(np.linalg.norm(ca - cr) / np.linalg.norm(cr), np.linalg.norm(fa - fr) / np.linalg.norm(fr)))
+    return {
+        "workload": "512 met cases, 8 towers on 256^2/512^2/1024^2 grids (default halo, all modes), n=64..256, "
+                    "u*~U[0.1,0.8], 1/L~U[-0.1,0.05], dir~U[0,360), z0 log-U[0.01,1], z_m~U[2,50] (seed 0)",
+        "value": 512 / (ms * 1e-3), "unit": "footprints/s", "ms_per_batch": ms,
+        "path": "one bldfm_solve_batch call (persistent FP32 sweep + batched transforms, CUDA graph)",
+        "relL2_vs_exact_max_8_towers": max(errs),
+    }
+
+
+def production_section(args, lib, dev, sptr, cpu):
+    """The production footprint: 512^2 physical, 500 m halo (1024^2 extended),
+    all 1024^2 modes, n = 256, unstable MOST (L = -50 m, u* = 0.3, z_m = 20 m,
+    4 m/s at 225 deg), FP64 (reference rounding), FP64 accurate and FP32 on
+    the GPU, the CPU port timed on the host cores, plus the constant-profile
+    analytic check."""
+    import ctypes
+
+    import torch
+
+    from bldfm_gb300 import _lib
+    from bldfm_gb300 import steady_state_transport_solver, vertical_profiles
+    from bldfm_gb300.solver import make_desc, plan
+    from bldfm_gb300.utils import compute_wind_fields
+
+    wind = compute_wind_fields(4.0, 225.0)
+    z, prof = vertical_profiles(256, 20.0, wind, ustar=0.3, mol=-50.0)
+    zz = np.ascontiguousarray(z, dtype=np.float64)
+    pr = np.ascontiguousarray(np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), zz.shape) for p in prof]))
+    lv = np.array([256], dtype=np.int64)
+    res = {}
+    outs = {}
+    for mode, reps in (("fp64", 2), ("fp64r", 2), ("fp32", 5)):
+        d = make_desc((512, 512), zz.size, (1000.0, 1000.0), (1024, 1024), (500.0, 500.0), 0.0, True, False, 500.0,
+                      "double", mode)
+        info = plan(d, 1)
+        ws = torch.empty(int(info.workspace_bytes), dtype=torch.uint8, device=dev)
+        co = torch.empty((info.out_ny, info.out_nx), dtype=torch.float64, device=dev)
+        fo = torch.empty_like(co)
+
+        def run():
+            _lib.check(lib.bldfm_solve(d, None, _lib.ptr(zz), _lib.ptr(pr), _lib.ptr(lv), 1,
+                                       ctypes.c_void_p(co.data_ptr()), ctypes.c_void_p(fo.data_ptr()),
+                                       ctypes.c_void_p(ws.data_ptr()), ctypes.c_size_t(ws.numel()), sptr), mode)
+
+        run()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.current_stream(dev))
+        for _ in range(reps):
+            run()
+        e1.record(torch.cuda.current_stream(dev))
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res[mode] = {"ms_per_footprint": ms, "footprints_per_s": 1e3 / ms}
+        outs[mode] = (co.cpu().numpy(), fo.cpu().numpy())
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    cr, fr = outs["fp64r"]
+    for mode in ("fp64", "fp32"):
+        res[mode]["relL2_vs_exact"] = max(rel(outs[mode][0], cr), rel(outs[mode][1], fr))
+    if cpu:
+        kw = dict(srf_flx=np.zeros((512, 512)), z=zz, profiles=tuple(pr), domain=(1000.0, 1000.0), levels=256,
+                  modes=(1024, 1024), meas_pt=(500.0, 500.0), footprint=True, precision="double", halo=500.0)
+        sec = cpu_port_time(kw, reps=1)
+        res["cpu_port"] = {"footprints_per_s": 1.0 / sec, "cores": os.cpu_count(), "kind": "port"}
+    # constant K / constant u: the analytic branch against the numerical solve
+    nz = zz.size
+    const = tuple(np.full(nz, v) for v in (2.83, 2.83, 1.5, 1.5, 1.5))
+    kwc = dict(srf_flx=np.zeros((256, 256)), z=zz, profiles=const, domain=(1000.0, 1000.0), levels=128,
+               modes=(256, 256), meas_pt=(500.0, 500.0), footprint=True, precision="double")
+    _, ca, fa = steady_state_transport_solver(**kwc, analytic=True, mode="fp64")
+    _, cn, fn = steady_state_transport_solver(**kwc, mode="fp64r")
+    res["analytic_check_relL2"] = max(rel(cn, ca), rel(fn, fa))
+    res["workload"] = ("footprint 512^2, halo 500 m (1024^2 extended), modes 1024^2, n=256 (%d levels), "
+                       "unstable MOST, u*=0.3, z_m=20 m" % nz)
+    return res
+
+
 def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
     """Footprints/s of the surrogate on batch 0's met cases (device-resident
     outputs, descriptors prepared once), its relL2 against the FP64 path, and
@@ -240,6 +411,10 @@ def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
+    from bldfm_gb300 import _lib
+    import ctypes
+
+    lib = _lib.load()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -248,6 +423,20 @@ def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    # per-stage times (CUDA events inside the library) over the same steps
+    lib.bldfm_set_stage_timing(1)
+    for _ in range(args.steps):
+        sur.solve_batch_prepared(bat)
+    torch.cuda.synchronize()
+    arr = (ctypes.c_float * 8)()
+    nst = lib.bldfm_stage_times(arr, 8)
+    lib.bldfm_set_stage_timing(0)
+    stages = [float(arr[i]) for i in range(max(nst, 0))]
+    serve_ms = stages[1] / B if len(stages) > 1 else None  # per footprint
+    nsolved = 131583
+    npad = (nsolved + 127) // 128 * 128
+    tflop = npad * (2 * 32 * 256 + 3 * 2 * 256 * 256) / 1e12  # tensor-core work per footprint
+    peaks = measured_peaks()
     if dist is not None:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -285,6 +474,17 @@ def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
         "in_box": int(sum(in_box)),
         "kernel": "sur_serve_kernel (features -> 4 tcgen05 BF16 layers, split-BF16 input layer -> 256x4 -> spectra) "
                   "over the step's footprints + batched output FFT",
+        "stage_ms_per_step": stages,
+        "serve_kernel": {
+            "ms_per_footprint": serve_ms,
+            "bound": "tensor",
+            "tensor_tflop_per_footprint": tflop,
+            "achieved": (tflop / (serve_ms * 1e-3)) if serve_ms else None,
+            "peak": peaks["bf16_tflops"],
+            "unit": "TFLOP/s",
+            "frac": (tflop / (serve_ms * 1e-3) / peaks["bf16_tflops"]) if serve_ms else None,
+            "peak_source": peaks["source"],
+        },
         "weights": {"box": box, **{k: meta[k] for k in meta if k in ("steps", "batch", "val_loss", "train_s")}},
         "training": {"ms_per_step": train_s / nsteps * 1e3, "samples_per_s": 65536 * nsteps / train_s,
                      "batch": 65536},
@@ -300,6 +500,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-extra", action="store_true", help="skip the timeseries and production sub-benchmarks")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -472,6 +673,12 @@ def main():
     # --- learned surrogate: fused features -> tcgen05 MLP -> spectra, trained weights ---
     sur_line = surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr)
 
+    # --- the mixed-grid timeseries and the production footprint (rank 0, N = 1) ---
+    ts_line = prod_line = None
+    if rank == 0 and world == 1 and not args.no_extra:
+        ts_line = timeseries_section(args, dev)
+        prod_line = production_section(args, lib, dev, sptr, not args.no_cpu_baseline)
+
     # --- e2e through the public batched API (numpy in, numpy out) ---
     esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True)
     e2e_steps = max(2, args.steps // 2)
@@ -560,7 +767,10 @@ def main():
                 "traffic": None,
                 "flops_per_launch": flops_launch,
             },
+            "transform": transform_section(stages_b, B, dev),
             "surrogate": sur_line,
+            "timeseries": ts_line,
+            "production": prod_line,
             "cpu_baseline": cpu,
             "gpu_launches": 3 * args.steps,
             "clocks": clk.summary(),

@@ -57,6 +57,7 @@ void factorize(int n, FftPlan &p)
         }
     }
     if (m > 1) p.radix[p.nstages++] = m;
+    fft_plan_finalize(p);
 }
 
 int64_t count_and_fill_modes(int nlx, int nly, std::vector<uint32_t> *out);
@@ -666,7 +667,7 @@ struct BatchBuild {
     std::vector<size_t> d_q0, d_A, d_scratch, d_Xp, d_Xq, d_Cb;
     size_t total = 0;
     int64_t ntiles = 0;
-    int G = 0, threads = 256, ncol = 0, nrow = 0, rpc = 2;
+    int G = 0, threads = 256, ncol = 0, nrow = 0, rpc = 2, cpc = 1;
     size_t sweep_smem = 0, col_smem = 0, row_smem = 0;
     std::vector<int64_t> tile0, col0, row0;
 };
@@ -695,8 +696,6 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
         const SolveGeom &g = B.hp[k].g;
         B.tile0[k] = B.ntiles;
         B.ntiles += (g.nsolved + B.threads - 1) / B.threads;
-        B.col0[k] = B.ncol;
-        B.ncol += g.nlvls * g.nbx;
         maxL = std::max(maxL, g.nz - 1);
         maxnz = std::max(maxnz, g.nz);
         maxnfy = std::max(maxnfy, g.nfy);
@@ -704,8 +703,11 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     }
     B.rpc = 2;
     while (B.rpc > 1 && (2 * (size_t)B.rpc + 1) * maxnfx * 8 > 190 * 1024) --B.rpc;
+    B.cpc = out_cols_per_cta(maxnfy, 8);
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
+        B.col0[k] = B.ncol;
+        B.ncol += g.nlvls * ((g.nbx + B.cpc - 1) / B.cpc);
         B.row0[k] = B.nrow;
         B.nrow += g.nlvls * ((g.out_ny + B.rpc - 1) / B.rpc);
     }
@@ -764,7 +766,7 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     }
     B.total = w;
     B.sweep_smem = (size_t)maxL * BLDFM_LV32 * 4 + (size_t)maxnz * 4 + 16;
-    B.col_smem = 3 * (size_t)maxnfy * 8;
+    B.col_smem = (2 * (size_t)B.cpc + 1) * maxnfy * 8;
     B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
     if (B.sweep_smem > 200 * 1024) return BLDFM_ERR_UNSUPPORTED;
     if (!dc) return BLDFM_OK;
@@ -834,6 +836,7 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
         x.col0 = B.col0[k];
         x.row0 = B.row0[k];
         x.rpc = B.rpc;
+        x.cpc = B.cpc;
         double *lv64 = (double *)(blob + B.off_lv64[k]);
         hx_level_table(nz, c.z_host, c.prof_host, lv64);
         if (g.iso)
@@ -849,7 +852,7 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
             tile_case[B.tile0[k] + t] = k;
             tile_cost.push_back((double)std::max(nz - 1, 1));
         }
-        for (int64_t i = 0; i < (int64_t)g.nlvls * g.nbx; ++i) col_case[B.col0[k] + i] = k;
+        for (int64_t i = 0; i < (int64_t)g.nlvls * ((g.nbx + B.cpc - 1) / B.cpc); ++i) col_case[B.col0[k] + i] = k;
         const int nblk = (g.out_ny + B.rpc - 1) / B.rpc;
         for (int64_t i = 0; i < (int64_t)g.nlvls * nblk; ++i) row_case[B.row0[k] + i] = k;
     }
@@ -1167,13 +1170,17 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
         c.tile0 = t;
         t += (g.nsolved + 127) / 128;
     }
+    timers_begin(dc);
+    tmark(dc, st);  // 0: upload
     CK(cudaMemcpyAsync(w + B.blob_at, blob, B.blob_bytes, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(w, 0, 64, st));
     CK(cudaEventRecord(slt->ev, st));
     MlpServing view;
     if ((rc = mlp_serving_view(net, &view)) != BLDFM_OK) return rc;
     char *wb = w + B.blob_at;
+    tmark(dc, st);  // 1: the fused features -> MLP -> spectra kernel
     CK(launch_sur_serve((const SurCase *)(wb + B.extra_off), n, t, view, (int *)w, dc.nsm, st));
+    tmark(dc, st);  // 2: the output transform
     BatchLaunch bl;
     memset(&bl, 0, sizeof(bl));
     bl.cases = (const BatchCase *)(wb + B.off_cases);
@@ -1188,6 +1195,7 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     bl.row_ctas = B.nrow;
     bl.row_smem = B.row_smem;
     CK(launch_batch_kernels(bl, st, 1));
+    tmark(dc, st);  // 3: end
     return BLDFM_OK;
 }
 

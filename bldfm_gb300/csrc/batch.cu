@@ -138,8 +138,10 @@ __global__ void __launch_bounds__(256) out_cols_batch_kernel(const BatchCase *__
     load_case(&sc, cases + k);
     __syncthreads();
     const int64_t local = (int64_t)blockIdx.x - sc.col0;
-    const int lvl = (int)(local / sc.g.nbx), b = (int)(local - (int64_t)lvl * sc.g.nbx);
-    out_col_line<float>(sc.g, sc.ply, sc.twy, sc.xband, sc.Xp, sc.Xq, sc.dc, sc.Cb, b, lvl, (float2 *)smem_raw);
+    const int ncb = (sc.g.nbx + sc.cpc - 1) / sc.cpc;  // column blocks per level
+    const int lvl = (int)(local / ncb), cb = (int)(local - (int64_t)lvl * ncb);
+    out_col_lines<float>(sc.g, sc.ply, sc.twy, sc.xband, sc.Xp, sc.Xq, sc.dc, sc.Cb, cb * sc.cpc, sc.cpc, lvl,
+                         (float2 *)smem_raw);
 }
 
 __global__ void __launch_bounds__(256) out_rows_batch_kernel(const BatchCase *__restrict__ cases,

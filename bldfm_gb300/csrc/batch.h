@@ -26,7 +26,7 @@ struct __align__(16) BatchCase {
     int64_t col0;   // first column-transform CTA
     int64_t row0;   // first row-transform CTA
     int32_t rpc;    // rows per row-transform CTA
-    int32_t pad;
+    int32_t cpc;    // band columns per column-transform CTA
 };
 
 struct BatchLaunch {

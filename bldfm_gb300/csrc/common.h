@@ -37,11 +37,59 @@ enum {
 };
 
 // Plan of one mixed-radix transform length.
+// floor(x / d) for 0 <= x < 2^31 as umulhi(x, m) >> s (Granlund-Montgomery
+// round-up multiplier, l = ceil(log2 d), m = ceil(2^(31 + l) / d) < 2^32,
+// s = l - 1); s < 0 marks d == 1.
+struct FDiv {
+    uint32_t m;
+    int32_t s;
+};
+
+inline FDiv fdiv_make(uint32_t d)
+{
+    FDiv f;
+    if (d <= 1) {
+        f.m = 0;
+        f.s = -1;
+        return f;
+    }
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    f.m = (uint32_t)(((1ull << (31 + l)) + d - 1) / d);
+    f.s = l - 1;
+    return f;
+}
+
 struct FftPlan {
     int32_t n;
     int32_t nstages;
     int32_t radix[BLDFM_MAX_STAGES];
+    int32_t rq[BLDFM_MAX_STAGES];   // stride of stage q: n / (L_{q-1} p_q)
+    FDiv drq[BLDFM_MAX_STAGES];     // division by rq
+    FDiv dnb[BLDFM_MAX_STAGES];     // division by n / p_q (butterflies per line)
 };
+
+// per-stage strides and division multipliers of a factorised plan
+inline void fft_plan_finalize(FftPlan &p)
+{
+    int L1 = 1;
+    for (int q = 0; q < p.nstages; ++q) {
+        const int P = p.radix[q];
+        p.rq[q] = p.n / (L1 * P);
+        p.drq[q] = fdiv_make((uint32_t)p.rq[q]);
+        p.dnb[q] = fdiv_make((uint32_t)(p.n / P));
+        L1 *= P;
+    }
+}
+
+// columns per CTA of the column pass for transform length n: a power of two,
+// as many as fit (2 cpc + 1) n complex in ~110 KB of shared memory, at most 4
+inline int out_cols_per_cta(int n, size_t csize)
+{
+    int cpc = 4;
+    while (cpc > 1 && (2 * (size_t)cpc + 1) * n * csize > 110 * 1024) cpc >>= 1;
+    return cpc;
+}
 
 // Everything a kernel needs to know about one solve (passed by value).
 struct SolveGeom {

@@ -58,18 +58,24 @@ __device__ __forceinline__ C cx_rot(C a, float s)
     return o;
 }
 
-template <typename C>
-__device__ __forceinline__ C tw_get(const C *tw, int m, int sign)
+template <typename C, int SIGN>
+__device__ __forceinline__ C tw_get(const C *tw, int m)
 {
     C w = tw[m];
-    if (sign > 0) w.y = -w.y;
+    if (SIGN > 0) w.y = -w.y;
     return w;
 }
 
-// Radix-p butterfly body for one (j1, k).  u[] already twiddled.
-template <typename C, int P>
-__device__ __forceinline__ void dft_small(C *u, int sign, const C *tw, int n)
+__device__ __forceinline__ uint32_t fdiv(uint32_t x, const FDiv &f)
 {
+    return f.s < 0 ? x : (__umulhi(x, f.m) >> f.s);
+}
+
+// Radix-p butterfly body for one (j1, k).  u[] already twiddled.
+template <typename C, int P, int SIGN>
+__device__ __forceinline__ void dft_small(C *u, const C *tw, int n)
+{
+    constexpr int sign = SIGN;
     typedef decltype(u[0].x) RR;
     if (P == 2) {
         C a = u[0], b = u[1];
@@ -145,7 +151,7 @@ __device__ __forceinline__ void dft_small(C *u, int sign, const C *tw, int n)
             C acc = u[0];
             for (int t = 1; t < 5; ++t) {
                 int m = ((j * t) % 5) * (n / 5);
-                acc = cx_add(acc, cx_mul(u[t], tw_get(tw, m, sign)));
+                acc = cx_add(acc, cx_mul(u[t], tw_get<C, SIGN>(tw, m)));
             }
             o[j] = acc;
         }
@@ -153,18 +159,18 @@ __device__ __forceinline__ void dft_small(C *u, int sign, const C *tw, int n)
     }
 }
 
-// One Stockham stage of specialised radix P over nlines lines of length n.
-template <typename C, int P>
-__device__ void stage_p(const C *__restrict__ src, C *__restrict__ dst, int n, int nlines, int L1,
-                        const C *__restrict__ tw, int sign)
+// One Stockham stage of specialised radix P over nlines lines of length n;
+// stage constants from the plan (rq, divisions by rq and by n / P).
+template <typename C, int P, int SIGN>
+__device__ void stage_p(const C *__restrict__ src, C *__restrict__ dst, int n, int nlines, int L1, int rq,
+                        const FDiv drq, const FDiv dnb, const C *__restrict__ tw)
 {
-    const int rq = n / (L1 * P);
     const int nb = n / P;  // butterflies per line
     const int total = nb * nlines;
     for (int b = threadIdx.x; b < total; b += blockDim.x) {
-        const int line = b / nb;
+        const int line = (int)fdiv((uint32_t)b, dnb);
         const int loc = b - line * nb;
-        const int j1 = loc / rq;
+        const int j1 = (int)fdiv((uint32_t)loc, drq);
         const int k = loc - j1 * rq;
         const C *s = src + (size_t)line * n;
         C *d = dst + (size_t)line * n;
@@ -173,28 +179,27 @@ __device__ void stage_p(const C *__restrict__ src, C *__restrict__ dst, int n, i
 #pragma unroll
         for (int t = 0; t < P; ++t) {
             C v = s[base + t * rq];
-            if (t > 0 && j1 > 0) v = cx_mul(v, tw_get(tw, j1 * t * rq, sign));
+            if (t > 0 && j1 > 0) v = cx_mul(v, tw_get<C, SIGN>(tw, j1 * t * rq));
             u[t] = v;
         }
-        dft_small<C, P>(u, sign, tw, n);
+        dft_small<C, P, SIGN>(u, tw, n);
 #pragma unroll
         for (int t = 0; t < P; ++t) d[(j1 + L1 * t) * rq + k] = u[t];
     }
 }
 
 // Generic radix (direct size-p DFT per butterfly, O(p^2)).
-template <typename C>
-__device__ void stage_generic(const C *__restrict__ src, C *__restrict__ dst, int n, int nlines, int L1,
-                              int p, const C *__restrict__ tw, int sign)
+template <typename C, int SIGN>
+__device__ void stage_generic(const C *__restrict__ src, C *__restrict__ dst, int n, int nlines, int L1, int p,
+                              int rq, const FDiv drq, const FDiv dnb, const C *__restrict__ tw)
 {
-    const int rq = n / (L1 * p);
     const int nb = n / p;
     const int total = nb * nlines;
     const int np_ = n / p;
     for (int b = threadIdx.x; b < total; b += blockDim.x) {
-        const int line = b / nb;
+        const int line = (int)fdiv((uint32_t)b, dnb);
         const int loc = b - line * nb;
-        const int j1 = loc / rq;
+        const int j1 = (int)fdiv((uint32_t)loc, drq);
         const int k = loc - j1 * rq;
         const C *s = src + (size_t)line * n;
         C *d = dst + (size_t)line * n;
@@ -203,31 +208,34 @@ __device__ void stage_generic(const C *__restrict__ src, C *__restrict__ dst, in
             C acc = s[base];
             for (int t = 1; t < p; ++t) {
                 C v = s[base + t * rq];
-                if (j1 > 0) v = cx_mul(v, tw_get(tw, j1 * t * rq, sign));
+                if (j1 > 0) v = cx_mul(v, tw_get<C, SIGN>(tw, j1 * t * rq));
                 int m = ((j2 * t) % p) * np_;
-                acc = cx_add(acc, cx_mul(v, tw_get(tw, m, sign)));
+                acc = cx_add(acc, cx_mul(v, tw_get<C, SIGN>(tw, m)));
             }
             d[(j1 + L1 * j2) * rq + k] = acc;
         }
     }
 }
 
-// Run all stages; returns the buffer holding the result (a or b).
-template <typename C>
-__device__ C *fft_run(C *a, C *b, const FftPlan &pl, int nlines, const C *__restrict__ tw, int sign)
+// Run all stages with a compile-time transform sign; returns the buffer
+// holding the result (a or b).
+template <typename C, int SIGN>
+__device__ C *fft_run_s(C *a, C *b, const FftPlan &pl, int nlines, const C *__restrict__ tw)
 {
     int L1 = 1;
     C *src = a, *dst = b;
     for (int q = 0; q < pl.nstages; ++q) {
         const int p = pl.radix[q];
+        const int rq = pl.rq[q];
+        const FDiv drq = pl.drq[q], dnb = pl.dnb[q];
         __syncthreads();
         switch (p) {
-        case 2: stage_p<C, 2>(src, dst, pl.n, nlines, L1, tw, sign); break;
-        case 3: stage_p<C, 3>(src, dst, pl.n, nlines, L1, tw, sign); break;
-        case 4: stage_p<C, 4>(src, dst, pl.n, nlines, L1, tw, sign); break;
-        case 5: stage_p<C, 5>(src, dst, pl.n, nlines, L1, tw, sign); break;
-        case 8: stage_p<C, 8>(src, dst, pl.n, nlines, L1, tw, sign); break;
-        default: stage_generic<C>(src, dst, pl.n, nlines, L1, p, tw, sign); break;
+        case 2: stage_p<C, 2, SIGN>(src, dst, pl.n, nlines, L1, rq, drq, dnb, tw); break;
+        case 3: stage_p<C, 3, SIGN>(src, dst, pl.n, nlines, L1, rq, drq, dnb, tw); break;
+        case 4: stage_p<C, 4, SIGN>(src, dst, pl.n, nlines, L1, rq, drq, dnb, tw); break;
+        case 5: stage_p<C, 5, SIGN>(src, dst, pl.n, nlines, L1, rq, drq, dnb, tw); break;
+        case 8: stage_p<C, 8, SIGN>(src, dst, pl.n, nlines, L1, rq, drq, dnb, tw); break;
+        default: stage_generic<C, SIGN>(src, dst, pl.n, nlines, L1, p, rq, drq, dnb, tw); break;
         }
         L1 *= p;
         C *t = src;
@@ -236,4 +244,10 @@ __device__ C *fft_run(C *a, C *b, const FftPlan &pl, int nlines, const C *__rest
     }
     __syncthreads();
     return src;
+}
+
+template <typename C>
+__device__ C *fft_run(C *a, C *b, const FftPlan &pl, int nlines, const C *__restrict__ tw, int sign)
+{
+    return sign > 0 ? fft_run_s<C, 1>(a, b, pl, nlines, tw) : fft_run_s<C, -1>(a, b, pl, nlines, tw);
 }

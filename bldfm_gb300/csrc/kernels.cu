@@ -544,18 +544,19 @@ __global__ void __launch_bounds__(256) fwd_cols_kernel(SolveGeom g, FftPlan pl, 
     }
 }
 
-// out_cols: one band column per CTA (blockIdx.x), one level (blockIdx.y).
+// out_cols: cols_per_cta band columns per CTA (blockIdx.x), one level (blockIdx.y).
 template <typename R>
 __global__ void __launch_bounds__(256) out_cols_kernel(SolveGeom g, FftPlan pl, const typename cvec<R>::T *__restrict__ tw,
                                                        const int4 *__restrict__ xband,
                                                        const typename cvec<R>::T *__restrict__ Xp,
                                                        const typename cvec<R>::T *__restrict__ Xq,
                                                        const double2 *__restrict__ dc,
-                                                       typename cvec<R>::T *__restrict__ Cout)
+                                                       typename cvec<R>::T *__restrict__ Cout, int cols_per_cta)
 {
     typedef typename cvec<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    out_col_line<R>(g, pl, tw, xband, Xp, Xq, dc, Cout, blockIdx.x, blockIdx.y, (C *)smem_raw);
+    out_col_lines<R>(g, pl, tw, xband, Xp, Xq, dc, Cout, blockIdx.x * cols_per_cta, cols_per_cta, blockIdx.y,
+                     (C *)smem_raw);
 }
 
 // out_rows: rows_per_cta output rows per CTA, one level (blockIdx.y).
@@ -746,8 +747,10 @@ cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftP
     typedef typename cvec<R>::T C;
     set_fft_smem_attr<R>();
     if (g.nbx <= 0 || g.out_ny <= 0 || g.out_nx <= 0 || g.nlvls <= 0) return cudaSuccess;
-    dim3 gc(g.nbx, g.nlvls);
-    out_cols_kernel<R><<<gc, 256, 3 * (size_t)ply.n * sizeof(C), st>>>(g, ply, twy, xband, Xp, Xq, dc, Cbuf);
+    const int cpc = out_cols_per_cta(ply.n, sizeof(C));
+    dim3 gc((g.nbx + cpc - 1) / cpc, g.nlvls);
+    out_cols_kernel<R><<<gc, 256, (2 * (size_t)cpc + 1) * ply.n * sizeof(C), st>>>(g, ply, twy, xband, Xp, Xq, dc,
+                                                                                   Cbuf, cpc);
     // two rows per CTA in FP32, one in FP64, bounded by shared memory
     int rpc = sizeof(C) == 8 ? 2 : 1;
     while (rpc > 1 && (2 * (size_t)rpc + 1) * plx.n * sizeof(C) > 190 * 1024) --rpc;

@@ -74,6 +74,7 @@ void na_factorize(int n, FftPlan &p)
             m /= f;
         }
     if (m > 1) p.radix[p.nstages++] = m;
+    fft_plan_finalize(p);
 }
 
 // solved modes of column c (Hermitian representatives plus unpaired modes),

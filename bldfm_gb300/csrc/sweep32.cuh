@@ -14,7 +14,7 @@
 // recursion is contractive (it follows the decaying solution), so FP32 loses
 // nothing to the cancellation that forces FP64 in the forward shooting form.
 // The running product Q_i = prod_{k>=i} (c_k R_k + a_k) is kept as an FP32
-// mantissa with an integer power-of-two exponent, renormalised every 4 steps.
+// mantissa with an integer power-of-two exponent, renormalised every 8 steps.
 __device__ __forceinline__ float2 csqrt_f(float2 w)
 {
     // principal branch, Kahan's formulation

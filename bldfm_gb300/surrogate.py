@@ -161,11 +161,14 @@ class TransferPool:
 
 
 def train(net, pool, steps, batch=65536, lr=1e-3, lr_final=1e-5, decay_from=0.3, seed=1, floor=1e-3,
-          log_every=100, callback=None):
+          log_every=100, callback=None, conc_weight=1.0):
     """Adam on fresh device-generated samples every step; the learning rate
     stays at ``lr`` for the first ``decay_from`` of the steps, then decays on a
-    cosine to ``lr_final``.  Returns [(step, loss)] every ``log_every`` steps."""
+    cosine to ``lr_final``.  ``conc_weight`` scales the concentration part of
+    the loss against the flux part.  Returns [(step, loss)] every
+    ``log_every`` steps."""
     norm = pool.norm if pool.norm is not None else pool.energies()
+    norm = norm * torch.tensor([1.0, float(conc_weight)], device=norm.device)
     X, T, W = pool.buffers(batch)
     hist = []
     for it in range(steps):
@@ -382,16 +385,19 @@ def _main(argv=None):
     ap.add_argument("--cases", type=int, default=16384)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--conc-weight", type=float, default=1.0)
     a = ap.parse_args(argv)
     pool = TransferPool(ncases=a.cases, seed=0)
     net = MLP(batch=a.batch, seed=a.seed)
     t0 = time.time()
     hist = train(net, pool, a.steps, batch=a.batch, lr=a.lr, seed=a.seed, log_every=max(a.steps // 50, 1),
+                 conc_weight=a.conc_weight,
                  callback=lambda i, l: print("step %d loss %.3e (%.0f s)" % (i, l, time.time() - t0), flush=True))
     torch.cuda.synchronize()
     dt = time.time() - t0
     val = validation_loss(net, pool)
     save(net, a.out, {"steps": a.steps, "batch": a.batch, "lr": a.lr, "cases": a.cases, "seed": a.seed,
+                      "conc_weight": a.conc_weight,
                       "train_s": dt, "val_loss": float(val), "train_box": TRAIN_BOX, "history": hist[-10:]})
     print("saved %s: validation loss %.3e, %.1f s" % (a.out, val, dt))
 
