@@ -542,7 +542,7 @@ def main():
     from bldfm_gb300 import autotune
     from bldfm_gb300.batch import BatchSolver, solve_batch
 
-    threads, per_sm = autotune.tune(kwb[0])
+    threads, per_sm, xlines = autotune.tune(kwb[0])
 
     def make_solves(mode):
         solves = []
@@ -627,14 +627,14 @@ def main():
         return ms, stages
 
     # --- headline: batched FP32 path replayed as a CUDA graph ---
-    gsolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True)
+    gsolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
     with ClockSampler(local) as clk:
         msb, _ = timed_batches(gsolver, args.steps, args.warmup)
     fps_batch = world * B * args.steps / (msb * 1e-3)
     if gsolver.status() != 0:
         raise RuntimeError("device status %d" % gsolver.status())
     # same batches without the graph, with per-stage CUDA-event timers (roofline)
-    tsolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=False)
+    tsolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=False, xform_lines=xlines)
     msnb, stages_b = timed_batches(tsolver, args.steps, args.warmup, stage_timing=True)
     fps_nograph = world * B * args.steps / (msnb * 1e-3)
 
@@ -680,7 +680,7 @@ def main():
         prod_line = production_section(args, lib, dev, sptr, not args.no_cpu_baseline)
 
     # --- e2e through the public batched API (numpy in, numpy out) ---
-    esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True)
+    esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
     e2e_steps = max(2, args.steps // 2)
     solve_batch(kwb[0], solver=esolver)
     t = time.perf_counter()
@@ -740,7 +740,7 @@ def main():
                 "footprints_per_step": B,
                 "path": "batched fp32 invariant-imbedding sweep + fp32 transforms, CUDA graph, device-resident",
                 "met_batches": NB,
-                "sweep_launch": {"threads": threads, "ctas_per_sm": per_sm, "autotuned": True},
+                "sweep_launch": {"threads": threads, "ctas_per_sm": per_sm, "xform_lines": xlines, "autotuned": True},
                 "l2": "inputs larger than L2: a step's 16 footprints use ~170 MB of spectra and outputs",
                 "parallelism": "replicas" if world > 1 else "single",
             },

@@ -90,7 +90,7 @@ class BatchOpts(ctypes.Structure):
         ("threads", ctypes.c_int32),
         ("ctas_per_sm", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("xform_lines", ctypes.c_int32),
     ]
 
 

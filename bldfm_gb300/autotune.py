@@ -1,9 +1,11 @@
-"""Autotuner for the batched sweep launch.
+"""Autotuner for the batched launch.
 
-Picks the sweep CTA size (modes per CTA tile) and the number of persistent
-CTAs per SM for a batch shape by timing candidates on the device with CUDA
-events, and caches the winner in a JSON file keyed by GPU name and a coarse
-shape signature (total solved modes, deepest level count, number of cases).
+Picks the sweep CTA size (modes per CTA tile), the number of persistent
+CTAs per SM and the lines per CTA of the output-transform passes for a batch
+shape by timing candidates on the device with CUDA events (first the sweep
+shape, then the transform lines with the best sweep shape), and caches the
+winner in a JSON file keyed by GPU name and a coarse shape signature (total
+solved modes, deepest level count, number of cases).
 Cache file: $BLDFM_GB300_CACHE or ~/.cache/bldfm_gb300/autotune.json.
 """
 
@@ -17,6 +19,7 @@ from . import _lib
 from .batch import BatchSolver
 
 CANDIDATES = [(256, 0), (256, 4), (256, 6), (128, 0), (128, 8), (128, 12)]
+XFORM_LINES = [4, 2, 1]
 
 
 def _cache_path():
@@ -61,32 +64,39 @@ def signature(cases):
                                         b(len(cases)))
 
 
+def _time(cases, reps, **opts):
+    s = BatchSolver(use_graph=False, **opts)
+    s.solve(cases)  # warm
+    s.stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s.stream)
+    for _ in range(reps):
+        s.solve(cases)
+    e1.record(s.stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return ms if s.status() == 0 else None
+
+
 def tune(cases, reps=3, use_cache=True):
-    """Return (threads, ctas_per_sm) for this batch shape (timed or cached)."""
+    """Return (threads, ctas_per_sm, xform_lines) for this batch shape (timed or cached)."""
     key = signature(cases)
     cache = _load() if use_cache else {}
-    if key in cache:
+    if key in cache and "xform_lines" in cache[key]:
         v = cache[key]
-        return int(v["threads"]), int(v["ctas_per_sm"])
+        return int(v["threads"]), int(v["ctas_per_sm"]), int(v["xform_lines"])
     best, best_ms = CANDIDATES[0], None
     for threads, per_sm in CANDIDATES:
-        s = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=False)
-        s.solve(cases)  # warm
-        s.stream.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(s.stream)
-        for _ in range(reps):
-            s.solve(cases)
-        e1.record(s.stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / reps
-        if s.status() != 0:
-            continue
-        if best_ms is None or ms < best_ms:
+        ms = _time(cases, reps, threads=threads, ctas_per_sm=per_sm)
+        if ms is not None and (best_ms is None or ms < best_ms):
             best, best_ms = (threads, per_sm), ms
+    best_xl, best_xms = 0, None
+    for xl in XFORM_LINES:
+        ms = _time(cases, reps, threads=best[0], ctas_per_sm=best[1], xform_lines=xl)
+        if ms is not None and (best_xms is None or ms < best_xms):
+            best_xl, best_xms = xl, ms
     if use_cache:
-        cache[key] = {"threads": best[0], "ctas_per_sm": best[1], "ms": best_ms}
+        cache[key] = {"threads": best[0], "ctas_per_sm": best[1], "xform_lines": best_xl, "ms": best_xms}
         _save(cache)
-    return best
-
+    return best[0], best[1], best_xl

@@ -39,10 +39,11 @@ class BatchSolver:
     are reused while the batch shape repeats.
     """
 
-    def __init__(self, device=None, threads=0, ctas_per_sm=0, use_graph=True):
+    def __init__(self, device=None, threads=0, ctas_per_sm=0, use_graph=True, xform_lines=0):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.stream = torch.cuda.Stream(device=self.device)
-        self.opts = _lib.BatchOpts(threads=int(threads), ctas_per_sm=int(ctas_per_sm), use_graph=int(use_graph))
+        self.opts = _lib.BatchOpts(threads=int(threads), ctas_per_sm=int(ctas_per_sm), use_graph=int(use_graph),
+                                   xform_lines=int(xform_lines))
         self._ws = None
         self._out_buf = None  # one device buffer holding every case's conc and flx
         self._srf = {}

@@ -695,15 +695,26 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
         if (rc != BLDFM_OK) return rc;
         const SolveGeom &g = B.hp[k].g;
         B.tile0[k] = B.ntiles;
-        B.ntiles += (g.nsolved + B.threads - 1) / B.threads;
+        const int64_t tm = (int64_t)B.threads * BATCH_MODES_PER_THREAD;
+        B.ntiles += (g.nsolved + tm - 1) / tm;
         maxL = std::max(maxL, g.nz - 1);
         maxnz = std::max(maxnz, g.nz);
         maxnfy = std::max(maxnfy, g.nfy);
         maxnfx = std::max(maxnfx, g.nfx);
     }
-    B.rpc = 2;
+    const int xl = opts ? opts->xform_lines : 0;
+    if (xl != 0 && xl != 1 && xl != 2 && xl != 4) return BLDFM_ERR_ARG;
+    B.rpc = xl > 0 ? xl : 2;
     while (B.rpc > 1 && (2 * (size_t)B.rpc + 1) * maxnfx * 8 > 190 * 1024) --B.rpc;
     B.cpc = out_cols_per_cta(maxnfy, 8);
+    if (xl > 0)
+        while (B.cpc > xl) B.cpc >>= 1;
+    if (xl > B.cpc)
+        for (int c = xl; c > B.cpc; c >>= 1)
+            if ((2 * (size_t)c + 1) * maxnfy * 8 <= 190 * 1024) {
+                B.cpc = c;
+                break;
+            }
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
         B.col0[k] = B.ncol;
@@ -847,7 +858,8 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
         if (g.footprint)
             hx_dc_values(nz, lv64, hp.slot.data(), g.q0dc_fp, 0.0, c.desc.srf_bg_conc,
                          g.precision == BLDFM_PREC_SINGLE, g.nlvls, 0, (double *)(blob + B.off_dc[k]));
-        const int64_t nt = (g.nsolved + B.threads - 1) / B.threads;
+        const int64_t tm = (int64_t)B.threads * BATCH_MODES_PER_THREAD;
+        const int64_t nt = (g.nsolved + tm - 1) / tm;
         for (int64_t t = 0; t < nt; ++t) {
             tile_case[B.tile0[k] + t] = k;
             tile_cost.push_back((double)std::max(nz - 1, 1));

@@ -36,10 +36,11 @@ __device__ __forceinline__ void load_case(BatchCase *dst, const BatchCase *src)
 }
 
 // Persistent sweep: CTA blockIdx.x owns tiles [cta_tiles[b], cta_tiles[b+1]);
-// a tile is blockDim.x consecutive solved modes of one case.  The case's level
+// a tile is BATCH_MODES_PER_THREAD * blockDim.x consecutive solved modes of
+// one case (two per thread, sharing the level-table loads).  The case's level
 // table is brought into shared memory by one bulk copy whenever the case
 // changes (the mbarrier flips phase each time; every wait is bounded).
-__global__ void __launch_bounds__(256) riccati32_batch_kernel(const BatchCase *__restrict__ cases,
+__global__ void __launch_bounds__(256, 2) riccati32_batch_kernel(const BatchCase *__restrict__ cases,
                                                               const int *__restrict__ tile_case,
                                                               const int64_t *__restrict__ cta_tiles, int *err)
 {
@@ -107,23 +108,27 @@ __global__ void __launch_bounds__(256) riccati32_batch_kernel(const BatchCase *_
         }
         const int L = sc.g.nz - 1;
         const int *s_slot = (const int *)(s_lv + (size_t)L * BLDFM_LV32);
-        const int64_t m = (t - sc.tile0) * (int64_t)blockDim.x + threadIdx.x;
-        if (m < sc.g.nsolved && sc.g.nsnap > 0) {
-            const bool single = sc.g.nsnap == 1;
-            if (sc.g.iso) {
-                if (single)
-                    ricc_mode<true, true>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq, sc.ax, sc.ay,
-                                          m);
+        // a tile is 2 blockDim.x modes: thread modes m0 and m0 + blockDim.x
+        const int64_t m0 = (t - sc.tile0) * BATCH_MODES_PER_THREAD * (int64_t)blockDim.x + threadIdx.x;
+        const int64_t m1 = m0 + blockDim.x;
+        if (m0 < sc.g.nsolved && sc.g.nsnap > 0) {
+            const int64_t mb = m1 < sc.g.nsolved ? m1 : -1;
+            if (sc.g.nsnap == 1) {
+                if (sc.g.iso)
+                    ricc_mode_pair<true>(sc.g, s_lv, sc.modes, sc.q0, sc.Xp, sc.Xq, sc.ax, sc.ay, m0, mb);
                 else
-                    ricc_mode<true, false>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq, sc.ax,
-                                           sc.ay, m);
+                    ricc_mode_pair<false>(sc.g, s_lv, sc.modes, sc.q0, sc.Xp, sc.Xq, sc.ax, sc.ay, m0, mb);
             } else {
-                if (single)
-                    ricc_mode<false, true>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq, sc.ax,
-                                           sc.ay, m);
-                else
-                    ricc_mode<false, false>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq, sc.ax,
-                                            sc.ay, m);
+                for (int u = 0; u < 2; ++u) {
+                    const int64_t m = u == 0 ? m0 : mb;
+                    if (m < 0) break;
+                    if (sc.g.iso)
+                        ricc_mode<true, false>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq, sc.ax,
+                                               sc.ay, m);
+                    else
+                        ricc_mode<false, false>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq,
+                                                sc.ax, sc.ay, m);
+                }
             }
         }
     }

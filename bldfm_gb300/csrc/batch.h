@@ -6,6 +6,9 @@
 
 #include "common.h"
 
+// solved modes per thread of the batched sweep (a tile is this many blocks)
+#define BATCH_MODES_PER_THREAD 2
+
 // One case of a batch as the device kernels see it.
 struct __align__(16) BatchCase {
     SolveGeom g;

@@ -59,6 +59,11 @@ struct StepCoef<true> {
     __device__ __forceinline__ void eval(const float *lv, float2 &a, float2 &b, float2 &c) const
     {
         const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+        eval_row(r0, r1, r2, a, b, c);
+    }
+    __device__ __forceinline__ void eval_row(const float4 r0, const float4 r1, const float4 r2, float2 &a, float2 &b,
+                                             float2 &c) const
+    {
         a = make_float2(fmaf(r0.x, k2, 1.f), r0.y * kw);
         b = make_float2(fmaf(r0.w, k2, r0.z), r1.x * kw);
         c = make_float2(fmaf(r1.z, k4, fmaf(r1.w, kw2, r1.y * k2)), fmaf(r2.y, k2kw, r2.x * kw));
@@ -78,6 +83,11 @@ struct StepCoef<false> {
     __device__ __forceinline__ void eval(const float *lv, float2 &a, float2 &b, float2 &c) const
     {
         const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+        eval_row(r0, r1, r2, a, b, c);
+    }
+    __device__ __forceinline__ void eval_row(const float4 r0, const float4 r1, const float4 r2, float2 &a, float2 &b,
+                                             float2 &c) const
+    {
         const float Tr = fmaf(r0.x, lx2, r0.y * ly2);
         const float Ti = fmaf(r0.z, lx, r0.w * ly);
         a = make_float2(fmaf(-r1.x, Tr, 1.f), -r1.x * Ti);
@@ -226,6 +236,95 @@ __device__ __forceinline__ void ricc_mode(const SolveGeom &g, const float *__res
         if (paired) {
             Xp[spec_idx(g, s, rm, cm)] = make_float2(p.x, -p.y);
             Xq[spec_idx(g, s, rm, cm)] = make_float2(q.x, -q.y);
+        }
+    }
+}
+
+// Two solved modes per thread with one output level (SINGLE): the same
+// arithmetic per mode as ricc_mode<ISO, true>, with the level-table row and
+// the loop control shared by the two interleaved recursions.  mb < 0: the
+// second slot repeats ma and writes nothing.
+template <bool ISO>
+__device__ __forceinline__ void ricc_mode_pair(const SolveGeom &g, const float *__restrict__ s_lv,
+                                               const uint32_t *__restrict__ modes,
+                                               const float2 *__restrict__ q0spec, float2 *__restrict__ Xp,
+                                               float2 *__restrict__ Xq, float ax, float ay, int64_t ma, int64_t mb)
+{
+    const int L = g.nz - 1;
+    const int jmax = g.jmax;
+    const int64_t mm[2] = {ma, mb >= 0 ? mb : ma};
+    int r[2], c[2], kx[2], ky[2];
+    bool paired[2];
+    StepCoef<ISO> sc[2];
+    float2 R[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        unpack_mode(modes[mm[u]], r[u], c[u], paired[u]);
+        kx[u] = freq_of_index(c[u], g.nlx);
+        ky[u] = freq_of_index(r[u], g.nly);
+        const float lx = ax * (float)kx[u], ly = ay * (float)ky[u];
+        sc[u].init(lx, ly, g.ex, g.ey);
+        const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
+                                     fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+        const float2 eg = csqrt_f(w);
+        const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+        const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
+        R[u] = make_float2(ke.x * inv, -ke.y * inv);
+    }
+    int i = L - 1;
+    for (; i >= jmax; --i) {
+        const float *lv = s_lv + (size_t)i * BLDFM_LV32;
+        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            float2 a, b, cc;
+            sc[u].eval_row(r0, r1, r2, a, b, cc);
+            ricc_step(R[u], a, b, cc);
+        }
+    }
+    float2 Rj[2] = {R[0], R[1]};
+    float2 Q[2] = {make_float2(1.f, 0.f), make_float2(1.f, 0.f)};
+    int E[2] = {0, 0};
+    int cnt = 0;
+    for (; i >= 0; --i) {
+        const float *lv = s_lv + (size_t)i * BLDFM_LV32;
+        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            float2 a, b, cc;
+            sc[u].eval_row(r0, r1, r2, a, b, cc);
+            ricc_step(R[u], a, b, cc);
+            flux_step(Q[u], R[u], a, cc);
+        }
+        if (++cnt == 8) {
+            cnt = 0;
+            renorm(Q[0], E[0]);
+            renorm(Q[1], E[1]);
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        if (u == 1 && mb < 0) break;
+        const float2 q0 = q0spec ? q0spec[(size_t)c[u] * g.nly + r[u]] : make_float2((float)g.q0dc_fp, 0.f);
+        float2 sh = make_float2(1.f, 0.f);
+        if (g.do_shift) {
+            const uint32_t turns = (uint32_t)kx[u] * g.turn_x + (uint32_t)ky[u] * g.turn_y;
+            float sn, cs;
+            sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
+            sh = make_float2(cs, sn);
+        }
+        const float2 ratio = make_float2(ldexpf(Q[u].x, E[u]), ldexpf(Q[u].y, E[u]));
+        float2 q = fc_mul(q0, ratio);
+        float2 p = fc_mul(Rj[u], q);
+        p = fc_mul(p, sh);
+        q = fc_mul(q, sh);
+        Xp[spec_idx(g, 0, r[u], c[u])] = p;
+        Xq[spec_idx(g, 0, r[u], c[u])] = q;
+        if (paired[u]) {
+            const int rm = index_of_freq(-ky[u], g.nly);
+            const int cm = index_of_freq(-kx[u], g.nlx);
+            Xp[spec_idx(g, 0, rm, cm)] = make_float2(p.x, -p.y);
+            Xq[spec_idx(g, 0, rm, cm)] = make_float2(q.x, -q.y);
         }
     }
 }

@@ -167,7 +167,9 @@ typedef struct bldfm_batch_opts {
     int32_t threads;     /* sweep CTA size: 128 or 256 (0: 256)            */
     int32_t ctas_per_sm; /* persistent sweep CTAs per SM (0: occupancy max) */
     int32_t use_graph;   /* capture the batch once, replay it afterwards   */
-    int32_t reserved;
+    int32_t xform_lines; /* lines per CTA of both output-transform passes:
+                          * 1, 2 or 4 (0: 4 columns / 2 rows), lowered to
+                          * what fits the shared memory                    */
 } bldfm_batch_opts;
 
 /* Workspace bytes for a batch (256-byte aligned workspace required). */

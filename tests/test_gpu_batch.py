@@ -86,7 +86,23 @@ def test_autotuner_returns_a_candidate(tmp_path, monkeypatch):
 
     monkeypatch.setenv("BLDFM_GB300_CACHE", str(tmp_path / "tune.json"))
     cases = _cases(3)
-    t, per_sm = autotune.tune(cases, reps=1)
-    assert (t, per_sm) in autotune.CANDIDATES
+    t, per_sm, xl = autotune.tune(cases, reps=1)
+    assert (t, per_sm) in autotune.CANDIDATES and xl in autotune.XFORM_LINES
     assert (tmp_path / "tune.json").exists()
-    assert autotune.tune(cases) == (t, per_sm)  # cached
+    assert autotune.tune(cases) == (t, per_sm, xl)  # cached
+
+
+@pytest.mark.parametrize("xl", [1, 2, 4])
+def test_transform_lines_per_cta_agree(xl):
+    """Every lines-per-CTA choice of the transform passes gives the same result."""
+    from bldfm_gb300.batch import BatchSolver
+
+    cases = _cases(4)
+    ref = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in BatchSolver(use_graph=False).solve(cases)]
+    s = BatchSolver(use_graph=False, xform_lines=xl)
+    out = s.solve(cases)
+    s.stream.synchronize()
+    assert s.status() == 0
+    for (c, f), (rc, rf) in zip(out, ref):
+        np.testing.assert_array_equal(c.cpu().numpy(), rc)
+        np.testing.assert_array_equal(f.cpu().numpy(), rf)
