@@ -98,7 +98,10 @@ def test_transform_lines_per_cta_agree(xl):
     from bldfm_gb300.batch import BatchSolver
 
     cases = _cases(4)
-    ref = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in BatchSolver(use_graph=False).solve(cases)]
+    r = BatchSolver(use_graph=False)
+    outs = r.solve(cases)
+    r.stream.synchronize()
+    ref = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in outs]
     s = BatchSolver(use_graph=False, xform_lines=xl)
     out = s.solve(cases)
     s.stream.synchronize()
