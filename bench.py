@@ -23,6 +23,8 @@ Reported:
                  n = 64..256) in one batched call per step
   production     the 1024^2-extended, n = 256 footprint: FP64 / FP64
                  accurate / FP32 on the GPU, the CPU port, analytic check
+  serving        surrogate serving with fallback on a 1024^2 footprint
+                 timeseries (10% outside the training box)
   cpu_baseline   the CPU oracle port (reference arithmetic, OpenMP on all
                  host cores) on a bounded sample
 
@@ -378,6 +380,76 @@ def production_section(args, lib, dev, sptr, cpu):
     return res
 
 
+def serving_cases(nsteps, seed=7):
+    """Footprint timeseries for surrogate serving: the production met case's
+    neighbourhood (z_m = 20 m, 4 m/s, unstable to slightly stable) on a 1024^2
+    grid (2000 m domain, default halo, modes 1024^2, n = 128), 10% of the
+    steps drawn outside the network's training box (strongly unstable)."""
+    from bldfm_gb300.surrogate import BOX, met_scalars
+
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < nsteps:
+        outside = len(out) % 10 == 9
+        ustar = float(rng.uniform(0.22, 0.38))
+        inv_l = float(rng.uniform(-0.1, -0.06) if outside else rng.uniform(-0.045, 0.01))
+        mol = 1.0 / inv_l if abs(inv_l) > 1e-6 else 1e6
+        wd = np.deg2rad(float(rng.uniform(0.0, 360.0)))
+        wind = (-4.0 * np.sin(wd), -4.0 * np.cos(wd))
+        _, s1, s2, _ = met_scalars(20.0, wind, ustar=ustar, mol=mol)
+        inside = BOX["s1"][0] <= s1 <= BOX["s1"][1] and BOX["s2"][0] <= s2 <= BOX["s2"][1]
+        if inside == outside:
+            continue
+        out.append(dict(n=N_LEVELS, zm=20.0, wind=wind, srf_shape=(1024, 1024), domain=(2000.0, 2000.0),
+                        modes=(1024, 1024), meas_pt=(1000.0, 1000.0), ustar=ustar, mol=mol))
+    return out
+
+
+def serving_section(args, dev):
+    """Surrogate serving with fallback on a 1024^2 footprint timeseries: wall
+    time of Surrogate.serve (batched fused launches, FP64 fallback for the
+    out-of-box steps, accurate-FP64 spot checks of every 64th served step),
+    and relL2 of served steps against the exact solution."""
+    import torch
+
+    from bldfm_gb300 import steady_state_transport_solver
+    from bldfm_gb300 import surrogate as S
+
+    if not os.path.exists(S.WEIGHTS):
+        return {"unavailable": "no trained weights"}
+    net, box, meta = S.load(S.WEIGHTS)
+    items = serving_cases(256)
+    sur = S.Surrogate(net, spot_every=64, tol=1e-3)
+    sur.serve(items[:16])  # warm (plans, twiddles, fallback path)
+    sur = S.Surrogate(net, spot_every=64, tol=1e-3)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    out, paths = sur.serve(items)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    # error distribution of served steps against the exact discrete solution
+    errs = []
+    served = [k for k, p in enumerate(paths) if p == "surrogate"]
+    for k in served[:: max(1, len(served) // 16)][:16]:
+        pr = sur.prepare(**items[k])
+        _, cr, fr = steady_state_transport_solver(**pr["kw"], mode="fp64r")
+        c, f = out[k]
+        errs.append(max(np.linalg.norm(c.cpu().numpy() - cr) / np.linalg.norm(cr),
+                        np.linalg.norm(f.cpu().numpy() - fr) / np.linalg.norm(fr)))
+    e = np.array(errs)
+    st = sur.stats
+    return {
+        "workload": "256-step footprint timeseries (10% outside the training box), 1024^2 grid, 2000 m domain, "
+                    "default halo, modes 1024^2, n=128, z_m=20 m, u*~U[0.22,0.38], 1/L~U[-0.045,0.01] "
+                    "(outside: U[-0.1,-0.06]), 4 m/s, dir~U[0,360)",
+        "value": len(items) / dt, "unit": "footprints/s (wall, incl. fallbacks and spot checks)",
+        "paths": {p: paths.count(p) for p in set(paths)},
+        "spot_checks": st["spot"], "spot_fail": st["spot_fail"], "spot_relL2": st["errors"],
+        "served_relL2_vs_exact": {"n": len(errs), "median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)),
+                                  "max": float(e.max()), "frac_le_1e-3": float((e <= 1e-3).mean())},
+    }
+
+
 def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
     """Footprints/s of the surrogate on batch 0's met cases (device-resident
     outputs, descriptors prepared once), its relL2 against the FP64 path, and
@@ -674,10 +746,11 @@ def main():
     sur_line = surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr)
 
     # --- the mixed-grid timeseries and the production footprint (rank 0, N = 1) ---
-    ts_line = prod_line = None
+    ts_line = prod_line = serve_line = None
     if rank == 0 and world == 1 and not args.no_extra:
         ts_line = timeseries_section(args, dev)
         prod_line = production_section(args, lib, dev, sptr, not args.no_cpu_baseline)
+        serve_line = serving_section(args, dev)
 
     # --- e2e through the public batched API (numpy in, numpy out) ---
     esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
@@ -771,6 +844,7 @@ def main():
             "surrogate": sur_line,
             "timeseries": ts_line,
             "production": prod_line,
+            "serving": serve_line,
             "cpu_baseline": cpu,
             "gpu_launches": 3 * args.steps,
             "clocks": clk.summary(),

@@ -335,6 +335,50 @@ class Surrogate:
         torch.cuda.synchronize(self.device)
         return int(self._ws[:4].view(torch.int32).item()) if self._ws is not None else 0
 
+    def classify(self, kw):
+        """True when the case (keyword dict of ``prepare``) lies in the training box."""
+        _, s1, s2, _ = met_scalars(kw["zm"], kw["wind"], kw.get("ustar"), kw.get("z0"), kw.get("mol", 1e9))
+        km = mode_kmax(kw["srf_shape"], kw["domain"], kw.get("modes", (512, 512)), kw.get("halo"))
+        return self.in_box(kw["n"], kw["zm"], s1, s2, km)
+
+    def serve(self, items, batch=16):
+        """Footprints of a met timeseries (keyword dicts of ``prepare``):
+        in-box cases through the network in batched fused launches, every
+        ``spot_every``-th of them also through the judge (the FP64 result is
+        kept when the surrogate misses ``tol``), out-of-box cases through the
+        fallback solver.  Returns (outputs, paths): outputs[k] = (conc, flx)
+        (device tensors for served cases, host arrays for solver results),
+        paths[k] in "surrogate", "fp64-spot", "fp64-box"."""
+        out, paths = [None] * len(items), [None] * len(items)
+        inbox = []
+        for k, kw in enumerate(items):
+            if self.classify(kw):
+                inbox.append(k)
+            else:
+                self.stats["out_of_box"] += 1
+                p = self.prepare(**kw)
+                _, c, f = steady_state_transport_solver(**p["kw"], mode=self.fallback)
+                out[k], paths[k] = (c, f), "fp64-box"
+        for i in range(0, len(inbox), batch):
+            ks = inbox[i : i + batch]
+            b = self.prepare_batch([items[k] for k in ks])
+            for k, pr, (c, f) in zip(ks, b["keep"], self.solve_batch_prepared(b)):
+                self.count += 1
+                self.stats["surrogate"] += 1
+                out[k], paths[k] = (c, f), "surrogate"
+                if self.spot_every > 0 and self.count % self.spot_every == 0:
+                    ref = steady_state_transport_solver(**pr["kw"], mode=self.judge)
+                    ca, fa = c.cpu().numpy(), f.cpu().numpy()
+                    err = max(_rell2(ca, ref[1]), _rell2(fa, ref[2]))
+                    self.stats["spot"] += 1
+                    self.stats["errors"].append(err)
+                    if err > self.tol:
+                        self.stats["spot_fail"] += 1
+                        if self.fallback != self.judge:
+                            ref = steady_state_transport_solver(**pr["kw"], mode=self.fallback)
+                        out[k], paths[k] = (ref[1], ref[2]), "fp64-spot"
+        return out, paths
+
     def footprint(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
                   ustar=None, z0=None, mol=1e9):
         """One footprint at z_m: (grid, conc, flx) as the solver returns them,

@@ -182,3 +182,33 @@ def test_trained_network_gains_over_solver():
     b = sur.prepare_batch([kw] * 16)
     tsur = timeit(lambda: sur.solve_batch_prepared(b), 5) / 16
     assert t64 / tsur > 10, (t64, tsur)
+
+
+def test_serve_timeseries_with_fallback():
+    """A short footprint timeseries: in-box steps through the network (with
+    spot checks), out-of-box steps through the FP64 fallback."""
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import Surrogate, load
+
+    net, box, meta = load()
+    rng = np.random.default_rng(2)
+    items = []
+    for k in range(18):
+        th = rng.uniform(0, 2 * np.pi)
+        mol = -150.0 if k % 9 else -12.0  # z_m / L = -1.7: outside the box
+        items.append(dict(n=128, zm=20.0, wind=(-4 * np.sin(th), -4 * np.cos(th)), srf_shape=(256, 256),
+                          domain=(500.0, 500.0), modes=(256, 256), meas_pt=(250.0, 250.0),
+                          ustar=float(rng.uniform(0.25, 0.35)), mol=mol))
+    sur = Surrogate(net, spot_every=8, tol=1e-3)
+    out, paths = sur.serve(items, batch=8)
+    assert paths.count("fp64-box") == 2 and sur.stats["out_of_box"] == 2
+    assert sur.stats["spot"] == 2
+    assert all(p in ("surrogate", "fp64-spot") for k, p in enumerate(paths) if k % 9)
+    for k in (1, 9):
+        p = sur.prepare(**items[k])
+        _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r" if k == 1 else "fp64")
+        c, f = out[k]
+        c = c.cpu().numpy() if hasattr(c, "cpu") else c
+        f = f.cpu().numpy() if hasattr(f, "cpu") else f
+        tol = 2e-3 if k == 1 else 1e-12
+        assert _rel(c, cr) <= tol and _rel(f, fr) <= tol, (k, _rel(c, cr), _rel(f, fr))
