@@ -24,10 +24,23 @@ from .solver import _normalise_levels, make_desc, plan
 def _host_inputs(kw):
     z = np.ascontiguousarray(kw["z"], dtype=np.float64)
     nz = z.shape[0]
-    prof = np.ascontiguousarray(
-        np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in kw["profiles"]])
-    )
-    levels, lv = _normalise_levels(kw["levels"], nz)
+    prof = None
+    try:  # five length-nz arrays: one conversion
+        prof = np.array(kw["profiles"], dtype=np.float64)
+        if prof.shape != (5, nz):
+            prof = None
+    except (ValueError, TypeError):
+        prof = None
+    if prof is None:  # scalars broadcast over the levels
+        prof = np.ascontiguousarray(
+            np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in kw["profiles"]])
+        )
+    levels = kw["levels"]
+    if isinstance(levels, (int, np.integer)) and -nz <= int(levels) < nz:
+        lv = np.array([int(levels)], dtype=np.int64)
+        levels = np.array([levels])
+    else:
+        levels, lv = _normalise_levels(levels, nz)
     return z, prof, levels, lv
 
 
@@ -59,33 +72,45 @@ class BatchSolver:
             t.copy_(torch.from_numpy(a).pin_memory(), non_blocking=True)
         return t
 
-    def prepare(self, cases):
-        """Build the C descriptors of a batch; returns (array, outputs, keepalive)."""
+    def prepare(self, cases, views=True):
+        """Build the C descriptors of a batch; returns (array, outputs, keepalive).
+
+        views=False skips the torch views of the outputs (outputs is then the
+        list of (nlvls, out_ny, out_nx) shapes; the results sit back to back,
+        conc then flx per case, at the start of the solver's output buffer)."""
         n = len(cases)
         arr = (_lib.Case * n)()
         outs, keep = [], []
         descs, shapes = [], []
         for kw in cases:
             z, prof, levels, lv = _host_inputs(kw)
-            d = make_desc(
-                np.shape(kw["srf_flx"]), len(z), kw["domain"], kw.get("modes", (512, 512)),
-                kw.get("meas_pt", (0.0, 0.0)), kw.get("srf_bg_conc", 0.0), bool(kw.get("footprint", False)), False,
-                kw.get("halo"), kw.get("precision", "single"), "fp32",
-            )
-            info = plan(d, lv.size)
-            descs.append((d, z, prof, levels, lv))
-            shapes.append((lv.size, info.out_ny, info.out_nx))
+            key = (np.shape(kw["srf_flx"]), len(z), tuple(float(v) for v in kw["domain"]),
+                   tuple(kw.get("modes", (512, 512))), tuple(float(v) for v in kw.get("meas_pt", (0.0, 0.0))),
+                   float(np.real(kw.get("srf_bg_conc", 0.0))), bool(kw.get("footprint", False)), kw.get("halo"),
+                   kw.get("precision", "single"), lv.size)
+            hit = _DESC_CACHE.get(key)
+            if hit is None:
+                d = make_desc(
+                    np.shape(kw["srf_flx"]), len(z), kw["domain"], kw.get("modes", (512, 512)),
+                    kw.get("meas_pt", (0.0, 0.0)), kw.get("srf_bg_conc", 0.0), bool(kw.get("footprint", False)),
+                    False, kw.get("halo"), kw.get("precision", "single"), "fp32",
+                )
+                info = plan(d, lv.size)
+                hit = (d, (lv.size, info.out_ny, info.out_nx))
+                if len(_DESC_CACHE) > 256:
+                    _DESC_CACHE.clear()
+                _DESC_CACHE[key] = hit
+            descs.append((hit[0], z, prof, levels, lv))
+            shapes.append(hit[1])
         total = 2 * sum(int(np.prod(sh)) for sh in shapes)
         if self._out_buf is None or self._out_buf.numel() < total:
             self._out_buf = torch.empty(total, dtype=torch.float64, device=self.device)
         self.out_elems = total
+        base = self._out_buf.data_ptr()
         off = 0
         for k, kw in enumerate(cases):
             d, z, prof, levels, lv = descs[k]
             sz = int(np.prod(shapes[k]))
-            conc = self._out_buf[off : off + sz].view(shapes[k])
-            flx = self._out_buf[off + sz : off + 2 * sz].view(shapes[k])
-            off += 2 * sz
             footprint = bool(kw.get("footprint", False))
             c = arr[k]
             c.desc = d
@@ -94,9 +119,14 @@ class BatchSolver:
             c.prof_host = prof.ctypes.data
             c.levels_host = lv.ctypes.data
             c.nlvls = lv.size
-            c.conc_dev = conc.data_ptr()
-            c.flx_dev = flx.data_ptr()
-            outs.append((conc, flx))
+            c.conc_dev = base + 8 * off
+            c.flx_dev = base + 8 * (off + sz)
+            if views:
+                outs.append((self._out_buf[off : off + sz].view(shapes[k]),
+                             self._out_buf[off + sz : off + 2 * sz].view(shapes[k])))
+            else:
+                outs.append(shapes[k])
+            off += 2 * sz
             keep.append((z, prof, lv, levels))
         return arr, outs, keep
 
@@ -142,6 +172,7 @@ class BatchSolver:
 
 
 _GRID_CACHE = {}
+_DESC_CACHE = {}  # descriptor and output shape per case geometry
 
 
 def _grid(z, levels, shape, domain):
@@ -168,10 +199,12 @@ def solve_batch(cases, *, solver=None):
     """Solve a list of cases (keyword-argument dicts of
     ``steady_state_transport_solver``) in FP32 on the GPU; returns a list of
     ``(grid, conc, flx)`` with the single-case function's shapes and dtypes.
-    All outputs come back in one device-to-host copy into pinned memory; the
-    grid arrays are shared read-only arrays."""
+    All outputs come back in one device-to-host copy into a fresh pinned
+    buffer that the returned arrays view; the grid arrays are shared
+    read-only arrays."""
     solver = solver or BatchSolver()
-    outs = solver.solve(cases)
+    shapes = solver.solve_prepared(solver.prepare(cases, views=False))
+    keep = solver._keep
     host = torch.empty(solver.out_elems, dtype=torch.float64, pin_memory=True)
     with torch.cuda.stream(solver.stream):
         host.copy_(solver._out_buf[: solver.out_elems], non_blocking=True)
@@ -181,8 +214,7 @@ def solve_batch(cases, *, solver=None):
     hn = host.numpy()
     results = []
     off = 0
-    for kw, (conc_d, _) in zip(cases, outs):
-        shape = tuple(conc_d.shape)
+    for kw, shape, (z, _, _, levels) in zip(cases, shapes, keep):
         sz = int(np.prod(shape))
         conc = hn[off : off + sz].reshape(shape)
         flx = hn[off + sz : off + 2 * sz].reshape(shape)
@@ -192,7 +224,6 @@ def solve_batch(cases, *, solver=None):
         xm, ym = kw.get("meas_pt", (0.0, 0.0))
         if precision == "single" and not footprint and not (xm**2 + ym**2 > 0.0):
             conc, flx = conc.astype(np.float32), flx.astype(np.float32)
-        z, _, levels, _ = _host_inputs(kw)
         grid = _grid(z, levels, np.shape(kw["srf_flx"]), kw["domain"])
         results.append((grid, np.squeeze(conc), np.squeeze(flx)))
     return results
