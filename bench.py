@@ -753,14 +753,28 @@ def main():
         serve_line = serving_section(args, dev)
 
     # --- e2e through the public batched API (numpy in, numpy out) ---
+    from bldfm_gb300.batch import solve_stream
+
     esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
-    e2e_steps = max(2, args.steps // 2)
+    e2e_steps = max(2, args.steps)
     solve_batch(kwb[0], solver=esolver)
     t = time.perf_counter()
     for i in range(e2e_steps):
         solve_batch(kwb[i % NB], solver=esolver)
+    e2e_sync = world * B * e2e_steps / (time.perf_counter() - t)
+    # the pipelined timeseries API over the same steps (two solvers alternate)
+    ssolvers = tuple(BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
+                     for _ in range(2))
+    # warm: graphs of both solvers and the pinned host blocks a consumer that
+    # holds one result while the next is produced keeps alive
+    warm = list(solve_stream([kwb[i % NB] for i in range(6)], solvers=ssolvers))
+    del warm
+    t = time.perf_counter()
+    nres = 0
+    for res in solve_stream((kwb[i % NB] for i in range(e2e_steps)), solvers=ssolvers):
+        nres += len(res)
     e2e_dt = time.perf_counter() - t
-    e2e_fps = world * B * e2e_steps / e2e_dt
+    e2e_fps = world * nres / e2e_dt
     nz = len(inputs[0][0])
     h2d = B * ((nz - 1) * (12 * 8 + 12 * 4) + nz * 4 + 32 + 640)
     d2h = B * 2 * NY * NX * 8
@@ -827,7 +841,9 @@ def main():
                      "fp64_peak_tflops": peak64.value / 1e12,
                      "frac": (achieved64 / (peak64.value / 1e12)) if achieved64 else None},
             "e2e": {"value": e2e_fps, "unit": "footprints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "api": "bldfm_gb300.batch.solve_batch (numpy in, numpy out)",
+                    "api": "bldfm_gb300.batch.solve_stream over the timed steps (numpy in, numpy out, "
+                           "pinned copies inside, each step's arrays fresh)",
+                    "solve_batch_synchronous": e2e_sync,
                     "single_case_dropin": e2e_single},
             "roofline": {
                 "bound": "fp32-pipe",

@@ -9,7 +9,9 @@ when the batch topology repeats (e.g. a met timeseries on fixed towers).
 
 ``solve_batch(cases)`` takes a list of keyword-argument dicts of
 ``steady_state_transport_solver`` and returns the list of ``(grid, conc, flx)``
-tuples.  ``BatchSolver`` keeps workspace and device outputs between batches.
+tuples; ``solve_stream(batches)`` does the same for a sequence of batches
+with the host work of one batch overlapping the GPU work of the previous.
+``BatchSolver`` keeps workspace and device outputs between batches.
 """
 
 import ctypes
@@ -166,9 +168,15 @@ class BatchSolver:
         return (arr, outs, keep, int(need.value))
 
     def status(self):
-        """Device status word of the last batch (0, or a BLDFM_ERR_* code)."""
+        """Device status word of the last batch (0, or a BLDFM_ERR_* code),
+        read through this solver's stream only (no device-wide sync)."""
+        if self._ws is None:
+            return 0
+        st = torch.empty(1, dtype=torch.int32, pin_memory=True)
+        with torch.cuda.stream(self.stream):
+            st.copy_(self._ws[:4].view(torch.int32), non_blocking=True)
         self.stream.synchronize()
-        return int(self._ws[:4].view(torch.int32).item()) if self._ws is not None else 0
+        return int(st[0])
 
 
 _GRID_CACHE = {}
@@ -195,20 +203,23 @@ def _grid(z, levels, shape, domain):
     return g
 
 
-def solve_batch(cases, *, solver=None):
-    """Solve a list of cases (keyword-argument dicts of
-    ``steady_state_transport_solver``) in FP32 on the GPU; returns a list of
-    ``(grid, conc, flx)`` with the single-case function's shapes and dtypes.
-    All outputs come back in one device-to-host copy into a fresh pinned
-    buffer that the returned arrays view; the grid arrays are shared
-    read-only arrays."""
-    solver = solver or BatchSolver()
+def _enqueue_batch(solver, cases):
+    """Enqueue a batch and the copy of its outputs into a fresh pinned host
+    buffer on the solver's stream; returns the pending state."""
     shapes = solver.solve_prepared(solver.prepare(cases, views=False))
-    keep = solver._keep
     host = torch.empty(solver.out_elems, dtype=torch.float64, pin_memory=True)
+    stat = torch.empty(1, dtype=torch.int32, pin_memory=True)
     with torch.cuda.stream(solver.stream):
         host.copy_(solver._out_buf[: solver.out_elems], non_blocking=True)
-    st = solver.status()
+        stat.copy_(solver._ws[:4].view(torch.int32), non_blocking=True)
+    return (solver, cases, shapes, solver._keep, host, stat)
+
+
+def _finish_batch(pending):
+    """Wait for an enqueued batch and build its (grid, conc, flx) results."""
+    solver, cases, shapes, keep, host, stat = pending
+    solver.stream.synchronize()
+    st = int(stat[0])
     if st != 0:
         _lib.check(st, "solve_batch")
     hn = host.numpy()
@@ -227,3 +238,32 @@ def solve_batch(cases, *, solver=None):
         grid = _grid(z, levels, np.shape(kw["srf_flx"]), kw["domain"])
         results.append((grid, np.squeeze(conc), np.squeeze(flx)))
     return results
+
+
+def solve_stream(batches, *, solvers=None, **opts):
+    """Solve an iterable of batches (each a list of keyword-argument dicts of
+    ``steady_state_transport_solver``) in FP32, yielding each batch's list of
+    ``(grid, conc, flx)`` in order.  Two solvers, each with its own stream,
+    workspace and outputs, alternate: batch i + 1 is prepared and enqueued
+    before batch i is waited for, so the host work, the kernels and the
+    copies back overlap.  ``opts`` go to the two BatchSolvers."""
+    solvers = solvers or (BatchSolver(**opts), BatchSolver(**opts))
+    pending = None
+    for i, cases in enumerate(batches):
+        nxt = _enqueue_batch(solvers[i % 2], cases)
+        if pending is not None:
+            yield _finish_batch(pending)
+        pending = nxt
+    if pending is not None:
+        yield _finish_batch(pending)
+
+
+def solve_batch(cases, *, solver=None):
+    """Solve a list of cases (keyword-argument dicts of
+    ``steady_state_transport_solver``) in FP32 on the GPU; returns a list of
+    ``(grid, conc, flx)`` with the single-case function's shapes and dtypes.
+    All outputs come back in one device-to-host copy into a fresh pinned
+    buffer that the returned arrays view; the grid arrays are shared
+    read-only arrays."""
+    solver = solver or BatchSolver()
+    return _finish_batch(_enqueue_batch(solver, cases))

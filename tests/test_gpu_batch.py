@@ -109,3 +109,18 @@ def test_transform_lines_per_cta_agree(xl):
     for (c, f), (rc, rf) in zip(out, ref):
         np.testing.assert_array_equal(c.cpu().numpy(), rc)
         np.testing.assert_array_equal(f.cpu().numpy(), rf)
+
+
+def test_solve_stream_matches_solve_batch():
+    """The pipelined timeseries API yields, batch by batch, what solve_batch returns."""
+    from bldfm_gb300.batch import solve_batch, solve_stream
+
+    batches = [_cases(5), _cases(6), _cases(7)]
+    ref = [solve_batch(b) for b in batches]
+    got = list(solve_stream(batches))
+    assert len(got) == 3
+    for rb, gb in zip(ref, got):
+        for (rg, rc, rf), (gg, gc, gf) in zip(rb, gb):
+            np.testing.assert_array_equal(rc, gc)
+            np.testing.assert_array_equal(rf, gf)
+            assert rc.dtype == gc.dtype
