@@ -330,10 +330,17 @@ class Surrogate:
         _lib.check(st, "surrogate_solve_batch")
         return b["outs"]
 
-    def status(self):
-        """Device status word of the last launch (0, or a BLDFM_ERR_* code)."""
-        torch.cuda.synchronize(self.device)
-        return int(self._ws[:4].view(torch.int32).item()) if self._ws is not None else 0
+    def status(self, stream=None):
+        """Device status word of the last launch (0, or a BLDFM_ERR_* code),
+        read through the launch stream (default: the current stream)."""
+        if self._ws is None:
+            return 0
+        s = stream or torch.cuda.current_stream(self.device)
+        st = torch.empty(1, dtype=torch.int32, pin_memory=True)
+        with torch.cuda.stream(s):
+            st.copy_(self._ws[:4].view(torch.int32), non_blocking=True)
+        s.synchronize()
+        return int(st[0])
 
     def classify(self, kw):
         """True when the case (keyword dict of ``prepare``) lies in the training box."""
