@@ -120,7 +120,8 @@ __global__ void sur_spectra_kernel(const SolveGeom g, const uint32_t *__restrict
 // BLDFM_ERR_TIMEOUT, waits (bounded) for its own copies and MMAs in flight,
 // frees TMEM and returns.
 // ---------------------------------------------------------------------------
-#define SV_K0 32  // K of the split input layer
+#define SV_K0 32     // K of the split input layer
+#define SV_WARPS 16  // 4 warps per TMEM lane quarter, each a quarter of the 256 columns
 
 struct SvSmem {
     uint16_t A[128 * MLP_H];    // activations (A operand)
@@ -128,7 +129,7 @@ struct SvSmem {
     uint16_t B0[MLP_H * SV_K0]; // split W0 (B operand of the input layer)
     float bias[4][MLP_H];
     float W4[MLP_H * MLP_OUT];
-    float4 Yp[2][128];  // output-layer partial sums of the two column halves
+    float4 Yp[SV_WARPS / 4][128];  // output-layer partial sums of the column quarters
     float b4[4];
 };
 
@@ -140,23 +141,23 @@ __device__ __forceinline__ void sv_put8(uint16_t *st, int r, int c, const float 
     *(uint4 *)(st + tc_core_offset(r, c, MLP_H) / 2) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-// epilogue of a hidden layer: this thread's row, 128 columns from c0, bias,
+// epilogue of a hidden layer: this thread's row, 64 columns from c0, bias,
 // GELU, BF16 into the A tile
 __device__ __forceinline__ void sv_epilogue_hidden(uint32_t tb, int row, int c0, const float *bias, uint16_t *A)
 {
 #pragma unroll 1
     for (int cc = 0; cc < 2; ++cc) {
-        float v[64];
-        tc_ld64(tb + 64 * cc, v);
-        const int cb = c0 + 64 * cc;
+        float v[32];
+        tc_ld32(tb + 32 * cc, v);
+        const int cb = c0 + 32 * cc;
 #pragma unroll
-        for (int i = 0; i < 64; ++i) v[i] = gelu_f(v[i] + bias[cb + i]);
+        for (int i = 0; i < 32; ++i) v[i] = gelu_f(v[i] + bias[cb + i]);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) sv_put8(A, row, cb + 8 * q, v + 8 * q);
+        for (int q = 0; q < 4; ++q) sv_put8(A, row, cb + 8 * q, v + 8 * q);
     }
 }
 
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(32 * SV_WARPS, 1)
     sur_serve_kernel(const SurCase *__restrict__ cases, int ncases, int64_t ntiles, const MlpServing net, int *err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -172,19 +173,19 @@ __global__ void __launch_bounds__(256, 1)
         tc_fence_init();
     }
     // split W0 [in][out] into the B operand [out][K = 32]
-    for (int e = tid; e < MLP_H * SV_K0; e += 256) {
+    for (int e = tid; e < MLP_H * SV_K0; e += blockDim.x) {
         const int f = e / SV_K0, k = e % SV_K0, grp = k >> 3, i = k & 7;
         const float w = net.P[MLP_OFF_W0 + i * MLP_H + f];
         const uint16_t wh = f2bf(w);
         const uint16_t wl = f2bf(w - bf2f(wh));
         S.B0[tc_core_offset(f, k, SV_K0) / 2] = grp < 2 ? wh : (grp == 2 ? wl : (uint16_t)0);
     }
-    for (int i = tid; i < MLP_H; i += 256) {
+    for (int i = tid; i < MLP_H; i += blockDim.x) {
         S.bias[0][i] = net.P[MLP_OFF_B0 + i];
 #pragma unroll
         for (int j = 1; j <= 3; ++j) S.bias[j][i] = net.P[MLP_OFF_B(j) + i];
     }
-    for (int i = tid; i < MLP_H * MLP_OUT; i += 256) S.W4[i] = net.P[MLP_OFF_W4 + i];
+    for (int i = tid; i < MLP_H * MLP_OUT; i += blockDim.x) S.W4[i] = net.P[MLP_OFF_W4 + i];
     if (tid < MLP_OUT) S.b4[tid] = net.P[MLP_OFF_B4 + tid];
     tc_fence_proxy_async();
     tc_fence_before();
@@ -201,10 +202,10 @@ __global__ void __launch_bounds__(256, 1)
         tc_bulk_load(S.W, net.Wt[0], WBYTES, &bar_w);
         pend_w = true;
     }
-    // epilogue geometry: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows), columns 128 (w / 4) .. +127
+    // epilogue geometry: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows), columns 64 (w / 4) .. +63
     const int qd = warp & 3, hf = warp >> 2;
     const int row = 32 * qd + lane;
-    const uint32_t tb = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(128 * hf);
+    const uint32_t tb = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(64 * hf);
     bool failed = false;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         if (tid < 32) {
@@ -305,17 +306,17 @@ __global__ void __launch_bounds__(256, 1)
             }
             tc_fence_after();
             if (j < 3) {
-                sv_epilogue_hidden(tb, row, 128 * hf, S.bias[j], S.A);
+                sv_epilogue_hidden(tb, row, 64 * hf, S.bias[j], S.A);
                 tc_fence_proxy_async();
             } else {
                 float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
                 for (int cc = 0; cc < 2; ++cc) {
-                    float v[64];
-                    tc_ld64(tb + 64 * cc, v);
-                    const int c0 = 128 * hf + 64 * cc;
+                    float v[32];
+                    tc_ld32(tb + 32 * cc, v);
+                    const int c0 = 64 * hf + 32 * cc;
 #pragma unroll
-                    for (int i = 0; i < 64; ++i) {
+                    for (int i = 0; i < 32; ++i) {
                         const float h = gelu_f(v[i] + S.bias[3][c0 + i]);
                         const float4 w4 = *(const float4 *)&S.W4[(c0 + i) * MLP_OUT];
                         y.x = fmaf(h, w4.x, y.x);
@@ -333,9 +334,13 @@ __global__ void __launch_bounds__(256, 1)
         if (tid < 128) {
             const int64_t m = lt * 128 + tid;
             if (m < g.nsolved) {
-                const float4 a = S.Yp[0][tid], b = S.Yp[1][tid];
-                const float y[4] = {a.x + b.x + S.b4[0], a.y + b.y + S.b4[1], a.z + b.z + S.b4[2],
-                                    a.w + b.w + S.b4[3]};
+                float4 a = S.Yp[0][tid];
+#pragma unroll
+                for (int qq = 1; qq < SV_WARPS / 4; ++qq) {
+                    const float4 b = S.Yp[qq][tid];
+                    a = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+                }
+                const float y[4] = {a.x + S.b4[0], a.y + S.b4[1], a.z + S.b4[2], a.w + S.b4[3]};
                 emit_spectrum(g, sc.modes[m], y, sc.ax, sc.ay, sc.zm, sc.inv_wind, sc.ktop, sc.utop, sc.Xp, sc.Xq);
             }
         }
@@ -383,7 +388,7 @@ cudaError_t launch_sur_serve(const SurCase *cases, int ncases, int64_t ntiles, c
         attr = true;
     }
     const int grid = (int)std::min<int64_t>(ntiles, std::max(nsm, 1));
-    sur_serve_kernel<<<grid, 256, sizeof(SvSmem), st>>>(cases, ncases, ntiles, net, err);
+    sur_serve_kernel<<<grid, 32 * SV_WARPS, sizeof(SvSmem), st>>>(cases, ncases, ntiles, net, err);
     return cudaGetLastError();
 }
 
