@@ -111,6 +111,10 @@ class ClockSampler:
             )
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler delivers (bounded wait)
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
@@ -566,7 +570,7 @@ def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -712,8 +716,9 @@ def main():
 
     # --- single-footprint FP32 solves (bldfm_solve), for comparison ---
     s32 = make_solves("fp32")
-    ms32, stages32 = timed(s32, args.steps, args.warmup, stage_timing=True)
-    fps32 = world * B * args.steps / (ms32 * 1e-3)
+    steps32 = min(args.steps, 60)
+    ms32, stages32 = timed(s32, steps32, args.warmup, stage_timing=True)
+    fps32 = world * B * steps32 / (ms32 * 1e-3)
 
     # --- FP64 path (reference rounding) ---
     s64 = make_solves("fp64")
@@ -756,7 +761,7 @@ def main():
     from bldfm_gb300.batch import solve_stream
 
     esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
-    e2e_steps = max(2, args.steps)
+    e2e_steps = max(2, min(args.steps, 300))
     solve_batch(kwb[0], solver=esolver)
     t = time.perf_counter()
     for i in range(e2e_steps):

@@ -3,6 +3,7 @@
 // launch plus one launch per transform pass, optionally replayed as a CUDA
 // graph.  Replaces the reference's per-case Python loop and process pool
 // (src/bldfm/interface.py:141-326) for the solve itself.
+#include "devattr.h"
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -166,13 +167,8 @@ __global__ void __launch_bounds__(256) out_rows_batch_kernel(const BatchCase *__
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(riccati32_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(out_cols_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(out_rows_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
-    }
+    static uint64_t attr = 0;
+    if (first_on_device(attr)) prepare_batch_attributes();
     // part 0: the sweep; part 1: the two transform passes
     if (part == 0 && bl.sweep_ctas > 0)
         riccati32_batch_kernel<<<bl.sweep_ctas, bl.threads, bl.sweep_smem, st>>>(bl.cases, bl.tile_case,

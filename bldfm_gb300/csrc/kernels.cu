@@ -11,6 +11,7 @@
 // FP64 kernels reproduce the reference's numpy rounding: every operation is an
 // explicit round-to-nearest intrinsic (no contraction), and complex products use
 // numpy's x86-64 pattern re = fma(ar, br, -(ai*bi)), im = fma(ar, bi, ai*br).
+#include "devattr.h"
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -610,11 +611,9 @@ cudaError_t launch_sweep64(const SolveGeom &g, const double *lvtab, const int *s
 {
     const int L = g.nz - 1;
     const size_t smem = (size_t)L * BLDFM_LV64 * sizeof(double) + (size_t)g.nz * sizeof(int) + 16;
-    static bool attr = false;
-    if (!attr) {
+    static uint64_t attr = 0;
+    if (first_on_device(attr))
         cudaFuncSetAttribute(sweep64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
-    }
     const int threads = 128;
     int64_t blocks = (g.nsolved + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
@@ -668,13 +667,12 @@ cudaError_t launch_riccati32(const SolveGeom &g, const float *lv32, const int *s
 {
     const int L = g.nz - 1;
     const size_t smem = (size_t)L * BLDFM_LV32 * sizeof(float) + (size_t)g.nz * sizeof(int) + 16;
-    static bool attr = false;
-    if (!attr) {
+    static uint64_t attr = 0;
+    if (first_on_device(attr)) {
         cudaFuncSetAttribute(riccati32_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(riccati32_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(riccati32_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(riccati32_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
     }
     if (threads <= 0) threads = 256;
     int64_t blocks = (g.nsolved + threads - 1) / threads;
@@ -711,13 +709,12 @@ static int lines_per_cta(int n, size_t elem, size_t budget)
 template <typename R>
 static void set_fft_smem_attr()
 {
-    static bool done = false;
-    if (done) return;
+    static uint64_t done = 0;
+    if (!first_on_device(done)) return;
     cudaFuncSetAttribute(fwd_rows_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(fwd_cols_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(out_cols_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(out_rows_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    done = true;
 }
 
 template <typename R>

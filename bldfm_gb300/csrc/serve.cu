@@ -3,6 +3,7 @@
 // One thread per solved mode in each kernel; the spectra kernel writes the
 // same (Xp, Xq) slots and Hermitian mirrors as the sweep, so the output
 // transform is the solver's own.
+#include "devattr.h"
 #include "../../include/bldfm_gb300.h"
 #include "devmath.cuh"
 #include "mlp_common.cuh"
@@ -380,12 +381,14 @@ cudaError_t launch_sur_serve(const SurCase *cases, int ncases, int64_t ntiles, c
                              int nsm, cudaStream_t st)
 {
     if (ntiles <= 0 || ncases <= 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
+    static uint64_t attr = 0;
+    if (first_on_device(attr)) {
         cudaError_t e = cudaFuncSetAttribute(sur_serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)sizeof(SvSmem));
-        if (e != cudaSuccess) return e;
-        attr = true;
+        if (e != cudaSuccess) {
+            attr = 0;
+            return e;
+        }
     }
     const int grid = (int)std::min<int64_t>(ntiles, std::max(nsm, 1));
     sur_serve_kernel<<<grid, 32 * SV_WARPS, sizeof(SvSmem), st>>>(cases, ncases, ntiles, net, err);

@@ -1,5 +1,6 @@
 // Learned surrogate of the per-mode transfer function: a BF16 MLP whose hidden
 // 256 x 256 layers run on the tcgen05 tensor cores (tcgemm.cuh).
+#include "devattr.h"
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -477,11 +478,9 @@ cudaError_t gemm(const uint16_t *A, const uint16_t *Bop, int tiles, int K, int s
                  cudaStream_t st)
 {
     const size_t smem = tc_gemm_smem(256);
-    static bool attr = false;
-    if (!attr) {
+    static uint64_t attr = 0;
+    if (first_on_device(attr))
         cudaFuncSetAttribute(tc_gemm_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
     tc_gemm_kernel<Epi><<<dim3(tiles, splits), 128, smem, st>>>(A, Bop, K, 256, epi, err);
     return cudaGetLastError();
 }
