@@ -175,6 +175,8 @@ _SIGS = {
         ctypes.c_int,
         [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P],
     ),
+    "bldfm_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
+                                                    ctypes.POINTER(ctypes.c_int64)]),
     "bldfm_surrogate_plan": (ctypes.c_int, [ctypes.POINTER(Desc), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
     "bldfm_surrogate_batch_plan": (
         ctypes.c_int, [ctypes.POINTER(Case), ctypes.POINTER(SurrogateCase), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256, 2) riccati32_batch_kernel(const BatchCase
             for (int i = threadIdx.x; i < sc.g.nz; i += blockDim.x) s_slot[i] = sc.slot[i];
             if (bytes > 0) {
                 uint32_t done = 0;
-                for (long it = 0; it < (1L << 24); ++it) {
+                for (long it = 0; it < BLDFM_WAIT_POLLS; ++it) {
                     asm volatile(
                         "{\n\t.reg .pred p;\n\t"
                         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"

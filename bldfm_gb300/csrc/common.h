@@ -14,6 +14,11 @@ template <> struct cvec<float> { typedef float2 T; };
 #define BLDFM_MAX_NZ 2048       // level table must fit in shared memory
 #define BLDFM_LV64 12           // doubles per FP64 level-table row
 #define BLDFM_LV32 12           // floats per FP32 level-table row
+// Polls of an mbarrier wait before it gives up and reports a timeout.  A
+// failed poll suspends the thread for about 4 us on GB300 (measured by
+// bldfm_selftest_wait_timeout), so a wait that never completes ends after
+// about 1 s; every copy or MMA waited on completes in well under 1 ms.
+#define BLDFM_WAIT_POLLS (1L << 18)
 
 // Columns of the FP64 level table (same layout as the CPU oracle's).
 enum {

@@ -91,7 +91,7 @@ __device__ __noinline__ static bool bulk_load_to_smem(void *dst, const void *src
         }
     }
     uint32_t done = 0;
-    for (long it = 0; it < (1L << 24); ++it) {
+    for (long it = 0; it < BLDFM_WAIT_POLLS; ++it) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "../../include/bldfm_gb300.h"
+#include "tc.cuh"
 
 namespace {
 
@@ -71,9 +72,63 @@ __global__ void meas_final_kernel(const double *__restrict__ part, int nparts, i
     out[b] = __dadd_rn(k.s, -k.c);
 }
 
+// One CTA waits on an mbarrier that nothing arrives at, with an iteration
+// limit: the bounded-wait path every waiting kernel takes on a timeout.  The
+// elapsed global-timer nanoseconds of the wait go to ns[0].
+__global__ void wait_timeout_kernel(long limit, int *status, long long *ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc_mbar_init(&bar, 1);
+        tc_fence_init();
+    }
+    __syncthreads();
+    unsigned long long t0, t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    const uint32_t a = tc_smem(&bar);
+    uint32_t done = 0;
+    for (long it = 0; it < limit && !done; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(0u)
+            : "memory");
+    }
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    if (__syncthreads_or(!done) && threadIdx.x == 0) {
+        *status = BLDFM_ERR_TIMEOUT;
+        *ns = (long long)(t1 - t0);
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+// Self-check of the failure-detection path (no reference counterpart): a
+// kernel whose wait can never complete gives up after `limit` polls and
+// reports BLDFM_ERR_TIMEOUT in *status_host, with the time the wait took in
+// *wait_ns_host; the context stays usable.
+int bldfm_selftest_wait_timeout(int64_t limit, int32_t *status_host, int64_t *wait_ns_host)
+{
+    if (!status_host || !wait_ns_host || limit < 1 || limit > ((int64_t)1 << 20)) return BLDFM_ERR_ARG;
+    void *d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return BLDFM_ERR_CUDA;
+    int rc = BLDFM_OK;
+    if (cudaMemset(d, 0, 16) != cudaSuccess) rc = BLDFM_ERR_CUDA;
+    if (rc == BLDFM_OK) {
+        wait_timeout_kernel<<<1, 64>>>((long)limit, (int *)d, (long long *)((char *)d + 8));
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = BLDFM_ERR_CUDA;
+    }
+    long long h[2] = {0, 0};
+    if (rc == BLDFM_OK && cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost) != cudaSuccess) rc = BLDFM_ERR_CUDA;
+    *status_host = (int32_t)(int)h[0];
+    *wait_ns_host = (int64_t)h[1];
+    cudaFree(d);
+    return rc;
+}
 
 // Scratch bytes bldfm_point_measurement needs for nbatch entries of n points.
 int64_t bldfm_point_measurement_workspace(int64_t n, int32_t nbatch)

@@ -9,7 +9,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#define TC_WAIT_LIMIT (1L << 24)
+#include "common.h"
+
+#define TC_WAIT_LIMIT BLDFM_WAIT_POLLS
 
 // byte offset of element (r, k) of an R x KC K-major operand block
 __host__ __device__ __forceinline__ uint32_t tc_core_offset(int r, int k, int kc)

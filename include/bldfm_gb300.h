@@ -225,6 +225,14 @@ int bldfm_point_measurement(const double *f_dev, const double *g_dev,
                             double *out_dev, void *workspace_dev,
                             size_t workspace_bytes, void *stream);
 
+/* Self-check of the failure detection (no reference counterpart): every
+ * device wait of the library is bounded and reports BLDFM_ERR_TIMEOUT in the
+ * status word instead of hanging or trapping.  This runs one kernel whose
+ * mbarrier wait can never complete, polled `limit` times (1..2^20), and
+ * returns its status in *status_host (BLDFM_ERR_TIMEOUT expected) and the
+ * time the bounded wait took in *wait_ns_host. */
+int bldfm_selftest_wait_timeout(int64_t limit, int32_t *status_host, int64_t *wait_ns_host);
+
 /* Training data of the surrogate (no reference counterpart): a pool of
  * nondimensional MOST met cases (s1 = z_m / L, s2 = ln(z_m / z0)) on the
  * n-level stretched grid of vertical_profiles (src/bldfm/pbl_model.py:8-204,

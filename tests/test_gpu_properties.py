@@ -74,3 +74,25 @@ def test_repeated_solves_do_not_grow_memory():
     free1, _ = torch.cuda.mem_get_info()
     assert free0 - free1 < 64 << 20  # device: no per-call growth beyond allocator noise
     assert _rss_bytes() < 1.2 * rss0
+
+
+def test_bounded_wait_reports_timeout_and_context_survives():
+    """Failure detection without a fault: a wait that nothing completes gives
+    up after its poll limit and reports BLDFM_ERR_TIMEOUT; the next solve on
+    the same context works."""
+    import ctypes
+
+    from bldfm_gb300 import _lib, steady_state_transport_solver, vertical_profiles
+
+    z, p = vertical_profiles(16, 10.0, (0.0, -5.0), ustar=0.4)
+    kw = dict(srf_flx=np.zeros((64, 48)), z=z, profiles=p, domain=(480.0, 640.0), levels=16, modes=(48, 64),
+              meas_pt=(240.0, 320.0), footprint=True)
+    before = steady_state_transport_solver(**kw)[2]
+    lib = _lib.load()
+    st, ns = ctypes.c_int32(0), ctypes.c_int64(0)
+    assert lib.bldfm_selftest_wait_timeout(1 << 10, ctypes.byref(st), ctypes.byref(ns)) == 0
+    assert st.value == _lib.ERR_TIMEOUT
+    assert 0 < ns.value < 10**10
+    print(f"bounded wait: 1024 polls in {ns.value / 1e3:.1f} us")
+    after = steady_state_transport_solver(**kw)[2]
+    assert np.array_equal(before, after)
