@@ -1280,15 +1280,34 @@ int bldfm_stage_times(float *ms, int n)
     return std::min(nst, n);
 }
 
-int bldfm_fma_peak(int fp64, double *flops_per_s, void *stream)
+int bldfm_sweep32_flops(int32_t nz, const double *prof_host, const int64_t *levels_host, int32_t nlvls,
+                        double *flops_per_mode)
+{
+    if (nz < 2 || !prof_host || !levels_host || nlvls < 1 || !flops_per_mode) return BLDFM_ERR_ARG;
+    int64_t jmax = -1;
+    for (int k = 0; k < nlvls; ++k) {
+        if (levels_host[k] < 0 || levels_host[k] >= nz) return BLDFM_ERR_ARG;
+        jmax = std::max(jmax, levels_host[k]);
+    }
+    double ex, ey;
+    const bool iso = hx_profiles_iso(nz, prof_host, &ex, &ey) != 0;
+    // flops per step (FMA 2, MUL/ADD/RCP 1): step coefficients, ratio update,
+    // flux product (StepCoef::eval_row, ricc_step, flux_step)
+    const double coef = iso ? 14.0 : 21.0, ratio = 28.0, flux = 14.0;
+    const double L = nz - 1;
+    *flops_per_mode = (L - (double)jmax) * (coef + ratio) + (double)jmax * (coef + ratio + flux);
+    return BLDFM_OK;
+}
+
+int bldfm_fma_peak(int kind, double *flops_per_s, void *stream)
 {
     std::lock_guard<std::mutex> lk(g_mutex);
-    if (!flops_per_s) return BLDFM_ERR_ARG;
+    if (!flops_per_s || kind < 0 || kind > 2) return BLDFM_ERR_ARG;
     int status = BLDFM_OK;
     DeviceCache &dc = cache_for_current(&status);
     if (status != BLDFM_OK) return status;
     double v = 0;
-    if (run_fma_peak(fp64 != 0, dc.nsm, (cudaStream_t)stream, &v) != cudaSuccess) return BLDFM_ERR_CUDA;
+    if (run_fma_peak(kind, dc.nsm, (cudaStream_t)stream, &v) != cudaSuccess) return BLDFM_ERR_CUDA;
     *flops_per_s = v;
     return BLDFM_OK;
 }

@@ -41,7 +41,7 @@ __device__ __forceinline__ void load_case(BatchCase *dst, const BatchCase *src)
 // one case (two per thread, sharing the level-table loads).  The case's level
 // table is brought into shared memory by one bulk copy whenever the case
 // changes (the mbarrier flips phase each time; every wait is bounded).
-__global__ void __launch_bounds__(256, 2) riccati32_batch_kernel(const BatchCase *__restrict__ cases,
+__global__ void __launch_bounds__(256, 4) riccati32_batch_kernel(const BatchCase *__restrict__ cases,
                                                               const int *__restrict__ tile_case,
                                                               const int64_t *__restrict__ cta_tiles, int *err)
 {

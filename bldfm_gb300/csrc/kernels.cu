@@ -810,10 +810,28 @@ __global__ void __launch_bounds__(256) fma_peak_kernel(T *out, int iters, T b, T
     if (s == (T)-12345.678) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_s)
+// Packed FP32: eight independent f32x2 FMA chains per thread.
+__global__ void __launch_bounds__(256) fma2_peak_kernel(float *out, int iters, float b, float c)
 {
+    float2 a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = make_float2((float)(threadIdx.x + k) * 1e-3f, (float)(threadIdx.x + 2 * k) * 1e-3f);
+    const float2 b2 = make_float2(b, b), c2 = make_float2(c, c);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = __ffma2_rn(a[k], b2, c2);
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k].x + a[k].y;
+    if (s == -12345.678f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t run_fma_peak(int kind, int nsm, cudaStream_t st, double *flops_per_s)
+{
+    const bool fp64 = kind == 1;
     const int threads = 256, blocks = nsm * 8;
-    const int iters = fp64 ? 2048 : 65536;
+    const int iters = fp64 ? 2048 : (kind == 2 ? 32768 : 65536);
     void *out = nullptr;
     cudaError_t e = cudaMalloc(&out, (size_t)threads * blocks * 8);
     if (e != cudaSuccess) return e;
@@ -825,6 +843,8 @@ cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_
         cudaEventRecord(a, st);
         if (fp64)
             fma_peak_kernel<double><<<blocks, threads, 0, st>>>((double *)out, iters, 0.999999, 1e-7);
+        else if (kind == 2)
+            fma2_peak_kernel<<<blocks, threads, 0, st>>>((float *)out, iters, 0.999999f, 1e-7f);
         else
             fma_peak_kernel<float><<<blocks, threads, 0, st>>>((float *)out, iters, 0.999999f, 1e-7f);
         cudaEventRecord(b, st);
@@ -837,7 +857,7 @@ cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaFree(out);
-    *flops_per_s = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3);
+    *flops_per_s = 2.0 * 8.0 * (kind == 2 ? 2 : 1) * iters * (double)threads * blocks / (best * 1e-3);
     return e;
 }
 

@@ -36,7 +36,7 @@ cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftP
 cudaError_t launch_tw_to_float(const double2 *src, float2 *dst, int n, cudaStream_t st);
 cudaError_t launch_spec_to_float(const double2 *src, float2 *dst, int64_t n, cudaStream_t st);
 cudaError_t launch_nonfinite(const double *a, const double *b, int64_t n, int *flag, int nsm, cudaStream_t st);
-cudaError_t run_fma_peak(bool fp64, int nsm, cudaStream_t st, double *flops_per_s);
+cudaError_t run_fma_peak(int kind, int nsm, cudaStream_t st, double *flops_per_s);
 void prepare_kernel_attributes();
 cudaError_t launch_riccati64(const SolveGeom &g, const double *lvtab, const int *slot, const uint32_t *modes,
                              const double2 *q0spec, double *scratch, double2 *Xp, double2 *Xq, int *err, int nsm,

@@ -100,8 +100,8 @@ struct StepCoef<false> {
 // One backward step: R <- (a R - b) / (a - c R).
 __device__ __forceinline__ void ricc_step(float2 &R, const float2 a, const float2 b, const float2 c)
 {
-    const float cRr = fmaf(c.x, R.x, -c.y * R.y), cRi = fmaf(c.x, R.y, c.y * R.x);
-    const float Dr = a.x - cRr, Di = a.y - cRi;
+    // D = a - c R with the product folded into the subtraction
+    const float Dr = fmaf(-c.x, R.x, fmaf(c.y, R.y, a.x)), Di = fmaf(-c.x, R.y, fmaf(-c.y, R.x, a.y));
     const float Nr = fmaf(a.x, R.x, fmaf(-a.y, R.y, -b.x));
     const float Ni = fmaf(a.x, R.y, fmaf(a.y, R.x, -b.y));
     const float inv = rcp_approx(fmaf(Dr, Dr, Di * Di));
@@ -240,9 +240,103 @@ __device__ __forceinline__ void ricc_mode(const SolveGeom &g, const float *__res
     }
 }
 
+// ---------------------------------------------------------------------------
+// Packed form for two modes: lane x of every f32x2 value belongs to the first
+// mode, lane y to the second, and each f32x2 instruction (fma/mul/add .rn)
+// does both modes' operation in one issue slot.  Every operation is the one
+// of the scalar functions above with the same operands, so each lane rounds
+// exactly as the scalar recursion does.
+// ---------------------------------------------------------------------------
+struct PCplx {
+    float2 re, im;
+};
+
+__device__ __forceinline__ float2 pbc(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pneg(float2 a) { return make_float2(-a.x, -a.y); }
+
+template <bool ISO>
+struct PStep;
+
+template <>
+struct PStep<true> {
+    float2 k2, kw, k4, kw2, k2kw;
+    __device__ __forceinline__ void init(const StepCoef<true> &a, const StepCoef<true> &b)
+    {
+        k2 = make_float2(a.k2, b.k2);
+        kw = make_float2(a.kw, b.kw);
+        k4 = make_float2(a.k4, b.k4);
+        kw2 = make_float2(a.kw2, b.kw2);
+        k2kw = make_float2(a.k2kw, b.k2kw);
+    }
+    // StepCoef<true>::eval_row in both lanes
+    __device__ __forceinline__ void eval_row(const float4 r0, const float4 r1, const float4 r2, PCplx &a, PCplx &b,
+                                             PCplx &c) const
+    {
+        a.re = pfma(pbc(r0.x), k2, pbc(1.f));
+        a.im = pmul(pbc(r0.y), kw);
+        b.re = pfma(pbc(r0.w), k2, pbc(r0.z));
+        b.im = pmul(pbc(r1.x), kw);
+        c.re = pfma(pbc(r1.z), k4, pfma(pbc(r1.w), kw2, pmul(pbc(r1.y), k2)));
+        c.im = pfma(pbc(r2.y), k2kw, pmul(pbc(r2.x), kw));
+    }
+};
+
+template <>
+struct PStep<false> {
+    float2 lx, ly, lx2, ly2;
+    __device__ __forceinline__ void init(const StepCoef<false> &a, const StepCoef<false> &b)
+    {
+        lx = make_float2(a.lx, b.lx);
+        ly = make_float2(a.ly, b.ly);
+        lx2 = make_float2(a.lx2, b.lx2);
+        ly2 = make_float2(a.ly2, b.ly2);
+    }
+    // StepCoef<false>::eval_row in both lanes
+    __device__ __forceinline__ void eval_row(const float4 r0, const float4 r1, const float4 r2, PCplx &a, PCplx &b,
+                                             PCplx &c) const
+    {
+        const float2 Tr = pfma(pbc(r0.x), lx2, pmul(pbc(r0.y), ly2));
+        const float2 Ti = pfma(pbc(r0.z), lx, pmul(pbc(r0.w), ly));
+        a.re = pfma(pbc(-r1.x), Tr, pbc(1.f));
+        a.im = pmul(pbc(-r1.x), Ti);
+        b.re = pfma(pbc(-r1.z), Tr, pbc(r1.y));
+        b.im = pmul(pbc(-r1.z), Ti);
+        const float2 t2r = pfma(Tr, Tr, pneg(pmul(Ti, Ti)));
+        c.re = pfma(pbc(-r2.x), t2r, pmul(pbc(r1.w), Tr));
+        c.im = pmul(Ti, pfma(pbc(r2.y), Tr, pbc(r1.w)));
+    }
+};
+
+// ricc_step in both lanes
+__device__ __forceinline__ void pricc_step(PCplx &R, const PCplx a, const PCplx b, const PCplx c)
+{
+    const float2 Dr = pfma(pneg(c.re), R.re, pfma(c.im, R.im, a.re));
+    const float2 Di = pfma(pneg(c.re), R.im, pfma(pneg(c.im), R.re, a.im));
+    const float2 Nr = pfma(a.re, R.re, pfma(pneg(a.im), R.im, pneg(b.re)));
+    const float2 Ni = pfma(a.re, R.im, pfma(a.im, R.re, pneg(b.im)));
+    const float2 den = pfma(Dr, Dr, pmul(Di, Di));
+    const float2 inv = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+    R.re = pmul(pfma(Nr, Dr, pmul(Ni, Di)), inv);
+    R.im = pmul(pfma(Ni, Dr, pneg(pmul(Nr, Di))), inv);
+}
+
+// flux_step in both lanes
+__device__ __forceinline__ void pflux_step(PCplx &Q, const PCplx R, const PCplx a, const PCplx c)
+{
+    const float2 fr = pfma(c.re, R.re, pfma(pneg(c.im), R.im, a.re));
+    const float2 fi = pfma(c.re, R.im, pfma(c.im, R.re, a.im));
+    const float2 qr = pfma(Q.re, fr, pneg(pmul(Q.im, fi)));
+    Q.im = pfma(Q.re, fi, pmul(Q.im, fr));
+    Q.re = qr;
+}
+
 // Two solved modes per thread with one output level (SINGLE): the same
 // arithmetic per mode as ricc_mode<ISO, true>, with the level-table row and
-// the loop control shared by the two interleaved recursions.  mb < 0: the
+// the loop control shared by the two recursions, which run in the two lanes
+// of the packed f32x2 operations.  mb < 0: the
 // second slot repeats ma and writes nothing.
 template <bool ISO>
 __device__ __forceinline__ void ricc_mode_pair(const SolveGeom &g, const float *__restrict__ s_lv,
@@ -271,37 +365,39 @@ __device__ __forceinline__ void ricc_mode_pair(const SolveGeom &g, const float *
         const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
         R[u] = make_float2(ke.x * inv, -ke.y * inv);
     }
+    // the two recursions run in the two lanes of packed f32x2 operations
+    PStep<ISO> ps;
+    ps.init(sc[0], sc[1]);
+    PCplx PR = {make_float2(R[0].x, R[1].x), make_float2(R[0].y, R[1].y)};
     int i = L - 1;
     for (; i >= jmax; --i) {
         const float *lv = s_lv + (size_t)i * BLDFM_LV32;
         const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            float2 a, b, cc;
-            sc[u].eval_row(r0, r1, r2, a, b, cc);
-            ricc_step(R[u], a, b, cc);
-        }
+        PCplx a, b, cc;
+        ps.eval_row(r0, r1, r2, a, b, cc);
+        pricc_step(PR, a, b, cc);
     }
-    float2 Rj[2] = {R[0], R[1]};
-    float2 Q[2] = {make_float2(1.f, 0.f), make_float2(1.f, 0.f)};
+    float2 Rj[2] = {make_float2(PR.re.x, PR.im.x), make_float2(PR.re.y, PR.im.y)};
+    PCplx PQ = {make_float2(1.f, 1.f), make_float2(0.f, 0.f)};
     int E[2] = {0, 0};
     int cnt = 0;
     for (; i >= 0; --i) {
         const float *lv = s_lv + (size_t)i * BLDFM_LV32;
         const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            float2 a, b, cc;
-            sc[u].eval_row(r0, r1, r2, a, b, cc);
-            ricc_step(R[u], a, b, cc);
-            flux_step(Q[u], R[u], a, cc);
-        }
+        PCplx a, b, cc;
+        ps.eval_row(r0, r1, r2, a, b, cc);
+        pricc_step(PR, a, b, cc);
+        pflux_step(PQ, PR, a, cc);
         if (++cnt == 8) {
             cnt = 0;
-            renorm(Q[0], E[0]);
-            renorm(Q[1], E[1]);
+            float2 q0 = make_float2(PQ.re.x, PQ.im.x), q1 = make_float2(PQ.re.y, PQ.im.y);
+            renorm(q0, E[0]);
+            renorm(q1, E[1]);
+            PQ.re = make_float2(q0.x, q1.x);
+            PQ.im = make_float2(q0.y, q1.y);
         }
     }
+    const float2 Q[2] = {make_float2(PQ.re.x, PQ.im.x), make_float2(PQ.re.y, PQ.im.y)};
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
         if (u == 1 && mb < 0) break;

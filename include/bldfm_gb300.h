@@ -140,10 +140,19 @@ int bldfm_vertical_profiles(int32_t n, double meas_height, double um, double vm,
 int bldfm_set_stage_timing(int enable);
 int bldfm_stage_times(float *ms, int n);
 
-/* Measured FMA throughput of this GPU (flops/s, an FMA counted as 2), FP32 or
- * FP64: the pipe peak the sweep kernels are held against (no reference
- * counterpart). */
-int bldfm_fma_peak(int fp64, double *flops_per_s, void *stream);
+/* Algorithmic flops of the FP32 Riccati sweep for one solved mode (an FMA
+ * counted as 2, MUL/ADD/RCP as 1) on the nz-level table of prof_host with
+ * output levels levels_host: the steps above the highest output level update
+ * only the ratio, the ones below also the flux product; isotropic profiles
+ * (Kx == Ky, one wind direction) take the cheaper coefficient form.  The
+ * numerator of the sweep roofline (no reference counterpart). */
+int bldfm_sweep32_flops(int32_t nz, const double *prof_host, const int64_t *levels_host, int32_t nlvls,
+                        double *flops_per_mode);
+
+/* Measured FMA throughput of this GPU (flops/s, an FMA counted as 2): kind 0
+ * scalar FP32, 1 FP64, 2 packed FP32 (f32x2 FMA, two per instruction).  The
+ * pipe peak the sweep kernels are held against (no reference counterpart). */
+int bldfm_fma_peak(int kind, double *flops_per_s, void *stream);
 
 /* ---- batches ------------------------------------------------------------
  * Many cases (towers x timesteps), each with its own grid, modes, levels and
