@@ -43,6 +43,25 @@ __device__ __forceinline__ float gelu_f(float z)
     const float hz = 0.5f * z;
     return fmaf(hz, tanh_approx(u), hz);
 }
+// gelu_f(v + b) for two values in the lanes of packed f32x2 operations (the
+// same operations and rounding as the scalar form, lane by lane)
+__device__ __forceinline__ float2 gelu2_bias(float2 v, float2 b)
+{
+    const float2 z = __fadd2_rn(v, b);
+    const float2 p = __ffma2_rn(make_float2(GELU_C * GELU_A, GELU_C * GELU_A), __fmul2_rn(z, z),
+                                make_float2(GELU_C, GELU_C));
+    const float2 u = __fmul2_rn(z, p);
+    const float2 hz = __fmul2_rn(make_float2(0.5f, 0.5f), z);
+    return __ffma2_rn(hz, make_float2(tanh_approx(u.x), tanh_approx(u.y)), hz);
+}
+
+// two floats -> BF16x2 (round to nearest even; first value in the low half)
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
 __device__ __forceinline__ float gelu_d(float z)
 {
     const float z2 = z * z;
@@ -54,6 +73,7 @@ __device__ __forceinline__ float gelu_d(float z)
 // parameters and the BF16 core-matrix blocks of Wt_1..3 (256 x 256 each)
 struct MlpServing {
     const float *P;
-    const uint16_t *Wt[3];
+    const uint16_t *Wt[3];  // 256 x 256 core-matrix blocks
+    const uint16_t *Wq[3];  // the same as four contiguous 128 x 128 quarters (N half, K half)
 };
 int mlp_serving_view(void *handle, MlpServing *out);

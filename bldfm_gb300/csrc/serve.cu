@@ -104,74 +104,207 @@ __global__ void sur_spectra_kernel(const SolveGeom g, const uint32_t *__restrict
 
 // ---------------------------------------------------------------------------
 // Fused serving kernel: features -> MLP -> spectra for 128 modes per tile,
-// one persistent CTA of 256 threads per SM.  All four matrix layers run on
-// the tensor cores (tcgen05.mma, M = 128, N = 256, FP32 accumulator in a
-// 256-column TMEM allocation); the epilogues (bias + GELU, from TMEM) and the
-// 256 -> 4 output layer run on the CUDA cores in FP32.
+// one persistent CTA of 512 threads per SM.  All four matrix layers run on
+// the tensor cores (tcgen05.mma, M = 128, FP32 accumulators in TMEM); the
+// epilogues (bias + GELU) and the 256 -> 4 output layer run on the CUDA cores
+// in FP32.
 //
 // Input layer in BF16 at FP32 accuracy: x = xh + xl and W0 = wh + wl split
 // into BF16 parts, K = 32 columns [xh | xl | xh | 0] x [wh | wh | wl | 0]
 // give x.W0 up to the xl.wl term (relative 2^-16).
 //
-// Shared memory: the tile's activations (BF16, core-matrix K-major layout: the
-// A operand of the next layer; the first 8 KB hold the input-layer operand
-// before its MMA), one 256 x 256 BF16 weight matrix streamed by bulk copy
-// while the previous layer's epilogue runs, the split W0, biases, W4.  Every
+// Overlap of tensor cores and epilogues: every layer's 256 outputs are two
+// N = 128 halves with their own accumulator (TMEM columns 0 and 128) and
+// their own completion barrier.  The epilogue of half 0 writes the low K half
+// of the next layer's activations (BF16 pairs, in TMEM: the A operand of the
+// next MMAs) while the tensor cores finish half 1; the next layer's first
+// quarter MMA (half 0, low K) then runs during the epilogue of half 1.  The
+// activations rotate through three K-half TMEM buffers so that no buffer is
+// rewritten while an MMA reads it.  The hidden weights stream through shared
+// memory as four 32 KB quarters (N half x K half); a quarter is reloaded with
+// the next layer's as soon as the MMAs reading it have completed.  Every
 // mbarrier wait is bounded; on a timeout the kernel records
 // BLDFM_ERR_TIMEOUT, waits (bounded) for its own copies and MMAs in flight,
 // frees TMEM and returns.
 // ---------------------------------------------------------------------------
 #define SV_K0 32     // K of the split input layer
-#define SV_WARPS 16  // 4 warps per TMEM lane quarter, each a quarter of the 256 columns
+#define SV_WARPS 16  // epilogue warps: 4 per TMEM lane quarter, each 32 columns of a half
+#define SV_THREADS (32 * SV_WARPS + 32)  // + one control warp (copies and MMAs)
+#define SV_AB(i) (256u + 64u * (uint32_t)(i))  // TMEM column of activation K-half buffer i
 
 struct SvSmem {
-    uint16_t A[128 * MLP_H];    // activations (A operand)
-    uint16_t W[MLP_H * MLP_H];  // Wt_j (B operand)
-    uint16_t B0[MLP_H * SV_K0]; // split W0 (B operand of the input layer)
+    uint16_t Wq[4][128 * 128];   // Wt_j quarters (N half, K half), B operands
+    uint16_t A0[128 * SV_K0];    // input-layer A operand (split features)
+    uint16_t B0[MLP_H * SV_K0];  // split W0 (B operand of the input layer)
     float bias[4][MLP_H];
     float W4[MLP_H * MLP_OUT];
-    float4 Yp[SV_WARPS / 4][128];  // output-layer partial sums of the column quarters
+    float4 Yp[SV_WARPS / 4][128];  // output-layer partial sums of the column groups
     float b4[4];
 };
 
-__device__ __forceinline__ void sv_put8(uint16_t *st, int r, int c, const float *v)
+// Quarter q = 2 nh + kh of Wt_j (Wq_j: four contiguous 32 KB quarters in the
+// layout of a 128 x 128 operand) into shared memory: one bulk copy.
+__device__ __forceinline__ void sv_load_quarter(uint16_t *dst, const uint16_t *Wq, int q, uint64_t *bar)
 {
-    uint32_t w[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) w[q] = (uint32_t)f2bf(v[2 * q]) | ((uint32_t)f2bf(v[2 * q + 1]) << 16);
-    *(uint4 *)(st + tc_core_offset(r, c, MLP_H) / 2) = make_uint4(w[0], w[1], w[2], w[3]);
+    const uint32_t bytes = 128 * 128 * 2;
+    tc_expect_tx(bar, bytes);
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     tc_smem(dst)),
+                 "l"((const char *)Wq + (size_t)q * bytes), "r"(bytes), "r"(tc_smem(bar))
+                 : "memory");
 }
 
-// epilogue of a hidden layer: this thread's row, 64 columns from c0, bias,
-// GELU, BF16 into the A tile
-__device__ __forceinline__ void sv_epilogue_hidden(uint32_t tb, int row, int c0, const float *bias, uint16_t *A)
+// D[dcol .. +127] (+)= A[TMEM acol .. +63] (K = 128) x quarter^T: 8 MMAs of
+// K = 16; bdesc is the quarter's descriptor (each K step advances the start
+// address by 256 bytes, 16 in the descriptor's address field)
+__device__ __forceinline__ void sv_mma_quarter(uint32_t dt, uint32_t at, uint64_t bdesc, uint32_t idesc,
+                                               bool accumulate)
 {
-#pragma unroll 1
-    for (int cc = 0; cc < 2; ++cc) {
-        float v[32];
-        tc_ld32(tb + 32 * cc, v);
-        const int cb = c0 + 32 * cc;
+    tc_mma_ts(dt, at, bdesc, idesc, accumulate ? 1u : 0u);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = gelu_f(v[i] + bias[cb + i]);
+    for (int s = 1; s < 8; ++s) tc_mma_ts(dt, at + 8 * s, bdesc + (uint64_t)(16 * s), idesc, 1u);
+}
+
+// Bounded wait for phase `parity` of an mbarrier that also gives up as soon
+// as another warp has recorded a failure in *fail.
+__device__ __forceinline__ bool sv_wait(uint64_t *bar, uint32_t parity, const volatile int *fail)
+{
+    const uint32_t a = tc_smem(bar);
+    for (long it = 0; it < BLDFM_WAIT_POLLS; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 63) == 63 && *fail) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void sv_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(tc_smem(bar)) : "memory");
+}
+
+// barrier of the epilogue warps only (the control warp does not take part)
+__device__ __forceinline__ void sv_epi_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * SV_WARPS) : "memory"); }
+// barrier of the feature / emit warps 0..3
+__device__ __forceinline__ void sv_row_sync() { asm volatile("bar.sync 2, 128;" ::: "memory"); }
+
+// features of row r of a tile -> [xh | xl | xh | 0] (input-layer A operand, K = 32)
+__device__ __forceinline__ void sv_features(const SurCase &c, int64_t tile, int r, uint16_t *A0)
+{
+    const int64_t m = (tile - c.tile0) * 128 + r;
+    float kpar = 1.f, kperp = 0.f;
+    if (m < c.g.nsolved) {
+        int rr, cc;
+        bool pr;
+        float k;
+        mode_k(c.g, c.modes[m], c.ax, c.ay, c.zm, rr, cc, pr, kpar, kperp, k);
+        kpar = fabsf(kpar);
+    }
+    float x[8], xl[8];
+    feature_row(x, kpar, kperp, c.s1, c.s2, c.s3);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) sv_put8(A, row, cb + 8 * q, v + 8 * q);
+    for (int i = 0; i < 8; ++i) xl[i] = x[i] - bf2f(f2bf(x[i]));
+    const uint4 hi = make_uint4(pack_bf16x2(x[0], x[1]), pack_bf16x2(x[2], x[3]), pack_bf16x2(x[4], x[5]),
+                                pack_bf16x2(x[6], x[7]));
+    const uint4 lo = make_uint4(pack_bf16x2(xl[0], xl[1]), pack_bf16x2(xl[2], xl[3]), pack_bf16x2(xl[4], xl[5]),
+                                pack_bf16x2(xl[6], xl[7]));
+    *(uint4 *)(A0 + tc_core_offset(r, 0, SV_K0) / 2) = hi;
+    *(uint4 *)(A0 + tc_core_offset(r, 8, SV_K0) / 2) = lo;
+    *(uint4 *)(A0 + tc_core_offset(r, 16, SV_K0) / 2) = hi;
+    *(uint4 *)(A0 + tc_core_offset(r, 24, SV_K0) / 2) = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// hidden-layer epilogue of 32 accumulator columns of this thread's row:
+// bias, GELU in f32x2 lanes, BF16 pairs into 16 activation columns
+__device__ __forceinline__ void sv_epilogue_hidden(uint32_t td, uint32_t ta, const float *bias)
+{
+    float v[32];
+    tc_ld32(td, v);
+    uint32_t w[16];
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+        const float2 g = gelu2_bias(make_float2(v[2 * p], v[2 * p + 1]), *(const float2 *)&bias[2 * p]);
+        w[p] = pack_bf16x2(g.x, g.y);
+    }
+    tc_st16(ta, w);
+}
+
+// last hidden layer's epilogue of 32 columns, folded into the 256 -> 4 output
+// layer: y += gelu(v + b) . W4 rows
+__device__ __forceinline__ void sv_epilogue_out(uint32_t td, const float *bias, const float *W4, float2 &y01,
+                                                float2 &y23)
+{
+    float v[32];
+    tc_ld32(td, v);
+#pragma unroll
+    for (int i = 0; i < 32; i += 2) {
+        const float2 h = gelu2_bias(make_float2(v[i], v[i + 1]), *(const float2 *)&bias[i]);
+        const float4 wa = *(const float4 *)&W4[i * MLP_OUT];
+        const float4 wb = *(const float4 *)&W4[(i + 1) * MLP_OUT];
+        y01 = __ffma2_rn(make_float2(h.x, h.x), make_float2(wa.x, wa.y), y01);
+        y23 = __ffma2_rn(make_float2(h.x, h.x), make_float2(wa.z, wa.w), y23);
+        y01 = __ffma2_rn(make_float2(h.y, h.y), make_float2(wb.x, wb.y), y01);
+        y23 = __ffma2_rn(make_float2(h.y, h.y), make_float2(wb.z, wb.w), y23);
     }
 }
 
-__global__ void __launch_bounds__(32 * SV_WARPS, 1)
+// Fused serving kernel: features -> MLP -> spectra for 128 modes per tile,
+// one persistent CTA per SM: 16 epilogue warps and one control warp.
+//
+// All four matrix layers run on the tensor cores (tcgen05.mma, M = 128, FP32
+// accumulators in TMEM); the epilogues (bias + GELU) and the 256 -> 4 output
+// layer run on the CUDA cores in FP32.  Input layer in BF16 at FP32 accuracy:
+// x = xh + xl and W0 = wh + wl split into BF16 parts, K = 32 columns
+// [xh | xl | xh | 0] x [wh | wh | wl | 0] give x.W0 up to the xl.wl term
+// (relative 2^-16).
+//
+// Overlap of tensor cores and epilogues: every layer's 256 outputs are two
+// N = 128 halves with their own accumulator (TMEM columns 0 and 128) and
+// completion barrier.  The epilogue of half 0 writes the low K half of the
+// next layer's activations (BF16 pairs in TMEM: the A operand of the next
+// MMAs) while the tensor cores finish half 1; the next layer's first quarter
+// MMA (half 0, low K) then runs during the epilogue of half 1.  Activations
+// rotate through three K-half TMEM buffers so that no buffer is rewritten
+// while an MMA reads it.  The hidden weights stream through shared memory as
+// four 32 KB quarters (N half x K half), each reloaded with the next layer's
+// as soon as the MMAs reading it have completed.  The control warp issues
+// every copy and MMA and hands work to the epilogue warps through mbarriers
+// only, so a blocked MMA issue never holds an epilogue back.  Every wait is
+// bounded; on a timeout the kernel records BLDFM_ERR_TIMEOUT, all warps leave
+// their loops, the control warp waits (bounded) for its copies and MMAs in
+// flight, and TMEM is freed.
+__global__ void __launch_bounds__(SV_THREADS, 1)
     sur_serve_kernel(const SurCase *__restrict__ cases, int ncases, int64_t ntiles, const MlpServing net, int *err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SvSmem &S = *reinterpret_cast<SvSmem *>(smem_raw);
-    __shared__ uint64_t bar_w, bar_mma;
+    // bar_m[h]: MMAs of accumulator half h done; bar_e[h]: epilogue of half h
+    // done (16 warp arrivals); bar_f: input operand written (128 thread
+    // arrivals); bar_q[q]: weight quarter q loaded
+    __shared__ uint64_t bar_m[2], bar_e[2], bar_f, bar_q[4];
     __shared__ uint32_t tmem_slot;
-    __shared__ SurCase sc;  // the current tile's case
+    __shared__ int s_fail;
+    __shared__ SurCase sc[2];         // cases of the current and the next tile (warps 0..3)
+    __shared__ int64_t s_case_t1[2];  // first tile after each
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (warp == 0) tc_tmem_alloc(&tmem_slot, 256);
+    const volatile int *fail = &s_fail;
+    if (warp == 0) tc_tmem_alloc(&tmem_slot, 512);
     if (tid == 0) {
-        tc_mbar_init(&bar_w, 1);
-        tc_mbar_init(&bar_mma, 1);
+        for (int i = 0; i < 2; ++i) {
+            tc_mbar_init(&bar_m[i], 1);
+            tc_mbar_init(&bar_e[i], SV_WARPS);
+        }
+        tc_mbar_init(&bar_f, 128);
+        for (int i = 0; i < 4; ++i) tc_mbar_init(&bar_q[i], 1);
         tc_fence_init();
+        s_fail = 0;
     }
     // split W0 [in][out] into the B operand [out][K = 32]
     for (int e = tid; e < MLP_H * SV_K0; e += blockDim.x) {
@@ -193,168 +326,198 @@ __global__ void __launch_bounds__(32 * SV_WARPS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t WBYTES = MLP_H * MLP_H * 2;
-    const uint32_t idesc = tc_idesc_bf16(128, MLP_H);
-    const uint32_t sbo = (MLP_H / 8) * 128, sbo0 = (SV_K0 / 8) * 128;
-    uint32_t wph = 0, mph = 0;
-    bool pend_w = false, pend_mma = false;  // thread 0: copies / MMAs not yet waited for
-    if (tid == 0 && (int64_t)blockIdx.x < ntiles) {
-        tc_expect_tx(&bar_w, WBYTES);
-        tc_bulk_load(S.W, net.Wt[0], WBYTES, &bar_w);
-        pend_w = true;
-    }
-    // epilogue geometry: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows), columns 64 (w / 4) .. +63
-    const int qd = warp & 3, hf = warp >> 2;
-    const int row = 32 * qd + lane;
-    const uint32_t tb = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(64 * hf);
-    bool failed = false;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (tid < 32) {
-            // the tile's case: last case with tile0 <= tile, copied to shared memory
-            int lo = 0, hi = ncases - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (cases[mid].tile0 <= tile) lo = mid;
-                else hi = mid - 1;
-            }
-            const uint32_t *src = (const uint32_t *)(cases + lo);
-            uint32_t *dst = (uint32_t *)&sc;
-            for (int i = tid; i < (int)(sizeof(SurCase) / 4); i += 32) dst[i] = src[i];
-        }
-        __syncthreads();
-        const SolveGeom &g = sc.g;
-        const int64_t lt = tile - sc.tile0;  // tile within the case
-        if (tid < 128) {
-            // features -> [xh | xl | xh | 0] of row tid (input-layer A operand, K = 32)
-            const int64_t m = lt * 128 + tid;
-            float kpar = 1.f, kperp = 0.f;
-            if (m < g.nsolved) {
-                int r, c;
-                bool pr;
-                float k;
-                mode_k(g, sc.modes[m], sc.ax, sc.ay, sc.zm, r, c, pr, kpar, kperp, k);
-                kpar = fabsf(kpar);
-            }
-            float x[8], xl[8];
-            feature_row(x, kpar, kperp, sc.s1, sc.s2, sc.s3);
+    // activation K-half buffers of layers 1..3: (lo, hi) = (0, 1), (2, 0), (1, 2)
+    auto buf_lo = [](int j) { return j == 0 ? 0 : (j == 1 ? 2 : 1); };
+    auto buf_hi = [](int j) { return j == 0 ? 1 : (j == 1 ? 0 : 2); };
+
+    if (warp == SV_WARPS) {
+        // ---------------- control warp: copies and MMAs (lane 0) ----------------
+        if (lane == 0) {
+            const uint32_t idesc = tc_idesc_bf16(128, 128);
+            uint64_t bq[4];  // descriptors of the weight quarters
+            for (int q = 0; q < 4; ++q) bq[q] = tc_desc(tc_smem(S.Wq[q]), 128, 2048);
+            const uint64_t da0 = tc_desc(tc_smem(S.A0), 128, 512), db0 = tc_desc(tc_smem(S.B0), 128, 512);
+            uint32_t ph_m[2] = {0u, 0u}, ph_e[2] = {0u, 0u}, ph_f = 0u, ph_q[4] = {0u, 0u, 0u, 0u};
+            bool pend_m[2] = {false, false}, pend_q[4] = {false, false, false, false};
+            bool ok = true;
+            if ((int64_t)blockIdx.x < ntiles)
 #pragma unroll
-            for (int i = 0; i < 8; ++i) xl[i] = x[i] - bf2f(f2bf(x[i]));
-            uint16_t *A0 = S.A;
-            uint32_t w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) w[q] = (uint32_t)f2bf(x[2 * q]) | ((uint32_t)f2bf(x[2 * q + 1]) << 16);
-            const uint4 hi = make_uint4(w[0], w[1], w[2], w[3]);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) w[q] = (uint32_t)f2bf(xl[2 * q]) | ((uint32_t)f2bf(xl[2 * q + 1]) << 16);
-            const uint4 lo = make_uint4(w[0], w[1], w[2], w[3]);
-            *(uint4 *)(A0 + tc_core_offset(tid, 0, SV_K0) / 2) = hi;
-            *(uint4 *)(A0 + tc_core_offset(tid, 8, SV_K0) / 2) = lo;
-            *(uint4 *)(A0 + tc_core_offset(tid, 16, SV_K0) / 2) = hi;
-            *(uint4 *)(A0 + tc_core_offset(tid, 24, SV_K0) / 2) = make_uint4(0u, 0u, 0u, 0u);
-        }
-        tc_fence_proxy_async();
-        __syncthreads();
-        // layers 0..3: input layer (split W0 in S.B0), then Wt_1..3 streamed through S.W
-        for (int j = 0; j < 4; ++j) {
-            bool bad = false;
-            if (j > 0) {
-                bad = !tc_mbar_wait(&bar_w, wph);
-                if (__syncthreads_or(bad)) {
-                    failed = true;
-                    break;
+                for (int q = 0; q < 4; ++q) {
+                    sv_load_quarter(S.Wq[q], net.Wq[0], q, &bar_q[q]);
+                    pend_q[q] = true;
                 }
-                wph ^= 1;
-            }
-            if (tid == 0) {
-                if (j > 0) pend_w = false;
+            for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                // input layer, both halves (B0 rows 128 h .. +127 start 8 KB
+                // apart); the previous tile's last epilogue has released both
+                // accumulator halves (its bar_e phases were waited below)
+                ok = sv_wait(&bar_f, ph_f, fail);
+                if (!ok) break;
+                ph_f ^= 1u;
                 tc_fence_after();
-                const uint32_t a0 = tc_smem(S.A);
-                if (j == 0) {
-                    const uint32_t b0 = tc_smem(S.B0);
-#pragma unroll 1
-                    for (int s = 0; s < SV_K0 / 16; ++s)
-                        tc_mma(tmem, tc_desc(a0 + s * 256, 128, sbo0), tc_desc(b0 + s * 256, 128, sbo0), idesc,
-                               s > 0 ? 1u : 0u);
-                } else {
-                    const uint32_t b0 = tc_smem(S.W);
-#pragma unroll 1
-                    for (int s = 0; s < MLP_H / 16; ++s)
-                        tc_mma(tmem, tc_desc(a0 + s * 256, 128, sbo), tc_desc(b0 + s * 256, 128, sbo), idesc,
-                               s > 0 ? 1u : 0u);
+                for (int h = 0; h < 2; ++h) {
+                    tc_mma(tmem + 128u * h, da0, db0 + (uint64_t)(512 * h), idesc, 0u);
+                    tc_mma(tmem + 128u * h, da0 + 16u, db0 + (uint64_t)(512 * h + 16), idesc, 1u);
+                    tc_commit(&bar_m[h]);
+                    pend_m[h] = true;
                 }
-                tc_commit(&bar_mma);
-                pend_mma = true;
+                for (int j = 0; j < 4 && ok; ++j) {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        if (!ok) break;
+                        // layer j's half h is complete: the quarters of Wt_j in N
+                        // half h are free for the next layer's (after the last
+                        // layer, the next tile's first)
+                        ok = sv_wait(&bar_m[h], ph_m[h], fail);
+                        if (!ok) break;
+                        ph_m[h] ^= 1u;
+                        pend_m[h] = false;
+                        if (j >= 1) {
+                            const uint16_t *next =
+                                j < 3 ? net.Wq[j] : (tile + gridDim.x < ntiles ? net.Wq[0] : nullptr);
+                            if (next)
+#pragma unroll
+                                for (int q = 2 * h; q < 2 * h + 2; ++q) {
+                                    sv_load_quarter(S.Wq[q], next, q, &bar_q[q]);
+                                    pend_q[q] = true;
+                                }
+                        }
+                        // the epilogue of half h has read the accumulator (and
+                        // written the activations it feeds)
+                        ok = sv_wait(&bar_e[h], ph_e[h], fail);
+                        if (!ok) break;
+                        ph_e[h] ^= 1u;
+                        if (j == 3) continue;
+                        tc_fence_after();
+                        const uint32_t alo = tmem + SV_AB(buf_lo(j)), ahi = tmem + SV_AB(buf_hi(j));
+#pragma unroll
+                        for (int q = h == 0 ? 0 : 1; q < (h == 0 ? 1 : 4); ++q) {
+                            if (!ok) break;
+                            ok = sv_wait(&bar_q[q], ph_q[q], fail);
+                            if (!ok) break;
+                            ph_q[q] ^= 1u;
+                            pend_q[q] = false;
+                            sv_mma_quarter(tmem + 128u * (q >> 1), (q & 1) ? ahi : alo, bq[q], idesc, (q & 1) != 0);
+                            if (q & 1) {
+                                tc_commit(&bar_m[q >> 1]);
+                                pend_m[q >> 1] = true;
+                            }
+                        }
+                    }
+                }
             }
-            bad = !tc_mbar_wait(&bar_mma, mph);
-            if (__syncthreads_or(bad)) {
-                failed = true;
+            if (!ok) {
+                s_fail = 1;
+                atomicExch(err, BLDFM_ERR_TIMEOUT);
+                const int never = 0;  // drain without the early exit on s_fail
+                for (int h = 0; h < 2; ++h)
+                    if (pend_m[h] && sv_wait(&bar_m[h], ph_m[h], &never)) ph_m[h] ^= 1u;
+                // MMAs issued after the last commit: one more commit tracks them all
+                tc_commit(&bar_m[0]);
+                sv_wait(&bar_m[0], ph_m[0], &never);
+                for (int q = 0; q < 4; ++q)
+                    if (pend_q[q]) sv_wait(&bar_q[q], ph_q[q], &never);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue warps ----------------
+        // warp w owns TMEM lanes 32 (w % 4) .. +31 (its rows) and columns
+        // 32 (w / 4) .. +31 of each accumulator half.  Warps 0..3 (one thread
+        // per row) also compute the features of the next tile (as soon as the
+        // input layer of the current one has read its operand) and write the
+        // spectra; the tile's case sits in one of two shared slots, so that a
+        // new case can be loaded while the previous one is still read.
+        const int qd = warp & 3, cg = warp >> 2;
+        const int row = 32 * qd + lane;
+        const uint32_t lane_off = (uint32_t)(32 * qd) << 16;
+        uint32_t ph_m[2] = {0u, 0u};
+        int slot = 0;
+        bool ok = true;
+        // the case of `tile` into slot `to` unless slot `from` already holds it
+        auto locate = [&](int64_t tile, int from, int to) -> int {
+            if (from >= 0 && tile >= sc[from].tile0 && tile < s_case_t1[from]) return from;
+            if (warp == 0) {
+                int lo = 0, hi = ncases - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (cases[mid].tile0 <= tile) lo = mid;
+                    else hi = mid - 1;
+                }
+                const uint32_t *src = (const uint32_t *)(cases + lo);
+                uint32_t *dst = (uint32_t *)&sc[to];
+                for (int i = lane; i < (int)(sizeof(SurCase) / 4); i += 32) dst[i] = src[i];
+                if (lane == 0) s_case_t1[to] = lo + 1 < ncases ? cases[lo + 1].tile0 : ntiles;
+            }
+            sv_row_sync();
+            return to;
+        };
+        if (warp < 4 && (int64_t)blockIdx.x < ntiles) {
+            slot = locate(blockIdx.x, -1, 0);
+            sv_features(sc[slot], blockIdx.x, tid, S.A0);
+            tc_fence_proxy_async();
+            sv_arrive(&bar_f);
+        }
+        for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            float2 y01 = make_float2(0.f, 0.f), y23 = make_float2(0.f, 0.f);
+            int next_slot = slot;
+            for (int j = 0; j < 4 && ok; ++j) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (!ok) break;
+                    ok = sv_wait(&bar_m[h], ph_m[h], fail);
+                    if (!ok) break;
+                    ph_m[h] ^= 1u;
+                    tc_fence_after();
+                    const uint32_t td = tmem + lane_off + 128u * h + 32u * cg;
+                    const float *bias = S.bias[j] + 128 * h + 32 * cg;
+                    if (j < 3) {
+                        const uint32_t ta = tmem + lane_off + SV_AB(h == 0 ? buf_lo(j) : buf_hi(j)) + 16u * cg;
+                        sv_epilogue_hidden(td, ta, bias);
+                        tc_wait_st();
+                    } else {
+                        sv_epilogue_out(td, bias, S.W4 + (128 * h + 32 * cg) * MLP_OUT, y01, y23);
+                    }
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) sv_arrive(&bar_e[h]);
+                    if (j == 0 && h == 1 && warp < 4 && tile + gridDim.x < ntiles) {
+                        // the input layer of this tile is complete: the next
+                        // tile's features into its operand
+                        next_slot = locate(tile + gridDim.x, slot, slot ^ 1);
+                        sv_features(sc[next_slot], tile + gridDim.x, tid, S.A0);
+                        tc_fence_proxy_async();
+                        sv_arrive(&bar_f);
+                    }
+                }
+            }
+            if (!ok) {
+                s_fail = 1;
                 break;
             }
-            mph ^= 1;
-            if (tid == 0) {
-                pend_mma = false;
-                // after layer j >= 1 the weights are free: stream in the next
-                // layer's (or, after the last, the next tile's first)
-                if (j >= 1) {
-                    const uint16_t *next =
-                        j < 3 ? net.Wt[j] : (tile + gridDim.x < ntiles ? net.Wt[0] : nullptr);
-                    if (next) {
-                        tc_expect_tx(&bar_w, WBYTES);
-                        tc_bulk_load(S.W, next, WBYTES, &bar_w);
-                        pend_w = true;
-                    }
-                }
-            }
-            tc_fence_after();
-            if (j < 3) {
-                sv_epilogue_hidden(tb, row, 64 * hf, S.bias[j], S.A);
-                tc_fence_proxy_async();
-            } else {
-                float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 1
-                for (int cc = 0; cc < 2; ++cc) {
-                    float v[32];
-                    tc_ld32(tb + 32 * cc, v);
-                    const int c0 = 64 * hf + 32 * cc;
+            S.Yp[cg][row] = make_float4(y01.x, y01.y, y23.x, y23.y);
+            sv_epi_sync();  // every column group's partial sums are in Yp
+            if (warp < 4) {
+                const SurCase &c = sc[slot];
+                const int64_t m = (tile - c.tile0) * 128 + tid;
+                if (m < c.g.nsolved) {
+                    float4 a = S.Yp[0][tid];
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        const float h = gelu_f(v[i] + S.bias[3][c0 + i]);
-                        const float4 w4 = *(const float4 *)&S.W4[(c0 + i) * MLP_OUT];
-                        y.x = fmaf(h, w4.x, y.x);
-                        y.y = fmaf(h, w4.y, y.y);
-                        y.z = fmaf(h, w4.z, y.z);
-                        y.w = fmaf(h, w4.w, y.w);
+                    for (int qq = 1; qq < SV_WARPS / 4; ++qq) {
+                        const float4 b = S.Yp[qq][tid];
+                        a = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
                     }
+                    const float y[4] = {a.x + S.b4[0], a.y + S.b4[1], a.z + S.b4[2], a.w + S.b4[3]};
+                    emit_spectrum(c.g, c.modes[m], y, c.ax, c.ay, c.zm, c.inv_wind, c.ktop, c.utop, c.Xp, c.Xq);
                 }
-                S.Yp[hf][row] = y;
             }
-            tc_fence_before();
-            __syncthreads();
+            slot = next_slot;
+            // Yp is rewritten only after this emit: the next tile's layer-1
+            // MMAs wait for the layer-0 epilogue of warps 0..3, which follows it
         }
-        if (failed) break;
-        if (tid < 128) {
-            const int64_t m = lt * 128 + tid;
-            if (m < g.nsolved) {
-                float4 a = S.Yp[0][tid];
-#pragma unroll
-                for (int qq = 1; qq < SV_WARPS / 4; ++qq) {
-                    const float4 b = S.Yp[qq][tid];
-                    a = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
-                }
-                const float y[4] = {a.x + S.b4[0], a.y + S.b4[1], a.z + S.b4[2], a.w + S.b4[3]};
-                emit_spectrum(g, sc.modes[m], y, sc.ax, sc.ay, sc.zm, sc.inv_wind, sc.ktop, sc.utop, sc.Xp, sc.Xq);
-            }
-        }
-        __syncthreads();  // sc is rewritten by the next tile
-    }
-    if (failed && tid == 0) {
-        atomicExch(err, BLDFM_ERR_TIMEOUT);
-        if (pend_mma) tc_mbar_wait(&bar_mma, mph);
-        if (pend_w) tc_mbar_wait(&bar_w, wph);
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc_tmem_free(tmem, 256);
+    if (warp == 0) tc_tmem_free(tmem, 512);
 }
 
 inline unsigned blocks_for(int64_t n) { return (unsigned)((n + 255) / 256); }
@@ -391,7 +554,7 @@ cudaError_t launch_sur_serve(const SurCase *cases, int ncases, int64_t ntiles, c
         }
     }
     const int grid = (int)std::min<int64_t>(ntiles, std::max(nsm, 1));
-    sur_serve_kernel<<<grid, 32 * SV_WARPS, sizeof(SvSmem), st>>>(cases, ncases, ntiles, net, err);
+    sur_serve_kernel<<<grid, SV_THREADS, sizeof(SvSmem), st>>>(cases, ncases, ntiles, net, err);
     return cudaGetLastError();
 }
 

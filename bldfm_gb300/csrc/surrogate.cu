@@ -428,26 +428,30 @@ __global__ void adam_kernel(float *P, const float *G, float *m, float *v, int n,
 }
 
 // BF16 operand blocks of the hidden weights: Wt_j (rows out, K in) for the
-// forward GEMM, W_j (rows in, K out) for the backward-data GEMM
-__global__ void weights_to_blocks_kernel(const float *__restrict__ P, uint16_t *Wt1, uint16_t *Wt2, uint16_t *Wt3,
-                                         uint16_t *W1, uint16_t *W2, uint16_t *W3)
+// forward GEMM, W_j (rows in, K out) for the backward-data GEMM, and Wq_j, Wt_j
+// as four contiguous 128 x 128 quarters (N half, K half) for the serving kernel
+struct WBlocks {
+    uint16_t *Wt[3], *W[3], *Wq[3];
+};
+
+__global__ void weights_to_blocks_kernel(const float *__restrict__ P, WBlocks wb)
 {
     const int j = blockIdx.y + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;  // out * 256 + in
     if (e >= MLP_H * MLP_H) return;
     const int out = e >> 8, in = e & 255;
     const uint16_t b = f2bf(P[MLP_OFF_WT(j) + e]);
-    uint16_t *wt = j == 1 ? Wt1 : (j == 2 ? Wt2 : Wt3);
-    uint16_t *w = j == 1 ? W1 : (j == 2 ? W2 : W3);
-    wt[tc_core_offset(out, in, MLP_H) / 2] = b;
-    w[tc_core_offset(in, out, MLP_H) / 2] = b;
+    wb.Wt[j - 1][tc_core_offset(out, in, MLP_H) / 2] = b;
+    wb.W[j - 1][tc_core_offset(in, out, MLP_H) / 2] = b;
+    const int q = (out >> 7) * 2 + (in >> 7);
+    wb.Wq[j - 1][(size_t)q * 128 * 128 + tc_core_offset(out & 127, in & 127, 128) / 2] = b;
 }
 
 struct Mlp {
     int B = 0;  // batch capacity, multiple of 256
     int step = 0;
     float *P = nullptr, *G = nullptr, *m = nullptr, *v = nullptr;
-    uint16_t *Wt[3] = {}, *W[3] = {};
+    uint16_t *Wt[3] = {}, *W[3] = {}, *Wq[3] = {};
     uint16_t *Hrows[3] = {}, *HT[3] = {};
     float *H4 = nullptr;  // last hidden layer, FP32 row-major (training)
     uint16_t *Gz[4] = {};
@@ -465,6 +469,17 @@ bool mlp_alloc(Mlp &M, T **p, size_t count)
     M.allocs.push_back(q);
     *p = (T *)q;
     return true;
+}
+
+WBlocks mlp_blocks(const Mlp &M)
+{
+    WBlocks b;
+    for (int j = 0; j < 3; ++j) {
+        b.Wt[j] = M.Wt[j];
+        b.W[j] = M.W[j];
+        b.Wq[j] = M.Wq[j];
+    }
+    return b;
 }
 
 void mlp_free(Mlp *M)
@@ -529,6 +544,7 @@ int bldfm_surrogate_create(int32_t batch, uint64_t seed, void **handle)
               mlp_alloc(*M, &M->Y, B * MLP_OUT) && mlp_alloc(*M, &M->loss, 1) && mlp_alloc(*M, &M->err, 1);
     for (int j = 0; j < 3 && ok; ++j)
         ok = mlp_alloc(*M, &M->Wt[j], (size_t)MLP_H * MLP_H) && mlp_alloc(*M, &M->W[j], (size_t)MLP_H * MLP_H) &&
+             mlp_alloc(*M, &M->Wq[j], (size_t)MLP_H * MLP_H) &&
              mlp_alloc(*M, &M->Hrows[j], B * MLP_H) && mlp_alloc(*M, &M->HT[j], B * MLP_H) &&
              mlp_alloc(*M, &M->dZrows[j], B * MLP_H) && mlp_alloc(*M, &M->dZT[j], B * MLP_H);
     for (int j = 0; j < 4 && ok; ++j) ok = mlp_alloc(*M, &M->Gz[j], B * MLP_H);
@@ -553,8 +569,7 @@ int bldfm_surrogate_create(int32_t batch, uint64_t seed, void **handle)
     cudaMemset(M->v, 0, MLP_NPARAM * 4);
     cudaMemset(M->G, 0, MLP_NPARAM * 4);
     cudaMemset(M->err, 0, 4);
-    weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, M->Wt[0], M->Wt[1], M->Wt[2], M->W[0],
-                                                                  M->W[1], M->W[2]);
+    weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, mlp_blocks(*M));
     if (cudaDeviceSynchronize() != cudaSuccess) {
         mlp_free(M);
         return BLDFM_ERR_CUDA;
@@ -585,8 +600,7 @@ int bldfm_surrogate_params(void *handle, float *host_out, const float *host_in)
         return BLDFM_ERR_CUDA;
     if (host_in) {
         if (cudaMemcpy(M->P, host_in, MLP_NPARAM * 4, cudaMemcpyHostToDevice) != cudaSuccess) return BLDFM_ERR_CUDA;
-        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, M->Wt[0], M->Wt[1], M->Wt[2], M->W[0],
-                                                                      M->W[1], M->W[2]);
+        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, mlp_blocks(*M));
         if (cudaDeviceSynchronize() != cudaSuccess) return BLDFM_ERR_CUDA;
     }
     return BLDFM_OK;
@@ -644,8 +658,7 @@ int bldfm_surrogate_train_step(void *handle, const float *X, const float *T, con
         const float c1 = 1.f / (1.f - powf(b1, (float)M->step)), c2 = 1.f / (1.f - powf(b2, (float)M->step));
         adam_kernel<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(M->P, M->G, M->m, M->v, MLP_NPARAM, lr, b1, b2, 1e-8f,
                                                               c1, c2);
-        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256, 0, st>>>(M->P, M->Wt[0], M->Wt[1], M->Wt[2],
-                                                                             M->W[0], M->W[1], M->W[2]);
+        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256, 0, st>>>(M->P, mlp_blocks(*M));
     }
     return cudaGetLastError() == cudaSuccess ? BLDFM_OK : BLDFM_ERR_CUDA;
 }
@@ -668,7 +681,10 @@ int mlp_serving_view(void *handle, MlpServing *out)
     Mlp *M = (Mlp *)handle;
     if (!M || !out) return BLDFM_ERR_ARG;
     out->P = M->P;
-    for (int j = 0; j < 3; ++j) out->Wt[j] = M->Wt[j];
+    for (int j = 0; j < 3; ++j) {
+        out->Wt[j] = M->Wt[j];
+        out->Wq[j] = M->Wq[j];
+    }
     return BLDFM_OK;
 }
 

@@ -112,6 +112,19 @@ __device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t 
         : "memory");
 }
 
+// D[tmem] (+)= A[tmem] * B[smem]^T: A (M x K, BF16) in tensor memory, one
+// lane per row and two K values per 32-bit column (K = 16 spans 8 columns)
+__device__ __forceinline__ void tc_mma_ts(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(dtmem),
+        "r"(atmem), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
 // arrive on bar once every MMA issued so far by this thread has completed
 __device__ __forceinline__ void tc_commit(uint64_t *bar)
 {
@@ -128,6 +141,21 @@ __device__ __forceinline__ void tc_fence_proxy_async()
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive 32-bit columns of this thread's TMEM lane (warp w writes
+// lanes 32 (w % 4) .. +31); complete them with tc_wait_st before the tensor
+// cores read them
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t *w)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7]), "r"(w[8]), "r"(w[9]),
+        "r"(w[10]), "r"(w[11]), "r"(w[12]), "r"(w[13]), "r"(w[14]), "r"(w[15])
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // 32 consecutive FP32 columns of this thread's TMEM lane (warp w reads lanes
 // 32 (w % 4) .. +31).  The load and its wait are one asm statement, so no use
