@@ -128,7 +128,7 @@ __global__ void sur_spectra_kernel(const SolveGeom g, const uint32_t *__restrict
 // frees TMEM and returns.
 // ---------------------------------------------------------------------------
 #define SV_K0 32     // K of the split input layer
-#define SV_WARPS 16  // epilogue warps: 4 per TMEM lane quarter, each 32 columns of a half
+#define SV_WARPS 8  // epilogue warps: 2 per TMEM lane quarter, each 2 x 32 columns of a half
 #define SV_THREADS (32 * SV_WARPS + 32)  // + one control warp (copies and MMAs)
 #define SV_AB(i) (256u + 64u * (uint32_t)(i))  // TMEM column of activation K-half buffer i
 
@@ -236,6 +236,24 @@ __device__ __forceinline__ void sv_epilogue_hidden(uint32_t td, uint32_t ta, con
     tc_st16(ta, w);
 }
 
+// the same for two 32-column groups of the half (accumulator columns td0,
+// td1), both TMEM loads in flight together
+__device__ __forceinline__ void sv_epilogue_hidden2(uint32_t td0, uint32_t td1, uint32_t ta0, uint32_t ta1,
+                                                    const float *bias0, const float *bias1)
+{
+    float v[64];
+    tc_ld32x2(td0, td1, v);
+    uint32_t w[32];
+#pragma unroll
+    for (int p = 0; p < 32; ++p) {
+        const float *b = p < 16 ? bias0 + 2 * p : bias1 + 2 * (p - 16);
+        const float2 g = gelu2_bias(make_float2(v[2 * p], v[2 * p + 1]), *(const float2 *)b);
+        w[p] = pack_bf16x2(g.x, g.y);
+    }
+    tc_st16(ta0, w);
+    tc_st16(ta1, w + 16);
+}
+
 // last hidden layer's epilogue of 32 columns, folded into the 256 -> 4 output
 // layer: y += gelu(v + b) . W4 rows
 __device__ __forceinline__ void sv_epilogue_out(uint32_t td, const float *bias, const float *W4, float2 &y01,
@@ -256,7 +274,7 @@ __device__ __forceinline__ void sv_epilogue_out(uint32_t td, const float *bias, 
 }
 
 // Fused serving kernel: features -> MLP -> spectra for 128 modes per tile,
-// one persistent CTA per SM: 16 epilogue warps and one control warp.
+// one persistent CTA per SM: 8 epilogue warps and one control warp.
 //
 // All four matrix layers run on the tensor cores (tcgen05.mma, M = 128, FP32
 // accumulators in TMEM); the epilogues (bias + GELU) and the 256 -> 4 output
@@ -286,7 +304,7 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SvSmem &S = *reinterpret_cast<SvSmem *>(smem_raw);
     // bar_m[h]: MMAs of accumulator half h done; bar_e[h]: epilogue of half h
-    // done (16 warp arrivals); bar_f: input operand written (128 thread
+    // done (one arrival per epilogue warp); bar_f: input operand written (128 thread
     // arrivals); bar_q[q]: weight quarter q loaded
     __shared__ uint64_t bar_m[2], bar_e[2], bar_f, bar_q[4];
     __shared__ uint32_t tmem_slot;
@@ -468,14 +486,17 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
                     if (!ok) break;
                     ph_m[h] ^= 1u;
                     tc_fence_after();
+                    // this warp's 32-column groups c = cg, cg + 2 of the half
                     const uint32_t td = tmem + lane_off + 128u * h + 32u * cg;
                     const float *bias = S.bias[j] + 128 * h + 32 * cg;
                     if (j < 3) {
                         const uint32_t ta = tmem + lane_off + SV_AB(h == 0 ? buf_lo(j) : buf_hi(j)) + 16u * cg;
-                        sv_epilogue_hidden(td, ta, bias);
+                        sv_epilogue_hidden2(td, td + 64u, ta, ta + 32u, bias, bias + 64);
                         tc_wait_st();
                     } else {
-                        sv_epilogue_out(td, bias, S.W4 + (128 * h + 32 * cg) * MLP_OUT, y01, y23);
+                        const float *w4 = S.W4 + (128 * h + 32 * cg) * MLP_OUT;
+                        sv_epilogue_out(td, bias, w4, y01, y23);
+                        sv_epilogue_out(td + 64u, bias + 64, w4 + 64 * MLP_OUT, y01, y23);
                     }
                     tc_fence_before();
                     __syncwarp();
