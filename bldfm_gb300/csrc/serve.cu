@@ -165,6 +165,14 @@ __device__ __forceinline__ void sv_mma_quarter(uint32_t dt, uint32_t at, uint64_
     for (int s = 1; s < 8; ++s) tc_mma_ts(dt, at + 8 * s, bdesc + (uint64_t)(16 * s), idesc, 1u);
 }
 
+// K steps s0 .. s0 + 3 of a quarter MMA (K = 64 of the 128)
+__device__ __forceinline__ void sv_mma_quarter_part(uint32_t dt, uint32_t at, uint64_t bdesc, uint32_t idesc, int s0)
+{
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        tc_mma_ts(dt, at + 8 * (s0 + s), bdesc + (uint64_t)(16 * (s0 + s)), idesc, 1u);
+}
+
 // Bounded wait for phase `parity` of an mbarrier that also gives up as soon
 // as another warp has recorded a failure in *fail.
 __device__ __forceinline__ bool sv_wait(uint64_t *bar, uint32_t parity, const volatile int *fail)
@@ -195,8 +203,16 @@ __device__ __forceinline__ void sv_epi_sync() { asm volatile("bar.sync 1, %0;" :
 // barrier of the feature / emit warps 0..3
 __device__ __forceinline__ void sv_row_sync() { asm volatile("bar.sync 2, 128;" ::: "memory"); }
 
-// features of row r of a tile -> [xh | xl | xh | 0] (input-layer A operand, K = 32)
-__device__ __forceinline__ void sv_features(const SurCase &c, int64_t tile, int r, uint16_t *A0)
+// mode word of row r of a tile (0 past the case's last mode)
+__device__ __forceinline__ uint32_t sv_mode_word(const SurCase &c, int64_t tile, int r)
+{
+    const int64_t m = (tile - c.tile0) * 128 + r;
+    return m < c.g.nsolved ? c.modes[m] : 0u;
+}
+
+// features of row r of a tile (mode word e) -> [xh | xl | xh | 0] (input-layer
+// A operand, K = 32)
+__device__ __forceinline__ void sv_features(const SurCase &c, int64_t tile, int r, uint32_t e, uint16_t *A0)
 {
     const int64_t m = (tile - c.tile0) * 128 + r;
     float kpar = 1.f, kperp = 0.f;
@@ -204,7 +220,7 @@ __device__ __forceinline__ void sv_features(const SurCase &c, int64_t tile, int 
         int rr, cc;
         bool pr;
         float k;
-        mode_k(c.g, c.modes[m], c.ax, c.ay, c.zm, rr, cc, pr, kpar, kperp, k);
+        mode_k(c.g, e, c.ax, c.ay, c.zm, rr, cc, pr, kpar, kperp, k);
         kpar = fabsf(kpar);
     }
     float x[8], xl[8];
@@ -237,21 +253,34 @@ __device__ __forceinline__ void sv_epilogue_hidden(uint32_t td, uint32_t ta, con
 }
 
 // the same for two 32-column groups of the half (accumulator columns td0,
-// td1), both TMEM loads in flight together
+// td1), both TMEM loads in flight together; when bar0 is given, the first
+// group's activations are announced on it (one arrival per warp) before the
+// second group is computed
 __device__ __forceinline__ void sv_epilogue_hidden2(uint32_t td0, uint32_t td1, uint32_t ta0, uint32_t ta1,
-                                                    const float *bias0, const float *bias1)
+                                                    const float *bias0, const float *bias1, uint64_t *bar0)
 {
     float v[64];
     tc_ld32x2(td0, td1, v);
-    uint32_t w[32];
+    uint32_t w[16];
 #pragma unroll
-    for (int p = 0; p < 32; ++p) {
-        const float *b = p < 16 ? bias0 + 2 * p : bias1 + 2 * (p - 16);
-        const float2 g = gelu2_bias(make_float2(v[2 * p], v[2 * p + 1]), *(const float2 *)b);
+    for (int p = 0; p < 16; ++p) {
+        const float2 g = gelu2_bias(make_float2(v[2 * p], v[2 * p + 1]), *(const float2 *)(bias0 + 2 * p));
         w[p] = pack_bf16x2(g.x, g.y);
     }
     tc_st16(ta0, w);
-    tc_st16(ta1, w + 16);
+    if (bar0) {
+        tc_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) sv_arrive(bar0);
+    }
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+        const float2 g =
+            gelu2_bias(make_float2(v[32 + 2 * p], v[32 + 2 * p + 1]), *(const float2 *)(bias1 + 2 * p));
+        w[p] = pack_bf16x2(g.x, g.y);
+    }
+    tc_st16(ta1, w);
 }
 
 // last hidden layer's epilogue of 32 columns, folded into the 256 -> 4 output
@@ -306,7 +335,8 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
     // bar_m[h]: MMAs of accumulator half h done; bar_e[h]: epilogue of half h
     // done (one arrival per epilogue warp); bar_f: input operand written (128 thread
     // arrivals); bar_q[q]: weight quarter q loaded
-    __shared__ uint64_t bar_m[2], bar_e[2], bar_f, bar_q[4];
+    // bar_p: the first 64 columns of half 1 done (one arrival per epilogue warp)
+    __shared__ uint64_t bar_m[2], bar_e[2], bar_p, bar_f, bar_q[4];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
     __shared__ SurCase sc[2];         // cases of the current and the next tile (warps 0..3)
@@ -320,6 +350,7 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
             tc_mbar_init(&bar_e[i], SV_WARPS);
         }
         tc_mbar_init(&bar_f, 128);
+        tc_mbar_init(&bar_p, SV_WARPS);
         for (int i = 0; i < 4; ++i) tc_mbar_init(&bar_q[i], 1);
         tc_fence_init();
         s_fail = 0;
@@ -355,7 +386,7 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
             uint64_t bq[4];  // descriptors of the weight quarters
             for (int q = 0; q < 4; ++q) bq[q] = tc_desc(tc_smem(S.Wq[q]), 128, 2048);
             const uint64_t da0 = tc_desc(tc_smem(S.A0), 128, 512), db0 = tc_desc(tc_smem(S.B0), 128, 512);
-            uint32_t ph_m[2] = {0u, 0u}, ph_e[2] = {0u, 0u}, ph_f = 0u, ph_q[4] = {0u, 0u, 0u, 0u};
+            uint32_t ph_m[2] = {0u, 0u}, ph_e[2] = {0u, 0u}, ph_p = 0u, ph_f = 0u, ph_q[4] = {0u, 0u, 0u, 0u};
             bool pend_m[2] = {false, false}, pend_q[4] = {false, false, false, false};
             bool ok = true;
             if ((int64_t)blockIdx.x < ntiles)
@@ -399,6 +430,19 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
                                     pend_q[q] = true;
                                 }
                         }
+                        const uint32_t alo = tmem + SV_AB(j < 3 ? buf_lo(j) : 0),
+                                       ahi = tmem + SV_AB(j < 3 ? buf_hi(j) : 0);
+                        if (h == 1 && j < 3) {
+                            // the first 64 activations of the high K half: the
+                            // first half of quarter 1 (layer j + 1, N half 0)
+                            ok = sv_wait(&bar_p, ph_p, fail) && sv_wait(&bar_q[1], ph_q[1], fail);
+                            if (!ok) break;
+                            ph_p ^= 1u;
+                            ph_q[1] ^= 1u;
+                            pend_q[1] = false;
+                            tc_fence_after();
+                            sv_mma_quarter_part(tmem, ahi, bq[1], idesc, 0);
+                        }
                         // the epilogue of half h has read the accumulator (and
                         // written the activations it feeds)
                         ok = sv_wait(&bar_e[h], ph_e[h], fail);
@@ -406,9 +450,13 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
                         ph_e[h] ^= 1u;
                         if (j == 3) continue;
                         tc_fence_after();
-                        const uint32_t alo = tmem + SV_AB(buf_lo(j)), ahi = tmem + SV_AB(buf_hi(j));
+                        if (h == 1) {
+                            sv_mma_quarter_part(tmem, ahi, bq[1], idesc, 4);
+                            tc_commit(&bar_m[0]);
+                            pend_m[0] = true;
+                        }
 #pragma unroll
-                        for (int q = h == 0 ? 0 : 1; q < (h == 0 ? 1 : 4); ++q) {
+                        for (int q = h == 0 ? 0 : 2; q < (h == 0 ? 1 : 4); ++q) {
                             if (!ok) break;
                             ok = sv_wait(&bar_q[q], ph_q[q], fail);
                             if (!ok) break;
@@ -469,15 +517,24 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
             sv_row_sync();
             return to;
         };
+        uint32_t mw = 0u;  // warps 0..3: mode word of this thread's row of the current tile
         if (warp < 4 && (int64_t)blockIdx.x < ntiles) {
             slot = locate(blockIdx.x, -1, 0);
-            sv_features(sc[slot], blockIdx.x, tid, S.A0);
+            mw = sv_mode_word(sc[slot], blockIdx.x, tid);
+            sv_features(sc[slot], blockIdx.x, tid, mw, S.A0);
             tc_fence_proxy_async();
             sv_arrive(&bar_f);
         }
         for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
             float2 y01 = make_float2(0.f, 0.f), y23 = make_float2(0.f, 0.f);
+            const bool has_next = tile + gridDim.x < ntiles;
             int next_slot = slot;
+            uint32_t mw_next = 0u;
+            if (warp < 4 && has_next) {
+                // the next tile's case and mode words, in flight while this tile runs
+                next_slot = locate(tile + gridDim.x, slot, slot ^ 1);
+                mw_next = sv_mode_word(sc[next_slot], tile + gridDim.x, tid);
+            }
             for (int j = 0; j < 4 && ok; ++j) {
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
@@ -491,7 +548,7 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
                     const float *bias = S.bias[j] + 128 * h + 32 * cg;
                     if (j < 3) {
                         const uint32_t ta = tmem + lane_off + SV_AB(h == 0 ? buf_lo(j) : buf_hi(j)) + 16u * cg;
-                        sv_epilogue_hidden2(td, td + 64u, ta, ta + 32u, bias, bias + 64);
+                        sv_epilogue_hidden2(td, td + 64u, ta, ta + 32u, bias, bias + 64, h == 1 ? &bar_p : nullptr);
                         tc_wait_st();
                     } else {
                         const float *w4 = S.W4 + (128 * h + 32 * cg) * MLP_OUT;
@@ -501,11 +558,10 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) sv_arrive(&bar_e[h]);
-                    if (j == 0 && h == 1 && warp < 4 && tile + gridDim.x < ntiles) {
+                    if (j == 0 && h == 1 && warp < 4 && has_next) {
                         // the input layer of this tile is complete: the next
                         // tile's features into its operand
-                        next_slot = locate(tile + gridDim.x, slot, slot ^ 1);
-                        sv_features(sc[next_slot], tile + gridDim.x, tid, S.A0);
+                        sv_features(sc[next_slot], tile + gridDim.x, tid, mw_next, S.A0);
                         tc_fence_proxy_async();
                         sv_arrive(&bar_f);
                     }
@@ -528,10 +584,11 @@ __global__ void __launch_bounds__(SV_THREADS, 1)
                         a = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
                     }
                     const float y[4] = {a.x + S.b4[0], a.y + S.b4[1], a.z + S.b4[2], a.w + S.b4[3]};
-                    emit_spectrum(c.g, c.modes[m], y, c.ax, c.ay, c.zm, c.inv_wind, c.ktop, c.utop, c.Xp, c.Xq);
+                    emit_spectrum(c.g, mw, y, c.ax, c.ay, c.zm, c.inv_wind, c.ktop, c.utop, c.Xp, c.Xq);
                 }
             }
             slot = next_slot;
+            mw = mw_next;
             // Yp is rewritten only after this emit: the next tile's layer-1
             // MMAs wait for the layer-0 epilogue of warps 0..3, which follows it
         }
