@@ -706,15 +706,10 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     if (xl != 0 && xl != 1 && xl != 2 && xl != 4) return BLDFM_ERR_ARG;
     B.rpc = xl > 0 ? xl : 2;
     while (B.rpc > 1 && (2 * (size_t)B.rpc + 1) * maxnfx * 8 > 190 * 1024) --B.rpc;
-    B.cpc = out_cols_per_cta(maxnfy, 8);
-    if (xl > 0)
-        while (B.cpc > xl) B.cpc >>= 1;
-    if (xl > B.cpc)
-        for (int c = xl; c > B.cpc; c >>= 1)
-            if ((2 * (size_t)c + 1) * maxnfy * 8 <= 190 * 1024) {
-                B.cpc = c;
-                break;
-            }
+    // column pass: (2 cpc + 1) lines of maxnfy in shared memory
+    auto col_bytes = [&](int c) { return (2 * (size_t)c + 1) * maxnfy * 8; };
+    B.cpc = xl > 0 ? xl : out_cols_per_cta(maxnfy, 8);
+    while (B.cpc > 1 && col_bytes(B.cpc) > 190 * 1024) B.cpc >>= 1;
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
         B.col0[k] = B.ncol;
@@ -777,7 +772,7 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     }
     B.total = w;
     B.sweep_smem = (size_t)maxL * BLDFM_LV32 * 4 + (size_t)maxnz * 4 + 16;
-    B.col_smem = (2 * (size_t)B.cpc + 1) * maxnfy * 8;
+    B.col_smem = col_bytes(B.cpc);
     B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
     if (B.sweep_smem > 200 * 1024) return BLDFM_ERR_UNSUPPORTED;
     if (!dc) return BLDFM_OK;

@@ -136,18 +136,26 @@ __global__ void __launch_bounds__(256, 4) riccati32_batch_kernel(const BatchCase
 }
 
 __global__ void __launch_bounds__(256) out_cols_batch_kernel(const BatchCase *__restrict__ cases,
-                                                             const int *__restrict__ cta_case)
+                                                             const int *__restrict__ cta_case, int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(16) BatchCase sc;
+    __shared__ uint64_t bar;
     const int k = cta_case[blockIdx.x];
     load_case(&sc, cases + k);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     __syncthreads();
     const int64_t local = (int64_t)blockIdx.x - sc.col0;
     const int ncb = (sc.g.nbx + sc.cpc - 1) / sc.cpc;  // column blocks per level
     const int lvl = (int)(local / ncb), cb = (int)(local - (int64_t)lvl * ncb);
-    out_col_lines<float>(sc.g, sc.ply, sc.twy, sc.xband, sc.Xp, sc.Xq, sc.dc, sc.Cb, cb * sc.cpc, sc.cpc, lvl,
-                         (float2 *)smem_raw);
+    if (!out_col_lines_staged(sc.g, sc.ply, sc.twy, sc.xband, sc.Xp, sc.Xq, sc.dc, sc.Cb, cb * sc.cpc, sc.cpc, lvl,
+                              (float2 *)smem_raw, &bar) &&
+        threadIdx.x == 0)
+        atomicExch(err, BLDFM_ERR_TIMEOUT_DEV);
 }
 
 __global__ void __launch_bounds__(256) out_rows_batch_kernel(const BatchCase *__restrict__ cases,
@@ -174,7 +182,7 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
         riccati32_batch_kernel<<<bl.sweep_ctas, bl.threads, bl.sweep_smem, st>>>(bl.cases, bl.tile_case,
                                                                                  bl.cta_tiles, bl.err);
     if (part == 1 && bl.col_ctas > 0)
-        out_cols_batch_kernel<<<bl.col_ctas, 256, bl.col_smem, st>>>(bl.cases, bl.col_case);
+        out_cols_batch_kernel<<<bl.col_ctas, 256, bl.col_smem, st>>>(bl.cases, bl.col_case, bl.err);
     if (part == 1 && bl.row_ctas > 0)
         out_rows_batch_kernel<<<bl.row_ctas, 256, bl.row_smem, st>>>(bl.cases, bl.row_case);
     return cudaGetLastError();
