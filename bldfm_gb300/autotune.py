@@ -2,8 +2,9 @@
 
 Picks the sweep CTA size (modes per CTA tile), the number of persistent
 CTAs per SM and the lines per CTA of the output-transform passes for a batch
-shape by timing candidates on the device with CUDA events (first the sweep
-shape, then the transform lines with the best sweep shape), and caches the
+shape by timing candidates on the device with the library's stage timers
+(CUDA events around each stage: first the sweep shape on the sweep's time,
+then the transform lines on the transforms' time), and caches the
 winner in a JSON file keyed by GPU name and a coarse shape signature (total
 solved modes, deepest level count, number of cases).
 Cache file: $BLDFM_GB300_CACHE or ~/.cache/bldfm_gb300/autotune.json.
@@ -64,22 +65,30 @@ def signature(cases):
                                         b(len(cases)))
 
 
-def _time(cases, reps, **opts):
+def _time(cases, reps, stage, **opts):
+    """Device time of one stage of the batched solve (the library's stage
+    timers: 1 = sweep, 2 = output transforms), averaged over reps solves."""
+    import ctypes
+
+    lib = _lib.load()
     s = BatchSolver(use_graph=False, **opts)
     s.solve(cases)  # warm
     s.stream.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s.stream)
-    for _ in range(reps):
-        s.solve(cases)
-    e1.record(s.stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    return ms if s.status() == 0 else None
+    _lib.check(lib.bldfm_set_stage_timing(1), "stage timing")
+    try:
+        for _ in range(reps):
+            s.solve(cases)
+        s.stream.synchronize()
+        arr = (ctypes.c_float * 8)()
+        nst = lib.bldfm_stage_times(arr, 8)
+    finally:
+        lib.bldfm_set_stage_timing(0)
+    if s.status() != 0 or nst <= stage:
+        return None
+    return float(arr[stage])
 
 
-def tune(cases, reps=3, use_cache=True):
+def tune(cases, reps=5, use_cache=True):
     """Return (threads, ctas_per_sm, xform_lines) for this batch shape (timed or cached)."""
     key = signature(cases)
     cache = _load() if use_cache else {}
@@ -88,12 +97,12 @@ def tune(cases, reps=3, use_cache=True):
         return int(v["threads"]), int(v["ctas_per_sm"]), int(v["xform_lines"])
     best, best_ms = CANDIDATES[0], None
     for threads, per_sm in CANDIDATES:
-        ms = _time(cases, reps, threads=threads, ctas_per_sm=per_sm)
+        ms = _time(cases, reps, 1, threads=threads, ctas_per_sm=per_sm)
         if ms is not None and (best_ms is None or ms < best_ms):
             best, best_ms = (threads, per_sm), ms
     best_xl, best_xms = 0, None
     for xl in XFORM_LINES:
-        ms = _time(cases, reps, threads=best[0], ctas_per_sm=best[1], xform_lines=xl)
+        ms = _time(cases, reps, 2, threads=best[0], ctas_per_sm=best[1], xform_lines=xl)
         if ms is not None and (best_xms is None or ms < best_xms):
             best_xl, best_xms = xl, ms
     if use_cache:

@@ -626,7 +626,7 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         }
         tmark(dc, st);  // 3: before the output transform
         CK(launch_output_fft<double>(g, hp.plx_out, hp.ply_out, twxo->d64, twyo->d64, xband, Xp, Xq, dcv,
-                                     (double2 *)(w + L.Cb), conc, flx, st));
+                                     (double2 *)(w + L.Cb), conc, flx, nullptr, st));
     } else {
         float2 *q0 = g.footprint ? nullptr : (float2 *)(w + L.q0);
         if (!g.footprint)
@@ -643,7 +643,7 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         if (!g.footprint) CK(launch_trapezoid32(g, lv64, slot, q0, p000, dcv, st));
         tmark(dc, st);  // 3: before the output transform
         CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
-                                    (float2 *)(w + L.Cb), conc, flx, st));
+                                    (float2 *)(w + L.Cb), conc, flx, err, st));
     }
     tmark(dc, st);  // 4: end
     if (f64 && g.analytic) CK(cudaEventRecord(slt->ev, st));
@@ -1106,7 +1106,7 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
         CK(launch_sur_spectra(g, ml->dev, Y, ax, ay, zm, inv_wind, ktop, utop, Xp, Xq, st));
     }
     CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
-                                (float2 *)(w + S.L.Cb), conc, flx, st));
+                                (float2 *)(w + S.L.Cb), conc, flx, (int *)(w + S.L.err), st));
     return BLDFM_OK;
 }
 

@@ -250,13 +250,32 @@ __device__ __forceinline__ void out_row_lines(const SolveGeom &g, const FftPlan 
     C *bufB = bufA + (size_t)rows_per_cta * n;
     C *stw = bufB + (size_t)rows_per_cta * n;
     const int nl = min(rows_per_cta, g.out_ny - y0);
+    // the rows' band values (contiguous: nl x nbx from row y0) go into
+    // registers first, so that their loads overlap the zero fill and the
+    // twiddle loads; entries past the first PF x blockDim are placed after
+    constexpr int PF = 8;
+    const int nb = g.nbx, tot = nl * nb;
+    const C *rows = Cin + ((size_t)lvl * g.out_ny + y0) * nb;
+    C pre[PF];
+#pragma unroll
+    for (int k = 0; k < PF; ++k) {
+        const int i = threadIdx.x + k * (int)blockDim.x;
+        if (i < tot) pre[k] = rows[i];
+    }
     for (int i = threadIdx.x; i < nl * n; i += blockDim.x) bufA[i] = cx_make<C>(0.0, 0.0);
     for (int i = threadIdx.x; i < n; i += blockDim.x) stw[i] = tw[i];
     __syncthreads();
-    for (int l = 0; l < nl; ++l) {
-        const C *row = Cin + ((size_t)lvl * g.out_ny + y0 + l) * g.nbx;
-        C *dst = bufA + (size_t)l * n;
-        for (int b = threadIdx.x; b < g.nbx; b += blockDim.x) dst[xband[b].x] = row[b];
+#pragma unroll
+    for (int k = 0; k < PF; ++k) {
+        const int i = threadIdx.x + k * (int)blockDim.x;
+        if (i < tot) {
+            const int l = i / nb, b = i - l * nb;
+            bufA[(size_t)l * n + xband[b].x] = pre[k];
+        }
+    }
+    for (int i = threadIdx.x + PF * (int)blockDim.x; i < tot; i += blockDim.x) {
+        const int l = i / nb, b = i - l * nb;
+        bufA[(size_t)l * n + xband[b].x] = rows[i];
     }
     C *res = fft_run<C>(bufA, bufB, pl, nl, stw, g.out_sign);
     for (int i = threadIdx.x; i < nl * g.out_nx; i += blockDim.x) {

@@ -552,12 +552,30 @@ __global__ void __launch_bounds__(256) out_cols_kernel(SolveGeom g, FftPlan pl, 
                                                        const typename cvec<R>::T *__restrict__ Xp,
                                                        const typename cvec<R>::T *__restrict__ Xq,
                                                        const double2 *__restrict__ dc,
-                                                       typename cvec<R>::T *__restrict__ Cout, int cols_per_cta)
+                                                       typename cvec<R>::T *__restrict__ Cout, int cols_per_cta,
+                                                       int *err)
 {
     typedef typename cvec<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    out_col_lines<R>(g, pl, tw, xband, Xp, Xq, dc, Cout, blockIdx.x * cols_per_cta, cols_per_cta, blockIdx.y,
-                     (C *)smem_raw);
+    if constexpr (sizeof(R) == 4) {
+        // FP32 spectra are Hermitian-complete: the staged gather
+        __shared__ uint64_t bar;
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(&bar)),
+                         "r"(1)
+                         : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncthreads();
+        if (!out_col_lines_staged(g, pl, tw, xband, Xp, Xq, dc, Cout, blockIdx.x * cols_per_cta, cols_per_cta,
+                                  blockIdx.y, (C *)smem_raw, &bar) &&
+            threadIdx.x == 0 && err)
+            atomicExch(err, BLDFM_ERR_TIMEOUT_DEV);
+    } else {
+        out_col_lines<R>(g, pl, tw, xband, Xp, Xq, dc, Cout, blockIdx.x * cols_per_cta, cols_per_cta, blockIdx.y,
+                         (C *)smem_raw);
+    }
 }
 
 // out_rows: rows_per_cta output rows per CTA, one level (blockIdx.y).
@@ -739,7 +757,7 @@ template <typename R>
 cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftPlan &ply,
                               const typename cvec<R>::T *twx, const typename cvec<R>::T *twy, const int4 *xband,
                               const typename cvec<R>::T *Xp, const typename cvec<R>::T *Xq, const double2 *dc,
-                              typename cvec<R>::T *Cbuf, double *conc, double *flx, cudaStream_t st)
+                              typename cvec<R>::T *Cbuf, double *conc, double *flx, int *err, cudaStream_t st)
 {
     typedef typename cvec<R>::T C;
     set_fft_smem_attr<R>();
@@ -747,7 +765,7 @@ cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftP
     const int cpc = out_cols_per_cta(ply.n, sizeof(C));
     dim3 gc((g.nbx + cpc - 1) / cpc, g.nlvls);
     out_cols_kernel<R><<<gc, 256, (2 * (size_t)cpc + 1) * ply.n * sizeof(C), st>>>(g, ply, twy, xband, Xp, Xq, dc,
-                                                                                   Cbuf, cpc);
+                                                                                   Cbuf, cpc, err);
     // two rows per CTA in FP32, one in FP64, bounded by shared memory
     int rpc = sizeof(C) == 8 ? 2 : 1;
     while (rpc > 1 && (2 * (size_t)rpc + 1) * plx.n * sizeof(C) > 190 * 1024) --rpc;
@@ -763,10 +781,10 @@ template cudaError_t launch_forward_fft<float>(const SolveGeom &, const FftPlan 
                                                const float2 *, const double *, float2 *, float2 *, cudaStream_t);
 template cudaError_t launch_output_fft<double>(const SolveGeom &, const FftPlan &, const FftPlan &, const double2 *,
                                                const double2 *, const int4 *, const double2 *, const double2 *,
-                                               const double2 *, double2 *, double *, double *, cudaStream_t);
+                                               const double2 *, double2 *, double *, double *, int *, cudaStream_t);
 template cudaError_t launch_output_fft<float>(const SolveGeom &, const FftPlan &, const FftPlan &, const float2 *,
                                               const float2 *, const int4 *, const float2 *, const float2 *,
-                                              const double2 *, float2 *, double *, double *, cudaStream_t);
+                                              const double2 *, float2 *, double *, double *, int *, cudaStream_t);
 
 cudaError_t launch_tw_to_float(const double2 *src, float2 *dst, int n, cudaStream_t st)
 {

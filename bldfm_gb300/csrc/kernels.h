@@ -32,7 +32,7 @@ template <typename R>
 cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftPlan &ply,
                               const typename cvec<R>::T *twx, const typename cvec<R>::T *twy, const int4 *xband,
                               const typename cvec<R>::T *Xp, const typename cvec<R>::T *Xq, const double2 *dc,
-                              typename cvec<R>::T *Cbuf, double *conc, double *flx, cudaStream_t st);
+                              typename cvec<R>::T *Cbuf, double *conc, double *flx, int *err, cudaStream_t st);
 cudaError_t launch_tw_to_float(const double2 *src, float2 *dst, int n, cudaStream_t st);
 cudaError_t launch_spec_to_float(const double2 *src, float2 *dst, int64_t n, cudaStream_t st);
 cudaError_t launch_nonfinite(const double *a, const double *b, int64_t n, int *flag, int nsm, cudaStream_t st);

@@ -371,6 +371,6 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
                                  (double2 *)(w + o_dc), st));
     NA_CK(launch_output_fft<float>(g, plx_out, ply_out, (const float2 *)(w + o_twxo), (const float2 *)(w + o_twyo),
                                    (const int4 *)(w + o_xb), Xp, Xq, (const double2 *)(w + o_dc), (float2 *)(w + o_Cb),
-                                   conc_dev, flx_dev, st));
+                                   conc_dev, flx_dev, (int *)(w + o_err), st));
     return BLDFM_OK;
 }
