@@ -51,6 +51,11 @@ N_LEVELS = 128
 ZM = 20.0
 MODES = (512, 512)
 MEAS = (500.0, 500.0)
+# DRAM traffic per launch of the batched FP32 sweep (16 footprints of the
+# workload), dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture:
+# 0.84 MB read + 8.46 MB written (a compute kernel; the spectra stay in L2)
+RICC_BATCH_DRAM_BYTES = 9.30e6
+
 # algorithmic flops per (mode, sweep step), FMA counted as 2; the FP32 sweep's
 # count per mode comes from bldfm_sweep32_flops (it depends on the output level)
 F64_FLOPS_PER_MODE_STEP = 88  # reference shooting step, both IVPs (src/bldfm/solver.py:357-368)
@@ -869,7 +874,10 @@ def main():
                                "(bldfm_fma_peak); not in MEASURED_PEAKS.json",
                 "peak_scalar_fp32": peak1.value / 1e12,
                 "peak_packed_fp32x2": peak2.value / 1e12,
-                "traffic": None,
+                # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+                # capture of this kernel on this workload, 16 footprints per launch
+                "traffic": RICC_BATCH_DRAM_BYTES,
+                "traffic_source": "ncu capture, profiles/riccati32_batch_kernel_metric_batch16.md",
                 "flops_per_launch": flops_launch,
             },
             "transform": transform_section(stages_b, B, dev),
