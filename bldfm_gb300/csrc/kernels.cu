@@ -299,8 +299,17 @@ __global__ void __launch_bounds__(256) riccati32_kernel(SolveGeom g, const float
     for (int i = threadIdx.x; i < g.nz; i += blockDim.x) s_slot[i] = slot_of_step[i];
     __syncthreads();
     const int64_t ns = g.nsolved;
-    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += (int64_t)gridDim.x * blockDim.x)
-        ricc_mode<ISO, SINGLE>(g, s_lv, s_slot, modes, q0spec, scratch, Xp, Xq, ax, ay, m);
+    if (SINGLE) {
+        // two modes per thread (m and m + blockDim.x) in the lanes of packed f32x2 operations
+        const int64_t step = 2 * (int64_t)gridDim.x * blockDim.x;
+        for (int64_t m = 2 * (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += step) {
+            const int64_t mb = m + blockDim.x < ns ? m + blockDim.x : -1;
+            ricc_mode_pair<ISO>(g, s_lv, modes, q0spec, Xp, Xq, ax, ay, m, mb);
+        }
+    } else {
+        for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < ns; m += (int64_t)gridDim.x * blockDim.x)
+            ricc_mode<ISO, SINGLE>(g, s_lv, s_slot, modes, q0spec, scratch, Xp, Xq, ax, ay, m);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -693,7 +702,8 @@ cudaError_t launch_riccati32(const SolveGeom &g, const float *lv32, const int *s
         cudaFuncSetAttribute(riccati32_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     }
     if (threads <= 0) threads = 256;
-    int64_t blocks = (g.nsolved + threads - 1) / threads;
+    const int64_t per_thread = g.nsnap == 1 ? 2 : 1;  // modes per thread
+    int64_t blocks = (g.nsolved + per_thread * threads - 1) / (per_thread * threads);
     if (blocks < 1) blocks = 1;
     if (blocks > 64LL * nsm) blocks = 64LL * nsm;
     const bool single = g.nsnap == 1;
@@ -762,13 +772,20 @@ cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftP
     typedef typename cvec<R>::T C;
     set_fft_smem_attr<R>();
     if (g.nbx <= 0 || g.out_ny <= 0 || g.out_nx <= 0 || g.nlvls <= 0) return cudaSuccess;
-    const int cpc = out_cols_per_cta(ply.n, sizeof(C));
+    // lines per CTA: as many as shared memory allows, but at least two CTAs
+    // per SM over the launch (a single footprint has few lines)
+    int dev = 0, nsm = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int cpc = out_cols_per_cta(ply.n, sizeof(C));
+    while (cpc > 1 && (int64_t)((g.nbx + cpc - 1) / cpc) * g.nlvls < 2 * (int64_t)nsm) cpc >>= 1;
     dim3 gc((g.nbx + cpc - 1) / cpc, g.nlvls);
     out_cols_kernel<R><<<gc, 256, (2 * (size_t)cpc + 1) * ply.n * sizeof(C), st>>>(g, ply, twy, xband, Xp, Xq, dc,
                                                                                    Cbuf, cpc, err);
-    // two rows per CTA in FP32, one in FP64, bounded by shared memory
+    // two rows per CTA in FP32, one in FP64, bounded by shared memory and by
+    // the same two CTAs per SM
     int rpc = sizeof(C) == 8 ? 2 : 1;
     while (rpc > 1 && (2 * (size_t)rpc + 1) * plx.n * sizeof(C) > 190 * 1024) --rpc;
+    while (rpc > 1 && (int64_t)((g.out_ny + rpc - 1) / rpc) * g.nlvls < 2 * (int64_t)nsm) --rpc;
     dim3 gr((g.out_ny + rpc - 1) / rpc, g.nlvls);
     out_rows_kernel<R><<<gr, 256, (2 * (size_t)rpc + 1) * plx.n * sizeof(C), st>>>(g, plx, twx, xband, Cbuf, conc,
                                                                                    flx, rpc);
