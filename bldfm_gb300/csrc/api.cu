@@ -669,6 +669,8 @@ struct BatchBuild {
     int64_t ntiles = 0;
     int G = 0, threads = 256, ncol = 0, nrow = 0, rpc = 2, cpc = 1;
     size_t sweep_smem = 0, col_smem = 0, row_smem = 0;
+    // persistent one-line transforms (lines per CTA 1)
+    int persist = 0, col_grid = 0, row_grid = 0, maxnfy = 0, maxnfx = 0, maxnly = 0;
     std::vector<int64_t> tile0, col0, row0;
 };
 
@@ -701,7 +703,10 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
         maxnz = std::max(maxnz, g.nz);
         maxnfy = std::max(maxnfy, g.nfy);
         maxnfx = std::max(maxnfx, g.nfx);
+        B.maxnly = std::max(B.maxnly, g.nly);
     }
+    B.maxnfy = maxnfy;
+    B.maxnfx = maxnfx;
     const int xl = opts ? opts->xform_lines : 0;
     if (xl != 0 && xl != 1 && xl != 2 && xl != 4) return BLDFM_ERR_ARG;
     B.rpc = xl > 0 ? xl : 2;
@@ -774,6 +779,22 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.sweep_smem = (size_t)maxL * BLDFM_LV32 * 4 + (size_t)maxnz * 4 + 16;
     B.col_smem = col_bytes(B.cpc);
     B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
+    B.persist = B.cpc == 1 && B.rpc == 1;
+    if (B.persist) {
+        B.col_smem = (3 * (size_t)maxnfy + 4 * (size_t)B.maxnly) * 8;
+        B.row_smem = 3 * (size_t)maxnfx * 8;
+        if (B.col_smem > 200 * 1024 || B.row_smem > 200 * 1024) return BLDFM_ERR_UNSUPPORTED;
+        // SMs of the current device (planning calls come without a device cache)
+        int nsm = dc ? dc->nsm : 0;
+        if (nsm <= 0) {
+            int dev = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess ||
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+                nsm = 1;
+        }
+        B.col_grid = (int)std::min<int64_t>(B.ncol, (int64_t)nsm * batch_xform_occupancy(1, B.col_smem));
+        B.row_grid = (int)std::min<int64_t>(B.nrow, (int64_t)nsm * batch_xform_occupancy(0, B.row_smem));
+    }
     if (B.sweep_smem > 200 * 1024) return BLDFM_ERR_UNSUPPORTED;
     if (!dc) return BLDFM_OK;
     // persistent sweep grid
@@ -913,6 +934,12 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
     bl.col_smem = B.col_smem;
     bl.row_ctas = B.nrow;
     bl.row_smem = B.row_smem;
+    bl.persist = B.persist;
+    bl.col_grid = B.col_grid;
+    bl.row_grid = B.row_grid;
+    bl.maxn_col = B.maxnfy;
+    bl.maxnly = B.maxnly;
+    bl.maxn_row = B.maxnfx;
     if (tdc) tmark(*tdc, st);  // 1: the sweep
     CK(launch_batch_kernels(bl, st, 0));
     if (tdc) tmark(*tdc, st);  // 2: the output transform
@@ -934,6 +961,9 @@ std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B,
     k.push_back((int64_t)B.col_smem);
     k.push_back(B.nrow);
     k.push_back((int64_t)B.row_smem);
+    k.push_back(B.persist);
+    k.push_back(B.col_grid);
+    k.push_back(B.row_grid);
     for (int i = 0; i < n; ++i) {
         const SolveGeom &g = B.hp[i].g;
         k.push_back(g.footprint);
@@ -1201,6 +1231,12 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     bl.col_smem = B.col_smem;
     bl.row_ctas = B.nrow;
     bl.row_smem = B.row_smem;
+    bl.persist = B.persist;
+    bl.col_grid = B.col_grid;
+    bl.row_grid = B.row_grid;
+    bl.maxn_col = B.maxnfy;
+    bl.maxnly = B.maxnly;
+    bl.maxn_row = B.maxnfx;
     CK(launch_batch_kernels(bl, st, 1));
     tmark(dc, st);  // 3: end
     return BLDFM_OK;

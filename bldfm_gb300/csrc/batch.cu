@@ -173,6 +173,213 @@ __global__ void __launch_bounds__(256) out_rows_batch_kernel(const BatchCase *__
                          (float2 *)smem_raw);
 }
 
+// Bounded wait on phase `parity` of an mbarrier by every thread of the block;
+// false (for all threads) if it ran out.
+__device__ __forceinline__ bool block_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    uint32_t done = 0;
+    for (long it = 0; it < BLDFM_WAIT_POLLS && !done; ++it)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+    return !__syncthreads_or(!done);
+}
+
+// Persistent column pass, one line at a time.  CTA b takes a contiguous range
+// of items (item = one band column of one level of one case, in case order)
+// and, while it transforms one line, the P-side spectrum column of the next
+// line of the same case arrives by bulk copy in the other of two staging
+// buffers (mbarrier per buffer, bounded waits); the case and its twiddles are
+// loaded when the case changes.  Cases whose arrays do not allow 16-byte
+// copies take out_col_lines, one line per item.  smem: 3 maxn + 4 maxnly complex.
+__global__ void __launch_bounds__(256) out_cols_persist_kernel(const BatchCase *__restrict__ cases,
+                                                               const int *__restrict__ col_case, int nitems, int maxn,
+                                                               int maxnly, int *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) BatchCase sc;
+    __shared__ uint64_t bar[2];
+    const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int lo = (int)blockIdx.x * per, hi = min(nitems, lo + per);
+    if (lo >= hi) return;
+    float2 *bufA = (float2 *)smem_raw, *bufB = bufA + maxn, *stw = bufB + maxn;
+    float2 *stg0 = stw + maxn, *stg1 = stg0 + 2 * (size_t)maxnly;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar[i])), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    uint32_t ph[2] = {0u, 0u};
+    bool pend[2] = {false, false};  // thread 0: copies issued, not yet waited for
+    int cur = -1, slot = 0;
+    bool fast = false, ok = true;
+    // item -> (level, band column) within the current case
+    auto geo = [&](int it, int &lvl, int &b) {
+        const int local = it - (int)sc.col0;
+        lvl = local / sc.g.nbx;
+        b = local - lvl * sc.g.nbx;
+    };
+    // thread 0: the P-side column of item `it` into staging buffer s
+    auto issue = [&](int it, int s) {
+        int lvl, b;
+        geo(it, lvl, b);
+        const int col = sc.xband[b].y;
+        if (col < 0) return;
+        const int nly = sc.g.nly;
+        const uint32_t colb = (uint32_t)nly * 8u;
+        float2 *dst = s ? stg1 : stg0;
+        const uint32_t ba = smem_u32(&bar[s]);
+        const size_t bp = ((size_t)lvl * sc.g.nlx + col) * nly;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ba), "r"(2u * colb) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(dst)),
+                     "l"(sc.Xp + bp), "r"(colb), "r"(ba)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(dst + nly)),
+                     "l"(sc.Xq + bp), "r"(colb), "r"(ba)
+                     : "memory");
+        pend[s] = true;
+    };
+    __syncthreads();
+    for (int it = lo; it < hi && ok; ++it) {
+        const int k = col_case[it];
+        if (k != cur) {
+            __syncthreads();  // the previous item is done with sc, the twiddles and the staging
+            load_case(&sc, cases + k);
+            __syncthreads();
+            cur = k;
+            const int n = sc.ply.n, nly = sc.g.nly;
+            fast = !((n | nly) & 1) && n <= maxn && nly <= maxnly &&
+                   !((((uintptr_t)sc.Xp) | ((uintptr_t)sc.Xq)) & 15);
+            if (fast) {
+                for (int i = threadIdx.x; i < n; i += blockDim.x) stw[i] = sc.twy[i];
+                if (threadIdx.x == 0) issue(it, slot);
+            }
+            __syncthreads();
+        }
+        int lvl, b;
+        geo(it, lvl, b);
+        if (!fast) {
+            out_col_lines<float>(sc.g, sc.ply, sc.twy, sc.xband, sc.Xp, sc.Xq, sc.dc, sc.Cb, b, 1, lvl, bufA);
+            __syncthreads();
+            continue;
+        }
+        const int4 bx = sc.xband[b];
+        // the next line of this case into the other buffer
+        if (threadIdx.x == 0 && it + 1 < hi && col_case[it + 1] == cur) issue(it + 1, slot ^ 1);
+        float2 *sp = slot ? stg1 : stg0;
+        if (bx.y >= 0) {
+            if (!block_wait(&bar[slot], ph[slot])) {
+                ok = false;
+                break;
+            }
+            ph[slot] ^= 1u;
+            if (threadIdx.x == 0) pend[slot] = false;
+        }
+        const int n = sc.ply.n;
+        col_line_from_staged(sc.g, bx, sp, sp + sc.g.nly, sc.Xp, sc.Xq, sc.dc, n, lvl, bufA);
+        float2 *res = fft_run<float2>(bufA, bufB, sc.ply, 1, stw, sc.g.out_sign);
+        float2 *o = sc.Cb + (size_t)lvl * sc.g.out_ny * sc.g.nbx + b;
+        for (int y = threadIdx.x; y < sc.g.out_ny; y += blockDim.x) o[(size_t)y * sc.g.nbx] = res[sc.g.py + y];
+        __syncthreads();
+        slot ^= 1;
+    }
+    if (!ok && threadIdx.x == 0) {
+        atomicExch(err, BLDFM_ERR_TIMEOUT_DEV);
+        // copies still in flight land before the block exits
+        for (int s = 0; s < 2; ++s) {
+            if (!pend[s]) continue;
+            const uint32_t a = smem_u32(&bar[s]);
+            uint32_t done = 0;
+            for (long i = 0; i < BLDFM_WAIT_POLLS && !done; ++i)
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                    "selp.u32 %0, 1, 0, p;\n\t}"
+                    : "=r"(done)
+                    : "r"(a), "r"(ph[s])
+                    : "memory");
+        }
+    }
+}
+
+// Persistent row pass, one output row at a time: CTA b takes a contiguous
+// range of items (item = one output row of one level of one case) and loads
+// the next row's band values into registers while it transforms the current
+// one; the case and its twiddles are loaded when the case changes.
+// smem: 3 maxn complex.
+__global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *__restrict__ cases,
+                                                               const int *__restrict__ row_case, int nitems, int maxn)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) BatchCase sc;
+    const int per = (nitems + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int lo = (int)blockIdx.x * per, hi = min(nitems, lo + per);
+    if (lo >= hi) return;
+    float2 *bufA = (float2 *)smem_raw, *bufB = bufA + maxn, *stw = bufB + maxn;
+    constexpr int PF = 8;  // band values per thread held in registers (rows of up to PF x 256 band columns)
+    float2 vc[PF], vn[PF];
+    int cur = -1;
+    for (int it = lo; it < hi; ++it) {
+        const int k = row_case[it];
+        if (k != cur) {
+            __syncthreads();  // the previous item is done with sc and the twiddles
+            load_case(&sc, cases + k);
+            __syncthreads();
+            cur = k;
+            for (int i = threadIdx.x; i < sc.plx.n; i += blockDim.x) stw[i] = sc.twx[i];
+            const float2 *row = sc.Cb + (size_t)(it - sc.row0) * sc.g.nbx;
+#pragma unroll
+            for (int j = 0; j < PF; ++j) {
+                const int bcol = threadIdx.x + j * (int)blockDim.x;
+                if (bcol < sc.g.nbx) vc[j] = row[bcol];
+            }
+        }
+        const int nb = sc.g.nbx, n = sc.plx.n;
+        const int local = it - (int)sc.row0;  // (level, row): rows of a case are consecutive in Cb
+        const float2 *row = sc.Cb + (size_t)local * nb;
+        // the next row of this case, in flight during this row's transform
+        const bool nxt = it + 1 < hi && row_case[it + 1] == cur;
+        if (nxt) {
+#pragma unroll
+            for (int j = 0; j < PF; ++j) {
+                const int bcol = threadIdx.x + j * (int)blockDim.x;
+                if (bcol < nb) vn[j] = row[nb + bcol];
+            }
+        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) bufA[i] = make_float2(0.f, 0.f);
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PF; ++j) {
+            const int bcol = threadIdx.x + j * (int)blockDim.x;
+            if (bcol < nb) bufA[sc.xband[bcol].x] = vc[j];
+        }
+        for (int bcol = threadIdx.x + PF * (int)blockDim.x; bcol < nb; bcol += blockDim.x)
+            bufA[sc.xband[bcol].x] = row[bcol];
+        float2 *res = fft_run<float2>(bufA, bufB, sc.plx, 1, stw, sc.g.out_sign);
+        const int lvl = local / sc.g.out_ny;
+        const int y = local - lvl * sc.g.out_ny;
+        const size_t o = ((size_t)lvl * sc.g.out_ny + y) * sc.g.out_nx;
+        for (int x = threadIdx.x; x < sc.g.out_nx; x += blockDim.x) {
+            const float2 v = res[sc.g.px + x];
+            sc.conc[o + x] = (double)v.x;
+            sc.flx[o + x] = (double)v.y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PF; ++j) vc[j] = vn[j];
+    }
+}
+
+void prepare_batch_attributes();
+
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part)
 {
     static uint64_t attr = 0;
@@ -181,10 +388,19 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
     if (part == 0 && bl.sweep_ctas > 0)
         riccati32_batch_kernel<<<bl.sweep_ctas, bl.threads, bl.sweep_smem, st>>>(bl.cases, bl.tile_case,
                                                                                  bl.cta_tiles, bl.err);
-    if (part == 1 && bl.col_ctas > 0)
-        out_cols_batch_kernel<<<bl.col_ctas, 256, bl.col_smem, st>>>(bl.cases, bl.col_case, bl.err);
-    if (part == 1 && bl.row_ctas > 0)
-        out_rows_batch_kernel<<<bl.row_ctas, 256, bl.row_smem, st>>>(bl.cases, bl.row_case);
+    if (part == 1 && bl.persist) {
+        if (bl.col_ctas > 0)
+            out_cols_persist_kernel<<<bl.col_grid, 256, bl.col_smem, st>>>(bl.cases, bl.col_case, bl.col_ctas,
+                                                                           bl.maxn_col, bl.maxnly, bl.err);
+        if (bl.row_ctas > 0)
+            out_rows_persist_kernel<<<bl.row_grid, 256, bl.row_smem, st>>>(bl.cases, bl.row_case, bl.row_ctas,
+                                                                           bl.maxn_row);
+    } else {
+        if (part == 1 && bl.col_ctas > 0)
+            out_cols_batch_kernel<<<bl.col_ctas, 256, bl.col_smem, st>>>(bl.cases, bl.col_case, bl.err);
+        if (part == 1 && bl.row_ctas > 0)
+            out_rows_batch_kernel<<<bl.row_ctas, 256, bl.row_smem, st>>>(bl.cases, bl.row_case);
+    }
     return cudaGetLastError();
 }
 
@@ -197,9 +413,22 @@ int batch_sweep_occupancy(int threads, size_t smem)
     return nb > 0 ? nb : 1;
 }
 
+// resident CTAs per SM of the persistent column (col != 0) or row transform
+int batch_xform_occupancy(int col, size_t smem)
+{
+    prepare_batch_attributes();
+    int nb = 0;
+    const cudaError_t e =
+        col ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, out_cols_persist_kernel, 256, smem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, out_rows_persist_kernel, 256, smem);
+    return e == cudaSuccess && nb > 0 ? nb : 1;
+}
+
 void prepare_batch_attributes()
 {
     cudaFuncSetAttribute(riccati32_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(out_cols_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(out_rows_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(out_cols_persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(out_rows_persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }

@@ -45,8 +45,12 @@ struct BatchLaunch {
     size_t col_smem;
     int row_ctas;
     size_t row_smem;
+    // persistent one-line transforms (col_ctas / row_ctas count items, launched
+    // on col_grid / row_grid CTAs); shared-memory sizes from the largest case
+    int persist, col_grid, row_grid, maxn_col, maxnly, maxn_row;
 };
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);
 int batch_sweep_occupancy(int threads, size_t smem);
+int batch_xform_occupancy(int col, size_t smem);
 void prepare_batch_attributes();

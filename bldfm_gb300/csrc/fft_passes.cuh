@@ -80,6 +80,91 @@ __device__ __forceinline__ void out_col_lines(const SolveGeom &g, const FftPlan 
     }
 }
 
+// Line of band column bx = (position, column of X at P, column of X at -P)
+// of level lvl, for a Hermitian-complete FP32 spectrum, from the P-side
+// column staged in shared memory (sp: Xp, sq: Xq, nly each); positions with
+// one side out of range and the zero mode read the -P side from global
+// memory.  The thread block writes the n entries of line.
+__device__ __forceinline__ void col_line_from_staged(const SolveGeom &g, const int4 bx, const float2 *sp,
+                                                     const float2 *sq, const float2 *__restrict__ Xp,
+                                                     const float2 *__restrict__ Xq, const double2 *__restrict__ dc,
+                                                     int n, int lvl, float2 *line)
+{
+    const int nly = g.nly;
+    const float h = 0.5f;
+    const int fmin = freq_min(nly), fmax = freq_max(nly);
+    {
+        if (bx.y > 0 && bx.z > 0) {
+            // both columns present and not the zero column: positions
+            // [0, fmax] and [n + fmin, n) hold mode kp = pos or pos - n (row
+            // pos or pos - n + nly); the mirror -kp is in range except at
+            // kp = fmin; position -fmin holds only the conjugate half of
+            // X(-P) at ky = fmin; every other position is zero
+            const int nlo = fmax + 1, nhi = -fmin;  // counts of the two runs
+            for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
+                const int pos = i < nlo ? i : n - nhi + (i - nlo);
+                const int r = i < nlo ? i : nly - nhi + (i - nlo);
+                const float2 p = sp[r], q = sq[r];
+                float re = p.x - q.y, im = p.y + q.x;
+                if (pos == n + fmin && -fmin > fmax) {  // kp = fmin: the mirror -fmin is out of range
+                    re = h * re;
+                    im = h * im;
+                }
+                line[pos] = make_float2(re, im);
+            }
+            for (int i = nlo + 1 + threadIdx.x; i < n - nhi; i += blockDim.x) line[i] = make_float2(0.f, 0.f);
+            if (threadIdx.x == 0) {
+                const size_t bm = ((size_t)lvl * g.nlx + bx.z) * nly + index_of_freq(fmin, nly);
+                const float2 p = Xp[bm], q = Xq[bm];
+                line[nlo] = make_float2(h * (p.x + q.y), h * (q.x - p.y));
+            }
+            return;
+        }
+#pragma unroll 4
+        for (int pos = threadIdx.x; pos < n; pos += blockDim.x) {
+            const int kp = pos <= fmax ? pos : (pos - n >= fmin ? pos - n : INT_MIN);
+            const int km = -pos >= fmin ? -pos : (n - pos <= fmax ? n - pos : INT_MIN);
+            const bool pin = bx.y >= 0 && kp != INT_MIN, min_ = bx.z >= 0 && km != INT_MIN;
+            float re = 0.f, im = 0.f;
+            if (pin && min_ && !(bx.y == 0 && kp == 0)) {
+                // mirror pair: H(P) = X(P)
+                const int r = index_of_freq(kp, nly);
+                const float2 p = sp[r], q = sq[r];
+                re = p.x - q.y;
+                im = p.y + q.x;
+            } else {
+                if (pin) {
+                    const int r = index_of_freq(kp, nly);
+                    float2 p = sp[r], q = sq[r];
+                    if (bx.y == 0 && r == 0) {
+                        const double2 dp = dc[2 * lvl], dq = dc[2 * lvl + 1];
+                        p = make_float2((float)dp.x, (float)dp.y);
+                        q = make_float2((float)dq.x, (float)dq.y);
+                    }
+                    re = h * (p.x - q.y);
+                    im = h * (p.y + q.x);
+                }
+                if (min_) {
+                    const int r = index_of_freq(km, nly);
+                    float2 p, q;
+                    if (bx.z == 0 && r == 0) {
+                        const double2 dp = dc[2 * lvl], dq = dc[2 * lvl + 1];
+                        p = make_float2((float)dp.x, (float)dp.y);
+                        q = make_float2((float)dq.x, (float)dq.y);
+                    } else {
+                        const size_t bm = ((size_t)lvl * g.nlx + bx.z) * nly;
+                        p = Xp[bm + r];
+                        q = Xq[bm + r];
+                    }
+                    re += h * (p.x + q.y);
+                    im += h * (q.x - p.y);
+                }
+            }
+            line[pos] = make_float2(re, im);
+        }
+    }
+}
+
 // out_col_lines (FP32) with its inputs staged by bulk copies.  The spectrum
 // of every solve is Hermitian-complete: each in-range mode P with -P also in
 // range holds X(-P) = conj X(P) exactly (the sweep writes the mirror), so
@@ -148,80 +233,9 @@ __device__ __forceinline__ bool out_col_lines_staged(const SolveGeom &g, const F
         }
     }
     if (__syncthreads_or(!done)) return false;
-    const float h = 0.5f;
-    const int fmin = freq_min(nly), fmax = freq_max(nly);
     for (int c = 0; c < nc; ++c) {
-        const int4 bx = xband[b0 + c];  // x = position, y = column of X at P, z = column of X at -P
-        float2 *line = bufA + (size_t)c * n;
-        const float2 *sp = bufB + (size_t)c * n, *sq = sp + nly;
-        if (bx.y > 0 && bx.z > 0) {
-            // both columns present and not the zero column: positions
-            // [0, fmax] and [n + fmin, n) hold mode kp = pos or pos - n (row
-            // pos or pos - n + nly); the mirror -kp is in range except at
-            // kp = fmin; position -fmin holds only the conjugate half of
-            // X(-P) at ky = fmin; every other position is zero
-            const int nlo = fmax + 1, nhi = -fmin;  // counts of the two runs
-            for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
-                const int pos = i < nlo ? i : n - nhi + (i - nlo);
-                const int r = i < nlo ? i : nly - nhi + (i - nlo);
-                const float2 p = sp[r], q = sq[r];
-                float re = p.x - q.y, im = p.y + q.x;
-                if (pos == n + fmin && -fmin > fmax) {  // kp = fmin: the mirror -fmin is out of range
-                    re = h * re;
-                    im = h * im;
-                }
-                line[pos] = make_float2(re, im);
-            }
-            for (int i = nlo + 1 + threadIdx.x; i < n - nhi; i += blockDim.x) line[i] = make_float2(0.f, 0.f);
-            if (threadIdx.x == 0) {
-                const size_t bm = ((size_t)lvl * g.nlx + bx.z) * nly + index_of_freq(fmin, nly);
-                const float2 p = Xp[bm], q = Xq[bm];
-                line[nlo] = make_float2(h * (p.x + q.y), h * (q.x - p.y));
-            }
-            continue;
-        }
-#pragma unroll 4
-        for (int pos = threadIdx.x; pos < n; pos += blockDim.x) {
-            const int kp = pos <= fmax ? pos : (pos - n >= fmin ? pos - n : INT_MIN);
-            const int km = -pos >= fmin ? -pos : (n - pos <= fmax ? n - pos : INT_MIN);
-            const bool pin = bx.y >= 0 && kp != INT_MIN, min_ = bx.z >= 0 && km != INT_MIN;
-            float re = 0.f, im = 0.f;
-            if (pin && min_ && !(bx.y == 0 && kp == 0)) {
-                // mirror pair: H(P) = X(P)
-                const int r = index_of_freq(kp, nly);
-                const float2 p = sp[r], q = sq[r];
-                re = p.x - q.y;
-                im = p.y + q.x;
-            } else {
-                if (pin) {
-                    const int r = index_of_freq(kp, nly);
-                    float2 p = sp[r], q = sq[r];
-                    if (bx.y == 0 && r == 0) {
-                        const double2 dp = dc[2 * lvl], dq = dc[2 * lvl + 1];
-                        p = make_float2((float)dp.x, (float)dp.y);
-                        q = make_float2((float)dq.x, (float)dq.y);
-                    }
-                    re = h * (p.x - q.y);
-                    im = h * (p.y + q.x);
-                }
-                if (min_) {
-                    const int r = index_of_freq(km, nly);
-                    float2 p, q;
-                    if (bx.z == 0 && r == 0) {
-                        const double2 dp = dc[2 * lvl], dq = dc[2 * lvl + 1];
-                        p = make_float2((float)dp.x, (float)dp.y);
-                        q = make_float2((float)dq.x, (float)dq.y);
-                    } else {
-                        const size_t bm = ((size_t)lvl * g.nlx + bx.z) * nly;
-                        p = Xp[bm + r];
-                        q = Xq[bm + r];
-                    }
-                    re += h * (p.x + q.y);
-                    im += h * (q.x - p.y);
-                }
-            }
-            line[pos] = make_float2(re, im);
-        }
+        const float2 *sp = bufB + (size_t)c * n;
+        col_line_from_staged(g, xband[b0 + c], sp, sp + nly, Xp, Xq, dc, n, lvl, bufA + (size_t)c * n);
     }
     float2 *res = fft_run<float2>(bufA, bufB, pl, nc, stw, g.out_sign);
     const int lc = 31 - __clz(ncols);  // log2 ncols

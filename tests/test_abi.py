@@ -90,3 +90,28 @@ def test_odd_modes_reference_message_through_solver():
         S(np.zeros((32, 32)), z, prof, (10.0, 10.0), 5, modes=(32, 32), precision="quad")
     with pytest.raises(IndexError):
         S(np.zeros((32, 32)), z, prof, (10.0, 10.0), 50, modes=(32, 32))
+
+
+@pytest.mark.parametrize("xform_lines", [0, 1, 2, 4])
+def test_batch_plan_sizes_without_device_cache(xform_lines):
+    """bldfm_batch_plan sizes a mixed batch on the host for every transform
+    setting (1 = the persistent one-line passes), without a device."""
+    import ctypes
+
+    lib = _lib.load()
+    keep, arr = [], (_lib.Case * 2)()
+    for k, (shape, modes, n) in enumerate([((96, 128), (128, 96), 20), ((64, 64), (64, 64), 12)]):
+        z, p = O.vertical_profiles(n, 10.0, (2.0, -1.0), ustar=0.3, mol=-50.0)
+        zz = np.ascontiguousarray(z, dtype=np.float64)
+        prof = np.ascontiguousarray(np.stack(p))
+        lv = np.array([n], dtype=np.int64)
+        keep += [zz, prof, lv]
+        c = arr[k]
+        c.desc = make_desc(shape, len(zz), (200.0, 150.0), modes, (80.0, 70.0), 0.0, True, False, None, "double",
+                           "fp32")
+        c.z_host, c.prof_host, c.levels_host, c.nlvls = zz.ctypes.data, prof.ctypes.data, lv.ctypes.data, 1
+        c.conc_dev = c.flx_dev = 256  # output addresses are only checked for presence when planning
+    opts = _lib.BatchOpts(0, 0, 0, xform_lines)
+    need = ctypes.c_int64(0)
+    assert lib.bldfm_batch_plan(arr, 2, ctypes.byref(opts), ctypes.byref(need)) == 0
+    assert need.value > 0
