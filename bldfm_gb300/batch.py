@@ -23,6 +23,14 @@ from . import _lib
 from .solver import _normalise_levels, make_desc, plan
 
 
+def _count(shape):
+    """Number of elements of a (nlvls, ny, nx) output shape."""
+    n = 1
+    for v in shape:
+        n *= int(v)
+    return n
+
+
 def _host_inputs(kw):
     z = np.ascontiguousarray(kw["z"], dtype=np.float64)
     nz = z.shape[0]
@@ -86,10 +94,10 @@ class BatchSolver:
         descs, shapes = [], []
         for kw in cases:
             z, prof, levels, lv = _host_inputs(kw)
-            key = (np.shape(kw["srf_flx"]), len(z), tuple(float(v) for v in kw["domain"]),
-                   tuple(kw.get("modes", (512, 512))), tuple(float(v) for v in kw.get("meas_pt", (0.0, 0.0))),
-                   float(np.real(kw.get("srf_bg_conc", 0.0))), bool(kw.get("footprint", False)), kw.get("halo"),
-                   kw.get("precision", "single"), lv.size)
+            dom, mp, md = kw["domain"], kw.get("meas_pt", (0.0, 0.0)), kw.get("modes", (512, 512))
+            key = (np.shape(kw["srf_flx"]), len(z), float(dom[0]), float(dom[1]), int(md[0]), int(md[1]),
+                   float(mp[0]), float(mp[1]), float(np.real(kw.get("srf_bg_conc", 0.0))),
+                   bool(kw.get("footprint", False)), kw.get("halo"), kw.get("precision", "single"), lv.size)
             hit = _DESC_CACHE.get(key)
             if hit is None:
                 d = make_desc(
@@ -104,7 +112,7 @@ class BatchSolver:
                 _DESC_CACHE[key] = hit
             descs.append((hit[0], z, prof, levels, lv))
             shapes.append(hit[1])
-        total = 2 * sum(int(np.prod(sh)) for sh in shapes)
+        total = 2 * sum(_count(sh) for sh in shapes)
         if self._out_buf is None or self._out_buf.numel() < total:
             self._out_buf = torch.empty(total, dtype=torch.float64, device=self.device)
         self.out_elems = total
@@ -112,7 +120,7 @@ class BatchSolver:
         off = 0
         for k, kw in enumerate(cases):
             d, z, prof, levels, lv = descs[k]
-            sz = int(np.prod(shapes[k]))
+            sz = _count(shapes[k])
             footprint = bool(kw.get("footprint", False))
             c = arr[k]
             c.desc = d
@@ -226,7 +234,7 @@ def _finish_batch(pending):
     results = []
     off = 0
     for kw, shape, (z, _, _, levels) in zip(cases, shapes, keep):
-        sz = int(np.prod(shape))
+        sz = _count(shape)
         conc = hn[off : off + sz].reshape(shape)
         flx = hn[off + sz : off + 2 * sz].reshape(shape)
         off += 2 * sz

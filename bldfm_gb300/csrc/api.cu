@@ -206,7 +206,16 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
     for (int i = 0; i < nz; ++i)
         if (hp.slot[i] >= 0) g.jmax = i;
     g.nsolved = solved_count(nlx, nly);
-    // output band columns: positions of frequencies [-h, h] mod nfx
+    // output band columns: positions of frequencies [-h, h] mod nfx; the map
+    // depends on (nlx, nfx) only and is memoised, like the transform plans
+    static std::mutex memo_mutex;
+    static std::map<std::pair<int, int>, std::vector<int4>> xband_memo;
+    static std::map<int, FftPlan> plan_memo;
+    std::lock_guard<std::mutex> memo_lock(memo_mutex);
+    auto xm = xband_memo.find(std::make_pair(nlx, g.nfx));
+    if (xm != xband_memo.end()) {
+        hp.xband = xm->second;
+    } else {
     hp.xband.clear();
     {
         const int f0 = freq_min(nlx), f1 = freq_max(nlx);
@@ -227,11 +236,22 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
             hp.xband.push_back(make_int4(pos, a, b, 0));
         }
     }
+    xband_memo[std::make_pair(nlx, g.nfx)] = hp.xband;
+    }
     g.nbx = (int)hp.xband.size();
-    factorize(g.nxe, hp.plx_fwd);
-    factorize(g.nye, hp.ply_fwd);
-    factorize(g.nfx, hp.plx_out);
-    factorize(g.nfy, hp.ply_out);
+    auto plan_of = [&](int n, FftPlan &p) {
+        auto it = plan_memo.find(n);
+        if (it != plan_memo.end()) {
+            p = it->second;
+            return;
+        }
+        factorize(n, p);
+        plan_memo[n] = p;
+    };
+    plan_of(g.nxe, hp.plx_fwd);
+    plan_of(g.nye, hp.ply_fwd);
+    plan_of(g.nfx, hp.plx_out);
+    plan_of(g.nfy, hp.ply_out);
     return BLDFM_OK;
 }
 
