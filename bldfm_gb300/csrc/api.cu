@@ -562,7 +562,10 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
     if ((rc = acquire_stage(dc, off_eig + al(eigb) + 256, &slt)) != BLDFM_OK) return rc;
     char *sg = (char *)slt->buf;
     timers_begin(dc);
-    hx_level_table(nz, z, prof, (double *)sg);
+    if (!f64 && g.footprint)
+        hx_level_dz_w(nz, z, prof, (double *)sg);  // the FP32 footprint reads only what the k = 0 values use
+    else
+        hx_level_table(nz, z, prof, (double *)sg);
     if (!f64) {
         if (g.iso)
             hx_level_table32_iso(nz, z, prof, g.ex, g.ey, (float *)(sg + off_lv32));
@@ -885,7 +888,10 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
         x.rpc = B.rpc;
         x.cpc = B.cpc;
         double *lv64 = (double *)(blob + B.off_lv64[k]);
-        hx_level_table(nz, c.z_host, c.prof_host, lv64);
+        if (g.footprint)
+            hx_level_dz_w(nz, c.z_host, c.prof_host, lv64);  // all the k = 0 values need (no trapezoid pass)
+        else
+            hx_level_table(nz, c.z_host, c.prof_host, lv64);
         if (g.iso)
             hx_level_table32_iso(nz, c.z_host, c.prof_host, g.ex, g.ey, (float *)(blob + B.off_lv32[k]));
         else

@@ -35,6 +35,19 @@ void hx_level_table(int nz, const double *z, const double *prof, double *lv)
     }
 }
 
+/* The two columns of hx_level_table that hx_dc_values reads (dz, column 10,
+   and the averaged 1/Kz weight, column 11), with the same arithmetic; the
+   other columns are left untouched. */
+void hx_level_dz_w(int nz, const double *z, const double *prof, double *lv)
+{
+    const double *Kz = prof + 4 * nz;
+    for (int i = 0; i < nz - 1; ++i) {
+        double *row = lv + (size_t)i * 12;
+        row[10] = z[i + 1] - z[i];
+        row[11] = 0.5 / Kz[i] + 0.5 / Kz[i + 1];
+    }
+}
+
 /* FP32 level table of the Riccati sweep, from the same per-step scalars. */
 void hx_level_table32(int nz, const double *z, const double *prof, float *lv)
 {

@@ -4,6 +4,7 @@
 extern "C" {
 #endif
 void hx_level_table(int nz, const double *z, const double *prof, double *lv);
+void hx_level_dz_w(int nz, const double *z, const double *prof, double *lv);
 void hx_level_table32(int nz, const double *z, const double *prof, float *lv);
 double hx_fftfreq_val(int n);
 void hx_eigval(int64_t m0, int64_t m1, const uint32_t *modes, int nlx, int nly, double valx, double valy,

@@ -320,7 +320,10 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     if (o > BLDFM_NOALLOC_SCRATCH_BYTES) return BLDFM_ERR_WORKSPACE;
 
     char *w = (char *)na_scratch_dev[dev];
-    hx_level_table(nz, z_host, prof_host, na_host.lv64);
+    if (d->footprint)
+        hx_level_dz_w(nz, z_host, prof_host, na_host.lv64);  // the k = 0 values read only these columns
+    else
+        hx_level_table(nz, z_host, prof_host, na_host.lv64);
     if (g.iso)
         hx_level_table32_iso(nz, z_host, prof_host, g.ex, g.ey, na_host.lv32);
     else
