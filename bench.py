@@ -804,12 +804,12 @@ def main():
     for i in range(e2e_steps):
         solve_batch(kwb[i % NB], solver=esolver)
     e2e_sync = world * B * e2e_steps / (time.perf_counter() - t)
-    # the pipelined timeseries API over the same steps (two solvers alternate)
+    # the pipelined timeseries API over the same steps (four solvers take the steps in turn)
     ssolvers = tuple(BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
-                     for _ in range(2))
+                     for _ in range(4))
     # warm: graphs of both solvers and the pinned host blocks a consumer that
     # holds one result while the next is produced keeps alive
-    warm = list(solve_stream([kwb[i % NB] for i in range(6)], solvers=ssolvers))
+    warm = list(solve_stream([kwb[i % NB] for i in range(8)], solvers=ssolvers))
     del warm
     t = time.perf_counter()
     nres = 0
@@ -893,7 +893,7 @@ def main():
                      "frac": (achieved64 / (peak64.value / 1e12)) if achieved64 else None},
             "e2e": {"value": e2e_fps, "unit": "footprints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "api": "bldfm_gb300.batch.solve_stream over the timed steps (numpy in, numpy out, "
-                           "pinned copies inside, each step's arrays fresh)",
+                           "pinned copies inside, each step's arrays fresh; four solvers in turn)",
                     "solve_batch_synchronous": e2e_sync,
                     "single_case_dropin": e2e_single},
             "roofline": {

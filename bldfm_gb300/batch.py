@@ -251,19 +251,24 @@ def _finish_batch(pending):
 def solve_stream(batches, *, solvers=None, **opts):
     """Solve an iterable of batches (each a list of keyword-argument dicts of
     ``steady_state_transport_solver``) in FP32, yielding each batch's list of
-    ``(grid, conc, flx)`` in order.  Two solvers, each with its own stream,
-    workspace and outputs, alternate: batch i + 1 is prepared and enqueued
-    before batch i is waited for, so the host work, the kernels and the
-    copies back overlap.  ``opts`` go to the two BatchSolvers."""
-    solvers = solvers or (BatchSolver(**opts), BatchSolver(**opts))
-    pending = None
+    ``(grid, conc, flx)`` in order.  The solvers (default four; each with its
+    own stream, workspace and outputs) take the batches in turn: batch i is
+    prepared and enqueued before batch i - len(solvers) + 1 is waited for, so
+    the host work, the kernels and the copies back of up to len(solvers)
+    batches overlap (with two, the copy back and the host work of a batch sit
+    in the latency the next batch has to hide).  ``opts`` go to the default
+    BatchSolvers."""
+    from collections import deque
+
+    solvers = solvers or tuple(BatchSolver(**opts) for _ in range(4))
+    ns = len(solvers)
+    pending = deque()
     for i, cases in enumerate(batches):
-        nxt = _enqueue_batch(solvers[i % 2], cases)
-        if pending is not None:
-            yield _finish_batch(pending)
-        pending = nxt
-    if pending is not None:
-        yield _finish_batch(pending)
+        pending.append(_enqueue_batch(solvers[i % ns], cases))
+        if len(pending) == ns:
+            yield _finish_batch(pending.popleft())
+    while pending:
+        yield _finish_batch(pending.popleft())
 
 
 def solve_batch(cases, *, solver=None):
