@@ -695,10 +695,10 @@ def main():
     def timed_batches(solvers, steps, warmup, stage_timing=False):
         # descriptors built once per met batch (input preparation); each timed
         # step is one bldfm_solve_batch call: level tables, k = 0 values and
-        # maps are computed from the profiles inside the call.  With two
+        # maps are computed from the profiles inside the call.  With several
         # solvers (own stream, workspace and graphs each) consecutive steps
-        # alternate between them, so one step's transforms overlap the next
-        # step's sweep; the timed region spans both streams.
+        # go to them in turn, so one step's transforms overlap the next
+        # step's sweep; the timed region spans all the streams.
         if not isinstance(solvers, (list, tuple)):
             solvers = [solvers]
         ns = len(solvers)
@@ -739,7 +739,7 @@ def main():
 
     # --- headline: batched FP32 path replayed as a CUDA graph ---
     gsolvers = [BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
-                for _ in range(2)]
+                for _ in range(4)]
     with ClockSampler(local) as clk:
         msb, _ = timed_batches(gsolvers, args.steps, args.warmup)
     fps_batch = world * B * args.steps / (msb * 1e-3)
@@ -876,7 +876,8 @@ def main():
                 "workload": WORKLOAD_NAME,
                 "footprints_per_step": B,
                 "path": "batched fp32 invariant-imbedding sweep + fp32 transforms, CUDA graph, device-resident; "
-                        "two solver streams alternate, so a step's transforms overlap the next step's sweep",
+                        "four solver streams take the steps in turn, so a step's transforms overlap the next "
+                        "step's sweep",
                 "met_batches": NB,
                 "sweep_launch": {"threads": threads, "ctas_per_sm": per_sm, "xform_lines": xlines, "autotuned": True},
                 "l2": "inputs larger than L2: a step's 16 footprints use ~170 MB of spectra and outputs",
