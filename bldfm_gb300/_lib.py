@@ -94,6 +94,25 @@ class BatchOpts(ctypes.Structure):
     ]
 
 
+class ProfileParams(ctypes.Structure):
+    """bldfm_profile_params: the arguments of one vertical_profiles evaluation."""
+
+    _fields_ = [
+        ("n", ctypes.c_int32),
+        ("closure", ctypes.c_int32),
+        ("meas_height", ctypes.c_double),
+        ("um", ctypes.c_double),
+        ("vm", ctypes.c_double),
+        ("ustar", ctypes.c_double),
+        ("z0", ctypes.c_double),
+        ("mol", ctypes.c_double),
+        ("prsc", ctypes.c_double),
+        ("domain_height", ctypes.c_double),
+        ("stretch", ctypes.c_double),
+        ("tke", ctypes.c_double),
+    ]
+
+
 class SurrogateCase(ctypes.Structure):
     """bldfm_surrogate_case: the met scalars of one surrogate footprint."""
 
@@ -175,6 +194,10 @@ _SIGS = {
     "bldfm_point_measurement": (
         ctypes.c_int,
         [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P],
+    ),
+    "bldfm_vertical_profiles_batch": (
+        ctypes.c_int,
+        [ctypes.c_int32, _P, _P, _P, ctypes.POINTER(ctypes.c_size_t), _P, _P, _P, ctypes.c_size_t, _P],
     ),
     "bldfm_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_int32),
                                                     ctypes.POINTER(ctypes.c_int64)]),

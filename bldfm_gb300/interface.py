@@ -14,17 +14,16 @@ runners replace the reference's per-case loop and process pool
 (interface.py:141-326) with the batched FP32 solver: every (tower, timestep)
 case of the call goes through ``solve_stream`` in batches of ``batch``
 cases, the FP32 invariant-imbedding sweep (relative L2 about 1e-6 against
-the exact discrete solution).  ``mode="fp64"`` runs them one by one through
-the drop-in instead.  Cases the batched solver does not take (the analytic
+the exact discrete solution); their profiles are evaluated for all cases in
+one device launch.  ``mode="fp64"`` runs the solves one by one through the
+drop-in instead.  Cases the batched solver does not take (the analytic
 branch) also go one by one.
 """
 
 import logging
 import warnings
 
-import numpy as np
-
-from .pbl_model import vertical_profiles
+from .pbl_model import vertical_profiles, vertical_profiles_batch
 from .solver import steady_state_transport_solver
 from .utils import compute_wind_fields, ideal_source
 
@@ -40,33 +39,50 @@ def _make_cache(config):
     return None
 
 
-def _case(config, tower, met_index, surface_flux):
-    """Solver keyword arguments of one (tower, timestep) case and its met step
-    (interface.py:71-134)."""
+def _profile_args(config, tower, met_index):
+    """vertical_profiles arguments of one (tower, timestep) case and its met
+    step (interface.py:71-99: z0 takes precedence over ustar)."""
     dom = config.domain
-    sol = config.solver
     met_step = config.met.get_step(met_index)
     u_wind, v_wind = compute_wind_fields(met_step["wind_speed"], met_step["wind_dir"])
+    args = dict(n=dom.nz, meas_height=tower.z_m, wind=(u_wind, v_wind), mol=met_step["mol"],
+                closure=config.solver.closure)
     z0_val = met_step.get("z0")
     if z0_val is not None:
-        z, profiles = vertical_profiles(n=dom.nz, meas_height=tower.z_m, wind=(u_wind, v_wind), z0=z0_val,
-                                        mol=met_step["mol"], closure=sol.closure)
+        args["z0"] = z0_val
     else:
-        z, profiles = vertical_profiles(n=dom.nz, meas_height=tower.z_m, wind=(u_wind, v_wind),
-                                        ustar=met_step["ustar"], mol=met_step["mol"], closure=sol.closure)
-    if surface_flux is None:
-        surface_flux = ideal_source((dom.nx, dom.ny), (dom.xmax, dom.ymax), src_loc=sol.src_loc,
-                                    shape=sol.surface_flux_shape)
+        args["ustar"] = met_step["ustar"]
+    return args, met_step
+
+
+def _source(config, surface_flux):
+    """The surface flux of the run: the given field, or the configured ideal
+    source (interface.py:101-110)."""
+    if surface_flux is not None:
+        return surface_flux
+    dom, sol = config.domain, config.solver
+    return ideal_source((dom.nx, dom.ny), (dom.xmax, dom.ymax), src_loc=sol.src_loc, shape=sol.surface_flux_shape)
+
+
+def _solver_kwargs(config, tower, z, profiles, surface_flux):
+    """Keyword arguments of steady_state_transport_solver (interface.py:112-134)."""
+    dom, sol = config.domain, config.solver
     if dom.output_levels:
         levels = dom.output_levels
     elif dom.full_output:
         levels = list(range(dom.nz + 1))
     else:
         levels = dom.nz
-    kw = dict(srf_flx=surface_flux, z=z, profiles=profiles, domain=(dom.xmax, dom.ymax), levels=levels,
-              modes=dom.modes, meas_pt=(tower.x, tower.y), footprint=sol.footprint, analytic=sol.analytic,
-              halo=dom.halo, precision=sol.precision)
-    return kw, met_step
+    return dict(srf_flx=surface_flux, z=z, profiles=profiles, domain=(dom.xmax, dom.ymax), levels=levels,
+                modes=dom.modes, meas_pt=(tower.x, tower.y), footprint=sol.footprint, analytic=sol.analytic,
+                halo=dom.halo, precision=sol.precision)
+
+
+def _case(config, tower, met_index, surface_flux):
+    """Solver keyword arguments of one (tower, timestep) case and its met step."""
+    args, met_step = _profile_args(config, tower, met_index)
+    z, profiles = vertical_profiles(**args)
+    return _solver_kwargs(config, tower, z, profiles, _source(config, surface_flux)), met_step
 
 
 def _result(grid, conc, flx, tower, met_step):
@@ -94,7 +110,12 @@ def _run_cases(config, pairs, surface_flux, mode, batch):
     """Results of (tower, met_index) pairs in order: batched FP32 through
     ``solve_stream``, or one by one through the drop-in."""
     cache = _make_cache(config)
-    cases = [(tower, i) + _case(config, tower, i, surface_flux) for tower, i in pairs]
+    # every case's profiles in one device launch, one shared surface flux
+    prof_args = [_profile_args(config, tower, i) for tower, i in pairs]
+    profs = vertical_profiles_batch([a for a, _ in prof_args])
+    src = _source(config, surface_flux)
+    cases = [(tower, i, _solver_kwargs(config, tower, z, p, src), met_step)
+             for (tower, i), (z, p), (_, met_step) in zip(pairs, profs, prof_args)]
     out = [None] * len(cases)
     todo = []
     for k, (tower, i, kw, met_step) in enumerate(cases):

@@ -128,6 +128,24 @@ int bldfm_vertical_profiles(int32_t n, double meas_height, double um, double vm,
                             double stretch, double tke, int32_t *nz_out,
                             double *z_dev, double *prof_dev, void *stream);
 
+/* Arguments of one vertical_profiles evaluation (meaning as for
+ * bldfm_vertical_profiles). */
+typedef struct bldfm_profile_params {
+    int32_t n, closure;
+    double meas_height, um, vm, ustar, z0, mol, prsc, domain_height, stretch, tke;
+} bldfm_profile_params;
+
+/* vertical_profiles for ncases parameter sets in one launch (one block per
+ * case; no reference counterpart: the reference evaluates one case per call,
+ * pbl_model.py:8-204).  nz_out[k] and zoff_out[k] (host) receive len(z) of
+ * case k and its offset in the concatenated output; *ws_bytes_out the device
+ * scratch the launch needs.  Call with z_dev == NULL to size everything.
+ * Case k's z is z_dev[zoff[k] .. + nz[k]) and its five profile rows (u, v, Kx,
+ * Ky, Kz, stride nz[k]) start at prof_dev + 5 zoff[k]. */
+int bldfm_vertical_profiles_batch(int32_t ncases, const bldfm_profile_params *params, int32_t *nz_out,
+                                  int64_t *zoff_out, size_t *ws_bytes_out, double *z_dev, double *prof_dev,
+                                  void *ws_dev, size_t ws_bytes, void *stream);
+
 /* Per-stage CUDA-event timers of bldfm_solve on the current device (no
  * counterpart in the reference, which only times whole runs with time.time,
  * runs/manuscript/low_level/comparison_analytic.py:43-49).  When enabled,

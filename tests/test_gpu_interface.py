@@ -38,3 +38,17 @@ def test_timeseries_with_cache_enabled():
     cfg.met.wind_dir = [225.0, 225.0]
     res = interface.run_bldfm_timeseries(cfg, cfg.towers[0])
     np.testing.assert_array_equal(res[0]["flx"], res[1]["flx"])
+
+
+def test_vertical_profiles_batch_equals_single_calls():
+    from bldfm_gb300.pbl_model import vertical_profiles, vertical_profiles_batch
+
+    cases = [dict(n=16, meas_height=10.0, wind=(2.0, -1.0), ustar=0.3, mol=-50.0),
+             dict(n=40, meas_height=25.0, wind=(-3.0, 0.5), z0=0.1, mol=120.0, closure="MOSTM"),
+             dict(n=24, meas_height=6.0, wind=(1.0, 1.0), ustar=0.2, mol=1e9, closure="CONSTANT"),
+             dict(n=32, meas_height=15.0, wind=(4.0, 0.0), ustar=0.35, closure="OAAHOC", tke=0.8)]
+    for (zb, pb), kw in zip(vertical_profiles_batch(cases), cases):
+        z, p = vertical_profiles(**kw)
+        np.testing.assert_array_equal(zb, z)
+        for a, b in zip(pb, p):
+            np.testing.assert_array_equal(a, b)

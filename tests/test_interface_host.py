@@ -15,6 +15,7 @@ def stubbed(monkeypatch):
 
     seen = []
     monkeypatch.setattr(interface, "vertical_profiles", O.vertical_profiles)
+    monkeypatch.setattr(interface, "vertical_profiles_batch", lambda cases: [O.vertical_profiles(**c) for c in cases])
 
     def fake_solver(**kw):
         seen.append(("single", kw))
