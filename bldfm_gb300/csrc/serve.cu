@@ -103,29 +103,7 @@ __global__ void sur_spectra_kernel(const SolveGeom g, const uint32_t *__restrict
 }
 
 // ---------------------------------------------------------------------------
-// Fused serving kernel: features -> MLP -> spectra for 128 modes per tile,
-// one persistent CTA of 512 threads per SM.  All four matrix layers run on
-// the tensor cores (tcgen05.mma, M = 128, FP32 accumulators in TMEM); the
-// epilogues (bias + GELU) and the 256 -> 4 output layer run on the CUDA cores
-// in FP32.
-//
-// Input layer in BF16 at FP32 accuracy: x = xh + xl and W0 = wh + wl split
-// into BF16 parts, K = 32 columns [xh | xl | xh | 0] x [wh | wh | wl | 0]
-// give x.W0 up to the xl.wl term (relative 2^-16).
-//
-// Overlap of tensor cores and epilogues: every layer's 256 outputs are two
-// N = 128 halves with their own accumulator (TMEM columns 0 and 128) and
-// their own completion barrier.  The epilogue of half 0 writes the low K half
-// of the next layer's activations (BF16 pairs, in TMEM: the A operand of the
-// next MMAs) while the tensor cores finish half 1; the next layer's first
-// quarter MMA (half 0, low K) then runs during the epilogue of half 1.  The
-// activations rotate through three K-half TMEM buffers so that no buffer is
-// rewritten while an MMA reads it.  The hidden weights stream through shared
-// memory as four 32 KB quarters (N half x K half); a quarter is reloaded with
-// the next layer's as soon as the MMAs reading it have completed.  Every
-// mbarrier wait is bounded; on a timeout the kernel records
-// BLDFM_ERR_TIMEOUT, waits (bounded) for its own copies and MMAs in flight,
-// frees TMEM and returns.
+// Fused serving kernel (sur_serve_kernel) and its helpers
 // ---------------------------------------------------------------------------
 #define SV_K0 32     // K of the split input layer
 #define SV_WARPS 8  // epilogue warps: 2 per TMEM lane quarter, each 2 x 32 columns of a half
@@ -237,25 +215,11 @@ __device__ __forceinline__ void sv_features(const SurCase &c, int64_t tile, int 
     *(uint4 *)(A0 + tc_core_offset(r, 24, SV_K0) / 2) = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// hidden-layer epilogue of 32 accumulator columns of this thread's row:
-// bias, GELU in f32x2 lanes, BF16 pairs into 16 activation columns
-__device__ __forceinline__ void sv_epilogue_hidden(uint32_t td, uint32_t ta, const float *bias)
-{
-    float v[32];
-    tc_ld32(td, v);
-    uint32_t w[16];
-#pragma unroll
-    for (int p = 0; p < 16; ++p) {
-        const float2 g = gelu2_bias(make_float2(v[2 * p], v[2 * p + 1]), *(const float2 *)&bias[2 * p]);
-        w[p] = pack_bf16x2(g.x, g.y);
-    }
-    tc_st16(ta, w);
-}
-
-// the same for two 32-column groups of the half (accumulator columns td0,
-// td1), both TMEM loads in flight together; when bar0 is given, the first
-// group's activations are announced on it (one arrival per warp) before the
-// second group is computed
+// hidden-layer epilogue of two 32-column groups of this thread's row
+// (accumulator columns td0, td1, both TMEM loads in flight together): bias,
+// GELU in f32x2 lanes, BF16 pairs into 16 activation columns each (ta0,
+// ta1); when bar0 is given, the first group's activations are announced on
+// it (one arrival per warp) before the second group is computed
 __device__ __forceinline__ void sv_epilogue_hidden2(uint32_t td0, uint32_t td1, uint32_t ta0, uint32_t ta1,
                                                     const float *bias0, const float *bias1, uint64_t *bar0)
 {
