@@ -41,7 +41,7 @@ __device__ __forceinline__ void load_case(BatchCase *dst, const BatchCase *src)
 // one case (two per thread, sharing the level-table loads).  The case's level
 // table is brought into shared memory by one bulk copy whenever the case
 // changes (the mbarrier flips phase each time; every wait is bounded).
-__global__ void __launch_bounds__(256, 4) riccati32_batch_kernel(const BatchCase *__restrict__ cases,
+__global__ void __launch_bounds__(256, BATCH_MODES_PER_THREAD == 2 ? 4 : 2) riccati32_batch_kernel(const BatchCase *__restrict__ cases,
                                                               const int *__restrict__ tile_case,
                                                               const int64_t *__restrict__ cta_tiles, int *err)
 {
@@ -109,20 +109,27 @@ __global__ void __launch_bounds__(256, 4) riccati32_batch_kernel(const BatchCase
         }
         const int L = sc.g.nz - 1;
         const int *s_slot = (const int *)(s_lv + (size_t)L * BLDFM_LV32);
-        // a tile is 2 blockDim.x modes: thread modes m0 and m0 + blockDim.x
+        // a tile is BATCH_MODES_PER_THREAD blockDim.x modes: thread modes
+        // m0 + u blockDim.x, u < BATCH_MODES_PER_THREAD
         const int64_t m0 = (t - sc.tile0) * BATCH_MODES_PER_THREAD * (int64_t)blockDim.x + threadIdx.x;
-        const int64_t m1 = m0 + blockDim.x;
         if (m0 < sc.g.nsolved && sc.g.nsnap > 0) {
-            const int64_t mb = m1 < sc.g.nsolved ? m1 : -1;
+            int64_t mm[BATCH_MODES_PER_THREAD];
+            int nvalid = 0;
+#pragma unroll
+            for (int u = 0; u < BATCH_MODES_PER_THREAD; ++u) {
+                mm[u] = m0 + (int64_t)u * blockDim.x;
+                if (mm[u] < sc.g.nsolved) nvalid = u + 1;
+            }
             if (sc.g.nsnap == 1) {
                 if (sc.g.iso)
-                    ricc_mode_pair<true>(sc.g, s_lv, sc.modes, sc.q0, sc.Xp, sc.Xq, sc.ax, sc.ay, m0, mb);
+                    ricc_modes_packed<true, BATCH_MODES_PER_THREAD / 2>(sc.g, s_lv, sc.modes, sc.q0, sc.Xp, sc.Xq,
+                                                                       sc.ax, sc.ay, mm, nvalid);
                 else
-                    ricc_mode_pair<false>(sc.g, s_lv, sc.modes, sc.q0, sc.Xp, sc.Xq, sc.ax, sc.ay, m0, mb);
+                    ricc_modes_packed<false, BATCH_MODES_PER_THREAD / 2>(sc.g, s_lv, sc.modes, sc.q0, sc.Xp, sc.Xq,
+                                                                        sc.ax, sc.ay, mm, nvalid);
             } else {
-                for (int u = 0; u < 2; ++u) {
-                    const int64_t m = u == 0 ? m0 : mb;
-                    if (m < 0) break;
+                for (int u = 0; u < nvalid; ++u) {
+                    const int64_t m = mm[u];
                     if (sc.g.iso)
                         ricc_mode<true, false>(sc.g, s_lv, s_slot, sc.modes, sc.q0, sc.scratch, sc.Xp, sc.Xq, sc.ax,
                                                sc.ay, m);

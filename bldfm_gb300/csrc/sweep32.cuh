@@ -333,94 +333,129 @@ __device__ __forceinline__ void pflux_step(PCplx &Q, const PCplx R, const PCplx 
     Q.re = qr;
 }
 
-// Two solved modes per thread with one output level (SINGLE): the same
+// 2 NP solved modes per thread with one output level (SINGLE): the same
 // arithmetic per mode as ricc_mode<ISO, true>, with the level-table row and
-// the loop control shared by the two recursions, which run in the two lanes
-// of the packed f32x2 operations.  mb < 0: the
-// second slot repeats ma and writes nothing.
+// the loop control shared by the recursions, which run in the two lanes of
+// NP independent chains of packed f32x2 operations.  Slots u >= nvalid
+// repeat mode m[0] and write nothing.  The mode's indices are unpacked again
+// for the final writes rather than held in registers through the sweep.
+template <bool ISO, int NP>
+__device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const float *__restrict__ s_lv,
+                                                  const uint32_t *__restrict__ modes,
+                                                  const float2 *__restrict__ q0spec, float2 *__restrict__ Xp,
+                                                  float2 *__restrict__ Xq, float ax, float ay, const int64_t *m,
+                                                  int nvalid)
+{
+    constexpr int NM = 2 * NP;
+    const int L = g.nz - 1;
+    const int jmax = g.jmax;
+    PStep<ISO> ps[NP];
+    PCplx PR[NP];
+#pragma unroll
+    for (int h = 0; h < NP; ++h) {
+        StepCoef<ISO> sc[2];
+        float2 R[2];
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const int u = 2 * h + l;
+            int r, c;
+            bool paired;
+            unpack_mode(modes[m[u < nvalid ? u : 0]], r, c, paired);
+            const float lx = ax * (float)freq_of_index(c, g.nlx), ly = ay * (float)freq_of_index(r, g.nly);
+            sc[l].init(lx, ly, g.ex, g.ey);
+            const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
+                                         fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+            const float2 eg = csqrt_f(w);
+            const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+            const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
+            R[l] = make_float2(ke.x * inv, -ke.y * inv);
+        }
+        ps[h].init(sc[0], sc[1]);
+        PR[h] = {make_float2(R[0].x, R[1].x), make_float2(R[0].y, R[1].y)};
+    }
+    int i = L - 1;
+    for (; i >= jmax; --i) {
+        const float *lv = s_lv + (size_t)i * BLDFM_LV32;
+        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+            PCplx a, b, cc;
+            ps[h].eval_row(r0, r1, r2, a, b, cc);
+            pricc_step(PR[h], a, b, cc);
+        }
+    }
+    PCplx Rj[NP], PQ[NP];
+    int E[NM];
+#pragma unroll
+    for (int h = 0; h < NP; ++h) {
+        Rj[h] = PR[h];
+        PQ[h] = {make_float2(1.f, 1.f), make_float2(0.f, 0.f)};
+        E[2 * h] = E[2 * h + 1] = 0;
+    }
+    int cnt = 0;
+    for (; i >= 0; --i) {
+        const float *lv = s_lv + (size_t)i * BLDFM_LV32;
+        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+            PCplx a, b, cc;
+            ps[h].eval_row(r0, r1, r2, a, b, cc);
+            pricc_step(PR[h], a, b, cc);
+            pflux_step(PQ[h], PR[h], a, cc);
+        }
+        if (++cnt == 8) {
+            cnt = 0;
+#pragma unroll
+            for (int h = 0; h < NP; ++h) {
+                float2 q0 = make_float2(PQ[h].re.x, PQ[h].im.x), q1 = make_float2(PQ[h].re.y, PQ[h].im.y);
+                renorm(q0, E[2 * h]);
+                renorm(q1, E[2 * h + 1]);
+                PQ[h].re = make_float2(q0.x, q1.x);
+                PQ[h].im = make_float2(q0.y, q1.y);
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < NM; ++u) {
+        if (u >= nvalid) break;
+        const int h = u >> 1;
+        const float2 Q = (u & 1) ? make_float2(PQ[h].re.y, PQ[h].im.y) : make_float2(PQ[h].re.x, PQ[h].im.x);
+        const float2 Rju = (u & 1) ? make_float2(Rj[h].re.y, Rj[h].im.y) : make_float2(Rj[h].re.x, Rj[h].im.x);
+        int r, c;
+        bool paired;
+        unpack_mode(modes[m[u]], r, c, paired);
+        const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
+        const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2((float)g.q0dc_fp, 0.f);
+        float2 sh = make_float2(1.f, 0.f);
+        if (g.do_shift) {
+            const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
+            float sn, cs;
+            sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
+            sh = make_float2(cs, sn);
+        }
+        const float2 ratio = make_float2(ldexpf(Q.x, E[u]), ldexpf(Q.y, E[u]));
+        float2 q = fc_mul(q0, ratio);
+        float2 p = fc_mul(Rju, q);
+        p = fc_mul(p, sh);
+        q = fc_mul(q, sh);
+        Xp[spec_idx(g, 0, r, c)] = p;
+        Xq[spec_idx(g, 0, r, c)] = q;
+        if (paired) {
+            const int rm = index_of_freq(-ky, g.nly);
+            const int cm = index_of_freq(-kx, g.nlx);
+            Xp[spec_idx(g, 0, rm, cm)] = make_float2(p.x, -p.y);
+            Xq[spec_idx(g, 0, rm, cm)] = make_float2(q.x, -q.y);
+        }
+    }
+}
+
+// Two solved modes per thread (ma and, if mb >= 0, mb) in one packed chain.
 template <bool ISO>
 __device__ __forceinline__ void ricc_mode_pair(const SolveGeom &g, const float *__restrict__ s_lv,
                                                const uint32_t *__restrict__ modes,
                                                const float2 *__restrict__ q0spec, float2 *__restrict__ Xp,
                                                float2 *__restrict__ Xq, float ax, float ay, int64_t ma, int64_t mb)
 {
-    const int L = g.nz - 1;
-    const int jmax = g.jmax;
-    const int64_t mm[2] = {ma, mb >= 0 ? mb : ma};
-    int r[2], c[2], kx[2], ky[2];
-    bool paired[2];
-    StepCoef<ISO> sc[2];
-    float2 R[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        unpack_mode(modes[mm[u]], r[u], c[u], paired[u]);
-        kx[u] = freq_of_index(c[u], g.nlx);
-        ky[u] = freq_of_index(r[u], g.nly);
-        const float lx = ax * (float)kx[u], ly = ay * (float)ky[u];
-        sc[u].init(lx, ly, g.ex, g.ey);
-        const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
-                                     fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
-        const float2 eg = csqrt_f(w);
-        const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
-        const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
-        R[u] = make_float2(ke.x * inv, -ke.y * inv);
-    }
-    // the two recursions run in the two lanes of packed f32x2 operations
-    PStep<ISO> ps;
-    ps.init(sc[0], sc[1]);
-    PCplx PR = {make_float2(R[0].x, R[1].x), make_float2(R[0].y, R[1].y)};
-    int i = L - 1;
-    for (; i >= jmax; --i) {
-        const float *lv = s_lv + (size_t)i * BLDFM_LV32;
-        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
-        PCplx a, b, cc;
-        ps.eval_row(r0, r1, r2, a, b, cc);
-        pricc_step(PR, a, b, cc);
-    }
-    float2 Rj[2] = {make_float2(PR.re.x, PR.im.x), make_float2(PR.re.y, PR.im.y)};
-    PCplx PQ = {make_float2(1.f, 1.f), make_float2(0.f, 0.f)};
-    int E[2] = {0, 0};
-    int cnt = 0;
-    for (; i >= 0; --i) {
-        const float *lv = s_lv + (size_t)i * BLDFM_LV32;
-        const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
-        PCplx a, b, cc;
-        ps.eval_row(r0, r1, r2, a, b, cc);
-        pricc_step(PR, a, b, cc);
-        pflux_step(PQ, PR, a, cc);
-        if (++cnt == 8) {
-            cnt = 0;
-            float2 q0 = make_float2(PQ.re.x, PQ.im.x), q1 = make_float2(PQ.re.y, PQ.im.y);
-            renorm(q0, E[0]);
-            renorm(q1, E[1]);
-            PQ.re = make_float2(q0.x, q1.x);
-            PQ.im = make_float2(q0.y, q1.y);
-        }
-    }
-    const float2 Q[2] = {make_float2(PQ.re.x, PQ.im.x), make_float2(PQ.re.y, PQ.im.y)};
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        if (u == 1 && mb < 0) break;
-        const float2 q0 = q0spec ? q0spec[(size_t)c[u] * g.nly + r[u]] : make_float2((float)g.q0dc_fp, 0.f);
-        float2 sh = make_float2(1.f, 0.f);
-        if (g.do_shift) {
-            const uint32_t turns = (uint32_t)kx[u] * g.turn_x + (uint32_t)ky[u] * g.turn_y;
-            float sn, cs;
-            sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
-            sh = make_float2(cs, sn);
-        }
-        const float2 ratio = make_float2(ldexpf(Q[u].x, E[u]), ldexpf(Q[u].y, E[u]));
-        float2 q = fc_mul(q0, ratio);
-        float2 p = fc_mul(Rj[u], q);
-        p = fc_mul(p, sh);
-        q = fc_mul(q, sh);
-        Xp[spec_idx(g, 0, r[u], c[u])] = p;
-        Xq[spec_idx(g, 0, r[u], c[u])] = q;
-        if (paired[u]) {
-            const int rm = index_of_freq(-ky[u], g.nly);
-            const int cm = index_of_freq(-kx[u], g.nlx);
-            Xp[spec_idx(g, 0, rm, cm)] = make_float2(p.x, -p.y);
-            Xq[spec_idx(g, 0, rm, cm)] = make_float2(q.x, -q.y);
-        }
-    }
+    const int64_t m[2] = {ma, mb};
+    ricc_modes_packed<ISO, 1>(g, s_lv, modes, q0spec, Xp, Xq, ax, ay, m, mb >= 0 ? 2 : 1);
 }
