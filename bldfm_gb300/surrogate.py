@@ -13,7 +13,7 @@ box and through the FP64 solver outside it, and re-solves every
 ``spot_every``-th case with the FP64 solver, returning the solver's result
 when the surrogate's relative L2 error exceeds ``tol``.
 
-The judge of a spot check is the accurate FP64 mode (``mode="fp64r"``: the
+The reference solve of a spot check is the accurate FP64 mode (``mode="fp64r"``: the
 same discrete problem solved without the shooting method's cancellation),
 because the reference-rounding FP64 result itself carries an error of order
 eps e^{2G} in high-|k| modes that exceeds 1e-3 for tall towers on fine grids;
@@ -224,14 +224,14 @@ class Surrogate:
     by the network, out-of-box fallbacks, spot checks and their failures.
     """
 
-    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0, judge="fp64r", fallback="fp64"):
+    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0, spot_mode="fp64r", fallback="fp64"):
         self.lib = _lib.load()
         self.net = net
         self.box = dict(BOX if box is None else box)
         self.spot_every = int(spot_every)
         self.tol = float(tol)
         self.variant = int(variant)  # 0 fused kernel, 1 exact transfer (check), 2 layer by layer
-        self.judge = judge
+        self.spot_mode = spot_mode
         self.fallback = fallback
         self.device = torch.device("cuda", torch.cuda.current_device())
         self._ws = None
@@ -351,9 +351,9 @@ class Surrogate:
     def serve(self, items, batch=16):
         """Footprints of a met timeseries (keyword dicts of ``prepare``):
         in-box cases through the network in batched fused launches, every
-        ``spot_every``-th of them also through the judge (the FP64 result is
-        kept when the surrogate misses ``tol``), out-of-box cases through the
-        fallback solver.  Returns (outputs, paths): outputs[k] = (conc, flx)
+        ``spot_every``-th of them also through the ``spot_mode`` solve (the
+        FP64 result is kept when the surrogate misses ``tol``), out-of-box
+        cases through the fallback solver.  Returns (outputs, paths): outputs[k] = (conc, flx)
         (device tensors for served cases, host arrays for solver results),
         paths[k] in "surrogate", "fp64-spot", "fp64-box"."""
         out, paths = [None] * len(items), [None] * len(items)
@@ -374,14 +374,14 @@ class Surrogate:
                 self.stats["surrogate"] += 1
                 out[k], paths[k] = (c, f), "surrogate"
                 if self.spot_every > 0 and self.count % self.spot_every == 0:
-                    ref = steady_state_transport_solver(**pr["kw"], mode=self.judge)
+                    ref = steady_state_transport_solver(**pr["kw"], mode=self.spot_mode)
                     ca, fa = c.cpu().numpy(), f.cpu().numpy()
                     err = max(_rell2(ca, ref[1]), _rell2(fa, ref[2]))
                     self.stats["spot"] += 1
                     self.stats["errors"].append(err)
                     if err > self.tol:
                         self.stats["spot_fail"] += 1
-                        if self.fallback != self.judge:
+                        if self.fallback != self.spot_mode:
                             ref = steady_state_transport_solver(**pr["kw"], mode=self.fallback)
                         out[k], paths[k] = (ref[1], ref[2]), "fp64-spot"
         return out, paths
@@ -401,13 +401,13 @@ class Surrogate:
         grid = _grid(p["z"], n, srf_shape, domain)
         self.stats["surrogate"] += 1
         if self.spot_every > 0 and self.count % self.spot_every == 0:
-            ref = steady_state_transport_solver(**p["kw"], mode=self.judge)
+            ref = steady_state_transport_solver(**p["kw"], mode=self.spot_mode)
             err = max(_rell2(conc, ref[1]), _rell2(flx, ref[2]))
             self.stats["spot"] += 1
             self.stats["errors"].append(err)
             if err > self.tol:
                 self.stats["spot_fail"] += 1
-                if self.fallback != self.judge:
+                if self.fallback != self.spot_mode:
                     ref = steady_state_transport_solver(**p["kw"], mode=self.fallback)
                 return ref, "fp64-spot"
         return (grid, conc, flx), "surrogate"

@@ -2,7 +2,7 @@
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its cpu_baseline
 leg and its ``--impl reference`` arm) may import this module, and only as the
-checker or the timed CPU baseline.  The GPU product path never imports it.
+test oracle or the timed CPU baseline.  The GPU product path never imports it.
 
 This is a restatement of the reference algorithm in numpy, written so that
 every floating-point operation of the reference's numpy evaluation happens in

@@ -2,8 +2,8 @@
  * CPU oracle -- test infrastructure, not product code.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py (its cpu_baseline leg and
- * its --impl reference arm) load this file's library, and only as the checker
- * or as the timed CPU baseline.  The GPU product path never calls it.
+ * its --impl reference arm) load this file's library, and only as the test
+ * oracle or as the timed CPU baseline.  The GPU product path never calls it.
  *
  * C restatement of the reference's linear-shooting sweep and the shooting
  * combination:

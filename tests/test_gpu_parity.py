@@ -2,9 +2,9 @@
 generated by the reference) and against the CPU oracle at full size.
 
 Tolerances (relative L2 over the output fields):
-  FP64 sweep (mode="fp64"):         1e-10  (spec bar for the FP64 path)
+  FP64 sweep (mode="fp64"):         1e-10  (the FP64 path's bar)
   float32 outputs (reference FFT in complex64): 2e-6
-  FP32 Riccati sweep (mode="fp32"): 1e-3   (spec bar for the fast path)
+  FP32 Riccati sweep (mode="fp32"): 1e-3   (the fast path's bar)
 
 The reference's FP64 output depends on the host's libm (csqrt for the top
 eigenvalues, pow for the per-level scalars): its shooting combination
