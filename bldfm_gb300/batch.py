@@ -31,27 +31,49 @@ def _count(shape):
     return n
 
 
+_INT_LEVELS = {}  # one integer output level -> (int64 array, its address, index array), read-only
+
+
+def _int_level(level):
+    """The shared read-only index arrays of one integer output level."""
+    key = int(level)
+    hit = _INT_LEVELS.get(key)
+    if hit is None:
+        lv = np.array([key], dtype=np.int64)
+        idx = np.array([level])
+        lv.flags.writeable = False
+        idx.flags.writeable = False
+        if len(_INT_LEVELS) > 4096:
+            _INT_LEVELS.clear()
+        hit = (lv, lv.ctypes.data, idx)
+        _INT_LEVELS[key] = hit
+    return hit
+
+
 def _host_inputs(kw):
-    z = np.ascontiguousarray(kw["z"], dtype=np.float64)
-    nz = z.shape[0]
-    prof = None
-    try:  # five length-nz arrays: one conversion
-        prof = np.array(kw["profiles"], dtype=np.float64)
-        if prof.shape != (5, nz):
-            prof = None
+    """A case's host inputs as the library reads them: ``zp`` = z followed by
+    the five profiles (u, v, Kx, Ky, Kz), nz float64 values each, in one
+    array; the output levels as given (an index array for the grid) and as
+    int64 with its address.  Returns (zp, nz, levels, lv, lv_address)."""
+    z, p = kw["z"], kw["profiles"]
+    nz = len(z)
+    zp = None
+    try:  # five length-nz profiles: one conversion for the six arrays
+        if len(p) == 5:
+            zp = np.concatenate((z, *p), dtype=np.float64)
     except (ValueError, TypeError):
-        prof = None
-    if prof is None:  # scalars broadcast over the levels
-        prof = np.ascontiguousarray(
-            np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in kw["profiles"]])
-        )
+        zp = None
+    if zp is None or zp.shape != (6 * nz,):  # scalars broadcast over the levels
+        zz = np.ascontiguousarray(z, dtype=np.float64).ravel()
+        prof = np.stack([np.broadcast_to(np.asarray(a, dtype=np.float64), (nz,)) for a in p])
+        zp = np.concatenate((zz, prof.ravel()))
     levels = kw["levels"]
     if isinstance(levels, (int, np.integer)) and -nz <= int(levels) < nz:
-        lv = np.array([int(levels)], dtype=np.int64)
-        levels = np.array([levels])
+        lv, lvp, levels = _int_level(levels)
     else:
         levels, lv = _normalise_levels(levels, nz)
-    return z, prof, levels, lv
+        lvp = lv.ctypes.data
+    return zp, nz, levels, lv, lvp
 
 
 class BatchSolver:
@@ -91,53 +113,57 @@ class BatchSolver:
         n = len(cases)
         arr = (_lib.Case * n)()
         outs, keep = [], []
-        descs, shapes = [], []
+        metas = []
         for kw in cases:
-            z, prof, levels, lv = _host_inputs(kw)
-            dom, mp, md = kw["domain"], kw.get("meas_pt", (0.0, 0.0)), kw.get("modes", (512, 512))
-            key = (np.shape(kw["srf_flx"]), len(z), float(dom[0]), float(dom[1]), int(md[0]), int(md[1]),
-                   float(mp[0]), float(mp[1]), float(np.real(kw.get("srf_bg_conc", 0.0))),
-                   bool(kw.get("footprint", False)), kw.get("halo"), kw.get("precision", "single"), lv.size)
+            zp, nz, levels, lv, lvp = _host_inputs(kw)
+            get = kw.get
+            bg = get("srf_bg_conc", 0.0)
+            if type(bg) is not float:
+                bg = float(np.real(bg))
+            key = (np.shape(kw["srf_flx"]), nz, tuple(kw["domain"]), tuple(get("modes", (512, 512))),
+                   tuple(get("meas_pt", (0.0, 0.0))), bg, bool(get("footprint", False)), get("halo"),
+                   get("precision", "single"), lv.size)
             hit = _DESC_CACHE.get(key)
             if hit is None:
                 d = make_desc(
-                    np.shape(kw["srf_flx"]), len(z), kw["domain"], kw.get("modes", (512, 512)),
-                    kw.get("meas_pt", (0.0, 0.0)), kw.get("srf_bg_conc", 0.0), bool(kw.get("footprint", False)),
-                    False, kw.get("halo"), kw.get("precision", "single"), "fp32",
+                    np.shape(kw["srf_flx"]), nz, kw["domain"], get("modes", (512, 512)), get("meas_pt", (0.0, 0.0)),
+                    get("srf_bg_conc", 0.0), bool(get("footprint", False)), False, get("halo"),
+                    get("precision", "single"), "fp32",
                 )
                 info = plan(d, lv.size)
-                hit = (d, (lv.size, info.out_ny, info.out_nx))
+                shape = (lv.size, info.out_ny, info.out_nx)
+                hit = (d, shape, _count(shape), bool(d.footprint))
                 if len(_DESC_CACHE) > 256:
                     _DESC_CACHE.clear()
                 _DESC_CACHE[key] = hit
-            descs.append((hit[0], z, prof, levels, lv))
-            shapes.append(hit[1])
-        total = 2 * sum(_count(sh) for sh in shapes)
+            metas.append((hit, zp, nz, levels, lv, lvp))
+        total = 2 * sum(m[0][2] for m in metas)
         if self._out_buf is None or self._out_buf.numel() < total:
+            if self._out_buf is not None:  # an earlier batch on the stream may still use it
+                self.stream.synchronize()
             self._out_buf = torch.empty(total, dtype=torch.float64, device=self.device)
         self.out_elems = total
         base = self._out_buf.data_ptr()
         off = 0
-        for k, kw in enumerate(cases):
-            d, z, prof, levels, lv = descs[k]
-            sz = _count(shapes[k])
-            footprint = bool(kw.get("footprint", False))
+        for k, ((d, shape, sz, footprint), zp, nz, levels, lv, lvp) in enumerate(metas):
             c = arr[k]
             c.desc = d
-            c.srf_flx_dev = None if footprint else self._srf_dev(k, kw["srf_flx"]).data_ptr()
-            c.z_host = z.ctypes.data
-            c.prof_host = prof.ctypes.data
-            c.levels_host = lv.ctypes.data
+            if not footprint:
+                c.srf_flx_dev = self._srf_dev(k, cases[k]["srf_flx"]).data_ptr()
+            zptr = zp.ctypes.data
+            c.z_host = zptr
+            c.prof_host = zptr + 8 * nz
+            c.levels_host = lvp
             c.nlvls = lv.size
             c.conc_dev = base + 8 * off
             c.flx_dev = base + 8 * (off + sz)
             if views:
-                outs.append((self._out_buf[off : off + sz].view(shapes[k]),
-                             self._out_buf[off + sz : off + 2 * sz].view(shapes[k])))
+                ob = self._out_buf
+                outs.append((ob[off : off + sz].view(shape), ob[off + sz : off + 2 * sz].view(shape)))
             else:
-                outs.append(shapes[k])
+                outs.append(shape)
             off += 2 * sz
-            keep.append((z, prof, lv, levels))
+            keep.append((zp, nz, lv, levels))
         return arr, outs, keep
 
     def solve(self, cases):
@@ -151,18 +177,31 @@ class BatchSolver:
         lib = _lib.load()
         arr, outs, keep = prepared[:3]
         n = len(arr)
-        if len(prepared) > 3:
-            need = prepared[3]
-        else:
-            nb = ctypes.c_int64(0)
-            _lib.check(lib.bldfm_batch_plan(arr, n, self.opts, ctypes.byref(nb)), "solve_batch")
-            need = int(nb.value)
-        if self._ws is None or self._ws.numel() < need:
-            self._ws = torch.empty(int(need), dtype=torch.uint8, device=self.device)
-        st = lib.bldfm_solve_batch(
-            arr, n, self.opts, ctypes.c_void_p(self._ws.data_ptr()), ctypes.c_size_t(self._ws.numel()),
-            ctypes.c_void_p(self.stream.cuda_stream),
-        )
+
+        def run():
+            return lib.bldfm_solve_batch(
+                arr, n, self.opts, ctypes.c_void_p(self._ws.data_ptr()), ctypes.c_size_t(self._ws.numel()),
+                ctypes.c_void_p(self.stream.cuda_stream),
+            )
+
+        # with a workspace in place, solve first: the library checks the size
+        # before it touches the stream, so a batch that needs more returns
+        # ERR_WORKSPACE with nothing enqueued and is planned and retried
+        st = _lib.ERR_WORKSPACE
+        if self._ws is not None and (len(prepared) <= 3 or self._ws.numel() >= prepared[3]):
+            st = run()
+        if st == _lib.ERR_WORKSPACE:
+            if len(prepared) > 3:
+                need = prepared[3]
+            else:
+                nb = ctypes.c_int64(0)
+                _lib.check(lib.bldfm_batch_plan(arr, n, self.opts, ctypes.byref(nb)), "solve_batch")
+                need = int(nb.value)
+            if self._ws is None or self._ws.numel() < need:
+                if self._ws is not None:  # an earlier batch on the stream may still use it
+                    self.stream.synchronize()
+                self._ws = torch.empty(int(need), dtype=torch.uint8, device=self.device)
+            st = run()
         _lib.check(st, "solve_batch")
         self._keep = keep
         return outs
@@ -195,7 +234,7 @@ def _grid(z, levels, shape, domain):
     """The reference's output grid (solver.py:292-297) as read-only arrays,
     shared between cases with the same levels, shape and domain."""
     zl = np.asarray(z)[levels]
-    key = (zl.tobytes(), tuple(shape), tuple(float(v) for v in domain))
+    key = (zl.tobytes(), tuple(shape), tuple(domain))
     g = _GRID_CACHE.get(key)
     if g is None:
         ny, nx = shape
@@ -232,19 +271,26 @@ def _finish_batch(pending):
         _lib.check(st, "solve_batch")
     hn = host.numpy()
     results = []
-    off = 0
-    for kw, shape, (z, _, _, levels) in zip(cases, shapes, keep):
-        sz = _count(shape)
-        conc = hn[off : off + sz].reshape(shape)
-        flx = hn[off + sz : off + 2 * sz].reshape(shape)
-        off += 2 * sz
+    n = len(cases)
+    if n and all(sh == shapes[0] for sh in shapes):  # one geometry: views of one reshaped array
+        sq = tuple(v for v in shapes[0] if v != 1)
+        hv = hn[: 2 * n * _count(shapes[0])].reshape((n, 2) + sq)
+        pairs = [(hv[k, 0, ...], hv[k, 1, ...]) for k in range(n)]
+    else:
+        pairs, off = [], 0
+        for shape in shapes:
+            sz = _count(shape)
+            pairs.append((np.squeeze(hn[off : off + sz].reshape(shape)),
+                          np.squeeze(hn[off + sz : off + 2 * sz].reshape(shape))))
+            off += 2 * sz
+    for kw, (zp, nz, _, levels), (conc, flx) in zip(cases, keep, pairs):
         footprint = bool(kw.get("footprint", False))
-        precision = kw.get("precision", "single")
-        xm, ym = kw.get("meas_pt", (0.0, 0.0))
-        if precision == "single" and not footprint and not (xm**2 + ym**2 > 0.0):
-            conc, flx = conc.astype(np.float32), flx.astype(np.float32)
-        grid = _grid(z, levels, np.shape(kw["srf_flx"]), kw["domain"])
-        results.append((grid, np.squeeze(conc), np.squeeze(flx)))
+        if kw.get("precision", "single") == "single" and not footprint:
+            xm, ym = kw.get("meas_pt", (0.0, 0.0))
+            if not (xm**2 + ym**2 > 0.0):
+                conc, flx = conc.astype(np.float32), flx.astype(np.float32)
+        grid = _grid(zp[:nz], levels, np.shape(kw["srf_flx"]), kw["domain"])
+        results.append((grid, conc, flx))
     return results
 
 

@@ -204,7 +204,9 @@ int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases,
                      const bldfm_batch_opts *opts, int64_t *workspace_bytes);
 
 /* Enqueue a batch on stream; returns once enqueued.  The int32 at workspace
- * offset 0 holds the device status after completion. */
+ * offset 0 holds the device status after completion.  A workspace smaller
+ * than the batch needs gives BLDFM_ERR_WORKSPACE before anything is
+ * enqueued, so a caller may solve first and plan only on that status. */
 int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases,
                       const bldfm_batch_opts *opts, void *workspace,
                       size_t workspace_bytes, void *stream);
