@@ -94,3 +94,33 @@ def test_finish_single_precision_without_shift_gives_float32():
     assert c0.dtype == np.float32 and f0.dtype == np.float32
     assert c1.dtype == np.float64 and c0.shape == (6, 8)
     np.testing.assert_array_equal(f0, host[48:96].reshape(6, 8).astype(np.float32))
+
+
+def test_prepare_fills_the_case_array():
+    """prepare() with a host stand-in for the device output buffer: every
+    case's pointers address its packed inputs and its slots of the output
+    buffer (conc then flx, back to back)."""
+    import ctypes
+
+    from bldfm_gb300 import _lib
+    from bldfm_gb300.batch import BatchSolver
+
+    s = object.__new__(BatchSolver)
+    s.device, s._srf, s._keep = torch.device("cpu"), {}, None
+    s._out_buf = torch.empty(10_000, dtype=torch.float64)
+    cases = [_case(footprint=True), _case(levels=[1, 2, 3], footprint=True, domain=(90.0, 60.0))]
+    arr, shapes, keep = s.prepare(cases, views=False)
+    base = s._out_buf.data_ptr()
+    off = 0
+    for k, (c, shape, (zp, nz, lv, levels)) in enumerate(zip(arr, shapes, keep)):
+        assert shape[0] == len(lv)
+        assert c.z_host == zp.ctypes.data and c.prof_host == c.z_host + 8 * nz
+        assert c.levels_host == lv.ctypes.data and c.nlvls == len(lv)
+        assert c.desc.footprint == 1 and c.desc.mode == _lib.MODE_FP32
+        got = np.ctypeslib.as_array((ctypes.c_double * (6 * nz)).from_address(c.z_host))
+        np.testing.assert_array_equal(got, np.concatenate((cases[k]["z"], *cases[k]["profiles"])))
+        sz = int(np.prod(shape))
+        assert c.conc_dev == base + 8 * off and c.flx_dev == base + 8 * (off + sz)
+        off += 2 * sz
+    assert s.out_elems == off
+    assert arr[0].desc.xmax == 80.0 and arr[1].desc.xmax == 90.0
