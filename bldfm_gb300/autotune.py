@@ -19,7 +19,7 @@ import torch
 from . import _lib
 from .batch import BatchSolver
 
-CANDIDATES = [(256, 0), (256, 4), (256, 6), (128, 0), (128, 8), (128, 12)]
+CANDIDATES = [(256, 0), (256, 6), (128, 0), (128, 12), (128, 18)]
 XFORM_LINES = [4, 2, 1]
 
 
