@@ -373,8 +373,9 @@ __device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const floa
         ps[h].init(sc[0], sc[1]);
         PR[h] = {make_float2(R[0].x, R[1].x), make_float2(R[0].y, R[1].y)};
     }
-    int i = L - 1;
-    for (; i >= jmax; --i) {
+    // one step of the ratio recursion (above the highest output level) and
+    // one of ratio and flux product (below it), at level row i
+    auto ratio_step = [&](int i) {
         const float *lv = s_lv + (size_t)i * BLDFM_LV32;
         const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
 #pragma unroll
@@ -383,17 +384,10 @@ __device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const floa
             ps[h].eval_row(r0, r1, r2, a, b, cc);
             pricc_step(PR[h], a, b, cc);
         }
-    }
+    };
     PCplx Rj[NP], PQ[NP];
     int E[NM];
-#pragma unroll
-    for (int h = 0; h < NP; ++h) {
-        Rj[h] = PR[h];
-        PQ[h] = {make_float2(1.f, 1.f), make_float2(0.f, 0.f)};
-        E[2 * h] = E[2 * h + 1] = 0;
-    }
-    int cnt = 0;
-    for (; i >= 0; --i) {
+    auto flux_step = [&](int i) {
         const float *lv = s_lv + (size_t)i * BLDFM_LV32;
         const float4 r0 = *(const float4 *)lv, r1 = *(const float4 *)(lv + 4), r2 = *(const float4 *)(lv + 8);
 #pragma unroll
@@ -403,18 +397,35 @@ __device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const floa
             pricc_step(PR[h], a, b, cc);
             pflux_step(PQ[h], PR[h], a, cc);
         }
-        if (++cnt == 8) {
-            cnt = 0;
+    };
+    // loops unrolled by 4 and 8 (no per-step loop control)
+    int i = L - 1;
+    for (; i - 3 >= jmax; i -= 4) {
 #pragma unroll
-            for (int h = 0; h < NP; ++h) {
-                float2 q0 = make_float2(PQ[h].re.x, PQ[h].im.x), q1 = make_float2(PQ[h].re.y, PQ[h].im.y);
-                renorm(q0, E[2 * h]);
-                renorm(q1, E[2 * h + 1]);
-                PQ[h].re = make_float2(q0.x, q1.x);
-                PQ[h].im = make_float2(q0.y, q1.y);
-            }
+        for (int s = 0; s < 4; ++s) ratio_step(i - s);
+    }
+    for (; i >= jmax; --i) ratio_step(i);
+#pragma unroll
+    for (int h = 0; h < NP; ++h) {
+        Rj[h] = PR[h];
+        PQ[h] = {make_float2(1.f, 1.f), make_float2(0.f, 0.f)};
+        E[2 * h] = E[2 * h + 1] = 0;
+    }
+    // below it: groups of 8 steps, each followed by the renormalisation of
+    // the flux product; then the remaining steps (fewer than 8)
+    for (; i >= 7; i -= 8) {
+#pragma unroll
+        for (int s = 0; s < 8; ++s) flux_step(i - s);
+#pragma unroll
+        for (int h = 0; h < NP; ++h) {
+            float2 q0 = make_float2(PQ[h].re.x, PQ[h].im.x), q1 = make_float2(PQ[h].re.y, PQ[h].im.y);
+            renorm(q0, E[2 * h]);
+            renorm(q1, E[2 * h + 1]);
+            PQ[h].re = make_float2(q0.x, q1.x);
+            PQ[h].im = make_float2(q0.y, q1.y);
         }
     }
+    for (; i >= 0; --i) flux_step(i);
 #pragma unroll
     for (int u = 0; u < NM; ++u) {
         if (u >= nvalid) break;
