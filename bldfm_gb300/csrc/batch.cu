@@ -42,9 +42,10 @@ __device__ __forceinline__ void load_case(BatchCase *dst, const BatchCase *src)
 // table is brought into shared memory by one bulk copy whenever the case
 // changes (the mbarrier flips phase each time; every wait is bounded).
 // NT = blockDim.x (128 or 256).  Register budgets: 256 threads x 4 CTAs
-// (64 registers, 32 warps per SM); 128 threads x 9 CTAs (56 registers with a
-// few spills outside the step loop, 36 warps per SM), which ran the
-// 16-footprint 512^2 sweep 5% faster.
+// (64 registers, 32 warps per SM); 128 threads x 9 CTAs (56 registers and
+// 56 bytes of spill stores, 36 warps per SM), which ran the 16-footprint
+// 512^2 sweep 5% faster before the step loops were unrolled; since then the
+// two run it in about the same time and the autotuner picks.
 template <int NT>
 __global__ void __launch_bounds__(NT, NT == 128 ? 9 : 4)
     riccati32_batch_kernel(const BatchCase *__restrict__ cases, const int *__restrict__ tile_case,
