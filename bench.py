@@ -880,7 +880,8 @@ def main():
                         "four solver streams take the steps in turn, so a step's transforms overlap the next "
                         "step's sweep",
                 "met_batches": NB,
-                "sweep_launch": {"threads": threads, "ctas_per_sm": per_sm, "xform_lines": xlines, "autotuned": True},
+                "sweep_launch": {"threads": threads, "ctas_per_sm": per_sm, "xform_lines": xlines, "autotuned": True,
+                                 "tuned_for": "four solver streams (pipelined)"},
                 "l2": "inputs larger than L2: a step's 16 footprints use ~170 MB of spectra and outputs",
                 "parallelism": "replicas" if world > 1 else "single",
             },

@@ -19,7 +19,10 @@ import torch
 from . import _lib
 from .batch import BatchSolver
 
-CANDIDATES = [(256, 0), (256, 6), (128, 0), (128, 12), (128, 18)]
+# sweep launch shapes (threads per CTA, CTAs per SM; 0 = as many as fit).
+# (256, 3) and (128, 7) leave registers free on every SM for a transform CTA
+# of another stream, which the pipelined timing below can reward.
+CANDIDATES = [(256, 0), (256, 6), (128, 0), (128, 12), (128, 18), (256, 3), (128, 7)]
 XFORM_LINES = [4, 2, 1]
 
 
@@ -88,9 +91,42 @@ def _time(cases, reps, stage, **opts):
     return float(arr[stage])
 
 
-def tune(cases, reps=5, use_cache=True):
-    """Return (threads, ctas_per_sm, xform_lines) for this batch shape (timed or cached)."""
-    key = signature(cases)
+def _time_pipeline(cases, streams, nbatch, **opts):
+    """Device time of nbatch solves of the batch taken in turn by `streams`
+    solvers (own stream, workspace and graphs each), as solve_stream runs
+    them: one batch's transforms overlap the next batch's sweep."""
+    solvers = [BatchSolver(use_graph=True, **opts) for _ in range(streams)]
+    preps = [s.prepare_cached(cases) for s in solvers]
+    for s, p in zip(solvers, preps):
+        s.solve_prepared(p)  # warm: captures each solver's graph
+    torch.cuda.synchronize()
+    main = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(main)
+    for s in solvers:
+        s.stream.wait_event(e0)
+    for i in range(nbatch):
+        solvers[i % streams].solve_prepared(preps[i % streams])
+    for s in solvers:
+        done = torch.cuda.Event()
+        done.record(s.stream)
+        main.wait_event(done)
+    e1.record(main)
+    e1.synchronize()
+    if any(s.status() != 0 for s in solvers):
+        return None
+    return e0.elapsed_time(e1)
+
+
+def tune(cases, reps=5, use_cache=True, streams=4):
+    """Return (threads, ctas_per_sm, xform_lines) for this batch shape (timed or cached).
+
+    The sweep shape is timed alone first and the transform lines per CTA for
+    it.  With streams > 1 (the solve_stream default of four solvers), every
+    sweep shape is then timed again in the pipelined run, where a shape that
+    leaves room for the other streams' transforms can win although its sweep
+    alone is slower; streams=1 tunes for synchronous solve_batch calls."""
+    key = signature(cases) + ("|streams%d" % streams if streams > 1 else "")
     cache = _load() if use_cache else {}
     if key in cache and "xform_lines" in cache[key]:
         v = cache[key]
@@ -105,6 +141,14 @@ def tune(cases, reps=5, use_cache=True):
         ms = _time(cases, reps, 2, threads=best[0], ctas_per_sm=best[1], xform_lines=xl)
         if ms is not None and (best_xms is None or ms < best_xms):
             best_xl, best_xms = xl, ms
+    if streams > 1:
+        best_pms = None
+        for threads, per_sm in CANDIDATES:
+            runs = [_time_pipeline(cases, streams, 8 * streams, threads=threads, ctas_per_sm=per_sm,
+                                   xform_lines=best_xl) for _ in range(2)]
+            runs = [r for r in runs if r is not None]
+            if runs and (best_pms is None or min(runs) < best_pms):
+                best, best_pms = (threads, per_sm), min(runs)
     if use_cache:
         cache[key] = {"threads": best[0], "ctas_per_sm": best[1], "xform_lines": best_xl, "ms": best_xms}
         _save(cache)
