@@ -11,6 +11,8 @@ reference lines they follow:
 
 * :func:`steady_state_transport_solver` -- src/bldfm/solver.py:16-304
 * :func:`ivp_sweep_numpy` -- src/bldfm/solver.py:307-374 (``ivp_solver``)
+* :func:`shooting_dd_sweep` -- src/bldfm/solver.py:220-235 and 307-374 in
+  double-double arithmetic (the extended-precision yardstick)
 * :func:`vertical_profiles` -- src/bldfm/pbl_model.py:8-204
 * :func:`psi`, :func:`phi` -- src/bldfm/pbl_model.py:207-250
 * :func:`compute_wind_fields` -- src/bldfm/utils.py:7-27
@@ -59,6 +61,11 @@ def load_port():
         ]
         lib.oracle_csqrt.restype = None
         lib.oracle_csqrt.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+        lib.oracle_sweep_dd.restype = ctypes.c_int
+        lib.oracle_sweep_dd.argtypes = [
+            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+        ]
         _lib = lib
     return _lib
 
@@ -184,6 +191,66 @@ def riccati_sweep(Lx, Ly, q0, eigval, Kz_top, profiles, z, levels):
     return p, q
 
 
+def hermitian_split(nlx, nly):
+    """Representatives of the masked modes under k -> -k.
+
+    Masked modes are the (nly, nlx) fftfreq grid in row-major order without
+    (0, 0), the order of the reference's ``Lx[msk]`` (solver.py:147-162).
+    Returns (rep, src): ``rep`` indexes the modes to solve (no mirror in the
+    grid, kx > 0, or kx = 0 and ky > 0); for every other mode ``src`` is the
+    masked index of its mirror, whose transfer is the complex conjugate.
+    """
+    fx = np.rint(fftfreq(nlx, d=1.0 / nlx)).astype(np.int64)
+    fy = np.rint(fftfreq(nly, d=1.0 / nly)).astype(np.int64)
+    FX, FY = np.meshgrid(fx, fy)
+    FX, FY = FX.ravel()[1:], FY.ravel()[1:]
+    has = (-FX >= fx.min()) & (-FX <= fx.max()) & (-FY >= fy.min()) & (-FY <= fy.max())
+    rep = ~has | (FX > 0) | ((FX == 0) & (FY > 0))
+    mflat = (np.mod(-FY, nly) * nlx + np.mod(-FX, nlx)) - 1
+    src = np.where(rep, -1, mflat)
+    return np.nonzero(rep)[0], src
+
+
+def shooting_dd_sweep(Lx, Ly, q0, eigval, profiles, z, levels, nlx, nly, nthreads=0):
+    """The reference's shooting sweep and combination (solver.py:220-235,
+    307-374) in double-double arithmetic (sweep_port.c: oracle_sweep_dd).
+
+    Solves one mode of each Hermitian pair (the transfer of the mirror is the
+    conjugate) and scales the per-unit-flux transfer by the source spectrum.
+    Returns (p, q) of shape (nlvls, nmodes).
+    """
+    lib = load_port()
+    if lib is None:
+        raise RuntimeError("oracle C port not built (oracle/build_oracle.py)")
+    nz = len(z)
+    nlvls = len(np.atleast_1d(levels))
+    slot, nsnap = snapshot_schedule(levels, nz)
+    rep, src = hermitian_split(nlx, nly)
+    lxr = np.ascontiguousarray(np.asarray(Lx, dtype=np.float64)[rep])
+    lyr = np.ascontiguousarray(np.asarray(Ly, dtype=np.float64)[rep])
+    eig = np.ascontiguousarray(np.asarray(eigval, dtype=np.complex128)[rep])
+    zz = np.ascontiguousarray(z, dtype=np.float64)
+    prof = np.ascontiguousarray(np.stack([np.asarray(a, dtype=np.float64) for a in profiles]))
+    n = lxr.shape[0]
+    ps = np.zeros((max(nsnap, 1), n), dtype=np.complex128)
+    qs = np.zeros_like(ps)
+    rc = lib.oracle_sweep_dd(n, lxr.ctypes.data, lyr.ctypes.data, eig.ctypes.data, nz, zz.ctypes.data,
+                             prof.ctypes.data, slot.ctypes.data, nsnap, ps.ctypes.data, qs.ctypes.data,
+                             int(nthreads))
+    if rc != 0:
+        raise RuntimeError("oracle_sweep_dd failed")
+    nm = np.asarray(Lx).shape[0]
+    P = np.zeros((nlvls, nm), dtype=np.complex128)
+    Q = np.zeros_like(P)
+    P[:nsnap, rep] = ps[:nsnap]
+    Q[:nsnap, rep] = qs[:nsnap]
+    mir = np.nonzero(src >= 0)[0]
+    P[:, mir] = np.conj(P[:, src[mir]])
+    Q[:, mir] = np.conj(Q[:, src[mir]])
+    q0 = np.asarray(q0, dtype=np.complex128)
+    return P * q0, Q * q0
+
+
 def shooting_sweep(Lx, Ly, q0, eigval, Kz_top, profiles, z, levels, nthreads=0, use_port=True):
     """Both IVPs plus the alpha combination; returns (p, q) of shape (nlvls, nmodes)."""
     nz = len(z)
@@ -280,7 +347,10 @@ def steady_state_transport_solver(
     Same signature and return convention as the reference.  ``cache`` is
     accepted and ignored (the oracle never memoises).  ``sweep="riccati"``
     replaces the shooting sweep by :func:`riccati_sweep` (the exact solution of
-    the same discrete problem, the yardstick of the accurate modes).
+    the same discrete problem, the yardstick of the accurate modes);
+    ``sweep="shooting_dd"`` runs the reference's own shooting method in
+    double-double arithmetic (:func:`shooting_dd_sweep`), an independent
+    extended-precision evaluation of the same discrete problem.
     """
     q0 = np.asarray(srf_flx)
     p000 = srf_bg_conc
@@ -354,11 +424,16 @@ def steady_state_transport_solver(
     else:
         if sweep == "riccati":
             pm, qm = riccati_sweep(Lx[msk], Ly[msk], tfftq0[msk], eigval, Kz[nz - 1], profiles, z, levels)
-        else:
+        elif sweep == "shooting_dd":
+            pm, qm = shooting_dd_sweep(Lx[msk], Ly[msk], tfftq0[msk], eigval, profiles, z, levels, nlx, nly,
+                                       nthreads=nthreads)
+        elif sweep == "shooting":
             pm, qm = shooting_sweep(
                 Lx[msk], Ly[msk], tfftq0[msk], eigval, Kz[nz - 1], profiles, z, levels,
                 nthreads=nthreads, use_port=use_port,
             )
+        else:
+            raise ValueError("sweep must be 'shooting', 'shooting_dd' or 'riccati'")
         tfftp[:, msk] = pm
         tfftq[:, msk] = qm
         # k = 0 mode by the trapezoid rule (solver.py:237-251)
