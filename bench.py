@@ -785,6 +785,21 @@ def main():
         e32x.append(max(np.linalg.norm(ca - cr) / np.linalg.norm(cr), np.linalg.norm(fa - fr) / np.linalg.norm(fr)))
         e64x.append(max(np.linalg.norm(cb - cr) / np.linalg.norm(cr), np.linalg.norm(fb - fr) / np.linalg.norm(fr)))
 
+    # the checker, outside every timed region: each case of the step against
+    # the oracle's double-double shooting (the reference's own algorithm in
+    # extended precision); the reference-rounding FP64 results beside it
+    from oracle import bldfm_oracle as O
+    from oracle import build_oracle
+
+    build_oracle()
+    e32e, e64e = [], []
+    for (ca, fa), b, kw in zip(outs, s64, kwb[0]):
+        _, ce, fe = O.steady_state_transport_solver(**kw, sweep="shooting_dd")
+        ca, fa = ca[0].cpu().numpy(), fa[0].cpu().numpy()
+        cb, fb = b[3].cpu().numpy(), b[4].cpu().numpy()
+        e32e.append(max(np.linalg.norm(ca - ce) / np.linalg.norm(ce), np.linalg.norm(fa - fe) / np.linalg.norm(fe)))
+        e64e.append(max(np.linalg.norm(cb - ce) / np.linalg.norm(ce), np.linalg.norm(fb - fe) / np.linalg.norm(fe)))
+
     # --- learned surrogate: fused features -> tcgen05 MLP -> spectra, trained weights ---
     sur_line = surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr)
 
@@ -885,6 +900,11 @@ def main():
                 "l2": "inputs larger than L2: a step's 16 footprints use ~170 MB of spectra and outputs",
                 "parallelism": "replicas" if world > 1 else "single",
             },
+            "relL2_fp32_vs_oracle_ext": max(e32e),
+            "relL2_fp32_vs_oracle_ext_per_case": e32e,
+            "relL2_fp64_reference_rounding_vs_oracle_ext_per_case": e64e,
+            "oracle_ext": "the reference's shooting sweep and combination (src/bldfm/solver.py:220-235, 307-374) "
+                          "in double-double arithmetic on the host (oracle/sweep_port.c), every case of step 0",
             "relL2_fp32_vs_fp64": rel32,
             "relL2_fp32_vs_exact": max(e32x),
             "relL2_fp64_reference_rounding_vs_exact": max(e64x),

@@ -23,6 +23,7 @@ ERR_WORKSPACE = -7
 ERR_CUDA = -8
 ERR_TIMEOUT = -9
 ERR_NONFINITE = -10
+ERR_PROFILE = -11
 
 PREC_SINGLE = 0
 PREC_DOUBLE = 1
@@ -215,7 +216,7 @@ _SIGS = {
     ),
     "bldfm_solve_noalloc": (
         ctypes.c_int,
-        [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P],
+        [ctypes.POINTER(Desc), _P, _P, _P, _P, ctypes.c_int32, _P, _P, _P, _P],
     ),
 }
 
@@ -257,8 +258,10 @@ def check(status, what="bldfm"):
         raise IndexError("boolean index did not match indexed array: " + msg)
     if status == ERR_BROADCAST:
         raise ValueError("operands could not be broadcast together: " + msg)
-    if status in (ERR_ARG, ERR_UNSUPPORTED, ERR_WORKSPACE):
+    if status in (ERR_ARG, ERR_UNSUPPORTED, ERR_WORKSPACE, ERR_PROFILE):
         raise ValueError("%s: %s" % (what, msg))
+    if status == ERR_NONFINITE:
+        raise FloatingPointError("%s: %s" % (what, msg))
     raise RuntimeError("%s: %s (status %d)" % (what, msg, status))
 
 

@@ -13,6 +13,13 @@ reference's file format, so the two caches can share a directory.
 
 ``get``/``put``/``clear`` keep the reference's signatures, so the object can
 be passed as ``cache=`` to ``steady_state_transport_solver``.
+
+Results of a sweep other than the reference's FP64 arithmetic (``mode`` =
+"fp32" or "fp64r") differ from the reference's by up to its rounding floor, so
+they are stored under a different key: the keyword ``variant`` (the mode
+name) is hashed after the reference's inputs.  A lookup with the reference's
+key therefore never returns them, and the reference's own cache class (which
+has no ``variant``) is never handed them.
 """
 
 import collections
@@ -23,8 +30,9 @@ import numpy as np
 import torch
 
 
-def cache_key(z, profiles, domain, modes, meas_pt, halo, precision):
-    """SHA-256 hex digest of the solver inputs (cache.py:34-45)."""
+def cache_key(z, profiles, domain, modes, meas_pt, halo, precision, variant=None):
+    """SHA-256 hex digest of the solver inputs (cache.py:34-45); a
+    ``variant`` other than None / "fp64" is hashed after them."""
     h = hashlib.sha256()
     h.update(np.asarray(z).tobytes())
     for arr in profiles:
@@ -34,10 +42,14 @@ def cache_key(z, profiles, domain, modes, meas_pt, halo, precision):
     h.update(np.asarray(meas_pt).tobytes())
     h.update(str(halo).encode())
     h.update(precision.encode())
+    if variant not in (None, "fp64"):
+        h.update(b"bldfm_gb300 sweep:" + str(variant).encode())
     return h.hexdigest()
 
 
 class GreensFunctionCache:
+    supports_variant = True  # get/put accept variant= (results of a non-reference sweep)
+
     def __init__(self, cache_dir=None, max_bytes=8 << 30, device=None):
         self.cache_dir = None if cache_dir is None else Path(cache_dir)
         if self.cache_dir is not None:
@@ -51,8 +63,8 @@ class GreensFunctionCache:
         self.hits = 0
         self.misses = 0
 
-    def _compute_key(self, z, profiles, domain, modes, meas_pt, halo, precision):
-        return cache_key(z, profiles, domain, modes, meas_pt, halo, precision)
+    def _compute_key(self, z, profiles, domain, modes, meas_pt, halo, precision, variant=None):
+        return cache_key(z, profiles, domain, modes, meas_pt, halo, precision, variant)
 
     def _insert(self, key, grid, conc, flx):
         if key in self._entries:
@@ -81,9 +93,9 @@ class GreensFunctionCache:
                 return self._entries[key]
         return None
 
-    def get(self, z, profiles, domain, modes, meas_pt, halo, precision):
+    def get(self, z, profiles, domain, modes, meas_pt, halo, precision, variant=None):
         """(grid, conc, flx) as host arrays, or None on a miss."""
-        e = self._lookup(self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision))
+        e = self._lookup(self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision, variant))
         if e is None:
             self.misses += 1
             return None
@@ -91,18 +103,18 @@ class GreensFunctionCache:
         grid, c, f, dt = e
         return grid, c.cpu().numpy().astype(dt, copy=False), f.cpu().numpy().astype(dt, copy=False)
 
-    def get_device(self, z, profiles, domain, modes, meas_pt, halo, precision):
+    def get_device(self, z, profiles, domain, modes, meas_pt, halo, precision, variant=None):
         """(conc, flx) as device tensors (shared with the cache: do not modify), or None."""
-        e = self._lookup(self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision))
+        e = self._lookup(self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision, variant))
         if e is None:
             self.misses += 1
             return None
         self.hits += 1
         return e[1], e[2]
 
-    def put(self, z, profiles, domain, modes, meas_pt, halo, precision, grid, conc, flx):
+    def put(self, z, profiles, domain, modes, meas_pt, halo, precision, grid, conc, flx, variant=None):
         """Store a result (in HBM, and on disk when cache_dir is set)."""
-        key = self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision)
+        key = self._compute_key(z, profiles, domain, modes, meas_pt, halo, precision, variant)
         self._insert(key, grid, conc, flx)
         if self.cache_dir is not None:
             X, Y, Z = grid
@@ -118,3 +130,16 @@ class GreensFunctionCache:
 
     def __len__(self):
         return len(self._entries)
+
+
+def cache_args(cache, mode):
+    """(usable, extra keyword arguments) for storing results of sweep ``mode``
+    in ``cache``: the reference's arithmetic ("fp64") uses the reference's key
+    in any cache; other modes only go to caches that key them apart."""
+    if cache is None:
+        return False, {}
+    if mode == "fp64":
+        return True, {}
+    if getattr(cache, "supports_variant", False):
+        return True, {"variant": mode}
+    return False, {}

@@ -14,6 +14,7 @@
 #include "../../include/bldfm_gb300.h"
 #include "batch.h"
 #include "common.h"
+#include "geometry.h"
 #include "host_exact.h"
 #include "kernels.h"
 #include "serve.h"
@@ -60,20 +61,6 @@ void factorize(int n, FftPlan &p)
     fft_plan_finalize(p);
 }
 
-int64_t count_and_fill_modes(int nlx, int nly, std::vector<uint32_t> *out);
-
-// number of solved modes per (nlx, nly), memoised (called under g_mutex)
-int64_t solved_count(int nlx, int nly)
-{
-    static std::map<std::pair<int, int>, int64_t> memo;
-    auto key = std::make_pair(nlx, nly);
-    auto it = memo.find(key);
-    if (it != memo.end()) return it->second;
-    const int64_t n = count_and_fill_modes(nlx, nly, nullptr);
-    memo[key] = n;
-    return n;
-}
-
 int64_t count_and_fill_modes(int nlx, int nly, std::vector<uint32_t> *out)
 {
     const int fx0 = freq_min(nlx), fx1 = freq_max(nlx), fy0 = freq_min(nly), fy1 = freq_max(nly);
@@ -96,147 +83,25 @@ int64_t count_and_fill_modes(int nlx, int nly, std::vector<uint32_t> *out)
 int make_plan(const bldfm_desc *d, const double *z, const double *prof, const int64_t *levels, int nlvls,
               HostPlan &hp)
 {
-    if (!d) return BLDFM_ERR_ARG;
-    if ((d->nlx % 2) != 0 || (d->nly % 2) != 0) return BLDFM_ERR_ODD_MODES;
-    if (d->precision != BLDFM_PREC_SINGLE && d->precision != BLDFM_PREC_DOUBLE) return BLDFM_ERR_PRECISION;
-    if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nlx < 0 || d->nly < 0 || nlvls < 1) return BLDFM_ERR_ARG;
-    if (d->mode != BLDFM_MODE_FP64 && d->mode != BLDFM_MODE_FP32 && d->mode != BLDFM_MODE_FP64R) return BLDFM_ERR_ARG;
-    if (!(d->xmax > 0) || !(d->ymax > 0)) return BLDFM_ERR_ARG;
-    if (d->nz > BLDFM_MAX_NZ) return BLDFM_ERR_UNSUPPORTED;
-    SolveGeom &g = hp.g;
-    memset(&g, 0, sizeof(g));
-    g.nx = d->nx;
-    g.ny = d->ny;
-    g.nz = d->nz;
-    const double dx = d->xmax / d->nx, dy = d->ymax / d->ny;
-    const double halo = d->has_halo ? d->halo : (d->xmax > d->ymax ? d->xmax : d->ymax);
-    if (!(halo >= 0)) return BLDFM_ERR_ARG;
-    const double pxd = halo / dx, pyd = halo / dy;
-    if (pxd > 1e7 || pyd > 1e7) return BLDFM_ERR_UNSUPPORTED;
-    g.px = (int)pxd;
-    g.py = (int)pyd;
-    g.nxe = g.nx + 2 * g.px;
-    g.nye = g.ny + 2 * g.py;
-    int nlx = d->nlx, nly = d->nly;
-    if (nlx > g.nxe || nly > g.nye) {
-        nlx = g.nxe;
-        nly = g.nye;
-    }
-    if (nlx < 1 || nly < 1) return BLDFM_ERR_ARG;
-    g.nlx = nlx;
-    g.nly = nly;
-    g.dlx = (g.nxe - nlx) / 2;
-    g.dly = (g.nye - nly) / 2;
-    g.nfx = nlx + 2 * g.dlx;
-    g.nfy = nly + 2 * g.dly;
-    g.out_ny = std::min(g.nye - g.py, g.nfy) - g.py;
-    g.out_nx = std::min(g.nxe - g.px, g.nfx) - g.px;
-    if (g.out_ny < 0) g.out_ny = 0;
-    if (g.out_nx < 0) g.out_nx = 0;
-    if (nlx > 32767 || nly > 32767) return BLDFM_ERR_UNSUPPORTED;
-    if (g.nfx > BLDFM_MAX_FFT_N || g.nfy > BLDFM_MAX_FFT_N) return BLDFM_ERR_UNSUPPORTED;
-    if (!d->footprint && (g.nxe > BLDFM_MAX_FFT_N || g.nye > BLDFM_MAX_FFT_N)) return BLDFM_ERR_UNSUPPORTED;
-    hp.shape_ok = ((g.nxe - nlx) % 2 == 0) && ((g.nye - nly) % 2 == 0);
-    if (!d->footprint && !hp.shape_ok) return BLDFM_ERR_SPECTRUM_SHAPE;
-    if (d->analytic && nlvls != 1) return BLDFM_ERR_BROADCAST;
-
-    g.nlvls = nlvls;
-    g.footprint = d->footprint ? 1 : 0;
-    g.analytic = d->analytic ? 1 : 0;
-    g.precision = d->precision;
-    g.mode = d->mode;
-    g.out_sign = d->footprint ? -1 : +1;
-    g.valx = hx_fftfreq_val(nlx);
-    g.valy = hx_fftfreq_val(nly);
-    g.lx_scale = 2.0 * M_PI / dx / g.nxe;
-    g.ly_scale = 2.0 * M_PI / dy / g.nye;
-    g.inv_nxe = 1.0 / g.nxe;
-    g.inv_nye = 1.0 / g.nye;
-    // numpy evaluates ones(complex128) / nxe / nye with Smith's reciprocal-scale
-    // division, i.e. (1/nxe) * (1/nye) (solver.py:134)
-    g.q0dc_fp = (1.0 / g.nxe) * (1.0 / g.nye);
-    if (d->footprint) {
-        g.do_shift = 1;
-        g.sx = d->meas_x + halo;
-        g.sy = d->meas_y + halo;
-    } else if (d->meas_x * d->meas_x + d->meas_y * d->meas_y > 0.0) {
-        g.do_shift = 1;
-        g.sx = d->meas_x - d->xmax / 2;
-        g.sy = d->meas_y - d->ymax / 2;
-    }
-    // phase shift as fixed-point turns for the FP32 path
-    {
-        long double tx = (long double)g.lx_scale * g.valx * g.sx / (2.0L * 3.14159265358979323846264338327950288L);
-        long double ty = (long double)g.ly_scale * g.valy * g.sy / (2.0L * 3.14159265358979323846264338327950288L);
-        tx -= floorl(tx);
-        ty -= floorl(ty);
-        g.turn_x = (uint32_t)(uint64_t)llrintl(tx * 4294967296.0L);
-        g.turn_y = (uint32_t)(uint64_t)llrintl(ty * 4294967296.0L);
-    }
-    const int nz = d->nz;
-    if (z && prof) {
-        const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Ky = prof + 3 * nz, *Kz = prof + 4 * nz;
-        const double kzinv = 1.0 / Kz[nz - 1];
-        g.kz_top = Kz[nz - 1];
-        g.kxk_top = Kx[nz - 1] * kzinv;
-        g.kyk_top = Ky[nz - 1] * kzinv;
-        g.uk_top = u[nz - 1] * kzinv;
-        g.vk_top = v[nz - 1] * kzinv;
-        double ex = 1.0, ey = 0.0;
-        g.iso = hx_profiles_iso(nz, prof, &ex, &ey);
-        g.ex = (float)ex;
-        g.ey = (float)ey;
-    }
-    // snapshot schedule (solver.py:350-372): slot s = s-th distinct level in [0, nz-1]
+    const int nz = d ? std::max(d->nz, 1) : 1;
     hp.slot.assign(nz, -1);
-    int ns = 0;
-    if (levels) {
-        for (int i = 0; i < nz; ++i) {
-            for (int k = 0; k < nlvls; ++k)
-                if (levels[k] == i) {
-                    hp.slot[i] = ns++;
-                    break;
-                }
-        }
-        for (int k = 0; k < nlvls; ++k)
-            if (levels[k] < -(int64_t)nz || levels[k] >= nz) return BLDFM_ERR_ARG;
-    }
-    g.nsnap = ns;
-    g.jmax = -1;
-    for (int i = 0; i < nz; ++i)
-        if (hp.slot[i] >= 0) g.jmax = i;
-    g.nsolved = solved_count(nlx, nly);
-    // output band columns: positions of frequencies [-h, h] mod nfx; the map
-    // depends on (nlx, nfx) only and is memoised, like the transform plans
+    int rc = solve_geometry(d, z, prof, levels, nlvls, hp.g, levels ? hp.slot.data() : nullptr, &hp.shape_ok);
+    if (rc != BLDFM_OK) return rc;
+    SolveGeom &g = hp.g;
+    // output band columns and the transform plans depend on sizes only and
+    // are memoised
     static std::mutex memo_mutex;
     static std::map<std::pair<int, int>, std::vector<int4>> xband_memo;
     static std::map<int, FftPlan> plan_memo;
     std::lock_guard<std::mutex> memo_lock(memo_mutex);
-    auto xm = xband_memo.find(std::make_pair(nlx, g.nfx));
+    auto xm = xband_memo.find(std::make_pair(g.nlx, g.nfx));
     if (xm != xband_memo.end()) {
         hp.xband = xm->second;
     } else {
-    hp.xband.clear();
-    {
-        const int f0 = freq_min(nlx), f1 = freq_max(nlx);
-        const int hmax = std::max(-f0, f1);
-        std::vector<char> seen(g.nfx, 0);
-        for (int f = -hmax; f <= hmax; ++f) {
-            const int pos = ((f % g.nfx) + g.nfx) % g.nfx;
-            if (seen[pos]) continue;
-            seen[pos] = 1;
-            auto colof = [&](int p) -> int {
-                if (p <= f1) return p;  // non-negative frequencies
-                if (p >= g.nfx + f0) return p - g.nfx + nlx;
-                return -1;
-            };
-            const int a = colof(pos);
-            const int b = colof((g.nfx - pos) % g.nfx);
-            if (a < 0 && b < 0) continue;
-            hp.xband.push_back(make_int4(pos, a, b, 0));
-        }
-    }
-    xband_memo[std::make_pair(nlx, g.nfx)] = hp.xband;
+        const int f0 = freq_min(g.nlx), f1 = freq_max(g.nlx);
+        hp.xband.resize(2 * std::max(-f0, f1) + 1);
+        hp.xband.resize(band_columns(g.nlx, g.nfx, hp.xband.data()));
+        xband_memo[std::make_pair(g.nlx, g.nfx)] = hp.xband;
     }
     g.nbx = (int)hp.xband.size();
     auto plan_of = [&](int n, FftPlan &p) {
@@ -649,7 +514,7 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         }
         tmark(dc, st);  // 3: before the output transform
         CK(launch_output_fft<double>(g, hp.plx_out, hp.ply_out, twxo->d64, twyo->d64, xband, Xp, Xq, dcv,
-                                     (double2 *)(w + L.Cb), conc, flx, nullptr, st));
+                                     (double2 *)(w + L.Cb), conc, flx, err, st));
     } else {
         float2 *q0 = g.footprint ? nullptr : (float2 *)(w + L.q0);
         if (!g.footprint)
@@ -1289,6 +1154,8 @@ const char *bldfm_status_str(int s)
     case BLDFM_ERR_CUDA: return "CUDA runtime error";
     case BLDFM_ERR_TIMEOUT: return "device wait timed out";
     case BLDFM_ERR_NONFINITE: return "non-finite values in the output";
+    case BLDFM_ERR_PROFILE:
+        return "z must be strictly increasing and the profiles finite with Kz > 0 and Kx, Ky >= 0";
     default: return "unknown status";
     }
 }
@@ -1460,7 +1327,7 @@ int bldfm_solve_host(const bldfm_desc *d, const double *srf_flx_host, const doub
     int err = 0;
     CK(cudaMemcpyAsync(&err, hb.ws, sizeof(int), cudaMemcpyDeviceToHost, hb.stream));
     CK(cudaStreamSynchronize(hb.stream));
-    if (err != 0) return BLDFM_ERR_TIMEOUT;
+    if (err != 0) return err == BLDFM_ERR_NONFINITE ? BLDFM_ERR_NONFINITE : BLDFM_ERR_TIMEOUT;
     return BLDFM_OK;
 }
 

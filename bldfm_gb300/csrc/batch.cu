@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256) out_cols_batch_kernel(const BatchCase *__
 }
 
 __global__ void __launch_bounds__(256) out_rows_batch_kernel(const BatchCase *__restrict__ cases,
-                                                             const int *__restrict__ cta_case)
+                                                             const int *__restrict__ cta_case, int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(16) BatchCase sc;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) out_rows_batch_kernel(const BatchCase *__
     const int nblk = (sc.g.out_ny + sc.rpc - 1) / sc.rpc;
     const int lvl = (int)(local / nblk), yb = (int)(local - (int64_t)lvl * nblk);
     out_row_lines<float>(sc.g, sc.plx, sc.twx, sc.xband, sc.Cb, sc.conc, sc.flx, yb * sc.rpc, sc.rpc, lvl,
-                         (float2 *)smem_raw);
+                         (float2 *)smem_raw, err);
 }
 
 // Bounded wait on phase `parity` of an mbarrier by every thread of the block;
@@ -329,7 +329,8 @@ __global__ void __launch_bounds__(256) out_cols_persist_kernel(const BatchCase *
 // one; the case and its twiddles are loaded when the case changes.
 // smem: 3 maxn complex.
 __global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *__restrict__ cases,
-                                                               const int *__restrict__ row_case, int nitems, int maxn)
+                                                               const int *__restrict__ row_case, int nitems, int maxn,
+                                                               int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(16) BatchCase sc;
@@ -340,6 +341,7 @@ __global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *
     constexpr int PF = 8;  // band values per thread held in registers (rows of up to PF x 256 band columns)
     float2 vc[PF], vn[PF];
     int cur = -1;
+    bool bad = false;  // a non-finite output value seen by this thread
     for (int it = lo; it < hi; ++it) {
         const int k = row_case[it];
         if (k != cur) {
@@ -384,11 +386,13 @@ __global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *
             const float2 v = res[sc.g.px + x];
             sc.conc[o + x] = (double)v.x;
             sc.flx[o + x] = (double)v.y;
+            bad |= !(isfinite(v.x) && isfinite(v.y));
         }
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < PF; ++j) vc[j] = vn[j];
     }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
 }
 
 void prepare_batch_attributes();
@@ -412,12 +416,12 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
                                                                            bl.maxn_col, bl.maxnly, bl.err);
         if (bl.row_ctas > 0)
             out_rows_persist_kernel<<<bl.row_grid, 256, bl.row_smem, st>>>(bl.cases, bl.row_case, bl.row_ctas,
-                                                                           bl.maxn_row);
+                                                                           bl.maxn_row, bl.err);
     } else {
         if (part == 1 && bl.col_ctas > 0)
             out_cols_batch_kernel<<<bl.col_ctas, 256, bl.col_smem, st>>>(bl.cases, bl.col_case, bl.err);
         if (part == 1 && bl.row_ctas > 0)
-            out_rows_batch_kernel<<<bl.row_ctas, 256, bl.row_smem, st>>>(bl.cases, bl.row_case);
+            out_rows_batch_kernel<<<bl.row_ctas, 256, bl.row_smem, st>>>(bl.cases, bl.row_case, bl.err);
     }
     return cudaGetLastError();
 }

@@ -248,7 +248,9 @@ __device__ __forceinline__ bool out_col_lines_staged(const SolveGeom &g, const F
 }
 
 // rpc output rows starting at y0 of level lvl: places the band columns,
-// transforms along x, writes the cropped window: conc = Re, flx = Im.
+// transforms along x, writes the cropped window: conc = Re, flx = Im.  A
+// non-finite output value sets *err to BLDFM_ERR_NONFINITE_DEV (if err is not
+// null and no earlier error is recorded).  Every thread of the block calls it.
 // smem: (2 rpc + 1) n complex.
 template <typename R>
 __device__ __forceinline__ void out_row_lines(const SolveGeom &g, const FftPlan &pl,
@@ -256,7 +258,7 @@ __device__ __forceinline__ void out_row_lines(const SolveGeom &g, const FftPlan 
                                               const int4 *__restrict__ xband,
                                               const typename cvec<R>::T *__restrict__ Cin, double *__restrict__ conc,
                                               double *__restrict__ flx, int y0, int rows_per_cta, int lvl,
-                                              typename cvec<R>::T *smem)
+                                              typename cvec<R>::T *smem, int *err)
 {
     typedef typename cvec<R>::T C;
     const int n = pl.n;
@@ -292,11 +294,14 @@ __device__ __forceinline__ void out_row_lines(const SolveGeom &g, const FftPlan 
         bufA[(size_t)l * n + xband[b].x] = rows[i];
     }
     C *res = fft_run<C>(bufA, bufB, pl, nl, stw, g.out_sign);
+    bool bad = false;
     for (int i = threadIdx.x; i < nl * g.out_nx; i += blockDim.x) {
         const int l = i / g.out_nx, x = i - l * g.out_nx;
         const C v = res[(size_t)l * n + g.px + x];
         const size_t o = ((size_t)lvl * g.out_ny + y0 + l) * g.out_nx + x;
         conc[o] = (double)v.x;
         flx[o] = (double)v.y;
+        bad |= !(isfinite(v.x) && isfinite(v.y));
     }
+    if (__syncthreads_or(bad) && threadIdx.x == 0 && err) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
 }

@@ -111,6 +111,23 @@ void hx_eigval(int64_t m0, int64_t m1, const uint32_t *modes, int nlx, int nly, 
 /* 1 when Kx == Ky at every level and (u, v) keeps one direction (ex, ey):
  * then T = -K k^2 - i U (ex kx + ey ky) with U = u ex + v ey (all four
  * closures of vertical_profiles have this form). */
+/* Input validation before any work: every z and profile value finite, z
+ * strictly increasing, Kz > 0 and Kx, Ky >= 0 at every level.  The sweep
+ * divides by Kz and by the top eigenvalue (src/bldfm/solver.py:164-174,
+ * 357-364); the reference itself returns NaN fields for such inputs.
+ * Returns 0 when the inputs are valid. */
+int hx_check_profiles(int nz, const double *z, const double *prof)
+{
+    for (int i = 0; i < nz; ++i) {
+        if (!isfinite(z[i])) return 1;
+        if (i > 0 && !(z[i] > z[i - 1])) return 1;
+        for (int k = 0; k < 5; ++k)
+            if (!isfinite(prof[k * nz + i])) return 1;
+        if (!(prof[4 * nz + i] > 0.0) || prof[2 * nz + i] < 0.0 || prof[3 * nz + i] < 0.0) return 1;
+    }
+    return 0;
+}
+
 int hx_profiles_iso(int nz, const double *prof, double *ex, double *ey)
 {
     const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Ky = prof + 3 * nz;

@@ -593,12 +593,12 @@ __global__ void __launch_bounds__(256) out_rows_kernel(SolveGeom g, FftPlan pl, 
                                                        const int4 *__restrict__ xband,
                                                        const typename cvec<R>::T *__restrict__ Cin,
                                                        double *__restrict__ conc, double *__restrict__ flx,
-                                                       int rows_per_cta)
+                                                       int rows_per_cta, int *err)
 {
     typedef typename cvec<R>::T C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     out_row_lines<R>(g, pl, tw, xband, Cin, conc, flx, blockIdx.x * rows_per_cta, rows_per_cta, blockIdx.y,
-                     (C *)smem_raw);
+                     (C *)smem_raw, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -788,7 +788,7 @@ cudaError_t launch_output_fft(const SolveGeom &g, const FftPlan &plx, const FftP
     while (rpc > 1 && (int64_t)((g.out_ny + rpc - 1) / rpc) * g.nlvls < 2 * (int64_t)nsm) --rpc;
     dim3 gr((g.out_ny + rpc - 1) / rpc, g.nlvls);
     out_rows_kernel<R><<<gr, 256, (2 * (size_t)rpc + 1) * plx.n * sizeof(C), st>>>(g, plx, twx, xband, Cbuf, conc,
-                                                                                   flx, rpc);
+                                                                                   flx, rpc, err);
     return LAUNCH_CHECK();
 }
 

@@ -7,6 +7,7 @@
 #include "common.h"
 
 #define BLDFM_ERR_TIMEOUT_DEV (-9)
+#define BLDFM_ERR_NONFINITE_DEV (-10)
 
 
 cudaError_t launch_sweep64(const SolveGeom &g, const double *lvtab, const int *slot, const uint32_t *modes,

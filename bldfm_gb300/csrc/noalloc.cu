@@ -1,13 +1,14 @@
 // Allocation-free FP32 solve: bldfm_solve_noalloc (include/bldfm_gb300.h).
 //
 // Who needs it: callers that may not allocate GPU memory at solve time --
-// code running inside a CUDA stream capture, embedded or real-time hosts that
-// pre-reserve all device memory, and plugin hosts whose allocator policy
-// forbids cudaMalloc from third-party libraries.  They pass inputs and
-// outputs; every intermediate the solve needs (twiddle tables, mode list,
-// band table, level tables, spectra, transform intermediate) lives in one
-// file-scope device array of BLDFM_NOALLOC_SCRATCH_BYTES (16 MiB).  Every GPU
-// that loads this library holds that array until the process exits.
+// embedded or real-time hosts that reserve all device memory up front and
+// treat a later cudaMalloc as a failure, and plugin hosts whose allocator
+// policy forbids cudaMalloc from third-party libraries (the host owns every
+// allocation and accounts for it).  They pass inputs and outputs; every
+// intermediate the solve needs (twiddle tables, mode list, band table, level
+// tables, spectra, transform intermediate) lives in one file-scope device
+// array of BLDFM_NOALLOC_SCRATCH_BYTES (16 MiB).  Every GPU that loads this
+// library holds that array until the process exits.
 //
 // Rules of use:
 //  - The first call on a device looks up the array's device address
@@ -20,6 +21,9 @@
 //  - FP32 mode only (the FP64 mode needs host-side libm values staged in
 //    pinned memory); problems whose scratch exceeds the array are rejected
 //    with BLDFM_ERR_WORKSPACE.
+//  - The device status of the call (a bounded wait that ran out, or a
+//    non-finite output value) is copied to the caller's status word when the
+//    stream reaches the end of the call.
 // Nothing here calls cudaMalloc, cudaFree, cudaHostAlloc or any other
 // allocating routine, and the host side uses fixed static buffers.
 #include <cuda_runtime.h>
@@ -31,6 +35,7 @@
 
 #include "../../include/bldfm_gb300.h"
 #include "common.h"
+#include "geometry.h"
 #include "host_exact.h"
 #include "kernels.h"
 
@@ -77,18 +82,6 @@ void na_factorize(int n, FftPlan &p)
     fft_plan_finalize(p);
 }
 
-// solved modes of column c (Hermitian representatives plus unpaired modes),
-// in the order the workspace entry point lists them
-int na_col_count(int c, int nlx, int nly)
-{
-    const int kx = freq_of_index(c, nlx);
-    const bool nyq_x = (nlx % 2 == 0) && kx == -(nlx / 2);
-    const bool even_y = nly % 2 == 0;
-    if (kx > 0 || nyq_x) return nly;
-    if (kx == 0) return freq_max(nly) + (even_y ? 1 : 0);
-    return even_y ? 1 : 0;
-}
-
 }  // namespace
 
 // One thread per (column, row): writes the packed mode entry of solved modes.
@@ -125,16 +118,19 @@ __global__ void na_twiddle_kernel(int n, float2 *__restrict__ tw)
 
 extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_dev, const double *z_host,
                                    const double *prof_host, const int64_t *levels_host, int32_t nlvls,
-                                   double *conc_dev, double *flx_dev, void *stream)
+                                   double *conc_dev, double *flx_dev, int32_t *status_dev, void *stream)
 {
     std::lock_guard<std::mutex> lk(na_mutex);
     if (!d || !z_host || !prof_host || !levels_host || !conc_dev || !flx_dev) return BLDFM_ERR_ARG;
-    if ((d->nlx % 2) != 0 || (d->nly % 2) != 0) return BLDFM_ERR_ODD_MODES;
-    if (d->precision != BLDFM_PREC_SINGLE && d->precision != BLDFM_PREC_DOUBLE) return BLDFM_ERR_PRECISION;
-    if (d->mode != BLDFM_MODE_FP32 || d->analytic) return BLDFM_ERR_UNSUPPORTED;
-    if (d->nx < 1 || d->ny < 1 || d->nz < 2 || nlvls < 1 || !(d->xmax > 0) || !(d->ymax > 0))
-        return BLDFM_ERR_ARG;
     if (d->nz > BLDFM_MAX_NZ || nlvls > BLDFM_MAX_NZ) return BLDFM_ERR_UNSUPPORTED;
+    // geometry and input checks shared with every other entry point
+    SolveGeom g;
+    bool shape_ok = true;
+    int rc = solve_geometry(d, z_host, prof_host, levels_host, nlvls, g, na_host.slot, &shape_ok);
+    if (rc != BLDFM_OK) return rc;
+    if (d->mode != BLDFM_MODE_FP32 || d->analytic) return BLDFM_ERR_UNSUPPORTED;
+    if (d->nz < 2) return BLDFM_ERR_ARG;  // at least one sweep step
+    if (!d->footprint && !srf_flx_dev) return BLDFM_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
 
     // per-device set-up: device address of the scratch array
@@ -148,128 +144,17 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return BLDFM_ERR_CUDA;
 
-    // geometry (solver.py:94-131)
-    SolveGeom g;
-    memset(&g, 0, sizeof(g));
-    g.nx = d->nx;
-    g.ny = d->ny;
-    g.nz = d->nz;
-    const double dx = d->xmax / d->nx, dy = d->ymax / d->ny;
-    const double halo = d->has_halo ? d->halo : (d->xmax > d->ymax ? d->xmax : d->ymax);
-    if (!(halo >= 0) || halo / dx > 1e7 || halo / dy > 1e7) return BLDFM_ERR_ARG;
-    g.px = (int)(halo / dx);
-    g.py = (int)(halo / dy);
-    g.nxe = g.nx + 2 * g.px;
-    g.nye = g.ny + 2 * g.py;
-    int nlx = d->nlx, nly = d->nly;
-    if (nlx > g.nxe || nly > g.nye) {
-        nlx = g.nxe;
-        nly = g.nye;
-    }
-    if (nlx < 1 || nly < 1 || nlx > 32767 || nly > 32767) return BLDFM_ERR_ARG;
-    g.nlx = nlx;
-    g.nly = nly;
-    g.dlx = (g.nxe - nlx) / 2;
-    g.dly = (g.nye - nly) / 2;
-    g.nfx = nlx + 2 * g.dlx;
-    g.nfy = nly + 2 * g.dly;
-    g.out_ny = (g.nye - g.py < g.nfy ? g.nye - g.py : g.nfy) - g.py;
-    g.out_nx = (g.nxe - g.px < g.nfx ? g.nxe - g.px : g.nfx) - g.px;
-    if (g.out_ny < 0) g.out_ny = 0;
-    if (g.out_nx < 0) g.out_nx = 0;
-    if (g.nfx > BLDFM_MAX_FFT_N || g.nfy > BLDFM_MAX_FFT_N) return BLDFM_ERR_UNSUPPORTED;
-    if (!d->footprint) {
-        if (!srf_flx_dev) return BLDFM_ERR_ARG;
-        if (g.nxe > BLDFM_MAX_FFT_N || g.nye > BLDFM_MAX_FFT_N) return BLDFM_ERR_UNSUPPORTED;
-        if ((g.nxe - nlx) % 2 != 0 || (g.nye - nly) % 2 != 0) return BLDFM_ERR_SPECTRUM_SHAPE;
-    }
-    const int nz = g.nz;
-    for (int k = 0; k < nlvls; ++k)
-        if (levels_host[k] < -(int64_t)nz || levels_host[k] >= nz) return BLDFM_ERR_ARG;
-    g.nlvls = nlvls;
-    g.footprint = d->footprint ? 1 : 0;
-    g.precision = d->precision;
-    g.mode = BLDFM_MODE_FP32;
-    g.out_sign = d->footprint ? -1 : +1;
-    g.valx = hx_fftfreq_val(nlx);
-    g.valy = hx_fftfreq_val(nly);
-    g.lx_scale = 2.0 * M_PI / dx / g.nxe;
-    g.ly_scale = 2.0 * M_PI / dy / g.nye;
-    g.inv_nxe = 1.0 / g.nxe;
-    g.inv_nye = 1.0 / g.nye;
-    g.q0dc_fp = (1.0 / g.nxe) * (1.0 / g.nye);
-    if (d->footprint) {
-        g.do_shift = 1;
-        g.sx = d->meas_x + halo;
-        g.sy = d->meas_y + halo;
-    } else if (d->meas_x * d->meas_x + d->meas_y * d->meas_y > 0.0) {
-        g.do_shift = 1;
-        g.sx = d->meas_x - d->xmax / 2;
-        g.sy = d->meas_y - d->ymax / 2;
-    }
+    const int nz = g.nz, nlx = g.nlx, nly = g.nly, ns = g.nsnap;
+    const int64_t nsolved = g.nsolved;
     {
-        const long double pi2 = 6.283185307179586476925286766559005768L;
-        long double tx = (long double)g.lx_scale * g.valx * g.sx / pi2;
-        long double ty = (long double)g.ly_scale * g.valy * g.sy / pi2;
-        tx -= floorl(tx);
-        ty -= floorl(ty);
-        g.turn_x = (uint32_t)(uint64_t)llrintl(tx * 4294967296.0L);
-        g.turn_y = (uint32_t)(uint64_t)llrintl(ty * 4294967296.0L);
-    }
-    {
-        const double *u = prof_host, *v = prof_host + nz, *Kx = prof_host + 2 * nz, *Ky = prof_host + 3 * nz,
-                     *Kz = prof_host + 4 * nz;
-        const double kzinv = 1.0 / Kz[nz - 1];
-        g.kz_top = Kz[nz - 1];
-        g.kxk_top = Kx[nz - 1] * kzinv;
-        g.kyk_top = Ky[nz - 1] * kzinv;
-        g.uk_top = u[nz - 1] * kzinv;
-        g.vk_top = v[nz - 1] * kzinv;
-        double ex = 1.0, ey = 0.0;
-        g.iso = hx_profiles_iso(nz, prof_host, &ex, &ey);
-        g.ex = (float)ex;
-        g.ey = (float)ey;
-    }
-    int ns = 0;
-    for (int i = 0; i < nz; ++i) {
-        na_host.slot[i] = -1;
-        for (int k = 0; k < nlvls; ++k)
-            if (levels_host[k] == i) {
-                na_host.slot[i] = ns++;
-                break;
-            }
-    }
-    g.nsnap = ns;
-    g.jmax = -1;
-    for (int i = 0; i < nz; ++i)
-        if (na_host.slot[i] >= 0) g.jmax = i;
-    int64_t nsolved = 0;
-    for (int c = 0; c < nlx; ++c) {
-        na_host.colstart[c] = (int)nsolved;
-        nsolved += na_col_count(c, nlx, nly);
-    }
-    na_host.colstart[nlx] = (int)nsolved;
-    g.nsolved = nsolved;
-    // band columns of the output transform (positions of frequencies [-h, h])
-    int nbx = 0;
-    {
-        const int f0 = freq_min(nlx), f1 = freq_max(nlx);
-        const int hmax = (-f0 > f1) ? -f0 : f1;
-        for (int f = -hmax; f <= hmax; ++f) {
-            const int pos = ((f % g.nfx) + g.nfx) % g.nfx;
-            bool dup = false;
-            if (f == hmax && hmax == -f0 && ((-hmax % g.nfx) + g.nfx) % g.nfx == pos) dup = true;
-            if (dup) continue;
-            auto colof = [&](int p) -> int {
-                if (p <= f1) return p;
-                if (p >= g.nfx + f0) return p - g.nfx + nlx;
-                return -1;
-            };
-            const int a = colof(pos), b = colof((g.nfx - pos) % g.nfx);
-            if (a < 0 && b < 0) continue;
-            na_host.xband[nbx++] = make_int4(pos, a, b, 0);
+        int64_t acc = 0;
+        for (int c = 0; c < nlx; ++c) {
+            na_host.colstart[c] = (int)acc;
+            acc += solved_in_column(c, nlx, nly);
         }
+        na_host.colstart[nlx] = (int)acc;
     }
+    const int nbx = band_columns(nlx, g.nfx, na_host.xband);
     g.nbx = nbx;
     FftPlan plx_out, ply_out, plx_fwd, ply_fwd;
     na_factorize(g.nfx, plx_out);
@@ -333,6 +218,7 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
         if ((x) != cudaSuccess) return BLDFM_ERR_CUDA;                                                                 \
     } while (0)
     // pageable host -> device copies: they return once the host buffer is read
+    // (outside a stream capture)
     NA_CK(cudaMemsetAsync(w + o_err, 0, 64, st));
     NA_CK(cudaMemcpyAsync(w + o_lv64, na_host.lv64, (size_t)L * BLDFM_LV64 * 8, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(w + o_lv32, na_host.lv32, (size_t)L * BLDFM_LV32 * 4, cudaMemcpyHostToDevice, st));
@@ -375,5 +261,7 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     NA_CK(launch_output_fft<float>(g, plx_out, ply_out, (const float2 *)(w + o_twxo), (const float2 *)(w + o_twyo),
                                    (const int4 *)(w + o_xb), Xp, Xq, (const double2 *)(w + o_dc), (float2 *)(w + o_Cb),
                                    conc_dev, flx_dev, (int *)(w + o_err), st));
+    if (status_dev)
+        NA_CK(cudaMemcpyAsync(status_dev, w + o_err, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
     return BLDFM_OK;
 }

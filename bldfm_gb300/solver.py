@@ -90,14 +90,22 @@ def steady_state_transport_solver(
     the reference's rounding; ``"fp32"`` integrates the same discrete problem
     with the FP32 invariant-imbedding sweep (relative L2 error about 1e-5).
     ``cache`` is a Green's-function cache with the reference's ``get``/``put``
-    interface (src/bldfm/cache.py:19-83), consulted in footprint mode only.
+    interface (src/bldfm/cache.py:19-83), consulted in footprint mode only;
+    results of ``mode`` "fp32"/"fp64r" are stored under their own key and only
+    in caches that support it (bldfm_gb300.cache.GreensFunctionCache).
+    Raises ``ValueError`` for invalid profiles (non-finite values, z not
+    strictly increasing, Kz <= 0) and ``FloatingPointError`` when the output
+    holds non-finite values (the reference returns such fields silently).
     """
-    if cache is not None and footprint:
-        cached = cache.get(z, profiles, domain, modes, meas_pt, halo, precision)
-        if cached is not None:
-            return cached
     if mode not in _MODES:
         raise ValueError("mode must be 'fp64', 'fp32' or 'fp64r'")
+    from .cache import cache_args
+
+    use_cache, ckw = cache_args(cache if footprint else None, mode)
+    if use_cache:
+        cached = cache.get(z, profiles, domain, modes, meas_pt, halo, precision, **ckw)
+        if cached is not None:
+            return cached
     lib = _lib.load()
     shape = np.shape(srf_flx)
     if len(shape) != 2:
@@ -130,6 +138,6 @@ def steady_state_transport_solver(
     Z, Y, X = np.meshgrid(zz[levels], y, x, indexing="ij")
     grid = (np.squeeze(X), np.squeeze(Y), np.squeeze(Z))
     result = (grid, np.squeeze(conc), np.squeeze(flx))
-    if cache is not None and footprint:
-        cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result)
+    if use_cache:
+        cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result, **ckw)
     return result

@@ -42,6 +42,8 @@ extern "C" {
 #define BLDFM_ERR_CUDA -8            /* a CUDA runtime call failed */
 #define BLDFM_ERR_TIMEOUT -9         /* a bounded device wait ran out */
 #define BLDFM_ERR_NONFINITE -10      /* non-finite values detected in the output */
+#define BLDFM_ERR_PROFILE -11        /* z not strictly increasing, a non-finite z or profile value,
+                                        Kz <= 0 or Kx, Ky < 0 (checked on the host before any work) */
 
 /* ---- descriptor -------------------------------------------------------- */
 #define BLDFM_PREC_SINGLE 0 /* reference precision="single": spectra stored as complex64 */
@@ -328,13 +330,16 @@ int bldfm_surrogate_solve(void *net, const bldfm_desc *d,
 
 /* Allocation-free FP32 solve.  No counterpart in the reference (which never
  * touches a GPU).  For callers that may not allocate device memory while they
- * solve: work enqueued inside a CUDA stream capture, hosts that reserve all
- * device memory up front, plugin hosts whose allocator policy forbids
+ * solve: hosts that reserve all device memory up front and treat any later
+ * cudaMalloc as a failure, and plugin hosts whose allocator policy forbids
  * cudaMalloc from libraries.  Same arguments as bldfm_solve minus the
  * workspace: every intermediate lives in one static device array of 16 MiB
  * that each GPU loading this library holds until exit.
- *  - BLDFM_MODE_FP32 only, analytic == 0; larger problems return
+ *  - BLDFM_MODE_FP32 only, analytic == 0, nz >= 2; larger problems return
  *    BLDFM_ERR_WORKSPACE (the 512^2 footprint with 512^2 modes needs ~7 MiB).
+ *  - status_dev (device int32, may be NULL) receives the call's device
+ *    status once the stream reaches the end of the call: 0, BLDFM_ERR_TIMEOUT
+ *    (a bounded device wait ran out) or BLDFM_ERR_NONFINITE.
  *  - The first call on a device looks up the array's address with that
  *    device current; make it before any stream capture.
  *  - All calls share the array: calls whose GPU work overlaps race; order
@@ -343,7 +348,8 @@ int bldfm_surrogate_solve(void *net, const bldfm_desc *d,
 int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_dev,
                         const double *z_host, const double *prof_host,
                         const int64_t *levels_host, int32_t nlvls,
-                        double *conc_dev, double *flx_dev, void *stream);
+                        double *conc_dev, double *flx_dev, int32_t *status_dev,
+                        void *stream);
 
 #ifdef __cplusplus
 }

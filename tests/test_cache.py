@@ -67,3 +67,24 @@ def test_point_measurement_batch_matches_numpy():
     g = rng.uniform(0, 1, (64, 48))
     assert abs(point_measurement(torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()) - np.sum(f * g)) < 1e-12
     assert point_measurement(f, g) == np.sum(f * g)
+
+
+def test_cache_key_variant_keeps_reference_key():
+    """The sweep mode keys non-reference results apart; the reference's
+    arithmetic (variant None or "fp64") keeps the reference's key."""
+    from bldfm_gb300.cache import cache_args, cache_key
+
+    with open(os.path.join(HERE, "golden", "cache_keys.json")) as f:
+        c = json.load(f)[0]
+    args = (np.asarray(c["z"]), [np.asarray(p) for p in c["profiles"]], c["domain"], c["modes"], c["meas_pt"],
+            c["halo"], c["precision"])
+    assert cache_key(*args) == cache_key(*args, variant="fp64") == c["key"]
+    assert cache_key(*args, variant="fp32") != c["key"]
+    assert cache_key(*args, variant="fp32") != cache_key(*args, variant="fp64r")
+
+    class ReferenceLikeCache:  # the reference's class: get/put without variant
+        pass
+
+    assert cache_args(ReferenceLikeCache(), "fp64") == (True, {})
+    assert cache_args(ReferenceLikeCache(), "fp32") == (False, {})
+    assert cache_args(None, "fp64") == (False, {})

@@ -16,7 +16,7 @@ def test_multitower_matches_single_solves(footprint):
     from bldfm_gb300 import interface
 
     cfg = IC.config(n_steps=3, towers=2, footprint=footprint, output_levels=None if footprint else [4, 16])
-    out = interface.run_bldfm_multitower(cfg, batch=4)
+    out = interface.run_bldfm_multitower(cfg, batch=4, mode="fp32")
     for tower in cfg.towers:
         for i, r in enumerate(out[tower.name]):
             r64 = interface.run_bldfm_single(cfg, tower, met_index=i, mode="fp64")
@@ -38,6 +38,36 @@ def test_timeseries_with_cache_enabled():
     cfg.met.wind_dir = [225.0, 225.0]
     res = interface.run_bldfm_timeseries(cfg, cfg.towers[0])
     np.testing.assert_array_equal(res[0]["flx"], res[1]["flx"])
+
+
+def test_fp32_results_never_answer_reference_key():
+    """Batched FP32 results go into the cache under the mode's own key: a
+    lookup with the reference's key (what the reference's own cache class
+    computes, src/bldfm/cache.py:34-45) misses, the FP32 lookup hits."""
+    from bldfm_gb300 import interface
+    from bldfm_gb300.cache import GreensFunctionCache
+
+    cfg = IC.config(n_steps=1, towers=1, use_cache=True)
+    calls = []
+    orig = interface._make_cache
+
+    def spy(config):
+        c = orig(config)
+        calls.append(c)
+        return c
+
+    interface._make_cache = spy
+    try:
+        res = interface.run_bldfm_timeseries(cfg, cfg.towers[0], mode="fp32")
+    finally:
+        interface._make_cache = orig
+    cache = calls[0]
+    assert isinstance(cache, GreensFunctionCache) and len(cache) == 1
+    kw = interface._case(cfg, cfg.towers[0], 0, None)[0]
+    args = (kw["z"], kw["profiles"], kw["domain"], kw["modes"], kw["meas_pt"], kw["halo"], kw["precision"])
+    assert cache.get(*args) is None
+    hit = cache.get(*args, variant="fp32")
+    assert hit is not None and np.array_equal(hit[2], res[0]["flx"])
 
 
 def test_vertical_profiles_batch_equals_single_calls():

@@ -73,7 +73,7 @@ def test_multitower_batches_every_pair_in_order(stubbed):
     from bldfm_gb300 import interface
 
     cfg = IC.config(n_steps=3, towers=2)
-    out = interface.run_bldfm_multitower(cfg, batch=4)
+    out = interface.run_bldfm_multitower(cfg, batch=4, mode="fp32")
     assert [e for e in stubbed if e[0] == "batch"] == [("batch", 4), ("batch", 2)]
     assert list(out) == ["T0", "T1"]
     for k, name in enumerate(["T0", "T1"]):
@@ -86,7 +86,7 @@ def test_fp64_mode_and_parallel_strategies(stubbed):
     from bldfm_gb300 import interface
 
     cfg = IC.config(n_steps=2, towers=1)
-    res = interface.run_bldfm_timeseries(cfg, cfg.towers[0], mode="fp64")
+    res = interface.run_bldfm_timeseries(cfg, cfg.towers[0])  # the default: the reference's arithmetic
     assert len(res) == 2 and all(e[0] == "single" for e in stubbed)
     with pytest.warns(UserWarning):
         out = interface.run_bldfm_parallel(cfg, parallel_over="both", surface_flux=np.zeros((64, 96)))

@@ -1,11 +1,14 @@
 """The allocation-free entry point bldfm_solve_noalloc against bldfm_solve.
 
 bldfm_solve_noalloc serves callers that cannot allocate GPU memory while they
-solve (stream capture, pre-reserved device memory, allocator policies of a
-plugin host): its scratch is one static 16 MiB device array.  This file runs
-last (pytest collects it after the others) and must pass both alone in a fresh
-process and after the rest of the suite.  Two calls in a row with different
-problems check that the shared array is reused and cleared correctly.
+solve: hosts that reserve all device memory up front and treat a later
+cudaMalloc as a failure, and plugin hosts whose allocator policy forbids
+allocations by libraries.  Its scratch is one static 16 MiB device array.
+This file runs last (pytest collects it after the others) and must pass both
+alone in a fresh process and after the rest of the suite.  Two calls in a row
+with different problems check that the shared array is reused and cleared
+correctly: the larger, multi-level dispersion case runs first, so the
+footprint case reads an array an earlier call has dirtied.
 """
 
 import ctypes
@@ -15,7 +18,10 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-FP32_TOL = 1e-3  # same bar as the FP32 parity tests
+# Both entry points run the same FP32 kernels on the same inputs; they differ
+# only in how the twiddle tables are made (device sincospi here, a host
+# long-double table in the cached path), about one float ulp.
+NOALLOC_TOL = 1e-5
 
 
 def _problem(footprint, levels, seed):
@@ -63,18 +69,22 @@ def test_noalloc_matches_workspace_entry_two_calls():
 
     lib = _lib.load()
     problems = [
-        _problem(True, [24], seed=1),              # footprint, one level
         _problem(False, [0, 12, 12, 24], seed=2),  # dispersion, duplicate level: slot left empty
+        _problem(True, [24], seed=1),              # footprint, one level, on the dirtied array
     ]
     prepared = [_solve_both(pb, torch, lib, _lib, make_desc, plan) for pb in problems]
-    # two allocation-free calls back to back on the same stream
-    for pb, pr in zip(problems, prepared):
+    # two allocation-free calls back to back on the same stream, each with its
+    # own device status word (preset to a value the call must overwrite)
+    status = torch.full((len(problems),), 12345, dtype=torch.int32, device="cuda:0")
+    for k, (pb, pr) in enumerate(zip(problems, prepared)):
         d, srf, c2, f2 = pr["noalloc_args"]
         st = lib.bldfm_solve_noalloc(
             d, ctypes.c_void_p(srf.data_ptr()), _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]),
-            len(pb["levels"]), ctypes.c_void_p(c2.data_ptr()), ctypes.c_void_p(f2.data_ptr()), None)
+            len(pb["levels"]), ctypes.c_void_p(c2.data_ptr()), ctypes.c_void_p(f2.data_ptr()),
+            ctypes.c_void_p(status[k:].data_ptr()), None)
         _lib.check(st, "bldfm_solve_noalloc")
     torch.cuda.synchronize()
+    assert status.cpu().tolist() == [0] * len(problems)
     for pb, pr in zip(problems, prepared):
         c1, f1 = (t.cpu().numpy() for t in pr["ws"])
         _, _, c2, f2 = pr["noalloc_args"]
@@ -82,7 +92,7 @@ def test_noalloc_matches_workspace_entry_two_calls():
         assert np.all(np.isfinite(c2)) and np.all(np.isfinite(f2))
         for a, b in ((c2, c1), (f2, f1)):
             err = np.linalg.norm(a - b) / np.linalg.norm(b)
-            assert err <= FP32_TOL, err
+            assert err <= NOALLOC_TOL, err
 
 
 def test_noalloc_rejects_what_it_cannot_do():
@@ -96,11 +106,11 @@ def test_noalloc_rejects_what_it_cannot_do():
     d = make_desc(pb["srf"].shape, len(pb["z"]), pb["domain"], pb["modes"], pb["meas"], 0.0, True, False, None,
                   "double", "fp64")
     st = lib.bldfm_solve_noalloc(d, None, _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]), 1,
-                                 _lib.ptr(out), _lib.ptr(out), None)
+                                 _lib.ptr(out), _lib.ptr(out), None, None)
     assert st == _lib.ERR_UNSUPPORTED
     # beyond the 16 MiB scratch array: 1024^2 modes on a 2048^2 extended grid
     d = make_desc((1024, 1024), len(pb["z"]), (1000.0, 1000.0), (1024, 1024), (500.0, 500.0), 0.0, True, False,
                   512.0, "double", "fp32")
     st = lib.bldfm_solve_noalloc(d, None, _lib.ptr(pb["z"]), _lib.ptr(pb["prof"]), _lib.ptr(pb["levels"]), 1,
-                                 _lib.ptr(out), _lib.ptr(out), None)
+                                 _lib.ptr(out), _lib.ptr(out), None, None)
     assert st == _lib.ERR_WORKSPACE
