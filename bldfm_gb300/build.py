@@ -58,7 +58,12 @@ def build(verbose=False, force=False):
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         if force or _needs(obj, [src] + headers):
-            jobs.append(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-std=gnu11", "-c", src, "-o", obj])
+            # -fno-builtin: every libm call (pow, csqrt) runs in the library at
+            # run time, as numpy's scalar ** and complex sqrt do; gcc would
+            # otherwise fold pow(x, 2.0) into x * x, which differs from libm's
+            # pow by one ulp for rare x
+            jobs.append(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fno-builtin", "-std=gnu11", "-c", src, "-o",
+                         obj])
     outs = []
     if jobs:
         with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:

@@ -2,7 +2,9 @@
  * Host-side arithmetic that must round exactly as the reference's numpy code.
  * Compiled with -ffp-contract=off: every + - * / below is one IEEE operation,
  * pow() and csqrt() are the process's libm (numpy's scalar ** and complex
- * sqrt call the same libm).
+ * sqrt call the same libm).  Also compiled with -fno-builtin, so that the
+ * compiler does not replace pow(x, 2.0) by x * x: libm's pow is not always
+ * correctly rounded, and the reference's dz**2 and Kzinv**2 are libm's.
  */
 #include <complex.h>
 #include <math.h>

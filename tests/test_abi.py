@@ -115,3 +115,27 @@ def test_batch_plan_sizes_without_device_cache(xform_lines):
     need = ctypes.c_int64(0)
     assert lib.bldfm_batch_plan(arr, 2, ctypes.byref(opts), ctypes.byref(need)) == 0
     assert need.value > 0
+
+
+def test_host_level_table_rounds_like_the_reference():
+    """The FP64 path's per-level scalars (dz**2, dz**3, Kzinv**2 through libm's
+    pow, src/bldfm/solver.py:361-364) equal the reference's numpy values bit
+    for bit over many grids.  A compiler that turned pow(x, 2.0) into x * x
+    would differ by one ulp for rare x, which the shooting method amplifies
+    by up to e^{2G} (about 1e25 on the 1024^2, n = 256 footprint)."""
+    import ctypes
+
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    lib.hx_level_table.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.hx_level_table.restype = None
+    bad = 0
+    for n in range(16, 520, 11):
+        for ustar in (0.2, 0.3, 0.5):
+            z, p = O.vertical_profiles(n, 20.0, O.compute_wind_fields(4.0, 225.0), ustar=ustar, mol=-50.0)
+            nz = len(z)
+            prof = np.ascontiguousarray(np.stack(p))
+            zz = np.ascontiguousarray(z)
+            lv = np.zeros((nz - 1, 12))
+            lib.hx_level_table(nz, zz.ctypes.data, prof.ctypes.data, lv.ctypes.data)
+            bad += int(np.sum(lv[:, :11] != O.level_table(z, p)[:, :11]))
+    assert bad == 0
