@@ -235,10 +235,12 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def transform_section(stages_b, B, dev):
+def transform_section(stages_b, B, dev, xlines):
     """Achieved GB/s of the batched output transform (algorithmic bytes: the
     two FP32 spectra read, conc and flx written) against the HBM peak, and a
-    cuFFT timing of the same transform size (torch.fft, comparison only)."""
+    cuFFT timing of the same transform size (torch.fft, comparison only).
+    xlines: the transform setting the step ran with (8: register-resident
+    passes, else shared-memory passes with that many lines per CTA)."""
     import torch
 
     peaks = measured_peaks()
@@ -260,7 +262,8 @@ def transform_section(stages_b, B, dev):
     cufft_ms = e0.elapsed_time(e1) / 5
     del x
     return {
-        "kernels": "out_cols_batch_kernel + out_rows_batch_kernel",
+        "kernels": ("rx_cols_batch_kernel + rx_rows_batch_kernel (register-resident lines)" if xlines in (0, 8)
+                    else "out_cols_batch_kernel + out_rows_batch_kernel (shared-memory lines, %d per CTA)" % xlines),
         "ms_per_footprint": ms / B if ms else None,
         "bytes_per_footprint": bytes_fp,
         "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -936,7 +939,7 @@ def main():
                 "traffic_source": "ncu capture, profiles/riccati32_batch_kernel_metric_batch16.md",
                 "flops_per_launch": flops_launch,
             },
-            "transform": transform_section(stages_b, B, dev),
+            "transform": transform_section(stages_b, B, dev, xlines),
             "surrogate": sur_line,
             "timeseries": ts_line,
             "production": prod_line,

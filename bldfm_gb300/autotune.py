@@ -23,7 +23,11 @@ from .batch import BatchSolver
 # (256, 3) and (128, 7) leave registers free on every SM for a transform CTA
 # of another stream, which the pipelined timing below can reward.
 CANDIDATES = [(256, 0), (256, 6), (128, 0), (128, 12), (128, 18), (256, 3), (128, 7)]
-XFORM_LINES = [4, 2, 1]
+# transform passes: 8 = register-resident lines (batches whose cases share a
+# supported line length; others fall back to the default), 4 / 2 / 1 =
+# shared-memory passes with that many lines per CTA
+XFORM_LINES = [8, 4, 2, 1]
+SIGNATURE_VERSION = 2  # bumped when the candidate set changes: older cached winners are ignored
 
 
 def _cache_path():
@@ -64,8 +68,8 @@ def signature(cases):
         total += int(info.nsolved)
         maxnz = max(maxnz, len(kw["z"]))
     b = lambda v: 1 << max(0, int(v - 1).bit_length())  # noqa: E731
-    return "%s|modes%d|nz%d|cases%d" % (torch.cuda.get_device_name(), b(total), 16 * ((maxnz + 15) // 16),
-                                        b(len(cases)))
+    return "v%d|%s|modes%d|nz%d|cases%d" % (SIGNATURE_VERSION, torch.cuda.get_device_name(), b(total),
+                                            16 * ((maxnz + 15) // 16), b(len(cases)))
 
 
 def _time(cases, reps, stage, **opts):

@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libbldfm_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
-CU_SOURCES = ["api.cu", "geometry.cu", "kernels.cu", "profiles.cu", "noalloc.cu", "batch.cu", "surrogate.cu", "serve.cu", "measure.cu"]
+CU_SOURCES = ["api.cu", "geometry.cu", "xform.cu", "kernels.cu", "profiles.cu", "noalloc.cu", "batch.cu", "surrogate.cu", "serve.cu", "measure.cu"]
 C_SOURCES = ["host_exact.c"]
 
 

@@ -559,6 +559,9 @@ struct BatchBuild {
     size_t sweep_smem = 0, col_smem = 0, row_smem = 0;
     // persistent one-line transforms (lines per CTA 1)
     int persist = 0, col_grid = 0, row_grid = 0, maxnfy = 0, maxnfx = 0, maxnly = 0;
+    // register-resident transform passes: config of the column / row line
+    // length shared by every case of the batch, or -1
+    int rx_col = -1, rx_row = -1;
     std::vector<int64_t> tile0, col0, row0;
 };
 
@@ -595,14 +598,28 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     }
     B.maxnfy = maxnfy;
     B.maxnfx = maxnfx;
-    const int xl = opts ? opts->xform_lines : 0;
-    if (xl != 0 && xl != 1 && xl != 2 && xl != 4) return BLDFM_ERR_ARG;
+    int xl = opts ? opts->xform_lines : 0;
+    if (xl != 0 && xl != 1 && xl != 2 && xl != 4 && xl != 8) return BLDFM_ERR_ARG;
+    // register-resident passes (xform_lines 0 or 8) when every case shares a
+    // supported column and row line length; otherwise the shared-memory passes
+    if (xl == 0 || xl == 8) {
+        B.rx_col = rx_config(B.hp[0].g.nfy);
+        B.rx_row = rx_config(B.hp[0].g.nfx);
+        for (int k = 1; k < n; ++k)
+            if (B.hp[k].g.nfy != B.hp[0].g.nfy || B.hp[k].g.nfx != B.hp[0].g.nfx) B.rx_col = -1;
+        if (B.rx_col < 0 || B.rx_row < 0) B.rx_col = B.rx_row = -1;
+        xl = 0;
+    }
     B.rpc = xl > 0 ? xl : 2;
     while (B.rpc > 1 && (2 * (size_t)B.rpc + 1) * maxnfx * 8 > 190 * 1024) --B.rpc;
     // column pass: (2 cpc + 1) lines of maxnfy in shared memory
     auto col_bytes = [&](int c) { return (2 * (size_t)c + 1) * maxnfy * 8; };
     B.cpc = xl > 0 ? xl : out_cols_per_cta(maxnfy, 8);
     while (B.cpc > 1 && col_bytes(B.cpc) > 190 * 1024) B.cpc >>= 1;
+    if (B.rx_col >= 0) {
+        B.cpc = rx_lines_per_cta(B.rx_col);
+        B.rpc = rx_lines_per_cta(B.rx_row);
+    }
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
         B.col0[k] = B.ncol;
@@ -668,6 +685,11 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.col_smem = col_bytes(B.cpc);
     B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
     B.persist = B.cpc == 1 && B.rpc == 1;
+    if (B.rx_col >= 0) {
+        B.col_smem = rx_smem(B.rx_col);
+        B.row_smem = rx_smem(B.rx_row);
+        B.persist = 0;
+    }
     if (B.persist) {
         B.col_smem = (3 * (size_t)maxnfy + 4 * (size_t)B.maxnly) * 8;
         B.row_smem = 3 * (size_t)maxnfx * 8;
@@ -831,6 +853,8 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
     bl.maxn_col = B.maxnfy;
     bl.maxnly = B.maxnly;
     bl.maxn_row = B.maxnfx;
+    bl.rx_col = B.rx_col;
+    bl.rx_row = B.rx_row;
     if (tdc) tmark(*tdc, st);  // 1: the sweep
     CK(launch_batch_kernels(bl, st, 0));
     if (tdc) tmark(*tdc, st);  // 2: the output transform
@@ -853,6 +877,8 @@ std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B,
     k.push_back(B.nrow);
     k.push_back((int64_t)B.row_smem);
     k.push_back(B.persist);
+    k.push_back(B.rx_col);
+    k.push_back(B.rx_row);
     k.push_back(B.col_grid);
     k.push_back(B.row_grid);
     for (int i = 0; i < n; ++i) {
@@ -1128,6 +1154,8 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     bl.maxn_col = B.maxnfy;
     bl.maxnly = B.maxnly;
     bl.maxn_row = B.maxnfx;
+    bl.rx_col = B.rx_col;
+    bl.rx_row = B.rx_row;
     CK(launch_batch_kernels(bl, st, 1));
     tmark(dc, st);  // 3: end
     return BLDFM_OK;

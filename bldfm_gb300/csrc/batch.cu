@@ -410,6 +410,11 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
             riccati32_batch_kernel<256><<<bl.sweep_ctas, 256, bl.sweep_smem, st>>>(bl.cases, bl.tile_case,
                                                                                   bl.cta_tiles, bl.err);
     }
+    if (part == 1 && bl.rx_col >= 0) {
+        cudaError_t e = launch_rx_pass(bl.rx_col, true, bl, bl.col_ctas, st);
+        if (e != cudaSuccess) return e;
+        return launch_rx_pass(bl.rx_row, false, bl, bl.row_ctas, st);
+    }
     if (part == 1 && bl.persist) {
         if (bl.col_ctas > 0)
             out_cols_persist_kernel<<<bl.col_grid, 256, bl.col_smem, st>>>(bl.cases, bl.col_case, bl.col_ctas,
@@ -449,6 +454,7 @@ int batch_xform_occupancy(int col, size_t smem)
 
 void prepare_batch_attributes()
 {
+    prepare_rx_attributes();
     cudaFuncSetAttribute(riccati32_batch_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(riccati32_batch_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(out_cols_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

@@ -48,9 +48,22 @@ struct BatchLaunch {
     // persistent one-line transforms (col_ctas / row_ctas count items, launched
     // on col_grid / row_grid CTAs); shared-memory sizes from the largest case
     int persist, col_grid, row_grid, maxn_col, maxnly, maxn_row;
+    // register-resident transform passes (xform.cu): line-length configs of
+    // the column and row passes, or -1 for the shared-memory passes
+    int rx_col, rx_row;
 };
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);
+
+// register-resident transform passes (xform.cu), for line lengths 512, 768,
+// 1024, 1536, 2048, 3072: config id of a length (-1 if unsupported), lines
+// per 256-thread CTA, dynamic shared memory per CTA, one-time attributes,
+// and the launch of the column (col) or row pass over nctas CTAs
+int rx_config(int n);
+int rx_lines_per_cta(int cfg);
+size_t rx_smem(int cfg);
+void prepare_rx_attributes();
+cudaError_t launch_rx_pass(int cfg, bool col, const BatchLaunch &bl, int nctas, cudaStream_t st);
 int batch_sweep_occupancy(int threads, size_t smem);
 int batch_xform_occupancy(int col, size_t smem);
 void prepare_batch_attributes();

@@ -1,0 +1,355 @@
+// Batched output transform (solver.py:264-290) with register-resident lines:
+// the column pass (spectrum columns -> band-column lines along y, crop) and
+// the row pass (band rows -> lines along x, crop, conc = Re, flx = Im) of
+// bldfm_solve_batch for line lengths 64 * E.  One CTA = 256 threads = G
+// groups of P threads, one line per group (xform_reg.cuh).  Inputs are read
+// straight from global memory into registers (consecutive threads read
+// consecutive positions of a line); the column pass stages its G lines'
+// kept rows through shared memory so that every row of the intermediate
+// gets whole 32-byte sectors; the row pass writes its outputs directly.
+#include <cuda_runtime.h>
+#include <limits.h>
+#include <stdint.h>
+
+#include "batch.h"
+#include "common.h"
+#include "devmath.cuh"
+#include "xform_reg.cuh"
+
+namespace {
+
+using S768 = rx::Shape<24, 4, 8>;
+using S512 = rx::Shape<8, 8, 8>;
+using S1024 = rx::Shape<16, 8, 8>;
+using S1536 = rx::Shape<24, 8, 8>;
+using S2048 = rx::Shape<32, 8, 8>;
+using S3072 = rx::Shape<48, 8, 8>;
+
+constexpr int kThreads = 256;
+
+// CTAs per SM the register budget is sized for: 3 (24 warps) up to E = 24,
+// else whatever fits
+template <class S>
+constexpr int min_ctas()
+{
+    return S::E <= 24 ? 3 : 1;
+}
+
+__device__ __forceinline__ void load_case_rx(BatchCase *dst, const BatchCase *src)
+{
+    const int nw = (int)(sizeof(BatchCase) / 4);
+    const int *s = (const int *)src;
+    int *d = (int *)dst;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) d[i] = s[i];
+}
+
+// Value at position pos of band column bx of level lvl: Z = Hp + i Hq,
+// H(P) = (X(P) + conj X(-P)) / 2 with -P taken on the periodic grid (the
+// k = 0 entry from dc).  The FP32 spectra are Hermitian-complete: the sweep
+// writes every paired mode's mirror as its exact conjugate, so where -P is
+// the signed mirror of P inside the mode range, H(P) = X(P).  That excludes
+// the Nyquist row and column of an untruncated spectrum, whose periodic
+// mirror (-N/2 -> -N/2) is a separately solved mode.  xpair: the column at -P
+// (bx.z) holds the signed mirror -kx of the column at P (bx.y).
+__device__ __forceinline__ float2 col_value(const SolveGeom &g, const int4 bx, bool xpair,
+                                            const float2 *__restrict__ Xp, const float2 *__restrict__ Xq,
+                                            const double2 *__restrict__ dc, int lvl, int n, int pos)
+{
+    const int nly = g.nly, fmin = freq_min(nly), fmax = freq_max(nly);
+    const int kp = pos <= fmax ? pos : (pos - n >= fmin ? pos - n : INT_MIN);
+    const int km = -pos >= fmin ? -pos : (n - pos <= fmax ? n - pos : INT_MIN);
+    const bool pin = bx.y >= 0 && kp != INT_MIN, mn = bx.z >= 0 && km != INT_MIN;
+    if (!pin && !mn) return make_float2(0.f, 0.f);
+    if (pin && mn && xpair && km == -kp && !(bx.y == 0 && kp == 0)) {
+        const size_t o = ((size_t)lvl * g.nlx + bx.y) * nly + index_of_freq(kp, nly);
+        const float2 p = __ldg(Xp + o), q = __ldg(Xq + o);
+        return make_float2(p.x - q.y, p.y + q.x);
+    }
+    float re = 0.f, im = 0.f;
+    if (pin) {
+        const int r = index_of_freq(kp, nly);
+        float2 p, q;
+        if (bx.y == 0 && r == 0) {
+            const double2 dp = dc[2 * lvl], dq = dc[2 * lvl + 1];
+            p = make_float2((float)dp.x, (float)dp.y);
+            q = make_float2((float)dq.x, (float)dq.y);
+        } else {
+            const size_t o = ((size_t)lvl * g.nlx + bx.y) * nly + r;
+            p = __ldg(Xp + o);
+            q = __ldg(Xq + o);
+        }
+        re = 0.5f * (p.x - q.y);
+        im = 0.5f * (p.y + q.x);
+    }
+    if (mn) {
+        const int r = index_of_freq(km, nly);
+        float2 p, q;
+        if (bx.z == 0 && r == 0) {
+            const double2 dp = dc[2 * lvl], dq = dc[2 * lvl + 1];
+            p = make_float2((float)dp.x, (float)dp.y);
+            q = make_float2((float)dq.x, (float)dq.y);
+        } else {
+            const size_t o = ((size_t)lvl * g.nlx + bx.z) * nly + r;
+            p = __ldg(Xp + o);
+            q = __ldg(Xq + o);
+        }
+        re += 0.5f * (p.x + q.y);
+        im += 0.5f * (q.x - p.y);
+    }
+    return make_float2(re, im);
+}
+
+// Band column of a line position along x: the band holds the frequencies
+// f in [-h, h] (h = max(-fmin, fmax) of nlx) at positions f mod nfx, in the
+// order of f; when 2 h = nfx the position of -h and h coincide and -h is
+// kept.  Returns -1 for positions outside the band.
+__device__ __forceinline__ int band_of(int pos, int h, int nfx)
+{
+    if (pos >= nfx - h) return pos - nfx + h;
+    if (pos <= h) return pos + h;
+    return -1;
+}
+
+// Column pass.  When a line's two spectrum columns (Xp and Xq at P, nly
+// complex each) fit in the group's exchange buffer, one thread of the group
+// brings them in with two bulk copies completing on the group's mbarrier
+// (every load of the line in flight at once, none in registers); the few
+// positions that need the column at -P read it from global memory.
+template <class S>
+__global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_cols_batch_kernel(const BatchCase *__restrict__ cases,
+                                                                                const int *__restrict__ cta_case,
+                                                                                int *err)
+{
+    constexpr int P = S::P, E = S::E, G = kThreads / P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *sbuf = (float2 *)smem_raw;
+    __shared__ __align__(16) BatchCase sc;
+    __shared__ uint64_t gbar[G];
+    load_case_rx(&sc, cases + cta_case[blockIdx.x]);
+    const int grp = threadIdx.x / P, t = threadIdx.x - grp * P;
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&gbar[grp])), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const SolveGeom &g = sc.g;
+    const int64_t local = (int64_t)blockIdx.x - sc.col0;
+    const int ncb = (g.nbx + G - 1) / G;
+    const int lvl = (int)(local / ncb), cb = (int)(local - (int64_t)lvl * ncb);
+    const int b = cb * G + grp;
+    const bool active = b < g.nbx;
+    const float cj = g.out_sign > 0 ? -1.f : 1.f;  // inverse transform: conjugate in and out
+    float2 *buf = sbuf + grp * S::BUF;
+    float2 x[E];
+    bool timed_out = false;
+    if (active) {
+        const int4 bx = sc.xband[b];
+        const bool xpair =
+            bx.y >= 0 && bx.z >= 0 && freq_of_index(bx.z, g.nlx) == -freq_of_index(bx.y, g.nlx);
+        const int nly = g.nly;
+        const size_t colp = ((size_t)lvl * g.nlx + (bx.y > 0 ? bx.y : 0)) * nly;
+        const bool stage = bx.y >= 0 && 2 * nly <= S::BUF && (nly & 1) == 0 &&
+                           ((((uintptr_t)sc.Xp) | ((uintptr_t)sc.Xq)) & 15) == 0;
+        if (stage) {
+            const uint32_t ba = smem_u32(&gbar[grp]);
+            if (t == 0) {
+                const uint32_t nb = (uint32_t)nly * 8u;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ba), "r"(2u * nb)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(buf)),
+                    "l"(sc.Xp + colp), "r"(nb), "r"(ba)
+                    : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(buf + nly)),
+                    "l"(sc.Xq + colp), "r"(nb), "r"(ba)
+                    : "memory");
+            }
+            uint32_t done = 0;
+            for (long it = 0; it < BLDFM_WAIT_POLLS && !done; ++it)
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                    "selp.u32 %0, 1, 0, p;\n\t}"
+                    : "=r"(done)
+                    : "r"(ba), "r"(0u)
+                    : "memory");
+            timed_out = !done;
+            const int fmin = freq_min(nly), fmax = freq_max(nly), n = S::N;
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                const int pos = t + P * m;
+                const int kp = pos <= fmax ? pos : (pos - n >= fmin ? pos - n : INT_MIN);
+                const int km = -pos >= fmin ? -pos : (n - pos <= fmax ? n - pos : INT_MIN);
+                const bool mn = bx.z >= 0 && km != INT_MIN;
+                float2 v = make_float2(0.f, 0.f);
+                if (kp != INT_MIN && mn && xpair && km == -kp && !(bx.y == 0 && kp == 0)) {
+                    const int r = index_of_freq(kp, nly);
+                    const float2 p = buf[r], q = buf[nly + r];
+                    v = make_float2(p.x - q.y, p.y + q.x);
+                } else if (kp != INT_MIN || mn) {
+                    v = col_value(g, bx, xpair, sc.Xp, sc.Xq, sc.dc, lvl, n, pos);
+                }
+                x[m] = make_float2(v.x, cj * v.y);
+            }
+            rx::group_bar(grp + 1, P);  // the staged columns are read before the buffer is reused
+        } else {
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                const float2 v = col_value(g, bx, xpair, sc.Xp, sc.Xq, sc.dc, lvl, S::N, t + P * m);
+                x[m] = make_float2(v.x, cj * v.y);
+            }
+        }
+        rx::line_fft<S>(x, t, buf, sc.twy, grp + 1);
+    }
+    if (__syncthreads_or(timed_out) && threadIdx.x == 0) atomicExch(err, BLDFM_ERR_TIMEOUT_DEV);
+    // kept rows [py, py + out_ny) of the G lines staged line-major, [G][ys]
+    // with ys = out_ny rounded up to 4 mod 16 words: conflict-free writes
+    // along y here and reads across the G lines below
+    const int ony = g.out_ny, py = g.py;
+    const int ys = ((ony + 11) & ~15) + 4;
+    if (active) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int y = t + P * m - py;
+            if (y >= 0 && y < ony) sbuf[(size_t)grp * ys + y] = make_float2(x[m].x, cj * x[m].y);
+        }
+    }
+    __syncthreads();
+    const int ng = min(G, g.nbx - cb * G);
+    float2 *o = sc.Cb + (size_t)lvl * ony * g.nbx + cb * G;
+    for (int i = threadIdx.x; i < ony * G; i += kThreads) {
+        const int y = i / G, gg = i - y * G;
+        if (gg < ng) o[(size_t)y * g.nbx + gg] = sbuf[(size_t)gg * ys + y];
+    }
+}
+
+template <class S>
+__global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_rows_batch_kernel(const BatchCase *__restrict__ cases,
+                                                                const int *__restrict__ cta_case, int *err)
+{
+    constexpr int P = S::P, E = S::E, G = kThreads / P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *sbuf = (float2 *)smem_raw;
+    __shared__ __align__(16) BatchCase sc;
+    load_case_rx(&sc, cases + cta_case[blockIdx.x]);
+    __syncthreads();
+    const SolveGeom &g = sc.g;
+    const int64_t local = (int64_t)blockIdx.x - sc.row0;
+    const int nblk = (g.out_ny + G - 1) / G;
+    const int lvl = (int)(local / nblk), yb = (int)(local - (int64_t)lvl * nblk);
+    const int grp = threadIdx.x / P, t = threadIdx.x - grp * P;
+    const int y = yb * G + grp;
+    bool bad = false;
+    if (y < g.out_ny) {
+        const float cj = g.out_sign > 0 ? -1.f : 1.f;
+        const int f0 = freq_min(g.nlx), f1 = freq_max(g.nlx);
+        const int h = -f0 > f1 ? -f0 : f1;
+        const float2 *row = sc.Cb + ((size_t)lvl * g.out_ny + y) * g.nbx;
+        float2 x[E];
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int bcol = band_of(t + P * m, h, S::N);
+            float2 v = make_float2(0.f, 0.f);
+            if (bcol >= 0) v = __ldg(row + bcol);
+            x[m] = make_float2(v.x, cj * v.y);
+        }
+        rx::line_fft<S>(x, t, sbuf + grp * S::BUF, sc.twx, grp + 1);
+        const int onx = g.out_nx, px = g.px;
+        const size_t ob = ((size_t)lvl * g.out_ny + y) * onx;
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int xo = t + P * m - px;
+            if (xo >= 0 && xo < onx) {
+                const float re = x[m].x, im = cj * x[m].y;
+                sc.conc[ob + xo] = (double)re;
+                sc.flx[ob + xo] = (double)im;
+                bad |= !(isfinite(re) && isfinite(im));
+            }
+        }
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
+}
+
+template <class S>
+size_t rx_smem_of()
+{
+    return (size_t)(kThreads / S::P) * S::BUF * sizeof(float2);
+}
+
+template <class S>
+void rx_set_attr()
+{
+    cudaFuncSetAttribute(rx_cols_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rx_smem_of<S>());
+    cudaFuncSetAttribute(rx_rows_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rx_smem_of<S>());
+}
+
+template <class S>
+cudaError_t rx_launch(bool col, const BatchLaunch &bl, int nctas, cudaStream_t st)
+{
+    if (col)
+        rx_cols_batch_kernel<S><<<nctas, kThreads, rx_smem_of<S>(), st>>>(bl.cases, bl.col_case, bl.err);
+    else
+        rx_rows_batch_kernel<S><<<nctas, kThreads, rx_smem_of<S>(), st>>>(bl.cases, bl.row_case, bl.err);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int rx_config(int n)
+{
+    switch (n) {
+    case 512: return 0;
+    case 768: return 1;
+    case 1024: return 2;
+    case 1536: return 3;
+    case 2048: return 4;
+    case 3072: return 5;
+    default: return -1;
+    }
+}
+
+int rx_lines_per_cta(int cfg)
+{
+    return cfg == 1 ? kThreads / S768::P : (cfg >= 0 ? kThreads / 64 : 0);
+}
+
+size_t rx_smem(int cfg)
+{
+    switch (cfg) {
+    case 0: return rx_smem_of<S512>();
+    case 1: return rx_smem_of<S768>();
+    case 2: return rx_smem_of<S1024>();
+    case 3: return rx_smem_of<S1536>();
+    case 4: return rx_smem_of<S2048>();
+    case 5: return rx_smem_of<S3072>();
+    default: return 0;
+    }
+}
+
+void prepare_rx_attributes()
+{
+    rx_set_attr<S512>();
+    rx_set_attr<S768>();
+    rx_set_attr<S1024>();
+    rx_set_attr<S1536>();
+    rx_set_attr<S2048>();
+    rx_set_attr<S3072>();
+}
+
+cudaError_t launch_rx_pass(int cfg, bool col, const BatchLaunch &bl, int nctas, cudaStream_t st)
+{
+    if (nctas <= 0) return cudaSuccess;
+    switch (cfg) {
+    case 0: return rx_launch<S512>(col, bl, nctas, st);
+    case 1: return rx_launch<S768>(col, bl, nctas, st);
+    case 2: return rx_launch<S1024>(col, bl, nctas, st);
+    case 3: return rx_launch<S1536>(col, bl, nctas, st);
+    case 4: return rx_launch<S2048>(col, bl, nctas, st);
+    case 5: return rx_launch<S3072>(col, bl, nctas, st);
+    default: return cudaErrorInvalidValue;
+    }
+}

@@ -77,44 +77,49 @@ __device__ __forceinline__ float2 mul_w(float2 u)
     return make_float2(u.x * c - u.y * s, u.x * s + u.y * c);
 }
 
-// In-register DFT of length N, forward sign, natural order in and out.
+// In-register DFT of length N, forward sign, in place: natural order in, and
+// X[k] left in x[Dft<N>::slot(k)] (a compile-time permutation, so that the
+// transform needs no second array of N values).  N = A F with A = 8, 4, 2
+// or 3:  X[k1 + A k2] = sum_s1 w_F^{s1 k2} w_N^{s1 k1} sum_s2 w_A^{s2 k1}
+// x[s1 + F s2]; the inner DFTs overwrite x[s1 + F k1], then each block
+// x[F k1 .. F k1 + F) is transformed in place.
 template <int N>
-__device__ __forceinline__ void dft(float2 *x)
-{
-    if constexpr (N == 1) {
-    } else if constexpr (N == 2 || N == 3 || N == 4 || N == 8) {
-        dft_small<float2, N, -1>(x, nullptr, 0);
-    } else {
-        constexpr int A = (N % 8 == 0) ? 8 : ((N % 4 == 0) ? 4 : ((N % 2 == 0) ? 2 : 3));
-        constexpr int F = N / A;
-        float2 t[N];
-        // X[k1 + A k2] = sum_s1 w_F^{s1 k2} w_N^{s1 k1} sum_s2 w_A^{s2 k1} x[s1 + F s2]
-        sfor<0, F>([&](auto S1) {
-            constexpr int s1 = decltype(S1)::value;
-            float2 u[A];
+struct Dft {
+    static constexpr bool direct = N == 1 || N == 2 || N == 3 || N == 4 || N == 8;
+    static constexpr int A = direct ? N : ((N % 8 == 0) ? 8 : ((N % 4 == 0) ? 4 : ((N % 2 == 0) ? 2 : 3)));
+    static constexpr int F = N / A;
+    static constexpr int slot(int k)
+    {
+        if constexpr (direct)
+            return k;
+        else
+            return F * (k % A) + Dft<F>::slot(k / A);
+    }
+    __device__ __forceinline__ static void run(float2 *x)
+    {
+        if constexpr (direct) {
+            if constexpr (N > 1) dft_small<float2, N, -1>(x, nullptr, 0);
+        } else {
+            sfor<0, F>([&](auto S1) {
+                constexpr int s1 = decltype(S1)::value;
+                float2 u[A];
 #pragma unroll
-            for (int s2 = 0; s2 < A; ++s2) u[s2] = x[s1 + F * s2];
-            dft_small<float2, A, -1>(u, nullptr, 0);
-            sfor<0, A>([&](auto K1) {
-                constexpr int k1 = decltype(K1)::value;
-                constexpr int m = (s1 * k1) % N;
-                if constexpr (m == 0)
-                    t[s1 * A + k1] = u[k1];
-                else
-                    t[s1 * A + k1] = mul_w<m, N>(u[k1]);
+                for (int s2 = 0; s2 < A; ++s2) u[s2] = x[s1 + F * s2];
+                dft_small<float2, A, -1>(u, nullptr, 0);
+                sfor<0, A>([&](auto K1) {
+                    constexpr int k1 = decltype(K1)::value;
+                    constexpr int m = (s1 * k1) % N;
+                    if constexpr (m == 0)
+                        x[s1 + F * k1] = u[k1];
+                    else
+                        x[s1 + F * k1] = mul_w<m, N>(u[k1]);
+                });
             });
-        });
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1) {
-            float2 v[F];
-#pragma unroll
-            for (int s1 = 0; s1 < F; ++s1) v[s1] = t[s1 * A + k1];
-            dft<F>(v);
-#pragma unroll
-            for (int k2 = 0; k2 < F; ++k2) x[k1 + A * k2] = v[k2];
+            for (int k1 = 0; k1 < A; ++k1) Dft<F>::run(x + F * k1);
         }
     }
-}
+};
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -143,33 +148,50 @@ struct Shape {
 // tw: exp(-2 pi i m / N), m < N (global, read through the read-only path).
 // bar: the group's named barrier id.  The group's threads call it together;
 // the buffer is free again when it returns.
+//
+// Twiddles: phase 1 needs w_N^{t k1}, k1 < E.  Per block of 8 consecutive
+// k1 one value is loaded and the rest follow by multiplying with w_N^t
+// (at most 7 products in a chain: relative error a few 1e-7, well inside the
+// FP32 path's error); phase 2 loads its R2 - 1 twiddles w_P^{u c} once.
 template <class S>
 __device__ __forceinline__ void line_fft(float2 *x, int t, float2 *buf, const float2 *__restrict__ tw, int bar)
 {
     constexpr int E = S::E, R2 = S::R2, R3 = S::R3, P = S::P;
+    using D = Dft<E>;
+    // loads that only depend on t go out before the first DFT
+    float2 wb[(E + 7) / 8];
+#pragma unroll
+    for (int b = 0; b < (E + 7) / 8; ++b) wb[b] = __ldg(tw + 8 * b * t);  // 8 b t < 8 (E / 8) P <= N
+    const float2 w1 = __ldg(tw + t);
+    const int u = t % R3, k1b = t / R3;
+    float2 w2[R2];
+#pragma unroll
+    for (int c = 1; c < R2; ++c) w2[c] = __ldg(tw + u * c * E);
     // phase 1: E-point DFT of the thread's values, twiddle w_N^{t k1}
-    dft<E>(x);
+    D::run(x);
 #pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) {
-        if (t > 0) x[k1] = cmul(x[k1], __ldg(tw + t * k1));
+    for (int b = 0; b < (E + 7) / 8; ++b) {
+        float2 w = wb[b];
+#pragma unroll
+        for (int j = 0; j < 8 && 8 * b + j < E; ++j) {
+            const int k1 = 8 * b + j;
+            const float2 y = k1 == 0 ? x[D::slot(0)] : cmul(x[D::slot(k1)], w);
+            buf[k1 * S::S1 + t] = y;
+            w = cmul(w, w1);
+        }
     }
-#pragma unroll
-    for (int k1 = 0; k1 < E; ++k1) buf[k1 * S::S1 + t] = x[k1];
     group_bar(bar, P);
     // phase 2: for (k1, u) = (t / R3 + R2 i, t % R3), R2-point DFT over v of
     // S1[k1][u + R3 v], twiddle w_P^{u c} = w_N^{u c E}
-    const int u = t % R3, k1b = t / R3;
 #pragma unroll
     for (int i = 0; i < E / R2; ++i) {
         float2 *v = x + i * R2;
         const int k1 = k1b + R2 * i;
 #pragma unroll
         for (int vv = 0; vv < R2; ++vv) v[vv] = buf[k1 * S::S1 + u + R3 * vv];
-        dft<R2>(v);
-        if (u > 0) {
+        Dft<R2>::run(v);  // R2 <= 8: natural order
 #pragma unroll
-            for (int c = 1; c < R2; ++c) v[c] = cmul(v[c], __ldg(tw + u * c * E));
-        }
+        for (int c = 1; c < R2; ++c) v[c] = cmul(v[c], w2[c]);
     }
     group_bar(bar, P);
 #pragma unroll
@@ -181,7 +203,6 @@ __device__ __forceinline__ void line_fft(float2 *x, int t, float2 *buf, const fl
     group_bar(bar, P);
     // phase 3: for h = t + P i (k1 = h % E, c = h / E), R3-point DFT over u of
     // S2[c][u][k1]; output d lands at position k1 + E (c + R2 d) = t + P (i + (E / R3) d)
-    float2 y[E];
 #pragma unroll
     for (int i = 0; i < E / R3; ++i) {
         const int h = t + P * i;
@@ -189,12 +210,10 @@ __device__ __forceinline__ void line_fft(float2 *x, int t, float2 *buf, const fl
         float2 w[R3];
 #pragma unroll
         for (int uu = 0; uu < R3; ++uu) w[uu] = buf[c * S::CS + uu * S::EU + k1];
-        dft<R3>(w);
+        Dft<R3>::run(w);
 #pragma unroll
-        for (int d = 0; d < R3; ++d) y[i + (E / R3) * d] = w[d];
+        for (int d = 0; d < R3; ++d) x[i + (E / R3) * d] = w[d];
     }
-#pragma unroll
-    for (int m = 0; m < E; ++m) x[m] = y[m];
     group_bar(bar, P);  // the buffer may be rewritten after this
 }
 

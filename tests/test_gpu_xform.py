@@ -1,0 +1,61 @@
+"""The register-resident output-transform passes (xform_lines 8, the default
+when every case of a batch shares a supported line length) against the
+shared-memory passes (xform_lines 2) and the CPU oracle, for every supported
+line length, both transform signs (footprint: fft2; dispersion: ifft2), several
+output levels, a phase shift and different x and y lengths.
+
+Tolerances (relative L2): register vs shared-memory passes 1e-5 (both FP32,
+different operation order); batched FP32 vs the oracle's double-double
+shooting 1e-3 (the fast path's bar)."""
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+# (ny, nx), domain, modes (nlx, nly), halo -> column length nfy, row length nfx
+SHAPES = [
+    ((256, 256), (500.0, 500.0), (512, 512), 250.0),     # 512 x 512, no truncation
+    ((256, 256), (1000.0, 1000.0), (256, 256), None),    # 768 x 768
+    ((512, 512), (1000.0, 1000.0), (1024, 1024), 500.0),  # 1024 x 1024 (the production footprint)
+    ((512, 512), (1000.0, 1000.0), (512, 512), None),    # 1536 x 1536 (the benchmark)
+    ((512, 512), (1000.0, 1000.0), (512, 512), 1500.0),  # 2048 x 2048
+    ((1024, 1024), (2000.0, 2000.0), (1024, 1024), None),  # 3072 x 3072
+    ((256, 512), (1000.0, 1000.0), (512, 256), None),    # rows 1536, columns 768
+]
+
+
+def _kw(shape, domain, modes, halo, footprint, seed):
+    from oracle import bldfm_oracle as O
+
+    rng = np.random.default_rng(seed)
+    wind = O.compute_wind_fields(4.0, float(rng.uniform(0, 360)))
+    z, p = O.vertical_profiles(24, 10.0, wind, ustar=float(rng.uniform(0.25, 0.4)), mol=-40.0)
+    src = np.zeros(shape)
+    if not footprint:
+        src = rng.random(shape)
+    levels = 24 if footprint else [3, 12, 24]
+    meas = (0.37 * domain[0], 0.61 * domain[1])
+    return dict(srf_flx=src, z=z, profiles=p, domain=domain, levels=levels, modes=modes, meas_pt=meas,
+                footprint=footprint, precision="double", halo=halo)
+
+
+@pytest.mark.parametrize("footprint", [True, False])
+@pytest.mark.parametrize("shape,domain,modes,halo", SHAPES)
+def test_register_passes_match_shared_memory_passes_and_oracle(shape, domain, modes, halo, footprint):
+    from bldfm_gb300.batch import BatchSolver, solve_batch
+    from oracle import bldfm_oracle as O
+
+    kws = [_kw(shape, domain, modes, halo, footprint, seed) for seed in (1, 2)]
+    rx = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=8))
+    sm = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=2))
+    for a, b in zip(rx, sm):
+        assert a[1].shape == b[1].shape
+        assert G.rel_l2(a[1], b[1]) <= 1e-5 and G.rel_l2(a[2], b[2]) <= 1e-5, (G.rel_l2(a[1], b[1]),
+                                                                            G.rel_l2(a[2], b[2]))
+    _, oc, of = O.steady_state_transport_solver(**kws[0], sweep="shooting_dd")
+    err = max(G.rel_l2(rx[0][1], oc), G.rel_l2(rx[0][2], of))
+    print(shape, modes, halo, footprint, "rx vs double-double %.2e" % err)
+    assert err <= 1e-3, err
