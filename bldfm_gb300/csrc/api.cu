@@ -617,8 +617,8 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.cpc = xl > 0 ? xl : out_cols_per_cta(maxnfy, 8);
     while (B.cpc > 1 && col_bytes(B.cpc) > 190 * 1024) B.cpc >>= 1;
     if (B.rx_col >= 0) {
-        B.cpc = rx_lines_per_cta(B.rx_col);
-        B.rpc = rx_lines_per_cta(B.rx_row);
+        B.cpc = rx_lines_per_cta(B.rx_col, true);
+        B.rpc = rx_lines_per_cta(B.rx_row, false);
     }
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
@@ -686,8 +686,8 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
     B.persist = B.cpc == 1 && B.rpc == 1;
     if (B.rx_col >= 0) {
-        B.col_smem = rx_smem(B.rx_col);
-        B.row_smem = rx_smem(B.rx_row);
+        B.col_smem = rx_smem(B.rx_col, true);
+        B.row_smem = rx_smem(B.rx_row, false);
         B.persist = 0;
     }
     if (B.persist) {

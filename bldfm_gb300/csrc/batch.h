@@ -57,11 +57,12 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
 
 // register-resident transform passes (xform.cu), for line lengths 512, 768,
 // 1024, 1536, 2048, 3072: config id of a length (-1 if unsupported), lines
-// per 256-thread CTA, dynamic shared memory per CTA, one-time attributes,
+// per 256-thread CTA and dynamic shared memory per CTA of the column (col)
+// or row pass, one-time attributes,
 // and the launch of the column (col) or row pass over nctas CTAs
 int rx_config(int n);
-int rx_lines_per_cta(int cfg);
-size_t rx_smem(int cfg);
+int rx_lines_per_cta(int cfg, bool col);
+size_t rx_smem(int cfg, bool col);
 void prepare_rx_attributes();
 cudaError_t launch_rx_pass(int cfg, bool col, const BatchLaunch &bl, int nctas, cudaStream_t st);
 int batch_sweep_occupancy(int threads, size_t smem);

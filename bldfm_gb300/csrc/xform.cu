@@ -2,7 +2,9 @@
 // the column pass (spectrum columns -> band-column lines along y, crop) and
 // the row pass (band rows -> lines along x, crop, conc = Re, flx = Im) of
 // bldfm_solve_batch for line lengths 64 * E.  One CTA = 256 threads = G
-// groups of P threads, one line per group (xform_reg.cuh).  Inputs are read
+// groups of P threads, one line per group (xform_reg.cuh); the row pass
+// runs two lines per group in the two lanes of packed FP32x2 arithmetic for
+// E <= 24.  Inputs are read
 // straight from global memory into registers (consecutive threads read
 // consecutive positions of a line); the column pass stages its G lines'
 // kept rows through shared memory so that every row of the intermediate
@@ -50,8 +52,11 @@ __device__ __forceinline__ void load_case_rx(BatchCase *dst, const BatchCase *sr
 // the signed mirror of P inside the mode range, H(P) = X(P).  That excludes
 // the Nyquist row and column of an untruncated spectrum, whose periodic
 // mirror (-N/2 -> -N/2) is a separately solved mode.  xpair: the column at -P
-// (bx.z) holds the signed mirror -kx of the column at P (bx.y).
-__device__ __forceinline__ float2 col_value(const SolveGeom &g, const int4 bx, bool xpair,
+// (bx.z) holds the signed mirror -kx of the column at P (bx.y).  Out of line:
+// the passes call it only for the few positions the staged one-sided path
+// does not cover, and inlining it at every unrolled position made the column
+// pass wait on instruction fetches.
+__device__ __noinline__ float2 col_value(const SolveGeom &g, const int4 bx, bool xpair,
                                             const float2 *__restrict__ Xp, const float2 *__restrict__ Xq,
                                             const double2 *__restrict__ dc, int lvl, int n, int pos)
 {
@@ -265,8 +270,8 @@ __global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_rows_batch_kernel(
             const int xo = t + P * m - px;
             if (xo >= 0 && xo < onx) {
                 const float re = x[m].x, im = cj * x[m].y;
-                sc.conc[ob + xo] = (double)re;
-                sc.flx[ob + xo] = (double)im;
+                rx::store_f64(sc.conc + ob + xo, re);
+                rx::store_f64(sc.flx + ob + xo, im);
                 bad |= !(isfinite(re) && isfinite(im));
             }
         }
@@ -274,27 +279,120 @@ __global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_rows_batch_kernel(
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
 }
 
+// Paired row pass: each group transforms output rows 2 grp and 2 grp + 1 of
+// the CTA's block together.
 template <class S>
-size_t rx_smem_of()
+__global__ void __launch_bounds__(kThreads, 2) rx2_rows_batch_kernel(const BatchCase *__restrict__ cases,
+                                                                    const int *__restrict__ cta_case, int *err)
 {
+    constexpr int P = S::P, E = S::E, G = kThreads / P, L = 2 * G;
+    using Q = rx::Pair<S>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    rx::C2 *sbuf = (rx::C2 *)smem_raw;
+    __shared__ __align__(16) BatchCase sc;
+    load_case_rx(&sc, cases + cta_case[blockIdx.x]);
+    __syncthreads();
+    const SolveGeom &g = sc.g;
+    const int64_t local = (int64_t)blockIdx.x - sc.row0;
+    const int nblk = (g.out_ny + L - 1) / L;
+    const int lvl = (int)(local / nblk), yb = (int)(local - (int64_t)lvl * nblk);
+    const int grp = threadIdx.x / P, t = threadIdx.x - grp * P;
+    const int yA = yb * L + 2 * grp;
+    bool bad = false;
+    if (yA < g.out_ny) {
+        const bool actB = yA + 1 < g.out_ny;
+        const float cj = g.out_sign > 0 ? -1.f : 1.f;
+        const int f0 = freq_min(g.nlx), f1 = freq_max(g.nlx);
+        const int h = -f0 > f1 ? -f0 : f1;
+        const float2 *rowA = sc.Cb + ((size_t)lvl * g.out_ny + yA) * g.nbx;
+        const float2 *rowB = rowA + (actB ? g.nbx : 0);
+        rx::C2 x[E];
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int bcol = band_of(t + P * m, h, S::N);
+            float2 va = make_float2(0.f, 0.f), vb = make_float2(0.f, 0.f);
+            if (bcol >= 0) {
+                va = __ldg(rowA + bcol);
+                vb = __ldg(rowB + bcol);
+            }
+            x[m].re = make_float2(va.x, vb.x);
+            x[m].im = make_float2(cj * va.y, cj * vb.y);
+        }
+        rx::line_fft2<S>(x, t, sbuf + grp * Q::BUF, sc.twx, grp + 1);
+        const int onx = g.out_nx, px = g.px;
+        const size_t oA = ((size_t)lvl * g.out_ny + yA) * onx, oB = oA + onx;
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int xo = t + P * m - px;
+            if (xo >= 0 && xo < onx) {
+                const float ra = x[m].re.x, ia = cj * x[m].im.x;
+                rx::store_f64(sc.conc + oA + xo, ra);
+                rx::store_f64(sc.flx + oA + xo, ia);
+                bad |= !(isfinite(ra) && isfinite(ia));
+                if (actB) {
+                    const float rb = x[m].re.y, ib = cj * x[m].im.y;
+                    rx::store_f64(sc.conc + oB + xo, rb);
+                    rx::store_f64(sc.flx + oB + xo, ib);
+                    bad |= !(isfinite(rb) && isfinite(ib));
+                }
+            }
+        }
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
+}
+
+// paired passes for line shapes up to E = 24 (registers: two lines' values
+// per thread), single-line passes beyond
+// Measured on the 16-footprint 512^2 batch (ncu, per launch): the paired row
+// pass ran in 41.3 us against 44.5 us single-line (29% fewer instructions at
+// half the resident warps); the paired column pass ran in 82.9 us against
+// 61.6 us (its doubled gather code stalls on instruction fetch).  So rows are
+// paired for line shapes up to E = 24 (two lines' values fit in 128
+// registers) and columns are not.
+template <class S>
+constexpr bool paired(bool col)
+{
+    return !col && S::E <= 24;
+}
+
+template <class S>
+size_t rx_smem_of(bool col)
+{
+    if (paired<S>(col))
+        return (size_t)(kThreads / S::P) * rx::Pair<S>::BUF * sizeof(rx::C2);
     return (size_t)(kThreads / S::P) * S::BUF * sizeof(float2);
 }
 
 template <class S>
 void rx_set_attr()
 {
-    cudaFuncSetAttribute(rx_cols_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rx_smem_of<S>());
-    cudaFuncSetAttribute(rx_rows_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rx_smem_of<S>());
+    if constexpr (S::E <= 24)
+        cudaFuncSetAttribute(rx2_rows_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)rx_smem_of<S>(false));
+    else
+        cudaFuncSetAttribute(rx_rows_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)rx_smem_of<S>(false));
+    cudaFuncSetAttribute(rx_cols_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)rx_smem_of<S>(true));
 }
 
 template <class S>
 cudaError_t rx_launch(bool col, const BatchLaunch &bl, int nctas, cudaStream_t st)
 {
+    const size_t b = rx_smem_of<S>(col);
     if (col)
-        rx_cols_batch_kernel<S><<<nctas, kThreads, rx_smem_of<S>(), st>>>(bl.cases, bl.col_case, bl.err);
+        rx_cols_batch_kernel<S><<<nctas, kThreads, b, st>>>(bl.cases, bl.col_case, bl.err);
+    else if constexpr (S::E <= 24)
+        rx2_rows_batch_kernel<S><<<nctas, kThreads, b, st>>>(bl.cases, bl.row_case, bl.err);
     else
-        rx_rows_batch_kernel<S><<<nctas, kThreads, rx_smem_of<S>(), st>>>(bl.cases, bl.row_case, bl.err);
+        rx_rows_batch_kernel<S><<<nctas, kThreads, b, st>>>(bl.cases, bl.row_case, bl.err);
     return cudaGetLastError();
+}
+
+template <class S>
+constexpr int rx_lines_of(bool col)
+{
+    return (paired<S>(col) ? 2 : 1) * (kThreads / S::P);
 }
 
 }  // namespace
@@ -312,20 +410,28 @@ int rx_config(int n)
     }
 }
 
-int rx_lines_per_cta(int cfg)
-{
-    return cfg == 1 ? kThreads / S768::P : (cfg >= 0 ? kThreads / 64 : 0);
-}
-
-size_t rx_smem(int cfg)
+int rx_lines_per_cta(int cfg, bool col)
 {
     switch (cfg) {
-    case 0: return rx_smem_of<S512>();
-    case 1: return rx_smem_of<S768>();
-    case 2: return rx_smem_of<S1024>();
-    case 3: return rx_smem_of<S1536>();
-    case 4: return rx_smem_of<S2048>();
-    case 5: return rx_smem_of<S3072>();
+    case 0: return rx_lines_of<S512>(col);
+    case 1: return rx_lines_of<S768>(col);
+    case 2: return rx_lines_of<S1024>(col);
+    case 3: return rx_lines_of<S1536>(col);
+    case 4: return rx_lines_of<S2048>(col);
+    case 5: return rx_lines_of<S3072>(col);
+    default: return 0;
+    }
+}
+
+size_t rx_smem(int cfg, bool col)
+{
+    switch (cfg) {
+    case 0: return rx_smem_of<S512>(col);
+    case 1: return rx_smem_of<S768>(col);
+    case 2: return rx_smem_of<S1024>(col);
+    case 3: return rx_smem_of<S1536>(col);
+    case 4: return rx_smem_of<S2048>(col);
+    case 5: return rx_smem_of<S3072>(col);
     default: return 0;
     }
 }

@@ -218,3 +218,196 @@ __device__ __forceinline__ void line_fft(float2 *x, int t, float2 *buf, const fl
 }
 
 }  // namespace rx
+
+// ---------------------------------------------------------------------------
+// Paired lines: two lines of the same length transformed together by one
+// group, line A in lane 0 and line B in lane 1 of packed FP32x2 arithmetic
+// (__fadd2_rn / __fmul2_rn / __ffma2_rn).  Every operation of the transform
+// is the same for both lines, so the arithmetic, the index arithmetic and the
+// shared-memory instructions are shared: one 16-byte exchange word carries
+// both lines' values.  Same rounding per lane as the single-line transform.
+// ---------------------------------------------------------------------------
+namespace rx {
+
+struct __align__(16) C2 {
+    float2 re, im;  // (A.re, B.re), (A.im, B.im)
+};
+
+__device__ __forceinline__ float2 bc(float v) { return make_float2(v, v); }
+__device__ __forceinline__ C2 c2add(C2 a, C2 b) { return {__fadd2_rn(a.re, b.re), __fadd2_rn(a.im, b.im)}; }
+__device__ __forceinline__ C2 c2sub(C2 a, C2 b)
+{
+    return {__ffma2_rn(b.re, bc(-1.f), a.re), __ffma2_rn(b.im, bc(-1.f), a.im)};
+}
+// a * (c + i s), the same scalar in both lanes
+__device__ __forceinline__ C2 c2mul(C2 a, float c, float s)
+{
+    return {__ffma2_rn(a.im, bc(-s), __fmul2_rn(a.re, bc(c))), __ffma2_rn(a.im, bc(c), __fmul2_rn(a.re, bc(s)))};
+}
+// a * (-i)
+__device__ __forceinline__ C2 c2rot_m(C2 a) { return {a.im, __fmul2_rn(a.re, bc(-1.f))}; }
+
+// forward DFTs of length 2, 3, 4, 8 on paired values, natural order (the
+// formulas of dft_small with sign -1)
+template <int N>
+__device__ __forceinline__ void dft2_small(C2 *u)
+{
+    if constexpr (N == 2) {
+        const C2 a = u[0], b = u[1];
+        u[0] = c2add(a, b);
+        u[1] = c2sub(a, b);
+    } else if constexpr (N == 4) {
+        const C2 a0 = c2add(u[0], u[2]), a1 = c2sub(u[0], u[2]);
+        const C2 b0 = c2add(u[1], u[3]), b1 = c2rot_m(c2sub(u[1], u[3]));
+        u[0] = c2add(a0, b0);
+        u[2] = c2sub(a0, b0);
+        u[1] = c2add(a1, b1);
+        u[3] = c2sub(a1, b1);
+    } else if constexpr (N == 3) {
+        const float s1 = -0.86602540378443864676f;
+        const C2 s = c2add(u[1], u[2]), d = c2sub(u[1], u[2]), a = u[0];
+        u[0] = c2add(a, s);
+        const C2 m = {__ffma2_rn(s.re, bc(-0.5f), a.re), __ffma2_rn(s.im, bc(-0.5f), a.im)};
+        const C2 r = {__fmul2_rn(d.im, bc(-s1)), __fmul2_rn(d.re, bc(s1))};  // i s1 d
+        u[1] = c2add(m, r);
+        u[2] = c2sub(m, r);
+    } else if constexpr (N == 8) {
+        C2 a[4], b[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            a[t] = u[2 * t];
+            b[t] = u[2 * t + 1];
+        }
+        dft2_small<4>(a);
+        dft2_small<4>(b);
+        const float h = 0.70710678118654752440f;
+        // b[k] *= w_8^k, w_8 = (1 - i) / sqrt2
+        b[1] = {__fmul2_rn(__fadd2_rn(b[1].re, b[1].im), bc(h)),
+                __fmul2_rn(__ffma2_rn(b[1].re, bc(-1.f), b[1].im), bc(h))};
+        b[2] = c2rot_m(b[2]);
+        b[3] = {__fmul2_rn(__ffma2_rn(b[3].re, bc(-1.f), b[3].im), bc(h)),
+                __fmul2_rn(__ffma2_rn(b[3].im, bc(-1.f), __fmul2_rn(b[3].re, bc(-1.f))), bc(h))};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            u[t] = c2add(a[t], b[t]);
+            u[t + 4] = c2sub(a[t], b[t]);
+        }
+    }
+}
+
+// In-place paired DFT, output permutation Dft<N>::slot.
+template <int N>
+__device__ __forceinline__ void dft2(C2 *x)
+{
+    using D = Dft<N>;
+    if constexpr (D::direct) {
+        if constexpr (N > 1) dft2_small<N>(x);
+    } else {
+        constexpr int A = D::A, F = D::F;
+        sfor<0, F>([&](auto S1) {
+            constexpr int s1 = decltype(S1)::value;
+            C2 u[A];
+#pragma unroll
+            for (int s2 = 0; s2 < A; ++s2) u[s2] = x[s1 + F * s2];
+            dft2_small<A>(u);
+            sfor<0, A>([&](auto K1) {
+                constexpr int k1 = decltype(K1)::value;
+                constexpr int m = (s1 * k1) % N;
+                if constexpr (m == 0)
+                    x[s1 + F * k1] = u[k1];
+                else
+                    x[s1 + F * k1] = c2mul(u[k1], Tw<m, N>::c, -Tw<m, N>::s);
+            });
+        });
+#pragma unroll
+        for (int k1 = 0; k1 < A; ++k1) dft2<F>(x + F * k1);
+    }
+}
+
+// Exchange layouts for 16-byte words (a quarter-warp per wavefront):
+// S1[k1][t] row stride P; S2[c][u][k1] u stride E + 1 (odd), c stride R3 (E + 1).
+template <class S>
+struct Pair {
+    static constexpr int S1 = S::P;
+    static constexpr int EU = S::E + 1;
+    static constexpr int CS = S::R3 * EU;
+    static constexpr int BUF = (S::E * S1 > S::R2 * CS) ? S::E * S1 : S::R2 * CS;  // C2 words per group
+};
+
+// The paired line transform: x holds the E paired values at positions
+// t + P m of lines A and B in, the paired outputs at the same positions out.
+// buf: the group's Pair<S>::BUF words.  Twiddles as in line_fft.
+template <class S>
+__device__ __forceinline__ void line_fft2(C2 *x, int t, C2 *buf, const float2 *__restrict__ tw, int bar)
+{
+    constexpr int E = S::E, R2 = S::R2, R3 = S::R3, P = S::P;
+    using D = Dft<E>;
+    using Q = Pair<S>;
+    float2 wb[(E + 7) / 8];
+#pragma unroll
+    for (int b = 0; b < (E + 7) / 8; ++b) wb[b] = __ldg(tw + 8 * b * t);
+    const float2 w1 = __ldg(tw + t);
+    const int u = t % R3, k1b = t / R3;
+    float2 w2[R2];
+#pragma unroll
+    for (int c = 1; c < R2; ++c) w2[c] = __ldg(tw + u * c * E);
+    dft2<E>(x);
+#pragma unroll
+    for (int b = 0; b < (E + 7) / 8; ++b) {
+        float2 w = wb[b];
+#pragma unroll
+        for (int j = 0; j < 8 && 8 * b + j < E; ++j) {
+            const int k1 = 8 * b + j;
+            buf[k1 * Q::S1 + t] = k1 == 0 ? x[D::slot(0)] : c2mul(x[D::slot(k1)], w.x, w.y);
+            w = cmul(w, w1);
+        }
+    }
+    group_bar(bar, P);
+#pragma unroll
+    for (int i = 0; i < E / R2; ++i) {
+        C2 *v = x + i * R2;
+        const int k1 = k1b + R2 * i;
+#pragma unroll
+        for (int vv = 0; vv < R2; ++vv) v[vv] = buf[k1 * Q::S1 + u + R3 * vv];
+        dft2<R2>(v);
+#pragma unroll
+        for (int c = 1; c < R2; ++c) v[c] = c2mul(v[c], w2[c].x, w2[c].y);
+    }
+    group_bar(bar, P);
+#pragma unroll
+    for (int i = 0; i < E / R2; ++i) {
+        const int k1 = k1b + R2 * i;
+#pragma unroll
+        for (int c = 0; c < R2; ++c) buf[c * Q::CS + u * Q::EU + k1] = x[i * R2 + c];
+    }
+    group_bar(bar, P);
+#pragma unroll
+    for (int i = 0; i < E / R3; ++i) {
+        const int h = t + P * i;
+        const int k1 = h % E, c = h / E;
+        C2 w[R3];
+#pragma unroll
+        for (int uu = 0; uu < R3; ++uu) w[uu] = buf[c * Q::CS + uu * Q::EU + k1];
+        dft2<R3>(w);
+#pragma unroll
+        for (int d = 0; d < R3; ++d) x[i + (E / R3) * d] = w[d];
+    }
+    group_bar(bar, P);
+}
+
+// Exact FP32 -> FP64 store without the FP64 pipe for normal numbers and zero
+// (sign, exponent rebiased by 1023 - 127, mantissa shifted by 29); subnormal,
+// infinite and NaN values take the conversion instruction.
+__device__ __forceinline__ void store_f64(double *p, float v)
+{
+    const uint32_t b = __float_as_uint(v), a = b & 0x7fffffffu;
+    if (a - 0x00800000u < 0x7f000000u) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(b << 29, (b & 0x80000000u) | ((a >> 3) + 0x38000000u));
+    } else if (a == 0) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(0u, b);
+    } else {
+        *p = (double)v;
+    }
+}
+
+}  // namespace rx
