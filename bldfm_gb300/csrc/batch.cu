@@ -41,13 +41,11 @@ __device__ __forceinline__ void load_case(BatchCase *dst, const BatchCase *src)
 // one case (two per thread, sharing the level-table loads).  The case's level
 // table is brought into shared memory by one bulk copy whenever the case
 // changes (the mbarrier flips phase each time; every wait is bounded).
-// NT = blockDim.x (128 or 256).  Register budgets: 256 threads x 4 CTAs
-// (64 registers, 32 warps per SM); 128 threads x 9 CTAs (56 registers and
-// 56 bytes of spill stores, 36 warps per SM), which ran the 16-footprint
-// 512^2 sweep 5% faster before the step loops were unrolled; since then the
-// two run it in about the same time and the autotuner picks.
+// NT = blockDim.x (128 or 256).  Register budget: 64 registers (no spills)
+// for both, 32 warps per SM (256 threads x 4 CTAs, 128 threads x 8 CTAs);
+// the autotuner picks the shape.
 template <int NT>
-__global__ void __launch_bounds__(NT, NT == 128 ? 9 : 4)
+__global__ void __launch_bounds__(NT, NT == 128 ? 8 : 4)
     riccati32_batch_kernel(const BatchCase *__restrict__ cases, const int *__restrict__ tile_case,
                            const int64_t *__restrict__ cta_tiles, int *err)
 {

@@ -360,7 +360,7 @@ __device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const floa
             const int u = 2 * h + l;
             int r, c;
             bool paired;
-            unpack_mode(modes[m[u < nvalid ? u : 0]], r, c, paired);
+            unpack_mode(modes[u < nvalid ? m[u] : m[0]], r, c, paired);
             const float lx = ax * (float)freq_of_index(c, g.nlx), ly = ay * (float)freq_of_index(r, g.nly);
             sc[l].init(lx, ly, g.ex, g.ey);
             const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
