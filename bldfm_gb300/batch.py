@@ -20,7 +20,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .solver import _normalise_levels, make_desc, plan
+from .solver import _normalise_levels, make_desc, output_grid, plan
 
 
 def _count(shape):
@@ -226,28 +226,8 @@ class BatchSolver:
         return int(st[0])
 
 
-_GRID_CACHE = {}
 _DESC_CACHE = {}  # descriptor and output shape per case geometry
-
-
-def _grid(z, levels, shape, domain):
-    """The reference's output grid (solver.py:292-297) as read-only arrays,
-    shared between cases with the same levels, shape and domain."""
-    zl = np.asarray(z)[levels]
-    key = (zl.tobytes(), tuple(shape), tuple(domain))
-    g = _GRID_CACHE.get(key)
-    if g is None:
-        ny, nx = shape
-        x = np.linspace(0, domain[0], nx, endpoint=False)
-        y = np.linspace(0, domain[1], ny, endpoint=False)
-        Z, Y, X = np.meshgrid(zl, y, x, indexing="ij")
-        g = tuple(np.squeeze(a) for a in (X, Y, Z))
-        for a in g:
-            a.flags.writeable = False
-        if len(_GRID_CACHE) > 64:
-            _GRID_CACHE.clear()
-        _GRID_CACHE[key] = g
-    return g
+_grid = output_grid
 
 
 def _enqueue_batch(solver, cases):

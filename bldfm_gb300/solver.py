@@ -10,6 +10,8 @@ steady_state_transport_solver``) or by assigning it to
 ``bldfm.interface.steady_state_transport_solver``.
 """
 
+import threading
+
 import numpy as np
 
 from . import _lib
@@ -33,6 +35,51 @@ def _normalise_levels(levels, nz):
     if np.any(bad):
         raise IndexError("index %d is out of bounds for axis 0 with size %d" % (int(lv[bad][0]), nz))
     return levels, np.ascontiguousarray(lv)
+
+
+_GRID_CACHE = {}
+
+
+def output_grid(z, levels, shape, domain):
+    """The reference's output grid (solver.py:292-297), squeezed like the
+    reference's, as read-only arrays shared between calls with the same
+    levels, shape and domain (building three fresh (ny, nx) arrays costs
+    more host time than an FP32 solve)."""
+    zl = np.asarray(z)[levels]
+    key = (zl.tobytes(), tuple(shape), tuple(domain))
+    g = _GRID_CACHE.get(key)
+    if g is None:
+        ny, nx = shape
+        x = np.linspace(0, domain[0], nx, endpoint=False)
+        y = np.linspace(0, domain[1], ny, endpoint=False)
+        Z, Y, X = np.meshgrid(zl, y, x, indexing="ij")
+        g = tuple(np.squeeze(a) for a in (X, Y, Z))
+        for a in g:
+            a.flags.writeable = False
+        if len(_GRID_CACHE) > 64:
+            _GRID_CACHE.clear()
+        _GRID_CACHE[key] = g
+    return g
+
+
+_FP32_SOLVERS = {}  # device index -> one-case batch solver of the FP32 drop-in calls
+_FP32_LOCK = threading.Lock()
+
+
+def _solve_fp32_one(kw):
+    """One FP32 solve through the batched path: cached plan and descriptors,
+    the case's host data in one pinned upload, graph replay while the shapes
+    repeat, outputs back in one copy into pinned memory."""
+    import torch
+
+    from .batch import BatchSolver, _enqueue_batch, _finish_batch
+
+    dev = torch.cuda.current_device()
+    with _FP32_LOCK:
+        s = _FP32_SOLVERS.get(dev)
+        if s is None:
+            s = _FP32_SOLVERS[dev] = BatchSolver(device=dev, use_graph=True)
+        return _finish_batch(_enqueue_batch(s, [kw]))[0]
 
 
 def make_desc(shape, nz, domain, modes, meas_pt, srf_bg_conc, footprint, analytic, halo, precision, mode):
@@ -88,7 +135,10 @@ def steady_state_transport_solver(
     Parameters are the reference's.  The keyword-only ``mode`` selects the
     sweep: ``"fp64"`` (default) integrates the reference's shooting method with
     the reference's rounding; ``"fp32"`` integrates the same discrete problem
-    with the FP32 invariant-imbedding sweep (relative L2 error about 1e-5).
+    with the FP32 invariant-imbedding sweep (relative L2 about 1e-6 against
+    the exact discrete solution), through the batched path as a batch of one;
+    ``"fp64r"`` is the invariant imbedding in FP64.  The grid arrays are
+    shared, read-only arrays (the same values and shapes as the reference's).
     ``cache`` is a Green's-function cache with the reference's ``get``/``put``
     interface (src/bldfm/cache.py:19-83), consulted in footprint mode only;
     results of ``mode`` "fp32"/"fp64r" are stored under their own key and only
@@ -110,6 +160,17 @@ def steady_state_transport_solver(
     shape = np.shape(srf_flx)
     if len(shape) != 2:
         raise ValueError("srf_flx must be a 2D array")
+    if mode == "fp32" and not analytic:
+        if (modes[0] % 2) or (modes[1] % 2):
+            raise ValueError("modes must consist of even numbers.")
+        if precision not in ("single", "double"):
+            raise ValueError("precision must be single (default) or double.")
+        result = _solve_fp32_one(dict(srf_flx=srf_flx, z=z, profiles=profiles, domain=domain, levels=levels,
+                                      modes=modes, meas_pt=meas_pt, srf_bg_conc=srf_bg_conc, footprint=footprint,
+                                      halo=halo, precision=precision))
+        if use_cache:
+            cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result, **ckw)
+        return result
     zz = np.ascontiguousarray(z, dtype=np.float64)
     nz = zz.shape[0]
     prof = np.ascontiguousarray(np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in profiles]))
@@ -131,12 +192,7 @@ def steady_state_transport_solver(
     if precision == "single" and not footprint and not (xm**2 + ym**2 > 0.0):
         conc = conc.astype(np.float32)
         flx = flx.astype(np.float32)
-    ny, nx = shape
-    xmx, ymx = domain
-    x = np.linspace(0, xmx, nx, endpoint=False)
-    y = np.linspace(0, ymx, ny, endpoint=False)
-    Z, Y, X = np.meshgrid(zz[levels], y, x, indexing="ij")
-    grid = (np.squeeze(X), np.squeeze(Y), np.squeeze(Z))
+    grid = output_grid(zz, levels, shape, domain)
     result = (grid, np.squeeze(conc), np.squeeze(flx))
     if use_cache:
         cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result, **ckw)

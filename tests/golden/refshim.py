@@ -22,6 +22,10 @@ import os
 import sys
 import types
 
+# The reference's src/ directory: BLDFM_REFERENCE_SRC, else the location of the
+# read-only reference checkout in the build container.  The GPU machines have
+# no reference tree; everything that imports it skips itself there
+# (reference_available()).
 REFERENCE_SRC = os.environ.get("BLDFM_REFERENCE_SRC", "/root/reference/src")
 
 

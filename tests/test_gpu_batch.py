@@ -44,9 +44,32 @@ def _cases(seed):
 
 
 def _single(kw):
-    from bldfm_gb300 import steady_state_transport_solver
+    """The single-solve FP32 entry point (bldfm_solve_host: riccati32_kernel
+    and the single-solve transforms), not the drop-in, which runs FP32 calls
+    through the batched path."""
+    from bldfm_gb300 import _lib
+    from bldfm_gb300.solver import _normalise_levels, make_desc, output_grid
 
-    return steady_state_transport_solver(**kw, mode="fp32")
+    lib = _lib.load()
+    z = np.ascontiguousarray(kw["z"], dtype=np.float64)
+    nz = len(z)
+    prof = np.ascontiguousarray(np.stack([np.broadcast_to(np.asarray(a, dtype=np.float64), (nz,))
+                                          for a in kw["profiles"]]))
+    levels, lv = _normalise_levels(kw["levels"], nz)
+    shape = np.shape(kw["srf_flx"])
+    d = make_desc(shape, nz, kw["domain"], kw["modes"], kw["meas_pt"], kw.get("srf_bg_conc", 0.0),
+                  kw["footprint"], False, kw.get("halo"), kw["precision"], "fp32")
+    info = _lib.PlanInfo()
+    _lib.check(lib.bldfm_plan(d, int(lv.size), info))
+    conc = np.empty((lv.size, info.out_ny, info.out_nx))
+    flx = np.empty_like(conc)
+    src = None if kw["footprint"] else np.ascontiguousarray(kw["srf_flx"], dtype=np.float64)
+    _lib.check(lib.bldfm_solve_host(d, _lib.ptr(src), _lib.ptr(z), _lib.ptr(prof), _lib.ptr(lv), int(lv.size),
+                                    _lib.ptr(conc), _lib.ptr(flx)))
+    xm, ym = kw["meas_pt"]
+    if kw["precision"] == "single" and not kw["footprint"] and not (xm**2 + ym**2 > 0.0):
+        conc, flx = conc.astype(np.float32), flx.astype(np.float32)
+    return output_grid(z, levels, shape, kw["domain"]), np.squeeze(conc), np.squeeze(flx)
 
 
 @pytest.mark.parametrize("use_graph", [False, True])
