@@ -1073,6 +1073,16 @@ int sur_batch_check(const bldfm_case *cs, const bldfm_surrogate_case *mets, int 
     return BLDFM_OK;
 }
 
+// Accuracy guard of the batched surrogate: every SUR_GUARD_STRIDE-th solved
+// mode of each case re-solved exactly (FP32 sweep) and compared with the
+// served spectra.  The blob's extra region holds the SurCase records, then
+// the guard's sample offsets; the per-case sums (4 floats) sit in the last
+// sur_guard_bytes(n) bytes of the planned workspace.
+enum { SUR_GUARD_STRIDE = 61 };  // prime: no alignment with the rows of a column
+size_t sur_prefix_off(int n) { return (sizeof(SurCase) * (size_t)n + 15) & ~(size_t)15; }
+size_t sur_extra_bytes(int n) { return sur_prefix_off(n) + 8 * ((size_t)n + 1); }
+size_t sur_guard_bytes(int n) { return al(16 * (size_t)n); }
+
 int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_case *mets, int n, void *ws,
                          size_t ws_bytes, cudaStream_t st)
 {
@@ -1085,8 +1095,8 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     if (status != BLDFM_OK) return status;
     BatchBuild B;
     bldfm_batch_opts opts = {256, 0, 0, 0};
-    if ((rc = batch_build(cs, n, &opts, &dc, B, sizeof(SurCase) * (size_t)n)) != BLDFM_OK) return rc;
-    if (ws_bytes < B.total) return BLDFM_ERR_WORKSPACE;
+    if ((rc = batch_build(cs, n, &opts, &dc, B, sur_extra_bytes(n))) != BLDFM_OK) return rc;
+    if (ws_bytes < B.total + sur_guard_bytes(n)) return BLDFM_ERR_WORKSPACE;
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
         const int nz = g.nz;
@@ -1124,6 +1134,12 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
         c.tile0 = t;
         t += (g.nsolved + 127) / 128;
     }
+    int64_t *prefix = (int64_t *)(blob + B.extra_off + sur_prefix_off(n));
+    prefix[0] = 0;
+    for (int k = 0; k < n; ++k) {
+        const int64_t s = (B.hp[k].g.nsolved + SUR_GUARD_STRIDE - 1) / SUR_GUARD_STRIDE;
+        prefix[k + 1] = prefix[k] + ((s + 31) & ~(int64_t)31);
+    }
     timers_begin(dc);
     tmark(dc, st);  // 0: upload
     CK(cudaMemcpyAsync(w + B.blob_at, blob, B.blob_bytes, cudaMemcpyHostToDevice, st));
@@ -1134,6 +1150,10 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     char *wb = w + B.blob_at;
     tmark(dc, st);  // 1: the fused features -> MLP -> spectra kernel
     CK(launch_sur_serve((const SurCase *)(wb + B.extra_off), n, t, view, (int *)w, dc.nsm, st));
+    float4 *acc = (float4 *)(w + B.total);
+    CK(cudaMemsetAsync(acc, 0, 16 * (size_t)n, st));
+    CK(launch_sur_guard((const BatchCase *)(wb + B.off_cases), n, (const int64_t *)(wb + B.extra_off + sur_prefix_off(n)),
+                        prefix[n], SUR_GUARD_STRIDE, acc, st));
     tmark(dc, st);  // 2: the output transform
     BatchLaunch bl;
     memset(&bl, 0, sizeof(bl));
@@ -1469,9 +1489,8 @@ int bldfm_surrogate_batch_plan(const bldfm_case *cases, const bldfm_surrogate_ca
     std::lock_guard<std::mutex> lk(g_mutex);
     BatchBuild B;
     bldfm_batch_opts opts = {256, 0, 0, 0};
-    if ((rc = batch_build(cases, ncases, &opts, nullptr, B, sizeof(SurCase) * (size_t)ncases)) != BLDFM_OK)
-        return rc;
-    *workspace_bytes = (int64_t)B.total;
+    if ((rc = batch_build(cases, ncases, &opts, nullptr, B, sur_extra_bytes(ncases))) != BLDFM_OK) return rc;
+    *workspace_bytes = (int64_t)(B.total + sur_guard_bytes(ncases));
     return BLDFM_OK;
 }
 

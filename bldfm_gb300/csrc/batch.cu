@@ -393,6 +393,60 @@ __global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
 }
 
+// Accuracy guard of the surrogate's batched footprints: sample i of the
+// batch is solved mode (i - prefix[k]) * stride of case k (prefix[k] <= i <
+// prefix[k + 1], every case's sample count padded to a multiple of 32, the
+// padding contributing nothing).  Each sample's exact FP32 values
+// (ricc_mode_value) are compared with the spectra the serving kernel wrote;
+// acc[k] accumulates (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2) of
+// case k (one atomic per warp and quantity).
+__global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restrict__ cases, int n,
+                                                        const int64_t *__restrict__ prefix, int stride,
+                                                        float4 *__restrict__ acc)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= prefix[n]) return;  // whole warps: prefix[n] is a multiple of 32
+    int k = 0;
+    while (k + 1 < n && prefix[k + 1] <= i) ++k;
+    const BatchCase &bc = cases[k];
+    const int64_t m = (i - prefix[k]) * (int64_t)stride;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (m < bc.g.nsolved) {
+        float2 pe, qe;
+        int r, c;
+        if (bc.g.iso)
+            ricc_mode_value<true>(bc.g, bc.lv32, bc.modes, bc.ax, bc.ay, m, pe, qe, r, c);
+        else
+            ricc_mode_value<false>(bc.g, bc.lv32, bc.modes, bc.ax, bc.ay, m, pe, qe, r, c);
+        const size_t o = spec_idx(bc.g, 0, r, c);
+        const float2 pn = bc.Xp[o], qn = bc.Xq[o];
+        const float dpx = pn.x - pe.x, dpy = pn.y - pe.y, dqx = qn.x - qe.x, dqy = qn.y - qe.y;
+        v = make_float4(dpx * dpx + dpy * dpy, pe.x * pe.x + pe.y * pe.y, dqx * dqx + dqy * dqy,
+                        qe.x * qe.x + qe.y * qe.y);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+        v.z += __shfl_down_sync(0xffffffffu, v.z, off);
+        v.w += __shfl_down_sync(0xffffffffu, v.w, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[k].x, v.x);
+        atomicAdd(&acc[k].y, v.y);
+        atomicAdd(&acc[k].z, v.z);
+        atomicAdd(&acc[k].w, v.w);
+    }
+}
+
+cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefix, int64_t nsamples, int stride,
+                             float4 *acc, cudaStream_t st)
+{
+    if (nsamples <= 0) return cudaSuccess;
+    sur_guard_kernel<<<(unsigned)((nsamples + 255) / 256), 256, 0, st>>>(cases, n, prefix, stride, acc);
+    return cudaGetLastError();
+}
+
 void prepare_batch_attributes();
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part)

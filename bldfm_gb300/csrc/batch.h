@@ -55,6 +55,13 @@ struct BatchLaunch {
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);
 
+// Accuracy guard of a surrogate batch (batch.cu: sur_guard_kernel): exact
+// FP32 values of every stride-th solved mode against the served spectra,
+// per-case sums into acc[k] = (|dXp|^2, |Xp|^2, |dXq|^2, |Xq|^2); prefix:
+// n + 1 sample offsets, each case's count padded to a multiple of 32.
+cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefix, int64_t nsamples, int stride,
+                             float4 *acc, cudaStream_t st);
+
 // register-resident transform passes (xform.cu), for line lengths 512, 768,
 // 1024, 1536, 2048, 3072: config id of a length (-1 if unsupported), lines
 // per 256-thread CTA and dynamic shared memory per CTA of the column (col)

@@ -470,3 +470,60 @@ __device__ __forceinline__ void ricc_mode_pair(const SolveGeom &g, const float *
     const int64_t m[2] = {ma, mb};
     ricc_modes_packed<ISO, 1>(g, s_lv, modes, q0spec, Xp, Xq, ax, ay, m, mb >= 0 ? 2 : 1);
 }
+
+// Exact FP32 values (p, q) of one solved mode m at the single output level,
+// phase-shifted like the solve's spectra, with the level table read from
+// global memory (rows of BLDFM_LV32 floats): the sweep of ricc_mode (ratio
+// above the output level, ratio and flux product below it) for a footprint
+// (unit source spectrum q0dc_fp).  (r, c) receive the mode's row and column.
+// Used by the surrogate's accuracy guard on a sample of modes.
+template <bool ISO>
+__device__ __forceinline__ void ricc_mode_value(const SolveGeom &g, const float *__restrict__ lv,
+                                                const uint32_t *__restrict__ modes, float ax, float ay, int64_t m,
+                                                float2 &p, float2 &q, int &r, int &c)
+{
+    const int L = g.nz - 1;
+    const int jmax = g.jmax;
+    bool paired;
+    unpack_mode(modes[m], r, c, paired);
+    const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
+    const float lx = ax * (float)kx, ly = ay * (float)ky;
+    StepCoef<ISO> sc;
+    sc.init(lx, ly, g.ex, g.ey);
+    const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
+                                 fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+    const float2 eg = csqrt_f(w);
+    const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+    const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
+    float2 R = make_float2(ke.x * inv, -ke.y * inv);
+    int i = L - 1;
+    for (; i >= jmax; --i) {
+        float2 a, b, cc;
+        sc.eval(lv + (size_t)i * BLDFM_LV32, a, b, cc);
+        ricc_step(R, a, b, cc);
+    }
+    const float2 Rj = R;
+    float2 Q = make_float2(1.f, 0.f);
+    int E = 0, cnt = 0;
+    for (; i >= 0; --i) {
+        float2 a, b, cc;
+        sc.eval(lv + (size_t)i * BLDFM_LV32, a, b, cc);
+        ricc_step(R, a, b, cc);
+        flux_step(Q, R, a, cc);
+        if (++cnt == 8) {
+            cnt = 0;
+            renorm(Q, E);
+        }
+    }
+    float2 sh = make_float2(1.f, 0.f);
+    if (g.do_shift) {
+        const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
+        float sn, cs;
+        sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
+        sh = make_float2(cs, sn);
+    }
+    const float2 q0 = make_float2((float)g.q0dc_fp, 0.f);
+    q = fc_mul(q0, make_float2(ldexpf(Q.x, E), ldexpf(Q.y, E)));
+    p = fc_mul(fc_mul(Rj, q), sh);
+    q = fc_mul(q, sh);
+}

@@ -9,8 +9,12 @@ top).  A 8 -> 4 x 256 GELU -> 4 MLP (``mlp.MLP``, tcgen05 BF16 GEMMs with FP32
 accumulation) learns that transfer from data the FP32 invariant-imbedding
 sweep generates on the device (``TransferPool``), trained with Adam
 (``train``); ``Surrogate`` serves footprints through it inside the training
-box and through the FP64 solver outside it, and re-solves every
-``spot_every``-th case with the FP64 solver, returning the solver's result
+box and through the FP64 solver outside it.  Every served case of a batch is
+checked by the library's accuracy guard: every 61st solved mode is re-solved
+exactly (FP32 sweep) on the device and compared with the served spectrum,
+which estimates the case's relative L2 error; cases whose estimate exceeds
+``guard_tol`` are re-solved by the FP32 solver.  Every ``spot_every``-th case
+is also re-solved in full by the FP64 solver, returning the solver's result
 when the surrogate's relative L2 error exceeds ``tol``.
 
 The reference solve of a spot check is the accurate FP64 mode (``mode="fp64r"``: the
@@ -224,7 +228,8 @@ class Surrogate:
     by the network, out-of-box fallbacks, spot checks and their failures.
     """
 
-    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0, spot_mode="fp64r", fallback="fp64"):
+    def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0, spot_mode="fp64r", fallback="fp64",
+                 guard_tol=None, guard_mode="fp32"):
         self.lib = _lib.load()
         self.net = net
         self.box = dict(BOX if box is None else box)
@@ -233,11 +238,18 @@ class Surrogate:
         self.variant = int(variant)  # 0 fused kernel, 1 exact transfer (check), 2 layer by layer
         self.spot_mode = spot_mode
         self.fallback = fallback
+        # the guard's estimate is the sampled spectral error over the extended
+        # grid; measured on 20 in-box 512^2 footprints it was 1.06 to 2.5 times
+        # the true error of the cropped fields (never below it), so cases
+        # above guard_tol (default: tol) are re-solved
+        self.guard_tol = self.tol if guard_tol is None else float(guard_tol)
+        self.guard_mode = guard_mode
         self.device = torch.device("cuda", torch.cuda.current_device())
         self._ws = None
         self._out = None
         self.count = 0
-        self.stats = {"surrogate": 0, "out_of_box": 0, "spot": 0, "spot_fail": 0, "errors": []}
+        self.stats = {"surrogate": 0, "out_of_box": 0, "spot": 0, "spot_fail": 0, "errors": [], "guard": [],
+                      "guard_fail": 0, "spot_guard": []}
 
     def in_box(self, n, zm, s1, s2, kmax):
         b = self.box
@@ -330,6 +342,22 @@ class Surrogate:
         _lib.check(st, "surrogate_solve_batch")
         return b["outs"]
 
+    def guard_estimates(self, b, stream=None):
+        """Per-case relative L2 error estimates of the last solve of prepared
+        batch b from the library's accuracy guard (sampled spectra against
+        the exact FP32 sweep): max over p and q of sqrt(sum |dX|^2 / sum |X|^2)."""
+        n = b["n"]
+        gb = (16 * n + 255) & ~255
+        off = b["need"] - gb
+        s = stream or torch.cuda.current_stream(self.device)
+        host = torch.empty(4 * n, dtype=torch.float32, pin_memory=True)
+        with torch.cuda.stream(s):
+            host.copy_(self._ws[off : off + 16 * n].view(torch.float32), non_blocking=True)
+        s.synchronize()
+        a = host.numpy().reshape(n, 4).astype(np.float64)
+        tiny = 1e-300
+        return np.sqrt(np.maximum(a[:, 0] / np.maximum(a[:, 1], tiny), a[:, 2] / np.maximum(a[:, 3], tiny)))
+
     def status(self, stream=None):
         """Device status word of the last launch (0, or a BLDFM_ERR_* code),
         read through the launch stream (default: the current stream)."""
@@ -353,9 +381,11 @@ class Surrogate:
         in-box cases through the network in batched fused launches, every
         ``spot_every``-th of them also through the ``spot_mode`` solve (the
         FP64 result is kept when the surrogate misses ``tol``), out-of-box
-        cases through the fallback solver.  Returns (outputs, paths): outputs[k] = (conc, flx)
-        (device tensors for served cases, host arrays for solver results),
-        paths[k] in "surrogate", "fp64-spot", "fp64-box"."""
+        cases through the fallback solver; a served case whose guard estimate
+        exceeds ``guard_tol`` is re-solved by ``guard_mode``.  Returns
+        (outputs, paths): outputs[k] = (conc, flx) (device tensors for served
+        cases, host arrays for solver results), paths[k] in "surrogate",
+        "fp32-guard", "fp64-spot", "fp64-box"."""
         out, paths = [None] * len(items), [None] * len(items)
         inbox = []
         for k, kw in enumerate(items):
@@ -369,16 +399,25 @@ class Surrogate:
         for i in range(0, len(inbox), batch):
             ks = inbox[i : i + batch]
             b = self.prepare_batch([items[k] for k in ks])
-            for k, pr, (c, f) in zip(ks, b["keep"], self.solve_batch_prepared(b)):
+            res = self.solve_batch_prepared(b)
+            est = self.guard_estimates(b)
+            for k, pr, (c, f), e in zip(ks, b["keep"], res, est):
                 self.count += 1
                 self.stats["surrogate"] += 1
+                self.stats["guard"].append(float(e))
                 out[k], paths[k] = (c, f), "surrogate"
+                if not e <= self.guard_tol:
+                    self.stats["guard_fail"] += 1
+                    _, gc, gf = steady_state_transport_solver(**pr["kw"], mode=self.guard_mode)
+                    out[k], paths[k] = (gc, gf), "fp32-guard"
+                    continue
                 if self.spot_every > 0 and self.count % self.spot_every == 0:
                     ref = steady_state_transport_solver(**pr["kw"], mode=self.spot_mode)
                     ca, fa = c.cpu().numpy(), f.cpu().numpy()
                     err = max(_rell2(ca, ref[1]), _rell2(fa, ref[2]))
                     self.stats["spot"] += 1
                     self.stats["errors"].append(err)
+                    self.stats["spot_guard"].append(float(e))
                     if err > self.tol:
                         self.stats["spot_fail"] += 1
                         if self.fallback != self.spot_mode:

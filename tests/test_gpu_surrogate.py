@@ -182,6 +182,20 @@ def test_trained_network_gains_over_solver():
     b = sur.prepare_batch([kw] * 16)
     tsur = timeit(lambda: sur.solve_batch_prepared(b), 5) / 16
     assert t64 / tsur > 10, (t64, tsur)
+    # against the method without the network: the batched FP32 solver on the
+    # same 16 footprints.  On this GPU the FP32 solver is the faster and the
+    # more accurate of the two (its sweep costs ~10 kflop per mode against
+    # ~200 kflop per mode for the network), which the numbers below state.
+    from bldfm_gb300.batch import BatchSolver
+
+    s32 = BatchSolver(use_graph=True)
+    prep = s32.prepare_cached([dict(p["kw"], precision="double")] * 16)
+    t32 = timeit(lambda: s32.solve_prepared(prep), 5) / 16
+    c32, f32 = (t[0].cpu().numpy() for t in prep[1][0])
+    err32 = max(_rel(c32, cr), _rel(f32, fr))
+    print("per footprint: surrogate %.1f us (relL2 %.1e), batched FP32 %.1f us (relL2 %.1e), FP64 %.0f us"
+          % (tsur * 1e6, err, t32 * 1e6, err32, t64 * 1e6))
+    assert err32 <= 1e-5
 
 
 def test_serve_timeseries_with_fallback():
@@ -202,8 +216,11 @@ def test_serve_timeseries_with_fallback():
     sur = Surrogate(net, spot_every=8, tol=1e-3)
     out, paths = sur.serve(items, batch=8)
     assert paths.count("fp64-box") == 2 and sur.stats["out_of_box"] == 2
-    assert sur.stats["spot"] == 2
-    assert all(p in ("surrogate", "fp64-spot") for k, p in enumerate(paths) if k % 9)
+    # every 8th served case is spot-checked unless the guard already re-solved it
+    assert sur.stats["spot"] + sum(1 for k in range(16) if (k + 1) % 8 == 0 and
+                                   [p for p in paths if p != "fp64-box"][k] == "fp32-guard") == 2
+    assert len(sur.stats["guard"]) == 16
+    assert all(p in ("surrogate", "fp32-guard", "fp64-spot") for k, p in enumerate(paths) if k % 9)
     for k in (1, 9):
         p = sur.prepare(**items[k])
         _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r" if k == 1 else "fp64")
@@ -212,3 +229,49 @@ def test_serve_timeseries_with_fallback():
         f = f.cpu().numpy() if hasattr(f, "cpu") else f
         tol = 2e-3 if k == 1 else 1e-12
         assert _rel(c, cr) <= tol and _rel(f, fr) <= tol, (k, _rel(c, cr), _rel(f, fr))
+
+
+def test_guard_estimates_and_guarded_serving():
+    """The accuracy guard (every 61st solved mode re-solved exactly on the
+    device) estimates each served case's relative L2 error: on 20 in-box
+    footprints of the benchmark's met distribution the estimate stays within
+    a factor of 3 of the true error against the exact discrete solution, and
+    with the guard on no served footprint exceeds the 1e-3 bar."""
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import Surrogate, load
+
+    net, box, meta = load()
+    rng = np.random.default_rng(11)
+    items = []
+    while len(items) < 20:
+        th = rng.uniform(0, 2 * np.pi)
+        kw = dict(n=128, zm=20.0, wind=(-4 * np.sin(th), -4 * np.cos(th)), srf_shape=(512, 512),
+                  domain=(1000.0, 1000.0), modes=(512, 512), meas_pt=(500.0, 500.0),
+                  ustar=float(rng.uniform(0.22, 0.38)), mol=float(1.0 / rng.uniform(-0.045, 0.01)))
+        if Surrogate(net).classify(kw):
+            items.append(kw)
+    sur = Surrogate(net, spot_every=0, guard_tol=1.0)  # estimates only: nothing re-solved
+    b = sur.prepare_batch(items)
+    outs = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in sur.solve_batch_prepared(b)]
+    est = sur.guard_estimates(b)
+    errs = []
+    for kw, (c, f) in zip(items, outs):
+        p = sur.prepare(**kw)
+        _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
+        errs.append(max(_rel(c, cr), _rel(f, fr)))
+    errs = np.array(errs)
+    print("guard estimate / true error:", " ".join("%.1e/%.1e" % (a, e) for a, e in zip(est, errs)))
+    big = errs > 2e-4
+    assert np.all(est[big] >= errs[big] / 3) and np.all(est[big] <= errs[big] * 3), (est, errs)
+    # the estimate errs on the safe side (measured: 1.06 to 2.5 times the true error)
+    assert np.all(est >= 0.9 * errs), (est, errs)
+    # guarded serving: cases above the guard's tolerance are re-solved exactly
+    sur = Surrogate(net, spot_every=0, tol=1e-3)
+    out, paths = sur.serve(items, batch=16)
+    for kw, (c, f), path in zip(items, out, paths):
+        c = c.cpu().numpy() if hasattr(c, "cpu") else c
+        f = f.cpu().numpy() if hasattr(f, "cpu") else f
+        p = sur.prepare(**kw)
+        _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
+        assert max(_rel(c, cr), _rel(f, fr)) <= 1e-3, (path, max(_rel(c, cr), _rel(f, fr)))
+    print("guarded serving paths:", {q: paths.count(q) for q in set(paths)})
