@@ -363,10 +363,13 @@ size_t rx_smem_of(bool col)
     return (size_t)(kThreads / S::P) * S::BUF * sizeof(float2);
 }
 
+// the kernel a pass launches, its shared memory and its lines per CTA all
+// follow paired<S>(col), so the three can never disagree
 template <class S>
 void rx_set_attr()
 {
-    if constexpr (S::E <= 24)
+    static_assert(!paired<S>(true), "the column pass has no paired kernel");
+    if constexpr (paired<S>(false))
         cudaFuncSetAttribute(rx2_rows_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)rx_smem_of<S>(false));
     else
@@ -382,7 +385,7 @@ cudaError_t rx_launch(bool col, const BatchLaunch &bl, int nctas, cudaStream_t s
     const size_t b = rx_smem_of<S>(col);
     if (col)
         rx_cols_batch_kernel<S><<<nctas, kThreads, b, st>>>(bl.cases, bl.col_case, bl.err);
-    else if constexpr (S::E <= 24)
+    else if constexpr (paired<S>(false))
         rx2_rows_batch_kernel<S><<<nctas, kThreads, b, st>>>(bl.cases, bl.row_case, bl.err);
     else
         rx_rows_batch_kernel<S><<<nctas, kThreads, b, st>>>(bl.cases, bl.row_case, bl.err);
