@@ -239,8 +239,10 @@ def transform_section(stages_b, B, dev, xlines):
     """Achieved GB/s of the batched output transform (algorithmic bytes: the
     two FP32 spectra read, conc and flx written) against the HBM peak, and a
     cuFFT timing of the same transform size (torch.fft, comparison only).
-    xlines: the transform setting the step ran with (8: register-resident
-    passes, else shared-memory passes with that many lines per CTA)."""
+    xlines: the transform setting the step ran with (16 or 0: register-
+    resident passes with the zoomed column pass where the geometry allows it,
+    8: register-resident passes, else shared-memory passes with that many
+    lines per CTA)."""
     import torch
 
     peaks = measured_peaks()
@@ -262,7 +264,9 @@ def transform_section(stages_b, B, dev, xlines):
     cufft_ms = e0.elapsed_time(e1) / 5
     del x
     return {
-        "kernels": ("rx_cols_batch_kernel + rx_rows_batch_kernel (register-resident lines)" if xlines in (0, 8)
+        "kernels": ("rz_cols_batch_kernel (zoomed register-resident column lines) + rx2_rows_batch_kernel"
+                    if xlines in (0, 16) else
+                    "rx_cols_batch_kernel + rx2_rows_batch_kernel (register-resident lines)" if xlines == 8
                     else "out_cols_batch_kernel + out_rows_batch_kernel (shared-memory lines, %d per CTA)" % xlines),
         "ms_per_footprint": ms / B if ms else None,
         "bytes_per_footprint": bytes_fp,
@@ -394,10 +398,13 @@ def production_section(args, lib, dev, sptr, cpu):
 
 
 def serving_cases(nsteps, seed=7):
-    """Footprint timeseries for surrogate serving: the production met case's
-    neighbourhood (z_m = 20 m, 4 m/s, unstable to slightly stable) on a 1024^2
-    grid (2000 m domain, default halo, modes 1024^2, n = 128), 10% of the
-    steps drawn outside the network's training box (strongly unstable)."""
+    """The production footprint as a met timeseries for surrogate serving:
+    512^2 grid on 1000 m with a 500 m halo (1024^2 extended, all 1024^2
+    modes), n = 256 (413 levels), z_m = 20 m, 4 m/s, the met case of the
+    production configuration varied around it (u* ~ U[0.22, 0.38] m/s,
+    1/L ~ U[-0.045, 0.01] 1/m, wind direction ~ U[0, 360) deg), 10% of the
+    steps drawn outside the network's training box (1/L ~ U[-0.1, -0.06]:
+    strongly unstable)."""
     from bldfm_gb300.surrogate import BOX, met_scalars
 
     rng = np.random.default_rng(seed)
@@ -413,55 +420,65 @@ def serving_cases(nsteps, seed=7):
         inside = BOX["s1"][0] <= s1 <= BOX["s1"][1] and BOX["s2"][0] <= s2 <= BOX["s2"][1]
         if inside == outside:
             continue
-        out.append(dict(n=N_LEVELS, zm=20.0, wind=wind, srf_shape=(1024, 1024), domain=(2000.0, 2000.0),
-                        modes=(1024, 1024), meas_pt=(1000.0, 1000.0), ustar=ustar, mol=mol))
+        out.append(dict(n=256, zm=20.0, wind=wind, srf_shape=(512, 512), domain=(1000.0, 1000.0),
+                        modes=(1024, 1024), meas_pt=(500.0, 500.0), halo=500.0, ustar=ustar, mol=mol))
     return out
 
 
-def serving_section(args, dev):
-    """Surrogate serving with fallback on a 1024^2 footprint timeseries: wall
-    time of Surrogate.serve (batched fused launches, FP64 fallback for the
-    out-of-box steps, the per-case accuracy guard with FP32 re-solves,
-    accurate-FP64 spot checks of every 64th served step), and relL2 of served
-    steps against the exact solution."""
+def serving_section(args, dev, nsteps=10000):
+    """Surrogate serving with fallback on the production footprint as a
+    10k-step met timeseries: wall time of Surrogate.serve (batched fused
+    launches of the n = 256 network, FP64 fallback for the out-of-box steps,
+    the per-case accuracy guard with FP32 re-solves, accurate-FP64 spot
+    checks of every 64th served step), the path counts, and the relL2
+    distribution of 16 served steps (sampled before the run) against the exact
+    solution."""
     import torch
 
     from bldfm_gb300 import steady_state_transport_solver
     from bldfm_gb300 import surrogate as S
 
-    if not os.path.exists(S.WEIGHTS):
-        return {"unavailable": "no trained weights"}
-    net, box, meta = S.load(S.WEIGHTS)
-    items = serving_cases(256)
-    sur = S.Surrogate(net, spot_every=64, tol=1e-3)
+    if not os.path.exists(S.WEIGHTS_N256):
+        return {"unavailable": "no trained n=256 weights (python -m bldfm_gb300.surrogate train --n 256 --kmax 48)"}
+    net, box, meta = S.load(S.WEIGHTS_N256)
+    items = serving_cases(nsteps)
+    sur = S.Surrogate(net, box=box, spot_every=64, tol=1e-3)
     sur.serve(items[:16])  # warm (plans, twiddles, fallback path)
-    sur = S.Surrogate(net, spot_every=64, tol=1e-3)
+    sur = S.Surrogate(net, box=box, spot_every=64, tol=1e-3)
+    sampled = list(range(5, nsteps, max(1, nsteps // 16)))[:16]
     torch.cuda.synchronize()
     t = time.perf_counter()
-    out, paths = sur.serve(items)
+    out, paths = sur.serve(items, keep=sampled)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
-    # error distribution of served steps against the exact discrete solution
+    # error distribution of the sampled served steps against the exact
+    # discrete solution
     errs = []
-    served = [k for k, p in enumerate(paths) if p == "surrogate"]
-    for k in served[:: max(1, len(served) // 16)][:16]:
+    for k in sampled:
+        if paths[k] != "surrogate":
+            continue
         pr = sur.prepare(**items[k])
         _, cr, fr = steady_state_transport_solver(**pr["kw"], mode="fp64r")
         c, f = out[k]
         errs.append(max(np.linalg.norm(c.cpu().numpy() - cr) / np.linalg.norm(cr),
                         np.linalg.norm(f.cpu().numpy() - fr) / np.linalg.norm(fr)))
-    e = np.array(errs)
+    e = np.array(errs) if errs else np.array([np.nan])
     st = sur.stats
+    g = np.array(st["guard"]) if st["guard"] else np.array([np.nan])
     return {
-        "workload": "256-step footprint timeseries (10% outside the training box), 1024^2 grid, 2000 m domain, "
-                    "default halo, modes 1024^2, n=128, z_m=20 m, u*~U[0.22,0.38], 1/L~U[-0.045,0.01] "
-                    "(outside: U[-0.1,-0.06]), 4 m/s, dir~U[0,360)",
-        "value": len(items) / dt, "unit": "footprints/s (wall, incl. fallbacks and spot checks)",
+        "workload": "%d-step footprint timeseries (10%% outside the training box): 512^2 grid, 1000 m domain, "
+                    "500 m halo (1024^2 extended), modes 1024^2, n=256 (413 levels), z_m=20 m, u*~U[0.22,0.38], "
+                    "1/L~U[-0.045,0.01] (outside: U[-0.1,-0.06]), 4 m/s, dir~U[0,360)" % nsteps,
+        "network": {"weights": os.path.basename(S.WEIGHTS_N256), "box": box,
+                    "train_steps": meta.get("steps"), "val_loss": meta.get("val_loss")},
+        "value": len(items) / dt, "unit": "footprints/s (wall, incl. fallbacks, guard re-solves and spot checks)",
+        "wall_s": dt,
         "paths": {p: paths.count(p) for p in set(paths)},
-        "spot_checks": st["spot"], "spot_fail": st["spot_fail"], "spot_relL2": st["errors"],
+        "spot_checks": st["spot"], "spot_fail": st["spot_fail"],
+        "spot_relL2": {"n": len(st["errors"]), "median": float(np.median(st["errors"])) if st["errors"] else None,
+                       "max": float(np.max(st["errors"])) if st["errors"] else None},
         "guard": {"re_solved_fp32": st["guard_fail"], "checked": len(st["guard"]),
-                  "estimate_median": float(np.median(st["guard"])) if st["guard"] else None,
-                  "estimate_p90": float(np.quantile(st["guard"], 0.9)) if st["guard"] else None,
+                  "estimate_median": float(np.median(g)), "estimate_p90": float(np.quantile(g, 0.9)),
                   "rule": "every 61st solved mode re-solved exactly on the device; estimate > 1e-3 -> FP32 solve"},
         "served_relL2_vs_exact": {"n": len(errs), "median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)),
                                   "max": float(e.max()), "frac_le_1e-3": float((e <= 1e-3).mean())},

@@ -23,11 +23,12 @@ from .batch import BatchSolver
 # (256, 3) and (128, 7) leave registers free on every SM for a transform CTA
 # of another stream, which the pipelined timing below can reward.
 CANDIDATES = [(256, 0), (256, 6), (128, 0), (128, 12), (128, 18), (256, 3), (128, 7)]
-# transform passes: 8 = register-resident lines (batches whose cases share a
-# supported line length; others fall back to the default), 4 / 2 / 1 =
-# shared-memory passes with that many lines per CTA
-XFORM_LINES = [8, 4, 2, 1]
-SIGNATURE_VERSION = 2  # bumped when the candidate set changes: older cached winners are ignored
+# transform passes: 16 = register-resident lines, the column pass zoomed
+# where every case's band and kept window allow it, 8 = register-resident lines (batches whose
+# cases share a supported line length; others fall back to the default),
+# 4 / 2 / 1 = shared-memory passes with that many lines per CTA
+XFORM_LINES = [16, 8, 4, 2, 1]
+SIGNATURE_VERSION = 3  # bumped when the candidate set changes: older cached winners are ignored
 
 
 def _cache_path():

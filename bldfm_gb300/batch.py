@@ -12,6 +12,11 @@ when the batch topology repeats (e.g. a met timeseries on fixed towers).
 tuples; ``solve_stream(batches)`` does the same for a sequence of batches
 with the host work of one batch overlapping the GPU work of the previous.
 ``BatchSolver`` keeps workspace and device outputs between batches.
+
+Every result states its error: the returned lists are ``BatchResults`` whose
+``error_estimates`` hold, per case, the relative L2 error of the FP32 spectra
+against the exact FP64 solution of the same discrete problem, estimated on
+the device from 256 sampled modes per case (``error_estimate``).
 """
 
 import ctypes
@@ -74,6 +79,26 @@ def _host_inputs(kw):
         levels, lv = _normalise_levels(levels, nz)
         lvp = lv.ctypes.data
     return zp, nz, levels, lv, lvp
+
+
+CHECK_SAMPLES = 256  # sampled modes per case of the device accuracy check (batch.h)
+
+
+def error_estimate(sums):
+    """Relative L2 error estimate of one case from the accuracy check's sums
+    (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2): the larger of the
+    concentration and the flux spectra's."""
+    dp, p, dq, q = (float(v) for v in sums)
+    ep = (dp / p) ** 0.5 if p > 0 else 0.0
+    eq = (dq / q) ** 0.5 if q > 0 else 0.0
+    return max(ep, eq)
+
+
+class BatchResults(list):
+    """A list of ``(grid, conc, flx)`` results with ``error_estimates``: per
+    case, the estimated relative L2 error against the exact FP64 solution."""
+
+    error_estimates = None
 
 
 class BatchSolver:
@@ -225,6 +250,19 @@ class BatchSolver:
         self.stream.synchronize()
         return int(st[0])
 
+    def error_estimates(self, n):
+        """Estimated relative L2 error of each of the last batch's n cases
+        against the exact FP64 solution (the device accuracy check's sums at
+        byte 64 of the workspace), read through this solver's stream."""
+        if self._ws is None:
+            return np.zeros(0)
+        h = torch.empty(16 * n, dtype=torch.uint8, pin_memory=True)
+        with torch.cuda.stream(self.stream):
+            h.copy_(self._ws[64 : 64 + 16 * n], non_blocking=True)
+        self.stream.synchronize()
+        sums = h.view(torch.float32).numpy().reshape(n, 4)
+        return np.array([error_estimate(r) for r in sums])
+
 
 _DESC_CACHE = {}  # descriptor and output shape per case geometry
 _grid = output_grid
@@ -235,23 +273,24 @@ def _enqueue_batch(solver, cases):
     buffer on the solver's stream; returns the pending state."""
     shapes = solver.solve_prepared(solver.prepare(cases, views=False))
     host = torch.empty(solver.out_elems, dtype=torch.float64, pin_memory=True)
-    stat = torch.empty(1, dtype=torch.int32, pin_memory=True)
+    head = torch.empty(64 + 16 * len(cases), dtype=torch.uint8, pin_memory=True)  # status word, check sums
     with torch.cuda.stream(solver.stream):
         host.copy_(solver._out_buf[: solver.out_elems], non_blocking=True)
-        stat.copy_(solver._ws[:4].view(torch.int32), non_blocking=True)
-    return (solver, cases, shapes, solver._keep, host, stat)
+        head.copy_(solver._ws[: head.numel()], non_blocking=True)
+    return (solver, cases, shapes, solver._keep, host, head)
 
 
 def _finish_batch(pending):
     """Wait for an enqueued batch and build its (grid, conc, flx) results."""
-    solver, cases, shapes, keep, host, stat = pending
+    solver, cases, shapes, keep, host, head = pending
     solver.stream.synchronize()
-    st = int(stat[0])
+    st = int(head[:4].view(torch.int32)[0])
     if st != 0:
         _lib.check(st, "solve_batch")
     hn = host.numpy()
-    results = []
+    results = BatchResults()
     n = len(cases)
+    results.error_estimates = np.array([error_estimate(r) for r in head[64:].view(torch.float32).numpy().reshape(n, 4)])
     if n and all(sh == shapes[0] for sh in shapes):  # one geometry: views of one reshaped array
         sq = tuple(v for v in shapes[0] if v != 1)
         hv = hn[: 2 * n * _count(shapes[0])].reshape((n, 2) + sq)

@@ -433,9 +433,9 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
         hx_level_table(nz, z, prof, (double *)sg);
     if (!f64) {
         if (g.iso)
-            hx_level_table32_iso(nz, z, prof, g.ex, g.ey, (float *)(sg + off_lv32));
+            hx_level_table32_iso(nz, z, prof, g.ex, g.ey, (float *)(sg + off_lv32), nullptr);
         else
-            hx_level_table32(nz, z, prof, (float *)(sg + off_lv32));
+            hx_level_table32(nz, z, prof, (float *)(sg + off_lv32), nullptr);
     }
     memcpy(sg + off_slot, hp.slot.data(), slotb);
     double2 *dcv = (double2 *)(w + L.dc);
@@ -550,7 +550,7 @@ struct BatchBuild {
     std::vector<TwTable *> twxo, twyo, twxf, twyf;
     std::vector<int4 *> xb;
     size_t off_cases = 0, off_tile_case = 0, off_cta_tiles = 0, off_col_case = 0, off_row_case = 0;
-    std::vector<size_t> off_lv32, off_lv64, off_slot, off_dc;
+    std::vector<size_t> off_lv32, off_lv64, off_lvd, off_slot, off_dc;
     size_t blob_bytes = 0, blob_at = 0, extra_off = 0;
     std::vector<size_t> d_q0, d_A, d_scratch, d_Xp, d_Xq, d_Cb;
     size_t total = 0;
@@ -599,15 +599,27 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.maxnfy = maxnfy;
     B.maxnfx = maxnfx;
     int xl = opts ? opts->xform_lines : 0;
-    if (xl != 0 && xl != 1 && xl != 2 && xl != 4 && xl != 8) return BLDFM_ERR_ARG;
-    // register-resident passes (xform_lines 0 or 8) when every case shares a
-    // supported column and row line length; otherwise the shared-memory passes
-    if (xl == 0 || xl == 8) {
+    if (xl != 0 && xl != 1 && xl != 2 && xl != 4 && xl != 8 && xl != 16) return BLDFM_ERR_ARG;
+    // register-resident passes (xform_lines 0, 8 or 16) when every case shares
+    // a supported column and row line length; otherwise the shared-memory
+    // passes.  0 and 16 take the zoomed column pass wherever every case's
+    // band and kept window allow it (3 M lines, the default halo).
+    if (xl == 0 || xl == 8 || xl == 16) {
         B.rx_col = rx_config(B.hp[0].g.nfy);
         B.rx_row = rx_config(B.hp[0].g.nfx);
         for (int k = 1; k < n; ++k)
             if (B.hp[k].g.nfy != B.hp[0].g.nfy || B.hp[k].g.nfx != B.hp[0].g.nfx) B.rx_col = -1;
         if (B.rx_col < 0 || B.rx_row < 0) B.rx_col = B.rx_row = -1;
+        if (B.rx_col >= 0 && xl != 8) {
+            int zc = 0;
+            for (int k = 0; k < n && zc >= 0; ++k) {
+                const SolveGeom &g = B.hp[k].g;
+                const int hy = std::max(-freq_min(g.nly), freq_max(g.nly));
+                const int c = rx_zoom_config(g.nfy, hy, g.out_ny);
+                zc = (c < 0 || (k > 0 && c != zc)) ? -1 : c;
+            }
+            if (zc >= 0) B.rx_col = zc;
+        }
         xl = 0;
     }
     B.rpc = xl > 0 ? xl : 2;
@@ -637,12 +649,15 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     o = al(o + 4 * (size_t)std::max(B.nrow, 1));
     B.off_lv32.resize(n);
     B.off_lv64.resize(n);
+    B.off_lvd.resize(n);
     B.off_slot.resize(n);
     B.off_dc.resize(n);
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
         B.off_lv32[k] = o;
         o = al(o + (size_t)std::max(g.nz - 1, 1) * BLDFM_LV32 * 4);
+        B.off_lvd[k] = o;
+        o = al(o + (size_t)std::max(g.nz - 1, 1) * BLDFM_LV32 * 8);
         B.off_lv64[k] = o;
         o = al(o + (size_t)std::max(g.nz - 1, 1) * BLDFM_LV64 * 8);
         B.off_slot[k] = o;
@@ -653,9 +668,10 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.extra_off = o;  // caller's region at the end of the blob
     o = al(o + extra_blob);
     B.blob_bytes = o;
-    // workspace: status word, blob, per-case device regions
+    // workspace: status word, the accuracy check's per-case sums (16 bytes
+    // per case from byte 64), blob, per-case device regions
     size_t w = 0;
-    w = al(w + 64);
+    w = al(w + 64 + 16 * (size_t)n);
     B.blob_at = w;
     w = al(w + B.blob_bytes);
     B.d_q0.resize(n);
@@ -767,6 +783,7 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
         x.xband = B.xb[k];
         x.conc = c.conc_dev;
         x.flx = c.flx_dev;
+        x.lvd = (const double *)(wb + B.off_lvd[k]);
         x.ax = (float)(g.lx_scale * g.valx);
         x.ay = (float)(g.ly_scale * g.valy);
         x.tile0 = B.tile0[k];
@@ -779,10 +796,11 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
             hx_level_dz_w(nz, c.z_host, c.prof_host, lv64);  // all the k = 0 values need (no trapezoid pass)
         else
             hx_level_table(nz, c.z_host, c.prof_host, lv64);
+        double *lvd = (double *)(blob + B.off_lvd[k]);
         if (g.iso)
-            hx_level_table32_iso(nz, c.z_host, c.prof_host, g.ex, g.ey, (float *)(blob + B.off_lv32[k]));
+            hx_level_table32_iso(nz, c.z_host, c.prof_host, g.ex, g.ey, (float *)(blob + B.off_lv32[k]), lvd);
         else
-            hx_level_table32(nz, c.z_host, c.prof_host, (float *)(blob + B.off_lv32[k]));
+            hx_level_table32(nz, c.z_host, c.prof_host, (float *)(blob + B.off_lv32[k]), lvd);
         memcpy(blob + B.off_slot[k], hp.slot.data(), (size_t)nz * 4);
         if (g.footprint)
             hx_dc_values(nz, lv64, hp.slot.data(), g.q0dc_fp, 0.0, c.desc.srf_bg_conc,
@@ -816,7 +834,7 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
 {
     if (tdc) tmark(*tdc, st);  // 0: upload and per-case forward transforms
     CK(cudaMemcpyAsync(ws + B.blob_at, blob_host, B.blob_bytes, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(ws, 0, 64, st));
+    CK(cudaMemsetAsync(ws, 0, 64 + 16 * (size_t)n, st));  // status word and the check's sums
     char *wb = ws + B.blob_at;
     for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
@@ -859,7 +877,9 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
     CK(launch_batch_kernels(bl, st, 0));
     if (tdc) tmark(*tdc, st);  // 2: the output transform
     CK(launch_batch_kernels(bl, st, 1));
-    if (tdc) tmark(*tdc, st);  // 3: end
+    if (tdc) tmark(*tdc, st);  // 3: the accuracy check
+    CK(launch_fp32_check(bl.cases, n, BATCH_CHECK_SAMPLES, (float4 *)(ws + 64), st));
+    if (tdc) tmark(*tdc, st);  // 4: end
     return BLDFM_OK;
 }
 

@@ -447,6 +447,136 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
     return cudaGetLastError();
 }
 
+// Accuracy check of a batched FP32 solve (no reference counterpart: the
+// statement of each result's error).  Sample j < ns of case k is the solved
+// mode at the centre of the j-th of ns equal slices of the case's mode list;
+// its exact value at the highest output level comes from the invariant-
+// imbedding recursion in FP64 on the case's FP64 level table (the rows of the
+// FP32 table before rounding), with the top radiation condition, flux
+// product, source spectrum and phase shift of the FP32 sweep
+// (riccati64_kernel's arithmetic).  acc[k] accumulates (sum |dXp|^2,
+// sum |Xp|^2, sum |dXq|^2, sum |Xq|^2) over the samples, one atomic per warp
+// and quantity; ns is a multiple of 32, so no warp spans two cases.
+template <bool ISO>
+__device__ __forceinline__ void coef64(const double *row, double lx, double ly, double ex, double ey, double2 &a,
+                                       double2 &b, double2 &c)
+{
+    if (ISO) {
+        // row = {AK, AU, B0, B1K, B1U, -HK, -C1K2, C1U2, -HU, -2 C1 K U}
+        const double k2 = fma(lx, lx, ly * ly), kw = fma(ex, lx, ey * ly);
+        a = make_double2(fma(row[0], k2, 1.0), row[1] * kw);
+        b = make_double2(fma(row[3], k2, row[2]), row[4] * kw);
+        c = make_double2(fma(row[6], k2 * k2, fma(row[7], kw * kw, row[5] * k2)), fma(row[9], k2 * kw, row[8] * kw));
+    } else {
+        // row = {-Kx, -Ky, -u, -v, A, B0, B1, H, C1, -2 C1}
+        const double Tr = fma(row[0], lx * lx, row[1] * ly * ly), Ti = fma(row[2], lx, row[3] * ly);
+        a = make_double2(fma(-row[4], Tr, 1.0), -row[4] * Ti);
+        b = make_double2(fma(-row[6], Tr, row[5]), -row[6] * Ti);
+        const double t2r = fma(Tr, Tr, -Ti * Ti);
+        c = make_double2(fma(-row[8], t2r, row[7] * Tr), Ti * fma(row[9], Tr, row[7]));
+    }
+}
+
+template <bool ISO>
+__device__ __forceinline__ void check_mode(const BatchCase &bc, int64_t m, float4 &v)
+{
+    const SolveGeom &g = bc.g;
+    int r, c;
+    bool paired;
+    unpack_mode(bc.modes[m], r, c, paired);
+    const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
+    const double lx = wavenumber(kx, g.valx, g.lx_scale), ly = wavenumber(ky, g.valy, g.ly_scale);
+    const double w2r = fma(g.kxk_top, lx * lx, g.kyk_top * ly * ly), w2i = fma(g.uk_top, lx, g.vk_top * ly);
+    // principal square root of the top eigenvalue argument (Kahan)
+    const double t = sqrt(0.5 * (fabs(w2r) + hypot(w2r, w2i)));
+    double2 eg = make_double2(0.0, 0.0);
+    if (t > 0.0)
+        eg = w2r >= 0.0 ? make_double2(t, w2i / (2.0 * t)) : make_double2(fabs(w2i) / (2.0 * t), copysign(t, w2i));
+    const double2 ke = make_double2(g.kz_top * eg.x, g.kz_top * eg.y);
+    const double kn = 1.0 / fma(ke.x, ke.x, ke.y * ke.y);
+    double2 R = make_double2(ke.x * kn, -ke.y * kn), Rj = R, Q = make_double2(1.0, 0.0);
+    int E = 0;
+    const int L = g.nz - 1, jmax = g.jmax;
+    for (int i = L - 1; i >= 0; --i) {
+        double2 a, b, cc;
+        coef64<ISO>(bc.lvd + (size_t)i * BLDFM_LV32, lx, ly, g.ex, g.ey, a, b, cc);
+        const double Dr = fma(-cc.x, R.x, fma(cc.y, R.y, a.x)), Di = fma(-cc.x, R.y, fma(-cc.y, R.x, a.y));
+        const double Nr = fma(a.x, R.x, fma(-a.y, R.y, -b.x)), Ni = fma(a.x, R.y, fma(a.y, R.x, -b.y));
+        const double dinv = 1.0 / fma(Dr, Dr, Di * Di);
+        R = make_double2(fma(Nr, Dr, Ni * Di) * dinv, fma(Ni, Dr, -Nr * Di) * dinv);
+        if (i == jmax) Rj = R;
+        if (i < jmax) {
+            const double fr = fma(cc.x, R.x, fma(-cc.y, R.y, a.x)), fi = fma(cc.x, R.y, fma(cc.y, R.x, a.y));
+            Q = make_double2(fma(Q.x, fr, -Q.y * fi), fma(Q.x, fi, Q.y * fr));
+            if ((i & 15) == 0) {
+                int e;
+                frexp(fmax(fabs(Q.x), fabs(Q.y)), &e);
+                Q.x = ldexp(Q.x, -e);
+                Q.y = ldexp(Q.y, -e);
+                E += e;
+            }
+        }
+    }
+    double2 q0 = make_double2(g.q0dc_fp, 0.0);
+    if (bc.q0) {
+        const float2 f = bc.q0[(size_t)c * g.nly + r];
+        q0 = make_double2(f.x, f.y);
+    }
+    const double2 ratio = make_double2(ldexp(Q.x, E), ldexp(Q.y, E));
+    double2 q = make_double2(fma(q0.x, ratio.x, -q0.y * ratio.y), fma(q0.x, ratio.y, q0.y * ratio.x));
+    double2 p = make_double2(fma(Rj.x, q.x, -Rj.y * q.y), fma(Rj.x, q.y, Rj.y * q.x));
+    if (g.do_shift) {
+        double sn, cs;
+        sincos(lx * g.sx + ly * g.sy, &sn, &cs);
+        p = make_double2(fma(p.x, cs, -p.y * sn), fma(p.x, sn, p.y * cs));
+        q = make_double2(fma(q.x, cs, -q.y * sn), fma(q.x, sn, q.y * cs));
+    }
+    const size_t o = spec_idx(g, bc.slot[jmax], r, c);
+    const float2 pn = bc.Xp[o], qn = bc.Xq[o];
+    const double dpx = pn.x - p.x, dpy = pn.y - p.y, dqx = qn.x - q.x, dqy = qn.y - q.y;
+    v = make_float4((float)(dpx * dpx + dpy * dpy), (float)(p.x * p.x + p.y * p.y), (float)(dqx * dqx + dqy * dqy),
+                    (float)(q.x * q.x + q.y * q.y));
+}
+
+__global__ void __launch_bounds__(128) fp32_check_kernel(const BatchCase *__restrict__ cases, int n, int ns,
+                                                         float4 *__restrict__ acc)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (int)(i / ns), j = (int)(i - (int64_t)k * ns);
+    if (k >= n) return;  // whole warps: ns is a multiple of 32
+    const BatchCase &bc = cases[k];
+    const int64_t nsol = bc.g.nsolved;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (nsol > 0 && bc.g.jmax >= 0 && bc.lvd) {
+        const int64_t m = ((2 * (int64_t)j + 1) * nsol) / (2 * (int64_t)ns);
+        if (bc.g.iso)
+            check_mode<true>(bc, m, v);
+        else
+            check_mode<false>(bc, m, v);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+        v.z += __shfl_down_sync(0xffffffffu, v.z, off);
+        v.w += __shfl_down_sync(0xffffffffu, v.w, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[k].x, v.x);
+        atomicAdd(&acc[k].y, v.y);
+        atomicAdd(&acc[k].z, v.z);
+        atomicAdd(&acc[k].w, v.w);
+    }
+}
+
+cudaError_t launch_fp32_check(const BatchCase *cases, int n, int ns, float4 *acc, cudaStream_t st)
+{
+    if (n <= 0 || ns <= 0) return cudaSuccess;
+    const int64_t nt = (int64_t)n * ns;
+    fp32_check_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(cases, n, ns, acc);
+    return cudaGetLastError();
+}
+
 void prepare_batch_attributes();
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part)

@@ -24,6 +24,7 @@ struct __align__(16) BatchCase {
     const float2 *twx, *twy;
     const int4 *xband;
     double *conc, *flx;
+    const double *lvd;  // FP64 rows of the level table (accuracy check)
     float ax, ay;
     int64_t tile0;  // first sweep tile of this case
     int64_t col0;   // first column-transform CTA
@@ -55,6 +56,13 @@ struct BatchLaunch {
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);
 
+// Accuracy check of a batched FP32 solve (batch.cu: fp32_check_kernel): ns
+// sampled modes per case (ns a multiple of 32) evaluated exactly in FP64 and
+// compared with the FP32 spectra at the highest output level; per case
+// acc[k] += (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2).
+#define BATCH_CHECK_SAMPLES 256
+cudaError_t launch_fp32_check(const BatchCase *cases, int n, int ns, float4 *acc, cudaStream_t st);
+
 // Accuracy guard of a surrogate batch (batch.cu: sur_guard_kernel): exact
 // FP32 values of every stride-th solved mode against the served spectra,
 // per-case sums into acc[k] = (|dXp|^2, |Xp|^2, |dXq|^2, |Xq|^2); prefix:
@@ -68,6 +76,11 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 // or row pass, one-time attributes,
 // and the launch of the column (col) or row pass over nctas CTAs
 int rx_config(int n);
+// zoomed column pass (xform_zoom.cuh) for a line of length n = 3 M (M = 256,
+// 512) whose band has at most 2 band_half + 1 <= M + 1 frequencies and whose
+// kept window nout <= M positions: config id RX_ZOOM_BASE + k, or -1
+#define RX_ZOOM_BASE 16
+int rx_zoom_config(int n, int band_half, int nout);
 int rx_lines_per_cta(int cfg, bool col);
 size_t rx_smem(int cfg, bool col);
 void prepare_rx_attributes();

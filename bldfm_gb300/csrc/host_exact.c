@@ -50,27 +50,32 @@ void hx_level_dz_w(int nz, const double *z, const double *prof, double *lv)
     }
 }
 
-/* FP32 level table of the Riccati sweep, from the same per-step scalars. */
-void hx_level_table32(int nz, const double *z, const double *prof, float *lv)
+/* FP32 level table of the Riccati sweep, from the same per-step scalars;
+ * lvd (may be NULL) receives the same rows unrounded, in FP64. */
+void hx_level_table32(int nz, const double *z, const double *prof, float *lv, double *lvd)
 {
     const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Ky = prof + 3 * nz, *Kz = prof + 4 * nz;
     for (int i = 0; i < nz - 1; ++i) {
         double k = 1.0 / Kz[i];
         double h = z[i + 1] - z[i];
-        float *row = lv + (size_t)i * 12;
         double c1 = k * h * h * h / 6.0;
-        row[0] = (float)(-Kx[i]);
-        row[1] = (float)(-Ky[i]);
-        row[2] = (float)(-u[i]);
-        row[3] = (float)(-v[i]);
-        row[4] = (float)(0.5 * k * h * h);
-        row[5] = (float)(-k * h);
-        row[6] = (float)(k * k * h * h * h / 6.0);
-        row[7] = (float)h;
-        row[8] = (float)c1;
-        row[9] = (float)(-2.0 * c1);
-        row[10] = 0.f;
-        row[11] = 0.f;
+        double r[12];
+        r[0] = -Kx[i];
+        r[1] = -Ky[i];
+        r[2] = -u[i];
+        r[3] = -v[i];
+        r[4] = 0.5 * k * h * h;
+        r[5] = -k * h;
+        r[6] = k * k * h * h * h / 6.0;
+        r[7] = h;
+        r[8] = c1;
+        r[9] = -2.0 * c1;
+        r[10] = 0.0;
+        r[11] = 0.0;
+        float *row = lv + (size_t)i * 12;
+        for (int j = 0; j < 12; ++j) row[j] = (float)r[j];
+        if (lvd)
+            for (int j = 0; j < 12; ++j) lvd[(size_t)i * 12 + j] = r[j];
     }
 }
 
@@ -161,8 +166,9 @@ int hx_profiles_iso(int nz, const double *prof, double *ex, double *ey)
 }
 
 /* Compact FP32 level table for isotropic profiles with a fixed wind
- * direction (row layout of StepCoef<true> in kernels.cu). */
-void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex, double ey, float *lv)
+ * direction (row layout of StepCoef<true> in sweep32.cuh); lvd (may be NULL)
+ * receives the same rows unrounded, in FP64. */
+void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex, double ey, float *lv, double *lvd)
 {
     const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Kz = prof + 4 * nz;
     for (int i = 0; i < nz - 1; ++i) {
@@ -171,19 +177,23 @@ void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex
         double K = Kx[i];
         double U = u[i] * ex + v[i] * ey;
         double A = 0.5 * k * h * h, B0 = -k * h, B1 = k * k * h * h * h / 6.0, C1 = k * h * h * h / 6.0;
+        double r[12];
+        r[0] = A * K;
+        r[1] = A * U;
+        r[2] = B0;
+        r[3] = B1 * K;
+        r[4] = B1 * U;
+        r[5] = -h * K;
+        r[6] = -C1 * K * K;
+        r[7] = C1 * U * U;
+        r[8] = -h * U;
+        r[9] = -2.0 * C1 * K * U;
+        r[10] = 0.0;
+        r[11] = 0.0;
         float *row = lv + (size_t)i * 12;
-        row[0] = (float)(A * K);
-        row[1] = (float)(A * U);
-        row[2] = (float)B0;
-        row[3] = (float)(B1 * K);
-        row[4] = (float)(B1 * U);
-        row[5] = (float)(-h * K);
-        row[6] = (float)(-C1 * K * K);
-        row[7] = (float)(C1 * U * U);
-        row[8] = (float)(-h * U);
-        row[9] = (float)(-2.0 * C1 * K * U);
-        row[10] = 0.f;
-        row[11] = 0.f;
+        for (int j = 0; j < 12; ++j) row[j] = (float)r[j];
+        if (lvd)
+            for (int j = 0; j < 12; ++j) lvd[(size_t)i * 12 + j] = r[j];
     }
 }
 

@@ -210,9 +210,9 @@ extern "C" int bldfm_solve_noalloc(const bldfm_desc *d, const double *srf_flx_de
     else
         hx_level_table(nz, z_host, prof_host, na_host.lv64);
     if (g.iso)
-        hx_level_table32_iso(nz, z_host, prof_host, g.ex, g.ey, na_host.lv32);
+        hx_level_table32_iso(nz, z_host, prof_host, g.ex, g.ey, na_host.lv32, nullptr);
     else
-        hx_level_table32(nz, z_host, prof_host, na_host.lv32);
+        hx_level_table32(nz, z_host, prof_host, na_host.lv32, nullptr);
 #define NA_CK(x)                                                                                                       \
     do {                                                                                                               \
         if ((x) != cudaSuccess) return BLDFM_ERR_CUDA;                                                                 \

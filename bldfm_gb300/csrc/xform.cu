@@ -17,6 +17,7 @@
 #include "common.h"
 #include "devmath.cuh"
 #include "xform_reg.cuh"
+#include "xform_zoom.cuh"
 
 namespace {
 
@@ -341,6 +342,178 @@ __global__ void __launch_bounds__(kThreads, 2) rx2_rows_batch_kernel(const Batch
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
 }
 
+// ---------------------------------------------------------------------------
+// Zoomed passes (xform_zoom.cuh): line length N = 3 M, band of at most M + 1
+// frequencies, at most M kept positions.  S is the M-point shape.
+// ---------------------------------------------------------------------------
+
+// Fill the CTA's twist table from the case record in global memory (threads
+// 0 .. 3 E + 2), so that it is ready after the block's first barrier.
+template <class S>
+__device__ __forceinline__ void zoom_twists_of(rx::ZoomTw<S> &z, const BatchCase *gc, bool col)
+{
+    if (threadIdx.x < 3 * S::E + 3) rx::zoom_twists<S>(z, col ? gc->twy : gc->twx, col ? gc->g.py : gc->g.px);
+}
+
+// Value Z = Hp + i Hq of frequency n (|n| <= M/2) of band column bx, from the
+// staged columns (sp: Xp at P, sp + nly: Xq at P) where -P is the signed
+// mirror inside the mode range, else from global memory (col_value).
+__device__ __forceinline__ float2 zoom_col_value(const SolveGeom &g, const int4 bx, bool xpair, const float2 *sp,
+                                                 bool staged, const BatchCase &sc, int lvl, int n_line, int n)
+{
+    const int nly = g.nly, fmin = freq_min(nly), fmax = freq_max(nly);
+    const bool pin = n >= fmin && n <= fmax, min_ = -n >= fmin && -n <= fmax && bx.z >= 0;
+    if (staged && pin && min_ && xpair && !(bx.y == 0 && n == 0)) {
+        const int r = index_of_freq(n, nly);
+        const float2 p = sp[r], q = sp[nly + r];
+        return make_float2(p.x - q.y, p.y + q.x);
+    }
+    if (!pin && !min_) return make_float2(0.f, 0.f);
+    return col_value(g, bx, xpair, sc.Xp, sc.Xq, sc.dc, lvl, n_line, n >= 0 ? n : n + n_line);
+}
+
+// Zoomed column pass: one band column per group of P threads; the kept rows
+// [py, py + out_ny) staged line-major as in rx_cols_batch_kernel.
+template <class S>
+__global__ void __launch_bounds__(kThreads, 3) rz_cols_batch_kernel(const BatchCase *__restrict__ cases,
+                                                                   const int *__restrict__ cta_case, int *err)
+{
+    constexpr int P = S::P, E = S::E, G = kThreads / P, M = S::N, N = 3 * M, MK = (E + 2) / 3;
+    using B = rx::ZoomBuf<S, float2>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *sbuf = (float2 *)smem_raw;
+    __shared__ __align__(16) BatchCase sc;
+    __shared__ __align__(16) rx::ZoomTw<S> zt;
+    __shared__ uint64_t gbar[G];
+    const BatchCase *gc = cases + cta_case[blockIdx.x];
+    load_case_rx(&sc, gc);
+    zoom_twists_of<S>(zt, gc, true);
+    const int grp = threadIdx.x / P, t = threadIdx.x - grp * P;
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&gbar[grp])), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const SolveGeom &g = sc.g;
+    const int64_t local = (int64_t)blockIdx.x - sc.col0;
+    const int ncb = (g.nbx + G - 1) / G;
+    const int lvl = (int)(local / ncb), cb = (int)(local - (int64_t)lvl * ncb);
+    const int b = cb * G + grp;
+    const bool active = b < g.nbx;
+    const float cj = g.out_sign > 0 ? -1.f : 1.f;  // inverse transform: conjugate in and out
+    float2 *buf = sbuf + grp * B::BUF;
+    float2 y[3 * E];
+    bool timed_out = false;
+    if (active) {
+        const int4 bx = sc.xband[b];
+        const bool xpair =
+            bx.y >= 0 && bx.z >= 0 && freq_of_index(bx.z, g.nlx) == -freq_of_index(bx.y, g.nlx);
+        const int nly = g.nly;
+        const size_t colp = ((size_t)lvl * g.nlx + (bx.y > 0 ? bx.y : 0)) * nly;
+        const bool stage = bx.y >= 0 && 2 * nly <= B::BUF && (nly & 1) == 0 &&
+                           ((((uintptr_t)sc.Xp) | ((uintptr_t)sc.Xq)) & 15) == 0;
+        if (stage) {
+            const uint32_t ba = smem_u32(&gbar[grp]);
+            if (t == 0) {
+                const uint32_t nb = (uint32_t)nly * 8u;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ba), "r"(2u * nb)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(buf)),
+                    "l"(sc.Xp + colp), "r"(nb), "r"(ba)
+                    : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(buf + nly)),
+                    "l"(sc.Xq + colp), "r"(nb), "r"(ba)
+                    : "memory");
+            }
+            uint32_t done = 0;
+            for (long it = 0; it < BLDFM_WAIT_POLLS && !done; ++it)
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                    "selp.u32 %0, 1, 0, p;\n\t}"
+                    : "=r"(done)
+                    : "r"(ba), "r"(0u)
+                    : "memory");
+            timed_out = !done;
+        }
+        float2 v[E];
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int n = t + P * m - (m >= E / 2 ? M : 0);
+            const float2 z = zoom_col_value(g, bx, xpair, buf, stage, sc, lvl, N, n);
+            v[m] = make_float2(z.x, cj * z.y);
+        }
+        float2 vp = make_float2(0.f, 0.f);
+        if (t == 0) {
+            const float2 z = zoom_col_value(g, bx, xpair, buf, stage, sc, lvl, N, M / 2);
+            vp = make_float2(z.x, cj * z.y);
+        }
+        if (stage) rx::group_bar(grp + 1, P);  // the staged columns are read before the buffer is reused
+        rx::zoom_line<S, float2>(y, v, vp, t, buf, sc.twy, zt, g.py, grp + 1);
+    }
+    if (__syncthreads_or(timed_out) && threadIdx.x == 0) atomicExch(err, BLDFM_ERR_TIMEOUT_DEV);
+    // kept rows j = 3 (t + P m) + r < out_ny of the G lines staged line-major,
+    // [G][ys], ys = out_ny rounded up to 4 mod 16 words
+    const int ony = g.out_ny;
+    const int ys = ((ony + 11) & ~15) + 4;
+    if (active) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int m = 0; m < MK; ++m) {
+                const int j = 3 * (t + P * m) + r;
+                if (j < ony) sbuf[(size_t)grp * ys + j] = make_float2(y[r * E + m].x, cj * y[r * E + m].y);
+            }
+    }
+    __syncthreads();
+    const int ng = min(G, g.nbx - cb * G);
+    float2 *o = sc.Cb + (size_t)lvl * ony * g.nbx + cb * G;
+    for (int i = threadIdx.x; i < ony * G; i += kThreads) {
+        const int yy = i / G, gg = i - yy * G;
+        if (gg < ng) o[(size_t)yy * g.nbx + gg] = sbuf[(size_t)gg * ys + yy];
+    }
+}
+
+using Z256 = rx::Shape<8, 4, 8>;
+using Z512 = rx::Shape<8, 8, 8>;
+
+// The zoomed form exists for the column pass only: a zoomed row pass (two
+// rows per group in FP32x2 lanes, outputs staged through shared memory for
+// contiguous stores) issued 13% fewer instructions than rx2_rows_batch_kernel
+// but ran 7% slower (43.3 against 40.6 us per 16 footprints, ncu): its
+// staging round trip added shared-memory and barrier waits at the same two
+// CTAs per SM.
+template <class S>
+size_t rz_smem_of()
+{
+    return (size_t)(kThreads / S::P) * rx::ZoomBuf<S, float2>::BUF * sizeof(float2);
+}
+
+template <class S>
+void rz_set_attr()
+{
+    cudaFuncSetAttribute(rz_cols_batch_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rz_smem_of<S>());
+}
+
+template <class S>
+cudaError_t rz_launch(bool col, const BatchLaunch &bl, int nctas, cudaStream_t st)
+{
+    if (!col) return cudaErrorInvalidValue;
+    rz_cols_batch_kernel<S><<<nctas, kThreads, rz_smem_of<S>(), st>>>(bl.cases, bl.col_case, bl.err);
+    return cudaGetLastError();
+}
+
+template <class S>
+constexpr int rz_lines_of(bool col)
+{
+    return col ? kThreads / S::P : 0;
+}
+
 // paired passes for line shapes up to E = 24 (registers: two lines' values
 // per thread), single-line passes beyond
 // Measured on the 16-footprint 512^2 batch (ncu, per launch): the paired row
@@ -400,6 +573,16 @@ constexpr int rx_lines_of(bool col)
 
 }  // namespace
 
+int rx_zoom_config(int n, int band_half, int nout)
+{
+    int m = 0;
+    if (n == 768) m = 256;
+    else if (n == 1536) m = 512;
+    else return -1;
+    if (2 * band_half > m || nout > m || nout < 1) return -1;
+    return m == 256 ? RX_ZOOM_BASE : RX_ZOOM_BASE + 1;
+}
+
 int rx_config(int n)
 {
     switch (n) {
@@ -416,6 +599,8 @@ int rx_config(int n)
 int rx_lines_per_cta(int cfg, bool col)
 {
     switch (cfg) {
+    case RX_ZOOM_BASE: return rz_lines_of<Z256>(col);
+    case RX_ZOOM_BASE + 1: return rz_lines_of<Z512>(col);
     case 0: return rx_lines_of<S512>(col);
     case 1: return rx_lines_of<S768>(col);
     case 2: return rx_lines_of<S1024>(col);
@@ -429,6 +614,8 @@ int rx_lines_per_cta(int cfg, bool col)
 size_t rx_smem(int cfg, bool col)
 {
     switch (cfg) {
+    case RX_ZOOM_BASE: return col ? rz_smem_of<Z256>() : 0;
+    case RX_ZOOM_BASE + 1: return col ? rz_smem_of<Z512>() : 0;
     case 0: return rx_smem_of<S512>(col);
     case 1: return rx_smem_of<S768>(col);
     case 2: return rx_smem_of<S1024>(col);
@@ -447,12 +634,16 @@ void prepare_rx_attributes()
     rx_set_attr<S1536>();
     rx_set_attr<S2048>();
     rx_set_attr<S3072>();
+    rz_set_attr<Z256>();
+    rz_set_attr<Z512>();
 }
 
 cudaError_t launch_rx_pass(int cfg, bool col, const BatchLaunch &bl, int nctas, cudaStream_t st)
 {
     if (nctas <= 0) return cudaSuccess;
     switch (cfg) {
+    case RX_ZOOM_BASE: return rz_launch<Z256>(col, bl, nctas, st);
+    case RX_ZOOM_BASE + 1: return rz_launch<Z512>(col, bl, nctas, st);
     case 0: return rx_launch<S512>(col, bl, nctas, st);
     case 1: return rx_launch<S768>(col, bl, nctas, st);
     case 2: return rx_launch<S1024>(col, bl, nctas, st);

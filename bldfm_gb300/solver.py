@@ -69,7 +69,8 @@ _FP32_LOCK = threading.Lock()
 def _solve_fp32_one(kw):
     """One FP32 solve through the batched path: cached plan and descriptors,
     the case's host data in one pinned upload, graph replay while the shapes
-    repeat, outputs back in one copy into pinned memory."""
+    repeat, outputs back in one copy into pinned memory.  Returns the result
+    and its estimated relative L2 error against the exact FP64 solution."""
     import torch
 
     from .batch import BatchSolver, _enqueue_batch, _finish_batch
@@ -79,7 +80,8 @@ def _solve_fp32_one(kw):
         s = _FP32_SOLVERS.get(dev)
         if s is None:
             s = _FP32_SOLVERS[dev] = BatchSolver(device=dev, use_graph=True)
-        return _finish_batch(_enqueue_batch(s, [kw]))[0]
+        res = _finish_batch(_enqueue_batch(s, [kw]))
+        return res[0], float(res.error_estimates[0])
 
 
 def make_desc(shape, nz, domain, modes, meas_pt, srf_bg_conc, footprint, analytic, halo, precision, mode):
@@ -129,6 +131,7 @@ def steady_state_transport_solver(
     cache=None,
     *,
     mode="fp64",
+    return_error=False,
 ):
     """Steady-state advection-diffusion solve on the GPU (solver.py:16-304).
 
@@ -146,6 +149,10 @@ def steady_state_transport_solver(
     Raises ``ValueError`` for invalid profiles (non-finite values, z not
     strictly increasing, Kz <= 0) and ``FloatingPointError`` when the output
     holds non-finite values (the reference returns such fields silently).
+    ``return_error=True`` (keyword-only) appends the result's error statement:
+    in mode "fp32" the relative L2 error against the exact FP64 solution of
+    the same discrete problem, estimated on the device from 256 sampled modes
+    (float); in the FP64 modes None (the result is the FP64 solution itself).
     """
     if mode not in _MODES:
         raise ValueError("mode must be 'fp64', 'fp32' or 'fp64r'")
@@ -155,7 +162,7 @@ def steady_state_transport_solver(
     if use_cache:
         cached = cache.get(z, profiles, domain, modes, meas_pt, halo, precision, **ckw)
         if cached is not None:
-            return cached
+            return (*cached, None) if return_error else cached
     lib = _lib.load()
     shape = np.shape(srf_flx)
     if len(shape) != 2:
@@ -165,12 +172,12 @@ def steady_state_transport_solver(
             raise ValueError("modes must consist of even numbers.")
         if precision not in ("single", "double"):
             raise ValueError("precision must be single (default) or double.")
-        result = _solve_fp32_one(dict(srf_flx=srf_flx, z=z, profiles=profiles, domain=domain, levels=levels,
-                                      modes=modes, meas_pt=meas_pt, srf_bg_conc=srf_bg_conc, footprint=footprint,
-                                      halo=halo, precision=precision))
+        result, err = _solve_fp32_one(dict(srf_flx=srf_flx, z=z, profiles=profiles, domain=domain, levels=levels,
+                                           modes=modes, meas_pt=meas_pt, srf_bg_conc=srf_bg_conc,
+                                           footprint=footprint, halo=halo, precision=precision))
         if use_cache:
             cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result, **ckw)
-        return result
+        return (*result, err) if return_error else result
     zz = np.ascontiguousarray(z, dtype=np.float64)
     nz = zz.shape[0]
     prof = np.ascontiguousarray(np.stack([np.broadcast_to(np.asarray(p, dtype=np.float64), (nz,)) for p in profiles]))
@@ -196,4 +203,4 @@ def steady_state_transport_solver(
     result = (grid, np.squeeze(conc), np.squeeze(flx))
     if use_cache:
         cache.put(z, profiles, domain, modes, meas_pt, halo, precision, *result, **ckw)
-    return result
+    return (*result, None) if return_error else result

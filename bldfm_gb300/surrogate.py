@@ -43,7 +43,18 @@ KAPPA = 0.4
 # the network is trained on TRAIN_BOX, which has a margin around it
 BOX = {"s1": (-1.0, 0.25), "s2": (4.5, 7.5), "kmin": 1e-3, "kmax": 40.0, "n": 128}
 TRAIN_BOX = {"s1": (-1.25, 0.35), "s2": (4.25, 7.75), "kmin": 1e-3, "kmax": 40.0, "n": 128}
-WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "surrogate_n128.npz")
+WEIGHT_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
+WEIGHTS = os.path.join(WEIGHT_DIR, "surrogate_n128.npz")
+# the network of the production footprint's level count (n = 256, 413 levels;
+# |k| z_m up to 48 covers all modes of a 1024^2 extended grid at dx = 1.95 m
+# and z_m = 20 m)
+WEIGHTS_N256 = os.path.join(WEIGHT_DIR, "surrogate_n256.npz")
+
+
+def boxes(n=128, kmax=40.0):
+    """(serving box, training box) of a network for n levels below z_m and
+    |k| z_m <= kmax: the training box keeps the margin in s1 and s2."""
+    return dict(BOX, n=int(n), kmax=float(kmax)), dict(TRAIN_BOX, n=int(n), kmax=float(kmax))
 
 
 def psi(x):
@@ -201,9 +212,10 @@ def validation_loss(net, pool, m=65536, seed=999, floor=1e-3):
     return net.grads()[1]
 
 
-def save(net, path, meta=None):
+def save(net, path, meta=None, box=None):
+    """Save the parameters with the serving box they hold for (default BOX)."""
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-    np.savez(path, params=net.params(), box=json.dumps(BOX), meta=json.dumps(meta or {}))
+    np.savez(path, params=net.params(), box=json.dumps(BOX if box is None else box), meta=json.dumps(meta or {}))
 
 
 def load(path=WEIGHTS, batch=65536):
@@ -376,7 +388,7 @@ class Surrogate:
         km = mode_kmax(kw["srf_shape"], kw["domain"], kw.get("modes", (512, 512)), kw.get("halo"))
         return self.in_box(kw["n"], kw["zm"], s1, s2, km)
 
-    def serve(self, items, batch=16):
+    def serve(self, items, batch=16, keep=None):
         """Footprints of a met timeseries (keyword dicts of ``prepare``):
         in-box cases through the network in batched fused launches, every
         ``spot_every``-th of them also through the ``spot_mode`` solve (the
@@ -385,8 +397,12 @@ class Surrogate:
         exceeds ``guard_tol`` is re-solved by ``guard_mode``.  Returns
         (outputs, paths): outputs[k] = (conc, flx) (device tensors for served
         cases, host arrays for solver results), paths[k] in "surrogate",
-        "fp32-guard", "fp64-spot", "fp64-box"."""
+        "fp32-guard", "fp64-spot", "fp64-box".  ``keep``: indices whose
+        outputs are returned (default all); the others are computed, checked
+        and dropped (outputs[k] = None), so a long timeseries does not hold
+        every footprint in memory."""
         out, paths = [None] * len(items), [None] * len(items)
+        kept = None if keep is None else set(keep)
         inbox = []
         for k, kw in enumerate(items):
             if self.classify(kw):
@@ -395,7 +411,7 @@ class Surrogate:
                 self.stats["out_of_box"] += 1
                 p = self.prepare(**kw)
                 _, c, f = steady_state_transport_solver(**p["kw"], mode=self.fallback)
-                out[k], paths[k] = (c, f), "fp64-box"
+                out[k], paths[k] = ((c, f) if kept is None or k in kept else None), "fp64-box"
         for i in range(0, len(inbox), batch):
             ks = inbox[i : i + batch]
             b = self.prepare_batch([items[k] for k in ks])
@@ -423,6 +439,10 @@ class Surrogate:
                         if self.fallback != self.spot_mode:
                             ref = steady_state_transport_solver(**pr["kw"], mode=self.fallback)
                         out[k], paths[k] = (ref[1], ref[2]), "fp64-spot"
+            if kept is not None:
+                for k in ks:
+                    if k not in kept:
+                        out[k] = None
         return out, paths
 
     def footprint(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
@@ -461,9 +481,11 @@ def _grid(z, level, shape, domain):
 
 
 def _main(argv=None):
-    """python -m bldfm_gb300.surrogate train [--steps N] [--out PATH]: train
-    the network on the GPU from solver-generated transfer functions and save
-    it (the shipped weights were made this way)."""
+    """python -m bldfm_gb300.surrogate train [--steps N] [--n LEVELS]
+    [--kmax K] [--out PATH]: train the network on the GPU from
+    solver-generated transfer functions for n levels below z_m and
+    |k| z_m <= K, and save it with its serving box (the shipped weights were
+    made this way: n = 128, K = 40, 300k steps; n = 256, K = 48)."""
     import argparse
     import time
 
@@ -474,10 +496,14 @@ def _main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--cases", type=int, default=16384)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--kmax", type=float, default=40.0)
     ap.add_argument("--conc-weight", type=float, default=1.0)
     a = ap.parse_args(argv)
-    pool = TransferPool(ncases=a.cases, seed=0)
+    serve_box, train_box = boxes(a.n, a.kmax)
+    out = a.out or os.path.join(WEIGHT_DIR, "surrogate_n%d.npz" % a.n)
+    pool = TransferPool(ncases=a.cases, seed=0, box=train_box)
     net = MLP(batch=a.batch, seed=a.seed)
     t0 = time.time()
     hist = train(net, pool, a.steps, batch=a.batch, lr=a.lr, seed=a.seed, log_every=max(a.steps // 50, 1),
@@ -486,10 +512,11 @@ def _main(argv=None):
     torch.cuda.synchronize()
     dt = time.time() - t0
     val = validation_loss(net, pool)
-    save(net, a.out, {"steps": a.steps, "batch": a.batch, "lr": a.lr, "cases": a.cases, "seed": a.seed,
-                      "conc_weight": a.conc_weight,
-                      "train_s": dt, "val_loss": float(val), "train_box": TRAIN_BOX, "history": hist[-10:]})
-    print("saved %s: validation loss %.3e, %.1f s" % (a.out, val, dt))
+    save(net, out, {"steps": a.steps, "batch": a.batch, "lr": a.lr, "cases": a.cases, "seed": a.seed,
+                    "conc_weight": a.conc_weight,
+                    "train_s": dt, "val_loss": float(val), "train_box": train_box, "history": hist[-10:]},
+         box=serve_box)
+    print("saved %s: validation loss %.3e, %.1f s" % (out, val, dt))
 
 
 if __name__ == "__main__":

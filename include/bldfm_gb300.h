@@ -196,9 +196,13 @@ typedef struct bldfm_batch_opts {
     int32_t threads;     /* sweep CTA size: 128 or 256 (0: 256)            */
     int32_t ctas_per_sm; /* persistent sweep CTAs per SM (0: occupancy max) */
     int32_t use_graph;   /* capture the batch once, replay it afterwards   */
-    int32_t xform_lines; /* lines per CTA of both output-transform passes:
-                          * 1, 2 or 4 (0: 4 columns / 2 rows), lowered to
-                          * what fits the shared memory                    */
+    int32_t xform_lines; /* output-transform passes: 1, 2 or 4 = shared-
+                          * memory passes with that many lines per CTA
+                          * (lowered to what fits the shared memory); 8 =
+                          * register-resident passes where every case has
+                          * the same supported line lengths; 16 or 0 = as
+                          * 8, with the zoomed column pass where every
+                          * case's band and kept window allow it           */
 } bldfm_batch_opts;
 
 /* Workspace bytes for a batch (256-byte aligned workspace required). */

@@ -56,13 +56,32 @@ def test_shared_integer_level_arrays_are_read_only():
     assert lv is lv2 and not lv.flags.writeable and not levels.flags.writeable
 
 
-def _pending(cases, shapes, host):
+def _pending(cases, shapes, host, sums=None):
     keep = []
     for kw in cases:
         zp, nz, levels, lv, _ = _host_inputs(kw)
         keep.append((zp, nz, lv, levels))
     solver = SimpleNamespace(stream=SimpleNamespace(synchronize=lambda: None))
-    return (solver, cases, shapes, keep, torch.from_numpy(host), torch.zeros(1, dtype=torch.int32))
+    # workspace head as the library leaves it: status word, then from byte 64
+    # the accuracy check's four float sums per case
+    head = torch.zeros(64 + 16 * len(cases), dtype=torch.uint8)
+    if sums is not None:
+        head[64:].view(torch.float32)[:] = torch.tensor(np.asarray(sums, np.float32).ravel())
+    return (solver, cases, shapes, keep, torch.from_numpy(host), head)
+
+
+def test_finish_states_each_case_error_from_the_check_sums():
+    from bldfm_gb300.batch import BatchResults, error_estimate
+
+    cases = [_case(footprint=True), _case(footprint=True), _case(footprint=True)]
+    shapes = [(1, 6, 8)] * 3
+    host = np.zeros(2 * 3 * 48)
+    # (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2) per case
+    sums = [[1e-12, 1.0, 4e-12, 1.0], [9e-14, 1e-2, 0.0, 4.0], [0.0, 0.0, 0.0, 0.0]]
+    res = _finish_batch(_pending(cases, shapes, host, sums))
+    assert isinstance(res, BatchResults) and len(res) == 3
+    np.testing.assert_allclose(res.error_estimates, [2e-6, 3e-6, 0.0], rtol=1e-6)
+    assert error_estimate(sums[0]) == pytest.approx(2e-6)
 
 
 @pytest.mark.parametrize("mixed", [False, True])

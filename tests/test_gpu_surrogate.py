@@ -275,3 +275,41 @@ def test_guard_estimates_and_guarded_serving():
         _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
         assert max(_rel(c, cr), _rel(f, fr)) <= 1e-3, (path, max(_rel(c, cr), _rel(f, fr)))
     print("guarded serving paths:", {q: paths.count(q) for q in set(paths)})
+
+
+def test_production_network_serves_the_production_footprint():
+    """The n = 256 network (|k| z_m <= 48) on the production footprint's
+    neighbourhood: 512^2 grid on 1000 m, 500 m halo (1024^2 extended, all
+    modes), 413 levels, z_m = 20 m.  Every guarded served footprint is within
+    1e-3 of the exact discrete solution; out-of-box steps go to the FP64
+    solver; outputs outside ``keep`` are dropped."""
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import WEIGHTS_N256, Surrogate, load
+
+    if not os.path.exists(WEIGHTS_N256):
+        pytest.skip("no n = 256 weights")
+    net, box, meta = load(WEIGHTS_N256)
+    assert box["n"] == 256 and box["kmax"] >= 45.5
+    rng = np.random.default_rng(5)
+    items = []
+    for k in range(10):
+        th = rng.uniform(0, 2 * np.pi)
+        inv_l = -0.08 if k == 9 else float(rng.uniform(-0.045, 0.01))  # the last one outside the box
+        items.append(dict(n=256, zm=20.0, wind=(-4 * np.sin(th), -4 * np.cos(th)), srf_shape=(512, 512),
+                          domain=(1000.0, 1000.0), modes=(1024, 1024), meas_pt=(500.0, 500.0), halo=500.0,
+                          ustar=float(rng.uniform(0.22, 0.38)), mol=1.0 / inv_l))
+    sur = Surrogate(net, box=box, spot_every=0, tol=1e-3)
+    keep = [0, 3, 7, 9]
+    out, paths = sur.serve(items, batch=8, keep=keep)
+    assert paths[9] == "fp64-box" and all(p in ("surrogate", "fp32-guard") for p in paths[:9]), paths
+    assert all((out[k] is None) == (k not in keep) for k in range(10))
+    for k in keep:
+        p = sur.prepare(**items[k])
+        _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r" if k != 9 else "fp64")
+        c, f = out[k]
+        c = c.cpu().numpy() if hasattr(c, "cpu") else c
+        f = f.cpu().numpy() if hasattr(f, "cpu") else f
+        err = max(_rel(c, cr), _rel(f, fr))
+        print("step %d path %s relL2 %.2e" % (k, paths[k], err))
+        assert err <= (1e-3 if k != 9 else 1e-12), (k, paths[k], err)
+    print("guard estimates:", " ".join("%.1e" % e for e in sur.stats["guard"]))

@@ -1,12 +1,15 @@
-"""The register-resident output-transform passes (xform_lines 8, the default
-when every case of a batch shares a supported line length) against the
-shared-memory passes (xform_lines 2) and the CPU oracle, for every supported
-line length, both transform signs (footprint: fft2; dispersion: ifft2), several
-output levels, a phase shift and different x and y lengths.
+"""The register-resident output-transform passes (xform_lines 8, used when
+every case of a batch shares a supported line length), the same with the
+zoomed column pass (xform_lines 0, the default, for 3 M lines with the band
+and kept window of the default halo) against the shared-memory passes (xform_lines 2) and the
+CPU oracle, for every supported line length, both transform signs
+(footprint: fft2; dispersion: ifft2), several output levels, a phase shift,
+different x and y lengths, a band narrower than the window and a window that
+does not start at M.
 
-Tolerances (relative L2): register vs shared-memory passes 1e-5 (both FP32,
-different operation order); batched FP32 vs the oracle's double-double
-shooting 1e-3 (the fast path's bar)."""
+Tolerances (relative L2): register or zoomed vs shared-memory passes 1e-5
+(all FP32, different operation order); batched FP32 vs the oracle's
+double-double shooting 1e-3 (the fast path's bar)."""
 
 import numpy as np
 import pytest
@@ -24,6 +27,8 @@ SHAPES = [
     ((512, 512), (1000.0, 1000.0), (512, 512), 1500.0),  # 2048 x 2048
     ((1024, 1024), (2000.0, 2000.0), (1024, 1024), None),  # 3072 x 3072
     ((256, 512), (1000.0, 1000.0), (512, 256), None),    # rows 1536, columns 768
+    ((512, 512), (1000.0, 1000.0), (256, 256), None),    # 1536, band of 257 in a zoom of 512
+    ((510, 510), (1000.0, 1000.0), (510, 510), 513.5 * 1000.0 / 510),  # 1536, kept window [513, 1023)
 ]
 
 
@@ -49,13 +54,16 @@ def test_register_passes_match_shared_memory_passes_and_oracle(shape, domain, mo
     from oracle import bldfm_oracle as O
 
     kws = [_kw(shape, domain, modes, halo, footprint, seed) for seed in (1, 2)]
+    zm = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=0))
     rx = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=8))
     sm = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=2))
-    for a, b in zip(rx, sm):
-        assert a[1].shape == b[1].shape
-        assert G.rel_l2(a[1], b[1]) <= 1e-5 and G.rel_l2(a[2], b[2]) <= 1e-5, (G.rel_l2(a[1], b[1]),
-                                                                            G.rel_l2(a[2], b[2]))
+    for variant in (rx, zm):
+        for a, b in zip(variant, sm):
+            assert a[1].shape == b[1].shape
+            assert G.rel_l2(a[1], b[1]) <= 1e-5 and G.rel_l2(a[2], b[2]) <= 1e-5, (G.rel_l2(a[1], b[1]),
+                                                                                G.rel_l2(a[2], b[2]))
     _, oc, of = O.steady_state_transport_solver(**kws[0], sweep="shooting_dd")
-    err = max(G.rel_l2(rx[0][1], oc), G.rel_l2(rx[0][2], of))
-    print(shape, modes, halo, footprint, "rx vs double-double %.2e" % err)
-    assert err <= 1e-3, err
+    for name, variant in (("rx", rx), ("zoom", zm)):
+        err = max(G.rel_l2(variant[0][1], oc), G.rel_l2(variant[0][2], of))
+        print(shape, modes, halo, footprint, "%s vs double-double %.2e" % (name, err))
+        assert err <= 1e-3, err
