@@ -978,7 +978,9 @@ def main():
             "production": prod_line,
             "serving": serve_line,
             "cpu_baseline": cpu,
-            "gpu_launches": 3 * args.steps,
+            # per timed step: the sweep, the column and row transform passes
+            # and the accuracy check
+            "gpu_launches": 4 * args.steps,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

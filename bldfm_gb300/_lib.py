@@ -92,6 +92,7 @@ class BatchOpts(ctypes.Structure):
         ("ctas_per_sm", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
         ("xform_lines", ctypes.c_int32),
+        ("skip_check", ctypes.c_int32),
     ]
 
 

@@ -205,6 +205,13 @@ struct DeviceCache {
     int nsm = 0;
     std::map<int, TwTable> tw;
     std::map<std::pair<int, int>, ModeList> modes;
+    // a second stream per caller stream: the batch's accuracy check runs on
+    // it beside the transform passes (fork and join by events)
+    struct Aux {
+        cudaStream_t s = nullptr;
+        cudaEvent_t fork = nullptr, join = nullptr;
+    };
+    std::map<cudaStream_t, Aux> aux;
     std::map<std::vector<int>, int4 *> xband;
     StageSlot stage[NSTAGE];  // ring of pinned staging buffers
     int stage_next = 0;
@@ -241,6 +248,22 @@ DeviceCache &cache_for_current(int *status)
         prepare_batch_attributes();
     }
     return dc;
+}
+
+// the auxiliary stream of caller stream st (created on first use)
+int get_aux(DeviceCache &dc, cudaStream_t st, DeviceCache::Aux **out)
+{
+    auto it = dc.aux.find(st);
+    if (it == dc.aux.end()) {
+        DeviceCache::Aux a;
+        if (cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming) != cudaSuccess)
+            return BLDFM_ERR_CUDA;
+        it = dc.aux.emplace(st, a).first;
+    }
+    *out = &it->second;
+    return BLDFM_OK;
 }
 
 int get_tw(DeviceCache &dc, int n, TwTable **out)
@@ -562,6 +585,7 @@ struct BatchBuild {
     // register-resident transform passes: config of the column / row line
     // length shared by every case of the batch, or -1
     int rx_col = -1, rx_row = -1;
+    int check = 1;  // run the accuracy check
     std::vector<int64_t> tile0, col0, row0;
 };
 
@@ -570,6 +594,7 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
 {
     if (!cs || n < 1) return BLDFM_ERR_ARG;
     B.threads = (opts && opts->threads > 0) ? opts->threads : 256;
+    B.check = !(opts && opts->skip_check);
     if (B.threads != 128 && B.threads != 256) return BLDFM_ERR_ARG;
     B.hp.resize(n);
     size_t o = 0;
@@ -783,7 +808,7 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
         x.xband = B.xb[k];
         x.conc = c.conc_dev;
         x.flx = c.flx_dev;
-        x.lvd = (const double *)(wb + B.off_lvd[k]);
+        x.lvff = (const float2 *)(wb + B.off_lvd[k]);
         x.ax = (float)(g.lx_scale * g.valx);
         x.ay = (float)(g.ly_scale * g.valy);
         x.tile0 = B.tile0[k];
@@ -796,11 +821,15 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
             hx_level_dz_w(nz, c.z_host, c.prof_host, lv64);  // all the k = 0 values need (no trapezoid pass)
         else
             hx_level_table(nz, c.z_host, c.prof_host, lv64);
-        double *lvd = (double *)(blob + B.off_lvd[k]);
-        if (g.iso)
-            hx_level_table32_iso(nz, c.z_host, c.prof_host, g.ex, g.ey, (float *)(blob + B.off_lv32[k]), lvd);
-        else
+        // FP32 table of the sweep; the accuracy check's float-pair table always
+        // in the generic row layout (u, v themselves, no rounded wind direction)
+        float *lvd = (float *)(blob + B.off_lvd[k]);
+        if (g.iso) {
+            hx_level_table32_iso(nz, c.z_host, c.prof_host, g.ex, g.ey, (float *)(blob + B.off_lv32[k]), nullptr);
+            hx_level_table32(nz, c.z_host, c.prof_host, nullptr, lvd);
+        } else {
             hx_level_table32(nz, c.z_host, c.prof_host, (float *)(blob + B.off_lv32[k]), lvd);
+        }
         memcpy(blob + B.off_slot[k], hp.slot.data(), (size_t)nz * 4);
         if (g.footprint)
             hx_dc_values(nz, lv64, hp.slot.data(), g.q0dc_fp, 0.0, c.desc.srf_bg_conc,
@@ -830,7 +859,7 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
 }
 
 int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const void *blob_host, cudaStream_t st,
-                  DeviceCache *tdc)
+                  DeviceCache *tdc, DeviceCache::Aux *aux)
 {
     if (tdc) tmark(*tdc, st);  // 0: upload and per-case forward transforms
     CK(cudaMemcpyAsync(ws + B.blob_at, blob_host, B.blob_bytes, cudaMemcpyHostToDevice, st));
@@ -875,10 +904,23 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
     bl.rx_row = B.rx_row;
     if (tdc) tmark(*tdc, st);  // 1: the sweep
     CK(launch_batch_kernels(bl, st, 0));
+    // the accuracy check reads the spectra, as the transform passes do: it
+    // runs beside them on the auxiliary stream (after them when the stages
+    // are timed, so that each stage's time is its own)
+    const bool fork = B.check && aux && !tdc;
+    if (fork) {
+        CK(cudaEventRecord(aux->fork, st));
+        CK(cudaStreamWaitEvent(aux->s, aux->fork, 0));
+        CK(launch_fp32_check(bl.cases, n, (float4 *)(ws + 64), aux->s));
+        CK(cudaEventRecord(aux->join, aux->s));
+    }
     if (tdc) tmark(*tdc, st);  // 2: the output transform
     CK(launch_batch_kernels(bl, st, 1));
     if (tdc) tmark(*tdc, st);  // 3: the accuracy check
-    CK(launch_fp32_check(bl.cases, n, BATCH_CHECK_SAMPLES, (float4 *)(ws + 64), st));
+    if (fork)
+        CK(cudaStreamWaitEvent(st, aux->join, 0));
+    else if (B.check)
+        CK(launch_fp32_check(bl.cases, n, (float4 *)(ws + 64), st));
     if (tdc) tmark(*tdc, st);  // 4: end
     return BLDFM_OK;
 }
@@ -899,6 +941,7 @@ std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B,
     k.push_back(B.persist);
     k.push_back(B.rx_col);
     k.push_back(B.rx_row);
+    k.push_back(B.check);
     k.push_back(B.col_grid);
     k.push_back(B.row_grid);
     for (int i = 0; i < n; ++i) {
@@ -1114,7 +1157,7 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     DeviceCache &dc = cache_for_current(&status);
     if (status != BLDFM_OK) return status;
     BatchBuild B;
-    bldfm_batch_opts opts = {256, 0, 0, 0};
+    bldfm_batch_opts opts = {256, 0, 0, 0, 1};
     if ((rc = batch_build(cs, n, &opts, &dc, B, sur_extra_bytes(n))) != BLDFM_OK) return rc;
     if (ws_bytes < B.total + sur_guard_bytes(n)) return BLDFM_ERR_WORKSPACE;
     for (int k = 0; k < n; ++k) {
@@ -1426,12 +1469,14 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch
     cudaStream_t st = (cudaStream_t)stream;
     char *ws = (char *)workspace;
     const bool graph = opts && opts->use_graph && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+    DeviceCache::Aux *aux = nullptr;
+    if ((rc = get_aux(dc, st, &aux)) != BLDFM_OK) return rc;
     if (!graph) {
         StageSlot *slt = nullptr;
         if ((rc = acquire_stage(dc, B.blob_bytes + 256, &slt)) != BLDFM_OK) return rc;
         batch_fill_blob(cases, ncases, B, ws, (char *)slt->buf);
         timers_begin(dc);
-        if ((rc = batch_enqueue(cases, ncases, B, ws, slt->buf, st, dc.timing ? &dc : nullptr)) != BLDFM_OK)
+        if ((rc = batch_enqueue(cases, ncases, B, ws, slt->buf, st, dc.timing ? &dc : nullptr, aux)) != BLDFM_OK)
             return rc;
         CK(cudaEventRecord(slt->ev, st));
         return BLDFM_OK;
@@ -1455,7 +1500,7 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch
         // capture the whole batch once; a failure leaves the stream usable
         cudaGraph_t graph_h = nullptr;
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        rc = batch_enqueue(cases, ncases, B, ws, x.pinned, st, nullptr);
+        rc = batch_enqueue(cases, ncases, B, ws, x.pinned, st, nullptr, aux);
         cudaError_t ce = cudaStreamEndCapture(st, &graph_h);
         if (rc != BLDFM_OK || ce != cudaSuccess) {
             if (graph_h) cudaGraphDestroy(graph_h);
@@ -1508,7 +1553,7 @@ int bldfm_surrogate_batch_plan(const bldfm_case *cases, const bldfm_surrogate_ca
     if (rc != BLDFM_OK) return rc;
     std::lock_guard<std::mutex> lk(g_mutex);
     BatchBuild B;
-    bldfm_batch_opts opts = {256, 0, 0, 0};
+    bldfm_batch_opts opts = {256, 0, 0, 0, 1};
     if ((rc = batch_build(cases, ncases, &opts, nullptr, B, sur_extra_bytes(ncases))) != BLDFM_OK) return rc;
     *workspace_bytes = (int64_t)(B.total + sur_guard_bytes(ncases));
     return BLDFM_OK;

@@ -24,7 +24,7 @@ struct __align__(16) BatchCase {
     const float2 *twx, *twy;
     const int4 *xband;
     double *conc, *flx;
-    const double *lvd;  // FP64 rows of the level table (accuracy check)
+    const float2 *lvff;  // the level table's FP64 rows as float pairs hi + lo (accuracy check)
     float ax, ay;
     int64_t tile0;  // first sweep tile of this case
     int64_t col0;   // first column-transform CTA
@@ -56,12 +56,11 @@ struct BatchLaunch {
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);
 
-// Accuracy check of a batched FP32 solve (batch.cu: fp32_check_kernel): ns
-// sampled modes per case (ns a multiple of 32) evaluated exactly in FP64 and
-// compared with the FP32 spectra at the highest output level; per case
-// acc[k] += (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2).
-#define BATCH_CHECK_SAMPLES 256
-cudaError_t launch_fp32_check(const BatchCase *cases, int n, int ns, float4 *acc, cudaStream_t st);
+// Accuracy check of a batched FP32 solve (batch.cu: fp32_check_kernel): a
+// stratified sample of 32 modes per case evaluated in float-float arithmetic
+// and compared with the FP32 spectra at the highest output level; per case
+// acc[k] = weighted (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2).
+cudaError_t launch_fp32_check(const BatchCase *cases, int n, float4 *acc, cudaStream_t st);
 
 // Accuracy guard of a surrogate batch (batch.cu: sur_guard_kernel): exact
 // FP32 values of every stride-th solved mode against the served spectra,

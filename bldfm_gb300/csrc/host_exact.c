@@ -50,9 +50,10 @@ void hx_level_dz_w(int nz, const double *z, const double *prof, double *lv)
     }
 }
 
-/* FP32 level table of the Riccati sweep, from the same per-step scalars;
- * lvd (may be NULL) receives the same rows unrounded, in FP64. */
-void hx_level_table32(int nz, const double *z, const double *prof, float *lv, double *lvd)
+/* FP32 level table of the Riccati sweep, from the same per-step scalars
+ * (lv may be NULL); lvff (may be NULL) receives the same rows unrounded as
+ * float pairs (hi, lo), hi + lo the FP64 value to about 2^-48. */
+void hx_level_table32(int nz, const double *z, const double *prof, float *lv, float *lvff)
 {
     const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Ky = prof + 3 * nz, *Kz = prof + 4 * nz;
     for (int i = 0; i < nz - 1; ++i) {
@@ -72,10 +73,14 @@ void hx_level_table32(int nz, const double *z, const double *prof, float *lv, do
         r[9] = -2.0 * c1;
         r[10] = 0.0;
         r[11] = 0.0;
-        float *row = lv + (size_t)i * 12;
-        for (int j = 0; j < 12; ++j) row[j] = (float)r[j];
-        if (lvd)
-            for (int j = 0; j < 12; ++j) lvd[(size_t)i * 12 + j] = r[j];
+        if (lv)
+            for (int j = 0; j < 12; ++j) lv[(size_t)i * 12 + j] = (float)r[j];
+        if (lvff)
+            for (int j = 0; j < 12; ++j) {
+                const float h = (float)r[j];
+                lvff[((size_t)i * 12 + j) * 2] = h;
+                lvff[((size_t)i * 12 + j) * 2 + 1] = (float)(r[j] - (double)h);
+            }
     }
 }
 
@@ -166,9 +171,9 @@ int hx_profiles_iso(int nz, const double *prof, double *ex, double *ey)
 }
 
 /* Compact FP32 level table for isotropic profiles with a fixed wind
- * direction (row layout of StepCoef<true> in sweep32.cuh); lvd (may be NULL)
- * receives the same rows unrounded, in FP64. */
-void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex, double ey, float *lv, double *lvd)
+ * direction (row layout of StepCoef<true> in sweep32.cuh); lvff (may be
+ * NULL) receives the same rows unrounded as float pairs (hi, lo). */
+void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex, double ey, float *lv, float *lvff)
 {
     const double *u = prof, *v = prof + nz, *Kx = prof + 2 * nz, *Kz = prof + 4 * nz;
     for (int i = 0; i < nz - 1; ++i) {
@@ -192,8 +197,12 @@ void hx_level_table32_iso(int nz, const double *z, const double *prof, double ex
         r[11] = 0.0;
         float *row = lv + (size_t)i * 12;
         for (int j = 0; j < 12; ++j) row[j] = (float)r[j];
-        if (lvd)
-            for (int j = 0; j < 12; ++j) lvd[(size_t)i * 12 + j] = r[j];
+        if (lvff)
+            for (int j = 0; j < 12; ++j) {
+                const float h = (float)r[j];
+                lvff[((size_t)i * 12 + j) * 2] = h;
+                lvff[((size_t)i * 12 + j) * 2 + 1] = (float)(r[j] - (double)h);
+            }
     }
 }
 

@@ -203,6 +203,8 @@ typedef struct bldfm_batch_opts {
                           * the same supported line lengths; 16 or 0 = as
                           * 8, with the zoomed column pass where every
                           * case's band and kept window allow it           */
+    int32_t skip_check;  /* 1: no accuracy check (the error sums from
+                          * workspace byte 64 stay zero); 0: check      */
 } bldfm_batch_opts;
 
 /* Workspace bytes for a batch (256-byte aligned workspace required). */
@@ -212,7 +214,13 @@ int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases,
 /* Enqueue a batch on stream; returns once enqueued.  The int32 at workspace
  * offset 0 holds the device status after completion.  A workspace smaller
  * than the batch needs gives BLDFM_ERR_WORKSPACE before anything is
- * enqueued, so a caller may solve first and plan only on that status. */
+ * enqueued, so a caller may solve first and plan only on that status.
+ * Error statement (no reference counterpart): from workspace byte 64, four
+ * floats per case, the weighted (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2,
+ * sum |Xq|^2) of the FP32 spectra at the highest output level against FP64
+ * re-solves of a stratified sample of 32 modes (the k = 0 mode, every mode
+ * with |kx|, |ky| <= 2, 19 equal slices of the mode list); the case's
+ * estimated relative L2 error is the larger of the two square-root ratios. */
 int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases,
                       const bldfm_batch_opts *opts, void *workspace,
                       size_t workspace_bytes, void *stream);

@@ -111,7 +111,7 @@ def test_batch_plan_sizes_without_device_cache(xform_lines):
                            "fp32")
         c.z_host, c.prof_host, c.levels_host, c.nlvls = zz.ctypes.data, prof.ctypes.data, lv.ctypes.data, 1
         c.conc_dev = c.flx_dev = 256  # output addresses are only checked for presence when planning
-    opts = _lib.BatchOpts(0, 0, 0, xform_lines)
+    opts = _lib.BatchOpts(0, 0, 0, xform_lines, 0)
     need = ctypes.c_int64(0)
     assert lib.bldfm_batch_plan(arr, 2, ctypes.byref(opts), ctypes.byref(need)) == 0
     assert need.value > 0

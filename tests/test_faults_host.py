@@ -71,7 +71,7 @@ def test_invalid_profiles_rejected_by_every_entry(name, z, prof):
     case.z_host, case.prof_host, case.levels_host = z.ctypes.data, prof.ctypes.data, lv.ctypes.data
     case.nlvls = 1
     case.conc_dev = case.flx_dev = out.ctypes.data  # planning never dereferences the outputs
-    opts = _lib.BatchOpts(0, 0, 0, 0)
+    opts = _lib.BatchOpts(0, 0, 0, 0, 0)
     nb = ctypes.c_int64(0)
     st = lib.bldfm_batch_plan(ctypes.byref(case), 1, ctypes.byref(opts), ctypes.byref(nb))
     assert st == _lib.ERR_PROFILE

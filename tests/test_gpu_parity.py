@@ -153,3 +153,24 @@ def test_fp32_against_exact_on_headline_workload():
     print("headline: fp32 vs exact %.2e, reference rounding vs exact %.2e" % (e32, floor))
     assert e32 <= 1e-4
     assert floor <= 1e-3
+
+
+@pytest.mark.parametrize("name", ["metric_footprint_512", "plume_3d", "source_area"])
+def test_dropin_states_its_error(name):
+    """``return_error=True``: an FP32 result comes with its estimated relative
+    L2 error against the exact discrete solution (the device accuracy check);
+    the estimate stays within a factor 10 of the true error (measured against
+    the accurate FP64 path) and below the 1e-3 bar; the FP64 modes state None.
+    Without ``return_error`` the result is the plain (grid, conc, flx)."""
+    from bldfm_gb300 import steady_state_transport_solver
+
+    d = G.load(name)
+    kw = G.kwargs_of(d)
+    grid, c32, f32, est = steady_state_transport_solver(**kw, mode="fp32", return_error=True)
+    _, cr, fr = _gpu_solve(kw, mode="fp64r")
+    true = max(G.rel_l2(c32, cr), G.rel_l2(f32, fr))
+    print("%s: stated %.2e, true %.2e" % (name, est, true))
+    assert est <= 1e-3 and 0.1 * true <= est <= 10.0 * true, (est, true)
+    *_, none = steady_state_transport_solver(**kw, mode="fp64", return_error=True)
+    assert none is None
+    assert len(steady_state_transport_solver(**kw, mode="fp32")) == 3

@@ -291,14 +291,17 @@ def test_production_network_serves_the_production_footprint():
     net, box, meta = load(WEIGHTS_N256)
     assert box["n"] == 256 and box["kmax"] >= 45.5
     rng = np.random.default_rng(5)
-    items = []
-    for k in range(10):
-        th = rng.uniform(0, 2 * np.pi)
-        inv_l = -0.08 if k == 9 else float(rng.uniform(-0.045, 0.01))  # the last one outside the box
-        items.append(dict(n=256, zm=20.0, wind=(-4 * np.sin(th), -4 * np.cos(th)), srf_shape=(512, 512),
-                          domain=(1000.0, 1000.0), modes=(1024, 1024), meas_pt=(500.0, 500.0), halo=500.0,
-                          ustar=float(rng.uniform(0.22, 0.38)), mol=1.0 / inv_l))
     sur = Surrogate(net, box=box, spot_every=0, tol=1e-3)
+    items = []
+    while len(items) < 10:
+        th = rng.uniform(0, 2 * np.pi)
+        outside = len(items) == 9  # the last one outside the box (strongly unstable)
+        inv_l = float(rng.uniform(-0.1, -0.06) if outside else rng.uniform(-0.045, 0.01))
+        kw = dict(n=256, zm=20.0, wind=(-4 * np.sin(th), -4 * np.cos(th)), srf_shape=(512, 512),
+                  domain=(1000.0, 1000.0), modes=(1024, 1024), meas_pt=(500.0, 500.0), halo=500.0,
+                  ustar=float(rng.uniform(0.22, 0.38)), mol=1.0 / inv_l)
+        if sur.classify(kw) != outside:
+            items.append(kw)
     keep = [0, 3, 7, 9]
     out, paths = sur.serve(items, batch=8, keep=keep)
     assert paths[9] == "fp64-box" and all(p in ("surrogate", "fp32-guard") for p in paths[:9]), paths
