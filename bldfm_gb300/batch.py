@@ -83,13 +83,24 @@ def _host_inputs(kw):
     return zp, nz, levels, lv, lvp
 
 
+# rounding of the FP32 output transform, per unit of the field it transforms:
+# one FP32 ulp (the transform carries conc + i flux as one complex field, so
+# each part's rounding scales with the norm of both)
+XFORM_ROUNDING = 2.0**-24
+
+
 def error_estimate(sums):
     """Relative L2 error estimate of one case from the accuracy check's sums
-    (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2): the larger of the
-    concentration and the flux spectra's."""
+    (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2, weighted over the
+    sampled modes and the output levels): for the concentration and the flux
+    spectra, the measured sweep error sqrt(sum |dX|^2 / sum |X|^2) combined
+    with the output transform's rounding, XFORM_ROUNDING times the combined
+    norm over the field's own, sqrt((|Xp|^2 + |Xq|^2) / |X|^2); the larger
+    of the two fields'."""
     dp, p, dq, q = (float(v) for v in sums)
-    ep = (dp / p) ** 0.5 if p > 0 else 0.0
-    eq = (dq / q) ** 0.5 if q > 0 else 0.0
+    tot = p + q
+    ep = (dp / p + XFORM_ROUNDING**2 * tot / p) ** 0.5 if p > 0 else 0.0
+    eq = (dq / q + XFORM_ROUNDING**2 * tot / q) ** 0.5 if q > 0 else 0.0
     return max(ep, eq)
 
 

@@ -551,7 +551,10 @@ int solve_impl(const bldfm_desc *d, const double *srf_dev, const double *z, cons
             CK(launch_riccati32(g, lv32, slot, ml->dev, q0, (float *)(w + L.scratch), Xp, Xq, ax, ay, err, dc.nsm,
                                 256, st));
         tmark(dc, st);  // 2: after the sweep
-        if (!g.footprint) CK(launch_trapezoid32(g, lv64, slot, q0, p000, dcv, st));
+        // the k = 0 source value as the FP64 sum of the source (partials in
+        // bytes 128..255 of the status region)
+        if (!g.footprint)
+            CK(launch_trapezoid32(g, lv64, slot, q0, p000, dcv, st, srf_dev, (double *)(w + L.err + 128)));
         tmark(dc, st);  // 3: before the output transform
         CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
                                     (float2 *)(w + L.Cb), conc, flx, err, st));
@@ -575,7 +578,7 @@ struct BatchBuild {
     size_t off_cases = 0, off_tile_case = 0, off_cta_tiles = 0, off_col_case = 0, off_row_case = 0;
     std::vector<size_t> off_lv32, off_lv64, off_lvd, off_slot, off_dc;
     size_t blob_bytes = 0, blob_at = 0, extra_off = 0;
-    std::vector<size_t> d_q0, d_A, d_scratch, d_Xp, d_Xq, d_Cb;
+    std::vector<size_t> d_q0, d_A, d_dcp, d_scratch, d_Xp, d_Xq, d_Cb;
     size_t total = 0;
     int64_t ntiles = 0;
     int G = 0, threads = 256, ncol = 0, nrow = 0, rpc = 2, cpc = 1;
@@ -701,6 +704,7 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     w = al(w + B.blob_bytes);
     B.d_q0.resize(n);
     B.d_A.resize(n);
+    B.d_dcp.resize(n);
     B.d_scratch.resize(n);
     B.d_Xp.resize(n);
     B.d_Xq.resize(n);
@@ -712,6 +716,8 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
         w = al(w + (g.footprint ? 0 : (size_t)g.nlx * g.nly * 8));
         B.d_A[k] = w;
         w = al(w + (g.footprint ? 0 : (size_t)g.nlx * g.ny * 8));
+        B.d_dcp[k] = w;  // FP64 partial sums of the source (the k = 0 source value)
+        w = al(w + (g.footprint ? 0 : DC_PARTS * sizeof(double)));
         B.d_scratch[k] = w;
         w = al(w + (g.nsnap > 1 ? (size_t)g.nsnap * 5 * g.nsolved * 4 : 0));
         B.d_Xp[k] = w;
@@ -877,7 +883,8 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
             CK(launch_forward_fft<float>(g, B.hp[k].plx_fwd, B.hp[k].ply_fwd, B.twxf[k]->d32, B.twyf[k]->d32,
                                          cs[k].srf_flx_dev, (float2 *)(ws + B.d_A[k]), q0, st));
             CK(launch_trapezoid32(g, (const double *)(wb + B.off_lv64[k]), (const int *)(wb + B.off_slot[k]), q0,
-                                  cs[k].desc.srf_bg_conc, (double2 *)(wb + B.off_dc[k]), st));
+                                  cs[k].desc.srf_bg_conc, (double2 *)(wb + B.off_dc[k]), st, cs[k].srf_flx_dev,
+                                  (double *)(ws + B.d_dcp[k])));
         }
     }
     BatchLaunch bl;
@@ -1136,9 +1143,10 @@ int sur_batch_check(const bldfm_case *cs, const bldfm_surrogate_case *mets, int 
     return BLDFM_OK;
 }
 
-// Accuracy guard of the batched surrogate: every SUR_GUARD_STRIDE-th solved
-// mode of each case re-solved exactly (FP32 sweep) and compared with the
-// served spectra.  The blob's extra region holds the SurCase records, then
+// Accuracy guard of the batched surrogate: a stratified sample of each case
+// (the k = 0 mode, the modes with |kx|, |ky| <= 2, every SUR_GUARD_STRIDE-th
+// solved mode) re-solved exactly (FP32 sweep) and compared with the served
+// spectra.  The blob's extra region holds the SurCase records, then
 // the guard's sample offsets; the per-case sums (4 floats) sit in the last
 // sur_guard_bytes(n) bytes of the planned workspace.
 enum { SUR_GUARD_STRIDE = 61 };  // prime: no alignment with the rows of a column
@@ -1200,7 +1208,8 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     int64_t *prefix = (int64_t *)(blob + B.extra_off + sur_prefix_off(n));
     prefix[0] = 0;
     for (int k = 0; k < n; ++k) {
-        const int64_t s = (B.hp[k].g.nsolved + SUR_GUARD_STRIDE - 1) / SUR_GUARD_STRIDE;
+        // the k = 0 mode, the low-wavenumber box, every stride-th solved mode
+        const int64_t s = 1 + SUR_GUARD_BOX + (B.hp[k].g.nsolved + SUR_GUARD_STRIDE - 1) / SUR_GUARD_STRIDE;
         prefix[k + 1] = prefix[k] + ((s + 31) & ~(int64_t)31);
     }
     timers_begin(dc);

@@ -394,13 +394,18 @@ __global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(err, 0, BLDFM_ERR_NONFINITE_DEV);
 }
 
-// Accuracy guard of the surrogate's batched footprints: sample i of the
-// batch is solved mode (i - prefix[k]) * stride of case k (prefix[k] <= i <
-// prefix[k + 1], every case's sample count padded to a multiple of 32, the
-// padding contributing nothing).  Each sample's exact FP32 values
-// (ricc_mode_value) are compared with the spectra the serving kernel wrote;
-// acc[k] accumulates (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2) of
-// case k (one atomic per warp and quantity).
+// Accuracy guard of the surrogate's batched footprints, a stratified sample
+// per case (the footprint's L2 norm sits in the low wavenumbers): local
+// sample j = i - prefix[k] of case k (prefix[k] <= i < prefix[k + 1], every
+// case's count padded to a multiple of 32, the padding contributing nothing)
+// is
+//   j = 0              the k = 0 mode (exact from the host, error 0),
+//   j = 1 .. GBOX      every solved mode with |kx|, |ky| <= 2 (weight 1),
+//   j > GBOX           solved mode (j - 1 - GBOX) * stride (weight stride),
+// each solved mode counted twice when its mirror is written from it.  The
+// exact FP32 values (ricc_rc_value) are compared with the spectra the serving
+// kernel wrote; acc[k] accumulates the weighted (sum |dXp|^2, sum |Xp|^2,
+// sum |dXq|^2, sum |Xq|^2) of case k (one atomic per warp and quantity).
 __global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restrict__ cases, int n,
                                                         const int64_t *__restrict__ prefix, int stride,
                                                         float4 *__restrict__ acc)
@@ -410,20 +415,50 @@ __global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restr
     int k = 0;
     while (k + 1 < n && prefix[k + 1] <= i) ++k;
     const BatchCase &bc = cases[k];
-    const int64_t m = (i - prefix[k]) * (int64_t)stride;
+    const SolveGeom &g = bc.g;
+    const int64_t j = i - prefix[k];
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (m < bc.g.nsolved) {
+    int r = -1, c = -1;
+    float wgt = 1.f;
+    if (j == 0) {
+        const double2 p = bc.dc[0], q = bc.dc[1];
+        v = make_float4(0.f, (float)(p.x * p.x + p.y * p.y), 0.f, (float)(q.x * q.x + q.y * q.y));
+    } else if (j <= SUR_GUARD_BOX) {
+        const int t = (int)j - 1;
+        int kx, ky;
+        if (t < 2) {
+            kx = 0;
+            ky = t + 1;
+        } else {
+            kx = 1 + (t - 2) / 5;
+            ky = (t - 2) % 5 - 2;
+        }
+        if (kx <= freq_max(g.nlx) && ky >= freq_min(g.nly) && ky <= freq_max(g.nly)) {
+            r = index_of_freq(ky, g.nly);
+            c = index_of_freq(kx, g.nlx);
+        }
+    } else {
+        const int64_t m = (j - 1 - SUR_GUARD_BOX) * (int64_t)stride;
+        if (m < g.nsolved) {
+            bool paired;
+            unpack_mode(bc.modes[m], r, c, paired);
+            wgt = (float)stride;
+        }
+    }
+    if (r >= 0) {
         float2 pe, qe;
-        int r, c;
-        if (bc.g.iso)
-            ricc_mode_value<true>(bc.g, bc.lv32, bc.modes, bc.ax, bc.ay, m, pe, qe, r, c);
+        if (g.iso)
+            ricc_rc_value<true>(g, bc.lv32, bc.ax, bc.ay, r, c, pe, qe);
         else
-            ricc_mode_value<false>(bc.g, bc.lv32, bc.modes, bc.ax, bc.ay, m, pe, qe, r, c);
-        const size_t o = spec_idx(bc.g, 0, r, c);
+            ricc_rc_value<false>(g, bc.lv32, bc.ax, bc.ay, r, c, pe, qe);
+        const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
+        if (-kx >= freq_min(g.nlx) && -kx <= freq_max(g.nlx) && -ky >= freq_min(g.nly) && -ky <= freq_max(g.nly))
+            wgt *= 2.f;
+        const size_t o = spec_idx(g, 0, r, c);
         const float2 pn = bc.Xp[o], qn = bc.Xq[o];
         const float dpx = pn.x - pe.x, dpy = pn.y - pe.y, dqx = qn.x - qe.x, dqy = qn.y - qe.y;
-        v = make_float4(dpx * dpx + dpy * dpy, pe.x * pe.x + pe.y * pe.y, dqx * dqx + dqy * dqy,
-                        qe.x * qe.x + qe.y * qe.y);
+        v = make_float4(wgt * (dpx * dpx + dpy * dpy), wgt * (pe.x * pe.x + pe.y * pe.y),
+                        wgt * (dqx * dqx + dqy * dqy), wgt * (qe.x * qe.x + qe.y * qe.y));
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -449,8 +484,8 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 }
 
 // Accuracy check of a batched FP32 solve (no reference counterpart: the
-// statement of each result's error).  The exact value of a sampled mode at the
-// highest output level comes from the invariant-imbedding recursion in
+// statement of each result's error).  The exact values of a sampled mode at
+// every output level come from the invariant-imbedding recursion in
 // float-float arithmetic (~48-bit significand, ffmath.cuh) on the case's
 // float-pair level table (the FP64 rows split into hi + lo, generic layout),
 // with the top radiation condition, flux product and source spectrum of the
@@ -464,7 +499,8 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 // each solved mode counted twice when its mirror is written from it; acc[k]
 // accumulates the weighted (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2).
 // Not included: the FP32 rounding of the phase factor and, off footprint
-// mode, of the forward transform of the source (both enter as given).
+// mode, of the forward transform of the source at k != 0 (both enter as
+// given; the k = 0 source value is an FP64 sum, dc_partial_kernel).
 //
 // One warp per sample, the levels split over its lanes: each step
 // R_i = (a R_{i+1} - b) / (a - c R_{i+1}) is the Moebius map of the matrix
@@ -472,8 +508,9 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 // [lo_l, hi_l) into M_l = A_lo ... A_{hi-1}; a suffix scan over the lanes
 // gives S_l = M_l ... M_31, from which lane l takes the ratio at the top of
 // its run, R_{hi_l} = S_{l+1}(R_L); each lane then runs its own levels (ratio
-// and flux factors c_i R_i + a_i below z_m), and the flux product is the
-// product over the lanes.  A serial float-float sweep took 0.32 ms per
+// and flux factors c_i R_i + a_i below the highest output level), and the
+// flux product at an output level is the product of the lower lanes' factors
+// and this lane's below it.  A serial float-float sweep took 0.32 ms per
 // 16-footprint batch (206 dependent steps per sample); the split one runs
 // about 7 levels per lane plus 5 scan steps.
 #define CHECK_NS 32
@@ -550,9 +587,19 @@ __device__ __forceinline__ void cff_renorm(cff &Q, int &E)
     }
 }
 
-// exact (p, q) of mode (r, c) at the highest output level vs the FP32
-// spectra, the whole warp together; lane 0 receives
-// v = (|dXp|^2, |Xp|^2, |dXq|^2, |Xq|^2)
+__device__ __forceinline__ cff cff_shfl_up(cff a, int d)
+{
+    return {{__shfl_up_sync(0xffffffffu, a.re.hi, d), __shfl_up_sync(0xffffffffu, a.re.lo, d)},
+            {__shfl_up_sync(0xffffffffu, a.im.hi, d), __shfl_up_sync(0xffffffffu, a.im.lo, d)}};
+}
+
+// exact (p, q) of mode (r, c) at every output level vs the FP32 spectra, the
+// whole warp together; every lane returns its part of
+// v = (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2) over the output levels
+// in its run of levels.  The flux product at output level j is
+// Q(j) = prod_{i < j} f_i, f_i = c_i R_i + a_i: the product of the lower
+// lanes' factors (an exclusive prefix product over the lanes) times this
+// lane's factors below j.
 __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, int lane, float4 &v)
 {
     const SolveGeom &g = bc.g;
@@ -589,44 +636,48 @@ __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, in
     }
     // ratio at the top of this lane's run: S_{lane+1}(R_L), or R_L for lane 31
     const mff Sn = mff_shfl_down(S, 1);
-    cff R = RL;
+    cff Rtop = RL;
     if (lane < 31)
-        R = cff_div(cff_add(cff_mul(Sn.m11, RL), Sn.m12), cff_add(cff_mul(Sn.m21, RL), Sn.m22));
-    // own levels: ratio, flux factors below z_m, the ratio at z_m
-    cff Q = one, Rj = RL;
-    int E = 0;
+        Rtop = cff_div(cff_add(cff_mul(Sn.m11, RL), Sn.m12), cff_add(cff_mul(Sn.m21, RL), Sn.m22));
+    // pass 1: this lane's flux factors below the highest output level
+    cff F = one, R = Rtop;
+    int EF = 0;
     for (int i = hi - 1; i >= lo; --i) {
         cff a, b, cc;
         coef_ff(bc.lvff + (size_t)i * BLDFM_LV32, lx, ly, lx2, ly2, a, b, cc);
         R = cff_div(cff_sub(cff_mul(a, R), b), cff_sub(a, cff_mul(cc, R)));
-        if (i == jm) Rj = R;
         if (i < jm) {
-            Q = cff_mul(Q, cff_add(cff_mul(cc, R), a));
-            cff_renorm(Q, E);
+            F = cff_mul(F, cff_add(cff_mul(cc, R), a));
+            cff_renorm(F, EF);
         }
     }
-    // the ratio at z_m from the lane that owns level jm (R_L when jm is the top)
-    const unsigned own = __ballot_sync(0xffffffffu, jm >= lo && jm < hi);
-    const int src = own ? __ffs(own) - 1 : -1;
-    if (src >= 0) Rj = cff_shfl(Rj, src);
-    // flux product over the lanes
+    // exclusive prefix product over the lanes: P = F_0 ... F_{lane-1}
+    cff P = F;
+    int EP = EF;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const cff Qo = cff_shfl_xor(Q, d);
-        const int Eo = __shfl_xor_sync(0xffffffffu, E, d);
-        Q = cff_mul(Q, Qo);
-        E += Eo;
-        cff_renorm(Q, E);
+        const cff Po = cff_shfl_up(P, d);
+        const int Eo = __shfl_up_sync(0xffffffffu, EP, d);
+        if (lane >= d) {
+            P = cff_mul(P, Po);
+            EP += Eo;
+            cff_renorm(P, EP);
+        }
     }
-    if (lane != 0) return;
+    P = cff_shfl_up(P, 1);
+    EP = __shfl_up_sync(0xffffffffu, EP, 1);
+    if (lane == 0) {
+        P = one;
+        EP = 0;
+    }
+    const cff PF = cff_mul(P, F);  // the flux product up to the top of this lane's run
+    const int EPF = EP + EF;
+    // source spectrum and the FP32 sweep's phase factor (taken as exact)
     cff q0 = {ff_from_double(g.q0dc_fp), ff_from(0.f)};
     if (bc.q0) {
         const float2 f = bc.q0[(size_t)c * g.nly + r];
         q0 = {ff_from(f.x), ff_from(f.y)};
     }
-    cff q = cff_mul(q0, Q);
-    cff p = cff_mul(Rj, q);
-    // the FP32 sweep's phase factor (32-bit fixed-point turns), taken as exact
     float2 sh = make_float2(1.f, 0.f);
     if (g.do_shift) {
         const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
@@ -634,19 +685,51 @@ __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, in
         sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
         sh = make_float2(cs, sn);
     }
-    const cff shf = {ff_from(sh.x), ff_from(sh.y)};
-    p = cff_mul(p, shf);
-    q = cff_mul(q, shf);
-    // values and differences (formed in float-float) scaled back by 2^E
-    const size_t o = spec_idx(g, bc.slot[jm], r, c);
-    const float2 pn = bc.Xp[o], qn = bc.Xq[o];
-    const float pe0 = ldexpf(p.re.hi, E) + ldexpf(p.re.lo, E), pe1 = ldexpf(p.im.hi, E) + ldexpf(p.im.lo, E);
-    const float qe0 = ldexpf(q.re.hi, E) + ldexpf(q.re.lo, E), qe1 = ldexpf(q.im.hi, E) + ldexpf(q.im.lo, E);
-    const float dpx = ldexpf(ff_sub(p.re, ff_from(ldexpf(pn.x, -E))).hi, E);
-    const float dpy = ldexpf(ff_sub(p.im, ff_from(ldexpf(pn.y, -E))).hi, E);
-    const float dqx = ldexpf(ff_sub(q.re, ff_from(ldexpf(qn.x, -E))).hi, E);
-    const float dqy = ldexpf(ff_sub(q.im, ff_from(ldexpf(qn.y, -E))).hi, E);
-    v = make_float4(dpx * dpx + dpy * dpy, pe0 * pe0 + pe1 * pe1, dqx * dqx + dqy * dqy, qe0 * qe0 + qe1 * qe1);
+    const cff qsh = cff_mul(q0, cff{ff_from(sh.x), ff_from(sh.y)});
+    v = make_float4(0.f, 0.f, 0.f, 0.f);
+    // exact values of output level j (flux product Qj * 2^E, ratio Rj) against
+    // the spectra of its slot
+    auto emit = [&](int j, cff Qj, int E, cff Rj) {
+        const cff q = cff_mul(qsh, Qj);
+        const cff p = cff_mul(Rj, q);
+        const size_t o = spec_idx(g, bc.slot[j], r, c);
+        const float2 pn = bc.Xp[o], qn = bc.Xq[o];
+        const float pe0 = ldexpf(p.re.hi, E) + ldexpf(p.re.lo, E), pe1 = ldexpf(p.im.hi, E) + ldexpf(p.im.lo, E);
+        const float qe0 = ldexpf(q.re.hi, E) + ldexpf(q.re.lo, E), qe1 = ldexpf(q.im.hi, E) + ldexpf(q.im.lo, E);
+        // differences formed in float-float, so they keep their digits
+        const float dpx = ldexpf(ff_sub(p.re, ff_from(ldexpf(pn.x, -E))).hi, E);
+        const float dpy = ldexpf(ff_sub(p.im, ff_from(ldexpf(pn.y, -E))).hi, E);
+        const float dqx = ldexpf(ff_sub(q.re, ff_from(ldexpf(qn.x, -E))).hi, E);
+        const float dqy = ldexpf(ff_sub(q.im, ff_from(ldexpf(qn.y, -E))).hi, E);
+        v.x += dpx * dpx + dpy * dpy;
+        v.y += pe0 * pe0 + pe1 * pe1;
+        v.z += dqx * dqx + dqy * dqy;
+        v.w += qe0 * qe0 + qe1 * qe1;
+    };
+    // the top level as an output level (no run contains it)
+    if (lane == 31 && jm == L && bc.slot[L] >= 0) emit(L, PF, EPF, RL);
+    // pass 2: the ratio again; at output level j, Q(j) = P F / (factors of
+    // this run from j up to min(hi, jm)), kept in V
+    cff V = one;
+    int EV = 0;
+    R = Rtop;
+    for (int i = hi - 1; i >= lo; --i) {
+        cff a, b, cc;
+        coef_ff(bc.lvff + (size_t)i * BLDFM_LV32, lx, ly, lx2, ly2, a, b, cc);
+        R = cff_div(cff_sub(cff_mul(a, R), b), cff_sub(a, cff_mul(cc, R)));
+        cff f = one;
+        if (i < jm) {
+            f = cff_add(cff_mul(cc, R), a);
+            V = cff_mul(V, f);
+            cff_renorm(V, EV);
+        }
+        if (i <= jm && bc.slot[i] >= 0) {
+            cff Qj = cff_div(PF, V);
+            int E = EPF - EV;
+            cff_renorm(Qj, E);
+            emit(i, Qj, E, R);
+        }
+    }
 }
 
 // true when -k of (kx, ky) lies in the mode range, so the sweep writes the
@@ -672,9 +755,15 @@ __global__ void __launch_bounds__(128) fp32_check_kernel(const BatchCase *__rest
     int kx = 0, ky = 0;
     bool have = false;
     if (j == 0) {
-        // k = 0: the host's exact values, no error
-        const double2 p = bc.dc[2 * bc.slot[g.jmax]], q = bc.dc[2 * bc.slot[g.jmax] + 1];
-        v = make_float4(0.f, (float)(p.x * p.x + p.y * p.y), 0.f, (float)(q.x * q.x + q.y * q.y));
+        // k = 0: the host's exact values at every output level, no error
+        if (lane == 0)
+            for (int i = 0; i <= g.jmax; ++i) {
+                const int sl = bc.slot[i];
+                if (sl < 0) continue;
+                const double2 p = bc.dc[2 * sl], q = bc.dc[2 * sl + 1];
+                v.y += (float)(p.x * p.x + p.y * p.y);
+                v.w += (float)(q.x * q.x + q.y * q.y);
+            }
     } else if (j <= NBOX) {
         const int t = j - 1;
         if (t < CHECK_BOX) {
@@ -700,6 +789,13 @@ __global__ void __launch_bounds__(128) fp32_check_kernel(const BatchCase *__rest
         check_mode(bc, index_of_freq(ky, g.nly), index_of_freq(kx, g.nlx), lane, v);
         if (mirrored(g, kx, ky)) wgt *= 2.f;
         v = make_float4(wgt * v.x, wgt * v.y, wgt * v.z, wgt * v.w);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            v.x += __shfl_down_sync(0xffffffffu, v.x, off);
+            v.y += __shfl_down_sync(0xffffffffu, v.y, off);
+            v.z += __shfl_down_sync(0xffffffffu, v.z, off);
+            v.w += __shfl_down_sync(0xffffffffu, v.w, off);
+        }
     }
     if (lane == 0) {
         atomicAdd(&acc[k].x, v.x);

@@ -58,7 +58,7 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
 
 // Accuracy check of a batched FP32 solve (batch.cu: fp32_check_kernel): a
 // stratified sample of 32 modes per case evaluated in float-float arithmetic
-// and compared with the FP32 spectra at the highest output level; per case
+// and compared with the FP32 spectra at every output level; per case
 // acc[k] = weighted (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2).
 cudaError_t launch_fp32_check(const BatchCase *cases, int n, float4 *acc, cudaStream_t st);
 
@@ -66,6 +66,7 @@ cudaError_t launch_fp32_check(const BatchCase *cases, int n, float4 *acc, cudaSt
 // FP32 values of every stride-th solved mode against the served spectra,
 // per-case sums into acc[k] = (|dXp|^2, |Xp|^2, |dXq|^2, |Xq|^2); prefix:
 // n + 1 sample offsets, each case's count padded to a multiple of 32.
+#define SUR_GUARD_BOX 12  // solved modes with |kx|, |ky| <= 2, sampled by the guard
 cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefix, int64_t nsamples, int stride,
                              float4 *acc, cudaStream_t st);
 

@@ -178,16 +178,24 @@ __global__ void __launch_bounds__(256) combine64_kernel(SolveGeom g, const uint3
 // reference's trapezoid values (solver.py:237-251) into dc[2 s] (p), dc[2 s + 1]
 // (q).  The terms (q0 dz_i) w_i are independent and computed in parallel; the
 // running difference keeps the reference's order on one thread.
+// dcp (may be NULL): DC_PARTS partial FP64 sums of the source field
+// (dc_partial_kernel); the k = 0 source value is then their sum / (nxe nye)
+// in FP64 instead of the transform's k = 0 output.
 template <typename C>
 __global__ void __launch_bounds__(256) trapezoid_kernel(SolveGeom g, const double *__restrict__ lvtab,
                                                         const int *__restrict__ slot_of_step,
                                                         const C *__restrict__ q0spec, double p000,
-                                                        double2 *__restrict__ dc)
+                                                        double2 *__restrict__ dc, const double *__restrict__ dcp)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *term = (double2 *)smem_raw;
     int *sl = (int *)(term + (g.nz > 1 ? g.nz - 1 : 1));
-    const double2 q0 = make_double2((double)q0spec[0].x, (double)q0spec[0].y);
+    double2 q0 = make_double2((double)q0spec[0].x, (double)q0spec[0].y);
+    if (dcp) {
+        double sum = 0.0;
+        for (int b = 0; b < DC_PARTS; ++b) sum += dcp[b];
+        q0 = make_double2(sum * g.inv_nxe * g.inv_nye, 0.0);
+    }
     const bool single = g.precision == 0;
     const double2 qs = single ? round_c64(q0) : q0;
     for (int s = threadIdx.x; s < g.nlvls; s += blockDim.x) {
@@ -663,15 +671,36 @@ cudaError_t launch_trapezoid64(const SolveGeom &g, const double *lvtab, const in
                                double p000, double2 *dc, cudaStream_t st)
 {
     const size_t smem = (size_t)(g.nz > 1 ? g.nz - 1 : 1) * sizeof(double2) + (size_t)g.nz * sizeof(int);
-    trapezoid_kernel<double2><<<1, 256, smem, st>>>(g, lvtab, slot, q0spec, p000, dc);
+    trapezoid_kernel<double2><<<1, 256, smem, st>>>(g, lvtab, slot, q0spec, p000, dc, nullptr);
     return LAUNCH_CHECK();
 }
 
+// FP64 partial sums of the source field: CTA b of DC_PARTS sums its slice in a
+// fixed order (deterministic), thread sums then a shared-memory tree
+__global__ void __launch_bounds__(256) dc_partial_kernel(const double *__restrict__ src, int64_t n,
+                                                         double *__restrict__ dcp)
+{
+    __shared__ double red[256];
+    const int64_t chunk = (n + DC_PARTS - 1) / DC_PARTS;
+    const int64_t b0 = (int64_t)blockIdx.x * chunk, b1 = b0 + chunk < n ? b0 + chunk : n;
+    double acc = 0.0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) acc += src[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) dcp[blockIdx.x] = red[0];
+}
+
 cudaError_t launch_trapezoid32(const SolveGeom &g, const double *lvtab, const int *slot, const float2 *q0spec,
-                               double p000, double2 *dc, cudaStream_t st)
+                               double p000, double2 *dc, cudaStream_t st, const double *src, double *dcp)
 {
     const size_t smem = (size_t)(g.nz > 1 ? g.nz - 1 : 1) * sizeof(double2) + (size_t)g.nz * sizeof(int);
-    trapezoid_kernel<float2><<<1, 256, smem, st>>>(g, lvtab, slot, q0spec, p000, dc);
+    const bool exact = src && dcp;
+    if (exact) dc_partial_kernel<<<DC_PARTS, 256, 0, st>>>(src, (int64_t)g.nx * g.ny, dcp);
+    trapezoid_kernel<float2><<<1, 256, smem, st>>>(g, lvtab, slot, q0spec, p000, dc, exact ? dcp : nullptr);
     return LAUNCH_CHECK();
 }
 

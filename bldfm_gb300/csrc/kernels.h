@@ -17,8 +17,14 @@ cudaError_t launch_combine64(const SolveGeom &g, const uint32_t *modes, const do
 // k = 0 mode from a device-resident q0 (dispersion mode) into dc[2 s], dc[2 s + 1]
 cudaError_t launch_trapezoid64(const SolveGeom &g, const double *lvtab, const int *slot, const double2 *q0spec,
                                double p000, double2 *dc, cudaStream_t st);
+// FP32 spectra: with src and dcp (DC_PARTS doubles of scratch), the k = 0
+// source value is the FP64 sum of the source field (dc_partial_kernel), not
+// the FP32 transform's k = 0 output, whose rounding (~1e-6 relative) would
+// dominate the mean of the concentration field
+#define DC_PARTS 16
 cudaError_t launch_trapezoid32(const SolveGeom &g, const double *lvtab, const int *slot, const float2 *q0spec,
-                               double p000, double2 *dc, cudaStream_t st);
+                               double p000, double2 *dc, cudaStream_t st, const double *src = nullptr,
+                               double *dcp = nullptr);
 cudaError_t launch_analytic64(const SolveGeom &g, const uint32_t *modes, const double2 *eig, const double2 *q0spec,
                               double p000, double kzinv, double hlev, double2 *Xp, double2 *Xq, double2 *dc,
                               cudaStream_t st);

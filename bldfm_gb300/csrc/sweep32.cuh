@@ -478,14 +478,11 @@ __device__ __forceinline__ void ricc_mode_pair(const SolveGeom &g, const float *
 // (unit source spectrum q0dc_fp).  (r, c) receive the mode's row and column.
 // Used by the surrogate's accuracy guard on a sample of modes.
 template <bool ISO>
-__device__ __forceinline__ void ricc_mode_value(const SolveGeom &g, const float *__restrict__ lv,
-                                                const uint32_t *__restrict__ modes, float ax, float ay, int64_t m,
-                                                float2 &p, float2 &q, int &r, int &c)
+__device__ __forceinline__ void ricc_rc_value(const SolveGeom &g, const float *__restrict__ lv, float ax, float ay,
+                                              int r, int c, float2 &p, float2 &q)
 {
     const int L = g.nz - 1;
     const int jmax = g.jmax;
-    bool paired;
-    unpack_mode(modes[m], r, c, paired);
     const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
     const float lx = ax * (float)kx, ly = ay * (float)ky;
     StepCoef<ISO> sc;
@@ -526,4 +523,15 @@ __device__ __forceinline__ void ricc_mode_value(const SolveGeom &g, const float 
     q = fc_mul(q0, make_float2(ldexpf(Q.x, E), ldexpf(Q.y, E)));
     p = fc_mul(fc_mul(Rj, q), sh);
     q = fc_mul(q, sh);
+}
+
+// the same for solved mode m of the mode list; (r, c) receive its row and column
+template <bool ISO>
+__device__ __forceinline__ void ricc_mode_value(const SolveGeom &g, const float *__restrict__ lv,
+                                                const uint32_t *__restrict__ modes, float ax, float ay, int64_t m,
+                                                float2 &p, float2 &q, int &r, int &c)
+{
+    bool paired;
+    unpack_mode(modes[m], r, c, paired);
+    ricc_rc_value<ISO>(g, lv, ax, ay, r, c, p, q);
 }

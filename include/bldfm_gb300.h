@@ -217,10 +217,12 @@ int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases,
  * enqueued, so a caller may solve first and plan only on that status.
  * Error statement (no reference counterpart): from workspace byte 64, four
  * floats per case, the weighted (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2,
- * sum |Xq|^2) of the FP32 spectra at the highest output level against FP64
- * re-solves of a stratified sample of 32 modes (the k = 0 mode, every mode
- * with |kx|, |ky| <= 2, 19 equal slices of the mode list); the case's
- * estimated relative L2 error is the larger of the two square-root ratios. */
+ * sum |Xq|^2) over the output levels of the FP32 spectra against
+ * float-float (~48-bit) re-solves of a stratified sample of 32 modes (the
+ * k = 0 mode, every mode with |kx|, |ky| <= 2, 19 equal slices of the mode
+ * list); per field the estimated relative L2 error combines the square-root
+ * ratio with the output transform's rounding, 2^-24 times
+ * sqrt((sum |Xp|^2 + sum |Xq|^2) / sum |X|^2); the case's is the larger. */
 int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases,
                       const bldfm_batch_opts *opts, void *workspace,
                       size_t workspace_bytes, void *stream);

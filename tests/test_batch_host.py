@@ -80,8 +80,13 @@ def test_finish_states_each_case_error_from_the_check_sums():
     sums = [[1e-12, 1.0, 4e-12, 1.0], [9e-14, 1e-2, 0.0, 4.0], [0.0, 0.0, 0.0, 0.0]]
     res = _finish_batch(_pending(cases, shapes, host, sums))
     assert isinstance(res, BatchResults) and len(res) == 3
-    np.testing.assert_allclose(res.error_estimates, [2e-6, 3e-6, 0.0], rtol=1e-6)
-    assert error_estimate(sums[0]) == pytest.approx(2e-6)
+    u2 = 2.0**-48  # the transform's rounding term, squared, per unit of field
+    want = [((4e-12 + 2 * u2) / 1.0) ** 0.5, ((9e-14 + 4.01 * u2) / 1e-2) ** 0.5, 0.0]
+    np.testing.assert_allclose(res.error_estimates, want, rtol=1e-6)
+    assert error_estimate(sums[0]) == pytest.approx(want[0])
+    # a flux field 100 times smaller than the concentration: the transform's
+    # rounding dominates its statement
+    assert error_estimate([0.0, 1.0, 0.0, 1e-4]) == pytest.approx(2.0**-24 * (1.0001 / 1e-4) ** 0.5)
 
 
 @pytest.mark.parametrize("mixed", [False, True])
