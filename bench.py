@@ -479,7 +479,9 @@ def serving_section(args, dev, nsteps=10000):
                        "max": float(np.max(st["errors"])) if st["errors"] else None},
         "guard": {"re_solved_fp32": st["guard_fail"], "checked": len(st["guard"]),
                   "estimate_median": float(np.median(g)), "estimate_p90": float(np.quantile(g, 0.9)),
-                  "rule": "every 61st solved mode re-solved exactly on the device; estimate > 1e-3 -> FP32 solve"},
+                  "guard_tol": sur.guard_tol,
+                  "rule": "stratified sample (k = 0, |kx|,|ky| <= 2, every 61st solved mode) re-solved exactly on "
+                          "the device; estimate > guard_tol (network's guard factor x 1e-3) -> FP32 solve"},
         "served_relL2_vs_exact": {"n": len(errs), "median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)),
                                   "max": float(e.max()), "frac_le_1e-3": float((e <= 1e-3).mean())},
     }

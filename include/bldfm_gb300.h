@@ -328,8 +328,9 @@ int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls,
  * cases[k] as for bldfm_solve_batch (footprint, one level at z_m, FP32 mode),
  * mets[k] its met scalars; workspace of bldfm_surrogate_batch_plan bytes,
  * 256-byte aligned; the int32 at offset 0 holds the device status.
- * Accuracy guard: every 61st solved mode of each case is re-solved exactly
- * (FP32 sweep) and compared with the served spectra; the last
+ * Accuracy guard: a stratified sample of each case (the k = 0 mode, the 12
+ * solved modes with |kx|, |ky| <= 2, every 61st solved mode weighted 61) is
+ * re-solved exactly (FP32 sweep) and compared with the served spectra; the last
  * (16 ncases + 255) & ~255 bytes of the planned workspace receive, per case,
  * four floats (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2), an estimate
  * of the case's relative L2 error (no reference counterpart). */

@@ -232,8 +232,8 @@ def test_serve_timeseries_with_fallback():
 
 
 def test_guard_estimates_and_guarded_serving():
-    """The accuracy guard (every 61st solved mode re-solved exactly on the
-    device) estimates each served case's relative L2 error: on 20 in-box
+    """The accuracy guard (a stratified sample of modes re-solved exactly on
+    the device) estimates each served case's relative L2 error: on 20 in-box
     footprints of the benchmark's met distribution the estimate stays within
     a factor of 3 of the true error against the exact discrete solution, and
     with the guard on no served footprint exceeds the 1e-3 bar."""
@@ -263,7 +263,8 @@ def test_guard_estimates_and_guarded_serving():
     print("guard estimate / true error:", " ".join("%.1e/%.1e" % (a, e) for a, e in zip(est, errs)))
     big = errs > 2e-4
     assert np.all(est[big] >= errs[big] / 3) and np.all(est[big] <= errs[big] * 3), (est, errs)
-    # the estimate errs on the safe side (measured: 1.06 to 2.5 times the true error)
+    # the estimate errs on the safe side for this network (measured: 0.98 to
+    # 2.5 times the true error; its guard factor is 1)
     assert np.all(est >= 0.9 * errs), (est, errs)
     # guarded serving: cases above the guard's tolerance are re-solved exactly
     sur = Surrogate(net, spot_every=0, tol=1e-3)
@@ -316,3 +317,49 @@ def test_production_network_serves_the_production_footprint():
         print("step %d path %s relL2 %.2e" % (k, paths[k], err))
         assert err <= (1e-3 if k != 9 else 1e-12), (k, paths[k], err)
     print("guard estimates:", " ".join("%.1e" % e for e in sur.stats["guard"]))
+
+
+def test_production_guard_calibration():
+    """The accuracy guard on the n = 256 network's production footprints
+    (1024^2 extended, 413 levels): estimate against the true error of 20
+    in-box cases, and guarded serving at the network's guard tolerance keeps
+    every served footprint within 1e-3 of the exact discrete solution."""
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import WEIGHTS_N256, Surrogate, load
+
+    if not os.path.exists(WEIGHTS_N256):
+        pytest.skip("no n = 256 weights")
+    net, box, meta = load(WEIGHTS_N256)
+    rng = np.random.default_rng(17)
+    probe = Surrogate(net, box=box)
+    items = []
+    while len(items) < 20:
+        th = rng.uniform(0, 2 * np.pi)
+        kw = dict(n=256, zm=20.0, wind=(-4 * np.sin(th), -4 * np.cos(th)), srf_shape=(512, 512),
+                  domain=(1000.0, 1000.0), modes=(1024, 1024), meas_pt=(500.0, 500.0), halo=500.0,
+                  ustar=float(rng.uniform(0.22, 0.38)), mol=float(1.0 / rng.uniform(-0.045, 0.01)))
+        if probe.classify(kw):
+            items.append(kw)
+    sur = Surrogate(net, box=box, spot_every=0, guard_tol=1.0)  # estimates only
+    b = sur.prepare_batch(items)
+    outs = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in sur.solve_batch_prepared(b)]
+    est = sur.guard_estimates(b)
+    errs = []
+    for kw, (c, f) in zip(items, outs):
+        p = sur.prepare(**kw)
+        _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
+        errs.append(max(_rel(c, cr), _rel(f, fr)))
+    errs = np.array(errs)
+    print("n256 guard estimate / true error:", " ".join("%.1e/%.1e" % (a, e) for a, e in zip(est, errs)))
+    print("ratio min %.2f median %.2f" % ((est / errs).min(), np.median(est / errs)))
+    sur = Surrogate(net, box=box, spot_every=0, tol=1e-3)
+    out, paths = sur.serve(items, batch=10)
+    worst = 0.0
+    for kw, (c, f), path in zip(items, out, paths):
+        c = c.cpu().numpy() if hasattr(c, "cpu") else c
+        f = f.cpu().numpy() if hasattr(f, "cpu") else f
+        p = sur.prepare(**kw)
+        _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
+        worst = max(worst, max(_rel(c, cr), _rel(f, fr)))
+    print("guarded serving paths:", {q: paths.count(q) for q in set(paths)}, "worst %.2e" % worst)
+    assert worst <= 1e-3, worst
