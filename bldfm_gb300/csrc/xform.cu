@@ -140,9 +140,10 @@ __global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_cols_batch_kernel(
     }
     __syncthreads();
     const SolveGeom &g = sc.g;
-    const int64_t local = (int64_t)blockIdx.x - sc.col0;
+    // 32-bit index arithmetic: a pass launches fewer than 2^31 CTAs
+    const int local = (int)((int64_t)blockIdx.x - sc.col0);
     const int ncb = (g.nbx + G - 1) / G;
-    const int lvl = (int)(local / ncb), cb = (int)(local - (int64_t)lvl * ncb);
+    const int lvl = local / ncb, cb = local - lvl * ncb;
     const int b = cb * G + grp;
     const bool active = b < g.nbx;
     const float cj = g.out_sign > 0 ? -1.f : 1.f;  // inverse transform: conjugate in and out
@@ -244,9 +245,9 @@ __global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_rows_batch_kernel(
     load_case_rx(&sc, cases + cta_case[blockIdx.x]);
     __syncthreads();
     const SolveGeom &g = sc.g;
-    const int64_t local = (int64_t)blockIdx.x - sc.row0;
+    const int local = (int)((int64_t)blockIdx.x - sc.row0);  // fewer than 2^31 CTAs
     const int nblk = (g.out_ny + G - 1) / G;
-    const int lvl = (int)(local / nblk), yb = (int)(local - (int64_t)lvl * nblk);
+    const int lvl = local / nblk, yb = local - lvl * nblk;
     const int grp = threadIdx.x / P, t = threadIdx.x - grp * P;
     const int y = yb * G + grp;
     bool bad = false;
@@ -294,9 +295,9 @@ __global__ void __launch_bounds__(kThreads, 2) rx2_rows_batch_kernel(const Batch
     load_case_rx(&sc, cases + cta_case[blockIdx.x]);
     __syncthreads();
     const SolveGeom &g = sc.g;
-    const int64_t local = (int64_t)blockIdx.x - sc.row0;
+    const int local = (int)((int64_t)blockIdx.x - sc.row0);  // fewer than 2^31 CTAs
     const int nblk = (g.out_ny + L - 1) / L;
-    const int lvl = (int)(local / nblk), yb = (int)(local - (int64_t)lvl * nblk);
+    const int lvl = local / nblk, yb = local - lvl * nblk;
     const int grp = threadIdx.x / P, t = threadIdx.x - grp * P;
     const int yA = yb * L + 2 * grp;
     bool bad = false;
@@ -396,9 +397,10 @@ __global__ void __launch_bounds__(kThreads, 3) rz_cols_batch_kernel(const BatchC
     }
     __syncthreads();
     const SolveGeom &g = sc.g;
-    const int64_t local = (int64_t)blockIdx.x - sc.col0;
+    // 32-bit index arithmetic: a pass launches fewer than 2^31 CTAs
+    const int local = (int)((int64_t)blockIdx.x - sc.col0);
     const int ncb = (g.nbx + G - 1) / G;
-    const int lvl = (int)(local / ncb), cb = (int)(local - (int64_t)lvl * ncb);
+    const int lvl = local / ncb, cb = local - lvl * ncb;
     const int b = cb * G + grp;
     const bool active = b < g.nbx;
     const float cj = g.out_sign > 0 ? -1.f : 1.f;  // inverse transform: conjugate in and out

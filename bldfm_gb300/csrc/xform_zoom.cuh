@@ -81,13 +81,14 @@ __device__ __forceinline__ void zoom_twists(ZoomTw<S> &z, const float2 *__restri
     if (i < 3 * E) {
         const int r = i / E, mp = i - r * E;
         const int kr = k0 + r;
-        long long e = (long long)P * mp * kr - (mp >= E / 2 ? (long long)M * kr : 0);
+        // |exponent| < M (N + 2) < 2^31 for the supported lengths: 32-bit
+        int e = P * mp * kr - (mp >= E / 2 ? M * kr : 0);
         e %= N;
         if (e < 0) e += N;
         z.U[i] = __ldg(tw + e);
     } else if (i < 3 * E + 3) {
         const int r = i - 3 * E;
-        z.Up[r] = __ldg(tw + (int)(((long long)(M / 2) * (k0 + r)) % N));
+        z.Up[r] = __ldg(tw + ((M / 2) * (k0 + r)) % N);
     }
 }
 
@@ -113,7 +114,7 @@ __device__ __forceinline__ void zoom_line(V (&y)[3 * S::E], const V (&v)[S::E], 
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int b = 0; b < (E + 7) / 8; ++b)
-            wb[r][b] = __ldg(tw + (int)(((long long)t * (k0 + r) + 24LL * b * t) % N));
+            wb[r][b] = __ldg(tw + (t * (k0 + r) + 24 * b * t) % N);  // < P (N + 24 E) < 2^31
     const float2 w1 = __ldg(tw + 3 * t);
     float2 w2[R2];
 #pragma unroll
