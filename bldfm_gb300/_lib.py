@@ -126,6 +126,7 @@ class SurrogateCase(ctypes.Structure):
         ("s3", ctypes.c_double),
         ("variant", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+        ("exact_kz", ctypes.c_double),
     ]
 
 

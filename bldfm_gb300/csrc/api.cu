@@ -1,6 +1,7 @@
 // C ABI of bldfm_gb300 (include/bldfm_gb300.h): host planning, per-device
 // plan cache, workspace layout and the orchestration of one solve.
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
@@ -980,7 +981,7 @@ std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B,
 // ---------------------------------------------------------------------------
 struct SurLayout {
     Layout L;
-    size_t X, Y, steps, tcase, total;
+    size_t X, Y, steps, tcase, lbcase, total;
     int64_t npad;
 };
 
@@ -998,6 +999,8 @@ SurLayout sur_layout(const SolveGeom &g)
     o = al(o + (size_t)std::max(g.nz - 1, 1) * 16);
     S.tcase = o;  // TransferCase (exact variant) or SurCase (fused kernel)
     o = al(o + std::max(sizeof(TransferCase), sizeof(SurCase)));
+    S.lbcase = o;  // LowBandCase of the exact low band
+    o = al(o + sizeof(LowBandCase));
     S.total = o;
     return S;
 }
@@ -1014,7 +1017,7 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
                    size_t ws_bytes, cudaStream_t st)
 {
     if (!met || !z || !prof || !levels || !conc || !flx || !ws || (met->variant != 1 && !net) || met->variant < 0 ||
-        met->variant > 2)
+        met->variant > 2 || !(met->exact_kz >= 0))
         return BLDFM_ERR_ARG;
     int rc = sur_check_desc(d, nlvls);
     if (rc != BLDFM_OK) return rc;
@@ -1046,8 +1049,11 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
     const size_t dcb = 32, stb = (size_t)std::max(nz - 1, 1) * 16;
     const size_t off_dc = al(lv64b), off_st = off_dc + al(dcb), off_tc = off_st + al(stb);
     const size_t tcb = std::max(sizeof(TransferCase), sizeof(SurCase));
+    // the exact low band (network variants): FP32 level table and band record
+    const size_t lv32b = (size_t)std::max(nz - 1, 0) * BLDFM_LV32 * 4;
+    const size_t off_lv32 = off_tc + al(tcb), off_lb = off_lv32 + al(lv32b);
     StageSlot *slt = nullptr;
-    if ((rc = acquire_stage(dc, off_tc + al(tcb) + 256, &slt)) != BLDFM_OK) return rc;
+    if ((rc = acquire_stage(dc, off_lb + al(sizeof(LowBandCase)) + 256, &slt)) != BLDFM_OK) return rc;
     char *sg = (char *)slt->buf;
     hx_level_table(nz, z, prof, (double *)sg);
     hx_dc_values(nz, (const double *)sg, hp.slot.data(), g.q0dc_fp, 0.0, d->srf_bg_conc, 1, 1, 0,
@@ -1090,8 +1096,25 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
         c->utop = utop;
         c->tile0 = 0;
     }
+    int lb_total = 0;
+    if (!exact && lv32b > 0) {
+        hx_level_table32_iso(nz, z, prof, g.ex, g.ey, (float *)(sg + off_lv32), nullptr);
+        LowBandCase *lb = (LowBandCase *)(sg + off_lb);
+        memset(lb, 0, sizeof(LowBandCase));
+        lb->g = g;
+        lb->lv32 = (const float *)(w + S.L.lv32);
+        lb->Xp = Xp;
+        lb->Xq = Xq;
+        lb->ax = ax;
+        lb->ay = ay;
+        lb_total = sur_lowband_setup(*lb, met->exact_kz, met->zm);
+    }
     double2 *dcv = (double2 *)(w + S.L.dc);
     CK(cudaMemsetAsync(w + S.L.err, 0, 64, st));
+    if (lb_total > 0) {
+        CK(cudaMemcpyAsync(w + S.L.lv32, sg + off_lv32, lv32b, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(w + S.lbcase, sg + off_lb, sizeof(LowBandCase), cudaMemcpyHostToDevice, st));
+    }
     CK(cudaMemcpyAsync(dcv, sg + off_dc, dcb, cudaMemcpyHostToDevice, st));
     if (exact) {
         CK(cudaMemcpyAsync(w + S.steps, sg + off_st, stb, cudaMemcpyHostToDevice, st));
@@ -1122,6 +1145,7 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
         }
         CK(launch_sur_spectra(g, ml->dev, Y, ax, ay, zm, inv_wind, ktop, utop, Xp, Xq, st));
     }
+    CK(launch_sur_lowband((const LowBandCase *)(w + S.lbcase), 1, lb_total, st));
     CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
                                 (float2 *)(w + S.L.Cb), conc, flx, (int *)(w + S.L.err), st));
     return BLDFM_OK;
@@ -1138,7 +1162,8 @@ int sur_batch_check(const bldfm_case *cs, const bldfm_surrogate_case *mets, int 
     for (int k = 0; k < n; ++k) {
         const int rc = sur_check_desc(&cs[k].desc, cs[k].nlvls);
         if (rc != BLDFM_OK) return rc;
-        if (mets[k].variant != 0 || !(mets[k].zm > 0) || !(mets[k].wind > 0)) return BLDFM_ERR_ARG;
+        if (mets[k].variant != 0 || !(mets[k].zm > 0) || !(mets[k].wind > 0) || !(mets[k].exact_kz >= 0))
+            return BLDFM_ERR_ARG;
     }
     return BLDFM_OK;
 }
@@ -1151,7 +1176,8 @@ int sur_batch_check(const bldfm_case *cs, const bldfm_surrogate_case *mets, int 
 // sur_guard_bytes(n) bytes of the planned workspace.
 enum { SUR_GUARD_STRIDE = 61 };  // prime: no alignment with the rows of a column
 size_t sur_prefix_off(int n) { return (sizeof(SurCase) * (size_t)n + 15) & ~(size_t)15; }
-size_t sur_extra_bytes(int n) { return sur_prefix_off(n) + 8 * ((size_t)n + 1); }
+size_t sur_lowband_off(int n) { return (sur_prefix_off(n) + 8 * ((size_t)n + 1) + 15) & ~(size_t)15; }
+size_t sur_extra_bytes(int n) { return sur_lowband_off(n) + sizeof(LowBandCase) * (size_t)n; }
 size_t sur_guard_bytes(int n) { return al(16 * (size_t)n); }
 
 int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_case *mets, int n, void *ws,
@@ -1205,6 +1231,25 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
         c.tile0 = t;
         t += (g.nsolved + 127) / 128;
     }
+    // the exact low band of each case: the case's level table and spectra
+    // from its BatchCase record in the blob
+    LowBandCase *lbc = (LowBandCase *)(blob + B.extra_off + sur_lowband_off(n));
+    const BatchCase *bcs = (const BatchCase *)(blob + B.off_cases);
+    int lb_total = 0;
+    for (int k = 0; k < n; ++k) {
+        LowBandCase &c = lbc[k];
+        memset(&c, 0, sizeof(c));
+        c.g = B.hp[k].g;
+        c.lv32 = bcs[k].lv32;
+        c.Xp = sc[k].Xp;
+        c.Xq = sc[k].Xq;
+        c.ax = sc[k].ax;
+        c.ay = sc[k].ay;
+        c.first = lb_total;
+        const int cnt = sur_lowband_setup(c, mets[k].exact_kz, mets[k].zm);
+        if (cnt > INT_MAX - lb_total) return BLDFM_ERR_ARG;
+        lb_total += cnt;
+    }
     int64_t *prefix = (int64_t *)(blob + B.extra_off + sur_prefix_off(n));
     prefix[0] = 0;
     for (int k = 0; k < n; ++k) {
@@ -1222,11 +1267,13 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     char *wb = w + B.blob_at;
     tmark(dc, st);  // 1: the fused features -> MLP -> spectra kernel
     CK(launch_sur_serve((const SurCase *)(wb + B.extra_off), n, t, view, (int *)w, dc.nsm, st));
+    tmark(dc, st);  // 2: the exact low band and the accuracy guard
+    CK(launch_sur_lowband((const LowBandCase *)(wb + B.extra_off + sur_lowband_off(n)), n, lb_total, st));
     float4 *acc = (float4 *)(w + B.total);
     CK(cudaMemsetAsync(acc, 0, 16 * (size_t)n, st));
     CK(launch_sur_guard((const BatchCase *)(wb + B.off_cases), n, (const int64_t *)(wb + B.extra_off + sur_prefix_off(n)),
                         prefix[n], SUR_GUARD_STRIDE, acc, st));
-    tmark(dc, st);  // 2: the output transform
+    tmark(dc, st);  // 3: the output transform
     BatchLaunch bl;
     memset(&bl, 0, sizeof(bl));
     bl.cases = (const BatchCase *)(wb + B.off_cases);
@@ -1249,7 +1296,7 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     bl.rx_col = B.rx_col;
     bl.rx_row = B.rx_row;
     CK(launch_batch_kernels(bl, st, 1));
-    tmark(dc, st);  // 3: end
+    tmark(dc, st);  // 4: end
     return BLDFM_OK;
 }
 

@@ -70,6 +70,25 @@ cudaError_t launch_fp32_check(const BatchCase *cases, int n, float4 *acc, cudaSt
 cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefix, int64_t nsamples, int stride,
                              float4 *acc, cudaStream_t st);
 
+// Exact low band of a surrogate footprint (batch.cu: sur_lowband_kernel):
+// the solved modes with |k| < kmax are re-solved by the exact FP32 sweep and
+// written over the served spectra, mirrors included, before the output
+// transform.  One thread per mode of the half box kx in [0, bx], ky in
+// [-by, by] (kx = 0: ky in [1, by]); modes outside the disc return at once.
+struct __align__(16) LowBandCase {
+    SolveGeom g;
+    const float *lv32;  // the case's FP32 level table (layout of g.iso)
+    float2 *Xp, *Xq;    // the served spectra
+    float ax, ay;       // wavenumber scales (Lx = ax kx, Ly = ay ky)
+    float kmax2;        // squared wavenumber bound (1/m^2)
+    int bx, by;         // index half-widths of the band's box
+    int first;          // the case's first thread in the launch
+};
+// Fill the band of a case for |k| z_m < exact_kz; returns its thread count
+// (0 when exact_kz <= 0).  g, lv32, Xp, Xq, ax, ay must be set.
+int sur_lowband_setup(LowBandCase &c, double exact_kz, double zm);
+cudaError_t launch_sur_lowband(const LowBandCase *cases, int n, int total, cudaStream_t st);
+
 // register-resident transform passes (xform.cu), for line lengths 512, 768,
 // 1024, 1536, 2048, 3072: config id of a length (-1 if unsupported), lines
 // per 256-thread CTA and dynamic shared memory per CTA of the column (col)

@@ -9,7 +9,11 @@ top).  A 8 -> 4 x 256 GELU -> 4 MLP (``mlp.MLP``, tcgen05 BF16 GEMMs with FP32
 accumulation) learns that transfer from data the FP32 invariant-imbedding
 sweep generates on the device (``TransferPool``), trained with Adam
 (``train``); ``Surrogate`` serves footprints through it inside the training
-box and through the FP64 solver outside it.  Every served case of a batch is
+box and through the FP64 solver outside it.  The footprint's lowest
+wavenumbers, |k| z_m < ``exact_kz`` (default 4), where its L2 norm and almost
+all of the network's error sit, take the exact FP32 sweep instead of the
+network (about 1% of the modes of the production footprint, 11% of the
+benchmark's 512^2 one).  Every served case of a batch is
 checked by the library's accuracy guard: a stratified sample of modes (the
 k = 0 mode, the lowest wavenumbers, every 61st solved mode) is re-solved
 exactly (FP32 sweep) on the device and compared with the served spectrum,
@@ -51,6 +55,11 @@ WEIGHTS = os.path.join(WEIGHT_DIR, "surrogate_n128.npz")
 # |k| z_m up to 48 covers all modes of a 1024^2 extended grid at dx = 1.95 m
 # and z_m = 20 m)
 WEIGHTS_N256 = os.path.join(WEIGHT_DIR, "surrogate_n256.npz")
+# |k| z_m below which the served modes are solved exactly (a network's box may
+# set its own "exact_kz").  On the production footprint this band holds 1.2% of
+# the modes and 97% (flux) to 99.7% (concentration) of the network's squared
+# L2 error: the exact band divides the error by ~6 for ~1% of an FP32 solve.
+EXACT_KZ = 4.0
 
 
 def boxes(n=128, kmax=40.0):
@@ -243,7 +252,7 @@ class Surrogate:
     """
 
     def __init__(self, net=None, box=None, spot_every=64, tol=1e-3, variant=0, spot_mode="fp64r", fallback="fp64",
-                 guard_tol=None, guard_mode="fp32"):
+                 guard_tol=None, guard_mode="fp32", exact_kz=None):
         self.lib = _lib.load()
         self.net = net
         self.box = dict(BOX if box is None else box)
@@ -256,16 +265,21 @@ class Surrogate:
         # grid; its ratio to the true error of the cropped fields depends on
         # the network and the grid, so the network's box carries a safety
         # factor (guard_factor, default 1): cases whose estimate exceeds
-        # guard_tol = guard_factor * tol are re-solved.  Measured: n = 128
-        # network on 512^2 footprints 0.98 to 2.5 (factor 1); n = 256 network
-        # on the production footprint 0.77 to 2.4, one case near 0.6 (factor 0.5)
+        # guard_tol = guard_factor * tol are re-solved.  Measured with the
+        # exact low band (errors 0.8e-4 to 1.3e-4): n = 128 network on 512^2
+        # footprints 0.9 to 2.0 (factor 1); n = 256 network on the production
+        # footprint 1.05 to 2.1, median 1.3 (factor 0.5, set when the network
+        # served every mode: 0.77 to 2.4, one case near 0.6)
         factor = float(self.box.get("guard_factor", 1.0))
         self.guard_tol = self.tol * factor if guard_tol is None else float(guard_tol)
         self.guard_mode = guard_mode
+        # |k| z_m of the exact low band (0: every mode from the network)
+        self.exact_kz = float(self.box.get("exact_kz", EXACT_KZ) if exact_kz is None else exact_kz)
         self.device = torch.device("cuda", torch.cuda.current_device())
         self._ws = None
         self._out = None
         self.count = 0
+        self.served = 0
         self.stats = {"surrogate": 0, "out_of_box": 0, "spot": 0, "spot_fail": 0, "errors": [], "guard": [],
                       "guard_fail": 0, "spot_guard": []}
 
@@ -288,7 +302,8 @@ class Surrogate:
         d = make_desc(srf_shape, z.size, domain, modes, meas_pt, 0.0, True, False, halo, "single", "fp32")
         info = _lib.PlanInfo()
         _lib.check(self.lib.bldfm_plan(d, 1, info), "surrogate")
-        met = _lib.SurrogateCase(zm=float(z[n]), wind=U, s1=s1, s2=s2, s3=s3, variant=self.variant)
+        met = _lib.SurrogateCase(zm=float(z[n]), wind=U, s1=s1, s2=s2, s3=s3, variant=self.variant,
+                                 exact_kz=self.exact_kz)
         lv = np.array([n], dtype=np.int64)
         need = ctypes.c_int64(0)
         _lib.check(self.lib.bldfm_surrogate_plan(d, 1, ctypes.byref(need)), "surrogate")
@@ -397,8 +412,9 @@ class Surrogate:
     def serve(self, items, batch=16, keep=None):
         """Footprints of a met timeseries (keyword dicts of ``prepare``):
         in-box cases through the network in batched fused launches, every
-        ``spot_every``-th of them also through the ``spot_mode`` solve (the
-        FP64 result is kept when the surrogate misses ``tol``), out-of-box
+        ``spot_every``-th footprint the network serves (the guard passed it)
+        also through the ``spot_mode`` solve (the FP64 result is kept when
+        the surrogate misses ``tol``), out-of-box
         cases through the fallback solver; a served case whose guard estimate
         exceeds ``guard_tol`` is re-solved by ``guard_mode``.  Returns
         (outputs, paths): outputs[k] = (conc, flx) (device tensors for served
@@ -433,7 +449,10 @@ class Surrogate:
                     _, gc, gf = steady_state_transport_solver(**pr["kw"], mode=self.guard_mode)
                     out[k], paths[k] = (gc, gf), "fp32-guard"
                     continue
-                if self.spot_every > 0 and self.count % self.spot_every == 0:
+                # spot checks count the footprints the network serves (those
+                # the guard passed): the re-solved ones are exact already
+                self.served += 1
+                if self.spot_every > 0 and self.served % self.spot_every == 0:
                     ref = steady_state_transport_solver(**pr["kw"], mode=self.spot_mode)
                     ca, fa = c.cpu().numpy(), f.cpu().numpy()
                     err = max(_rell2(ca, ref[1]), _rell2(fa, ref[2]))

@@ -320,6 +320,11 @@ typedef struct bldfm_surrogate_case {
                        *    path; net may be NULL);
                        * 2: the MLP layer by layer (bldfm_surrogate_forward) */
     int32_t reserved;
+    double exact_kz;  /* variants 0 and 2: the solved modes with |k| z_m <
+                       * exact_kz (the footprint's low band, where its L2
+                       * norm sits) take the exact FP32 sweep instead of the
+                       * network, written over the served spectra before the
+                       * output transform; 0: every mode from the network */
 } bldfm_surrogate_case;
 int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls,
                          int64_t *workspace_bytes);
