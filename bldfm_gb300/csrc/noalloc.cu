@@ -12,8 +12,10 @@
 //
 // Rules of use:
 //  - The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    (cudaGetSymbolAddress) with that device current.
+//  - Calls are not for stream capture: the small host tables are copied from
+//    the static pageable buffer na_host, which every call rewrites (a graph
+//    would replay the buffer's contents at replay time).
 //  - All calls share the one array and it keeps the previous call's contents;
 //    this file clears what must start at zero.  Calls whose GPU work overlaps
 //    (different streams, or different host threads without ordering) race on

@@ -366,7 +366,11 @@ int bldfm_surrogate_solve(void *net, const bldfm_desc *d,
  *    status once the stream reaches the end of the call: 0, BLDFM_ERR_TIMEOUT
  *    (a bounded device wait ran out) or BLDFM_ERR_NONFINITE.
  *  - The first call on a device looks up the array's address with that
- *    device current; make it before any stream capture.
+ *    device current.
+ *  - Not for CUDA stream capture: each call copies its small host tables
+ *    (level tables, slot map, band map) from one static pageable host buffer,
+ *    which the next call rewrites; a captured graph would replay whatever
+ *    that buffer holds then.  Use bldfm_solve_batch (use_graph) for graphs.
  *  - All calls share the array: calls whose GPU work overlaps race; order
  *    them on one stream.
  *  - Calls no cudaMalloc/cudaFree/cudaHostAlloc; host staging is static. */
