@@ -565,7 +565,8 @@ def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
     lib.bldfm_set_stage_timing(0)
     stages = [float(arr[i]) for i in range(max(nst, 0))]
     serve_ms = stages[1] / B if len(stages) > 1 else None  # per footprint
-    band_ms = stages[2] / B if len(stages) > 2 else None  # exact low band + guard, per footprint
+    band_ms = stages[2] / B if len(stages) > 2 else None  # exact low band, per footprint
+    guard_ms = stages[3] / B if len(stages) > 3 else None  # accuracy guard, per footprint
     nsolved = 131583
     npad = (nsolved + 127) // 128 * 128
     tflop = npad * (2 * 32 * 256 + 3 * 2 * 256 * 256) / 1e12  # tensor-core work per footprint
@@ -610,8 +611,9 @@ def surrogate_section(kwb, inputs, s64, B, args, dev, dist, world, sr):
                   "sur_lowband_kernel) and the accuracy guard, then the batched output FFT; two workspaces on two "
                   "streams take the steps in turn" % sur.exact_kz,
         "stage_ms_per_step": stages,
-        "stages": ["upload", "serve kernel", "exact low band + guard", "output transform"],
-        "low_band_and_guard_ms_per_footprint": band_ms,
+        "stages": ["upload", "serve kernel", "exact low band", "accuracy guard", "output transform"],
+        "low_band_ms_per_footprint": band_ms,
+        "guard_ms_per_footprint": guard_ms,
         "serve_kernel": {
             "ms_per_footprint": serve_ms,
             "bound": "tensor",

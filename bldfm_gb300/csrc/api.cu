@@ -1145,7 +1145,7 @@ int sur_solve_impl(void *net, const bldfm_desc *d, const bldfm_surrogate_case *m
         }
         CK(launch_sur_spectra(g, ml->dev, Y, ax, ay, zm, inv_wind, ktop, utop, Xp, Xq, st));
     }
-    CK(launch_sur_lowband((const LowBandCase *)(w + S.lbcase), 1, lb_total, st));
+    CK(launch_sur_lowband((const LowBandCase *)(w + S.lbcase), 1, lb_total, nz, st));
     CK(launch_output_fft<float>(g, hp.plx_out, hp.ply_out, twxo->d32, twyo->d32, xband, Xp, Xq, dcv,
                                 (float2 *)(w + S.L.Cb), conc, flx, (int *)(w + S.L.err), st));
     return BLDFM_OK;
@@ -1235,7 +1235,7 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     // from its BatchCase record in the blob
     LowBandCase *lbc = (LowBandCase *)(blob + B.extra_off + sur_lowband_off(n));
     const BatchCase *bcs = (const BatchCase *)(blob + B.off_cases);
-    int lb_total = 0;
+    int lb_total = 0, lb_maxnz = 2;
     for (int k = 0; k < n; ++k) {
         LowBandCase &c = lbc[k];
         memset(&c, 0, sizeof(c));
@@ -1245,17 +1245,18 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
         c.Xq = sc[k].Xq;
         c.ax = sc[k].ax;
         c.ay = sc[k].ay;
-        c.first = lb_total;
-        const int cnt = sur_lowband_setup(c, mets[k].exact_kz, mets[k].zm);
-        if (cnt > INT_MAX - lb_total) return BLDFM_ERR_ARG;
-        lb_total += cnt;
+        c.block0 = lb_total;
+        const int nb = sur_lowband_setup(c, mets[k].exact_kz, mets[k].zm);
+        if (nb > INT_MAX - lb_total) return BLDFM_ERR_ARG;
+        lb_total += nb;
+        lb_maxnz = std::max(lb_maxnz, c.g.nz);
     }
     int64_t *prefix = (int64_t *)(blob + B.extra_off + sur_prefix_off(n));
     prefix[0] = 0;
     for (int k = 0; k < n; ++k) {
         // the k = 0 mode, the low-wavenumber box, every stride-th solved mode
         const int64_t s = 1 + SUR_GUARD_BOX + (B.hp[k].g.nsolved + SUR_GUARD_STRIDE - 1) / SUR_GUARD_STRIDE;
-        prefix[k + 1] = prefix[k] + ((s + 31) & ~(int64_t)31);
+        prefix[k + 1] = prefix[k] + (s + SUR_GUARD_CTA - 1) / SUR_GUARD_CTA * SUR_GUARD_CTA;
     }
     timers_begin(dc);
     tmark(dc, st);  // 0: upload
@@ -1267,13 +1268,14 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     char *wb = w + B.blob_at;
     tmark(dc, st);  // 1: the fused features -> MLP -> spectra kernel
     CK(launch_sur_serve((const SurCase *)(wb + B.extra_off), n, t, view, (int *)w, dc.nsm, st));
-    tmark(dc, st);  // 2: the exact low band and the accuracy guard
-    CK(launch_sur_lowband((const LowBandCase *)(wb + B.extra_off + sur_lowband_off(n)), n, lb_total, st));
+    tmark(dc, st);  // 2: the exact low band
+    CK(launch_sur_lowband((const LowBandCase *)(wb + B.extra_off + sur_lowband_off(n)), n, lb_total, lb_maxnz, st));
+    tmark(dc, st);  // 3: the accuracy guard
     float4 *acc = (float4 *)(w + B.total);
     CK(cudaMemsetAsync(acc, 0, 16 * (size_t)n, st));
     CK(launch_sur_guard((const BatchCase *)(wb + B.off_cases), n, (const int64_t *)(wb + B.extra_off + sur_prefix_off(n)),
-                        prefix[n], SUR_GUARD_STRIDE, acc, st));
-    tmark(dc, st);  // 3: the output transform
+                        prefix[n], SUR_GUARD_STRIDE, lb_maxnz, acc, st));
+    tmark(dc, st);  // 4: the output transform
     BatchLaunch bl;
     memset(&bl, 0, sizeof(bl));
     bl.cases = (const BatchCase *)(wb + B.off_cases);
@@ -1296,7 +1298,7 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     bl.rx_col = B.rx_col;
     bl.rx_row = B.rx_row;
     CK(launch_batch_kernels(bl, st, 1));
-    tmark(dc, st);  // 4: end
+    tmark(dc, st);  // 5: end
     return BLDFM_OK;
 }
 

@@ -397,33 +397,24 @@ __global__ void __launch_bounds__(256) out_rows_persist_kernel(const BatchCase *
 // Accuracy guard of the surrogate's batched footprints, a stratified sample
 // per case (the footprint's L2 norm sits in the low wavenumbers): local
 // sample j = i - prefix[k] of case k (prefix[k] <= i < prefix[k + 1], every
-// case's count padded to a multiple of 32, the padding contributing nothing)
-// is
+// case's count padded to a multiple of SUR_GUARD_CTA, so that a CTA's samples
+// belong to one case; the padding contributes nothing) is
 //   j = 0              the k = 0 mode (exact from the host, error 0),
 //   j = 1 .. GBOX      every solved mode with |kx|, |ky| <= 2 (weight 1),
 //   j > GBOX           solved mode (j - 1 - GBOX) * stride (weight stride),
-// each solved mode counted twice when its mirror is written from it.  The
-// exact FP32 values (ricc_rc_value) are compared with the spectra the serving
-// kernel wrote; acc[k] accumulates the weighted (sum |dXp|^2, sum |Xp|^2,
-// sum |dXq|^2, sum |Xq|^2) of case k (one atomic per warp and quantity).
-__global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restrict__ cases, int n,
-                                                        const int64_t *__restrict__ prefix, int stride,
-                                                        float4 *__restrict__ acc)
+// each solved mode counted twice when its mirror is written from it.  A CTA
+// stages the case's level table in shared memory and each thread takes
+// samples j and j + 256 in the two lanes of packed f32x2 operations
+// (ricc_rc_pair, the exact FP32 values as ricc_rc_value computes them),
+// compares them with the spectra the serving kernel (and the exact low band)
+// wrote and accumulates into acc[k] the weighted (sum |dXp|^2, sum |Xp|^2,
+// sum |dXq|^2, sum |Xq|^2) (one atomic per warp and quantity).
+__device__ __forceinline__ bool guard_sample(const BatchCase &bc, int64_t j, int stride, int &r, int &c, float &wgt)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= prefix[n]) return;  // whole warps: prefix[n] is a multiple of 32
-    int k = 0;
-    while (k + 1 < n && prefix[k + 1] <= i) ++k;
-    const BatchCase &bc = cases[k];
     const SolveGeom &g = bc.g;
-    const int64_t j = i - prefix[k];
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    int r = -1, c = -1;
-    float wgt = 1.f;
-    if (j == 0) {
-        const double2 p = bc.dc[0], q = bc.dc[1];
-        v = make_float4(0.f, (float)(p.x * p.x + p.y * p.y), 0.f, (float)(q.x * q.x + q.y * q.y));
-    } else if (j <= SUR_GUARD_BOX) {
+    r = c = -1;
+    wgt = 1.f;
+    if (j >= 1 && j <= SUR_GUARD_BOX) {
         const int t = (int)j - 1;
         int kx, ky;
         if (t < 2) {
@@ -437,7 +428,7 @@ __global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restr
             r = index_of_freq(ky, g.nly);
             c = index_of_freq(kx, g.nlx);
         }
-    } else {
+    } else if (j > SUR_GUARD_BOX) {
         const int64_t m = (j - 1 - SUR_GUARD_BOX) * (int64_t)stride;
         if (m < g.nsolved) {
             bool paired;
@@ -445,20 +436,69 @@ __global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restr
             wgt = (float)stride;
         }
     }
-    if (r >= 0) {
-        float2 pe, qe;
+    return r >= 0;
+}
+
+__device__ __forceinline__ float4 guard_terms(const BatchCase &bc, int r, int c, float wgt, float2 pe, float2 qe)
+{
+    const SolveGeom &g = bc.g;
+    const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
+    if (-kx >= freq_min(g.nlx) && -kx <= freq_max(g.nlx) && -ky >= freq_min(g.nly) && -ky <= freq_max(g.nly))
+        wgt *= 2.f;
+    const size_t o = spec_idx(g, 0, r, c);
+    const float2 pn = bc.Xp[o], qn = bc.Xq[o];
+    const float dpx = pn.x - pe.x, dpy = pn.y - pe.y, dqx = qn.x - qe.x, dqy = qn.y - qe.y;
+    return make_float4(wgt * (dpx * dpx + dpy * dpy), wgt * (pe.x * pe.x + pe.y * pe.y),
+                       wgt * (dqx * dqx + dqy * dqy), wgt * (qe.x * qe.x + qe.y * qe.y));
+}
+
+__global__ void __launch_bounds__(SUR_GUARD_THREADS) sur_guard_kernel(const BatchCase *__restrict__ cases, int n,
+                                                                      const int64_t *__restrict__ prefix, int stride,
+                                                                      float4 *__restrict__ acc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *s_lv = (float4 *)smem_raw;
+    const int64_t i0 = (int64_t)blockIdx.x * SUR_GUARD_CTA;
+    int k = 0;
+    while (k + 1 < n && prefix[k + 1] <= i0) ++k;
+    const BatchCase &bc = cases[k];
+    const SolveGeom &g = bc.g;
+    const int nrow4 = (g.nz - 1) * (BLDFM_LV32 / 4);
+    const float4 *src = (const float4 *)bc.lv32;
+    for (int i = threadIdx.x; i < nrow4; i += blockDim.x) s_lv[i] = src[i];
+    __syncthreads();
+    const int64_t j = i0 - prefix[k] + threadIdx.x;
+    int r[2], c[2];
+    float w[2];
+    const bool v0 = guard_sample(bc, j, stride, r[0], c[0], w[0]);
+    const bool v1 = guard_sample(bc, j + SUR_GUARD_THREADS, stride, r[1], c[1], w[1]);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j == 0) {
+        const double2 p = bc.dc[0], q = bc.dc[1];
+        v = make_float4(0.f, (float)(p.x * p.x + p.y * p.y), 0.f, (float)(q.x * q.x + q.y * q.y));
+    }
+    if (v0 || v1) {
+        if (!v0) {
+            r[0] = r[1];
+            c[0] = c[1];
+        } else if (!v1) {
+            r[1] = r[0];
+            c[1] = c[0];
+        }
+        float2 pe[2], qe[2];
         if (g.iso)
-            ricc_rc_value<true>(g, bc.lv32, bc.ax, bc.ay, r, c, pe, qe);
+            ricc_rc_pair<true>(g, (const float *)s_lv, bc.ax, bc.ay, r, c, pe, qe);
         else
-            ricc_rc_value<false>(g, bc.lv32, bc.ax, bc.ay, r, c, pe, qe);
-        const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
-        if (-kx >= freq_min(g.nlx) && -kx <= freq_max(g.nlx) && -ky >= freq_min(g.nly) && -ky <= freq_max(g.nly))
-            wgt *= 2.f;
-        const size_t o = spec_idx(g, 0, r, c);
-        const float2 pn = bc.Xp[o], qn = bc.Xq[o];
-        const float dpx = pn.x - pe.x, dpy = pn.y - pe.y, dqx = qn.x - qe.x, dqy = qn.y - qe.y;
-        v = make_float4(wgt * (dpx * dpx + dpy * dpy), wgt * (pe.x * pe.x + pe.y * pe.y),
-                        wgt * (dqx * dqx + dqy * dqy), wgt * (qe.x * qe.x + qe.y * qe.y));
+            ricc_rc_pair<false>(g, (const float *)s_lv, bc.ax, bc.ay, r, c, pe, qe);
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            if (!(l ? v1 : v0)) continue;
+            const float4 t = guard_terms(bc, r[l], c[l], w[l], pe[l], qe[l]);
+            v.x += t.x;
+            v.y += t.y;
+            v.z += t.z;
+            v.w += t.w;
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -476,10 +516,17 @@ __global__ void __launch_bounds__(256) sur_guard_kernel(const BatchCase *__restr
 }
 
 cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefix, int64_t nsamples, int stride,
-                             float4 *acc, cudaStream_t st)
+                             int max_nz, float4 *acc, cudaStream_t st)
 {
     if (nsamples <= 0) return cudaSuccess;
-    sur_guard_kernel<<<(unsigned)((nsamples + 255) / 256), 256, 0, st>>>(cases, n, prefix, stride, acc);
+    const size_t smem = (size_t)std::max(max_nz - 1, 1) * BLDFM_LV32 * sizeof(float);
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(sur_guard_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    sur_guard_kernel<<<(unsigned)((nsamples + SUR_GUARD_CTA - 1) / SUR_GUARD_CTA), SUR_GUARD_THREADS, smem, st>>>(
+        cases, n, prefix, stride, acc);
     return cudaGetLastError();
 }
 
@@ -487,20 +534,18 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 // in its lowest wavenumbers (with the network's errors: on the production
 // footprint 97% of the flux error and 99.7% of the concentration error come
 // from |k| z_m < 4, 1.2% of the modes), so those modes take the exact FP32
-// sweep (ricc_rc_value, the level table read from global memory) and the
-// network serves the rest.  Thread j of a case maps to the half box:
+// sweep and the network serves the rest.  CTA b of case k (block0 <= b <
+// block0 + its CTAs) stages the level table in shared memory and sweeps box
+// positions j = 512 (b - block0) + t and j + 256 of the half box, two modes
+// in the lanes of packed f32x2 operations (ricc_rc_pair, which rounds as the
+// guard's ricc_rc_value does):
 //   j < by            kx = 0, ky = j + 1,
 //   otherwise         kx = 1 + (j - by) / (2 by + 1), ky = (j - by) % (2 by + 1) - by,
 // the solved representative of each mirror pair (kx > 0, or kx = 0 and
 // ky > 0; the band stays inside the mode range, so every mirror exists).
-__global__ void __launch_bounds__(256) sur_lowband_kernel(const LowBandCase *__restrict__ cases, int n, int total)
+__device__ __forceinline__ bool lowband_mode(const LowBandCase &lb, int j, int &r, int &c)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
-    int k = 0;
-    while (k + 1 < n && cases[k + 1].first <= i) ++k;
-    const LowBandCase &lb = cases[k];
-    const int j = i - lb.first;
+    if (j >= lb.count) return false;
     int kx, ky;
     if (j < lb.by) {
         kx = 0;
@@ -511,39 +556,81 @@ __global__ void __launch_bounds__(256) sur_lowband_kernel(const LowBandCase *__r
         ky = t - (kx - 1) * w - lb.by;
     }
     const float lx = lb.ax * (float)kx, ly = lb.ay * (float)ky;
-    if (!(fmaf(lx, lx, ly * ly) < lb.kmax2)) return;
+    if (!(fmaf(lx, lx, ly * ly) < lb.kmax2)) return false;
+    r = index_of_freq(ky, lb.g.nly);
+    c = index_of_freq(kx, lb.g.nlx);
+    return true;
+}
+
+__global__ void __launch_bounds__(SUR_LOWBAND_THREADS) sur_lowband_kernel(const LowBandCase *__restrict__ cases,
+                                                                         int n)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *s_lv = (float4 *)smem_raw;
+    const int b = blockIdx.x;
+    int k = 0;
+    while (k + 1 < n && cases[k + 1].block0 <= b) ++k;
+    const LowBandCase &lb = cases[k];
     const SolveGeom &g = lb.g;
-    const int r = index_of_freq(ky, g.nly), c = index_of_freq(kx, g.nlx);
-    float2 p, q;
+    const int nrow4 = (g.nz - 1) * (BLDFM_LV32 / 4);
+    const float4 *src = (const float4 *)lb.lv32;
+    for (int i = threadIdx.x; i < nrow4; i += blockDim.x) s_lv[i] = src[i];
+    __syncthreads();
+    const int j = (b - lb.block0) * SUR_LOWBAND_MODES + threadIdx.x;
+    int r[2] = {0, 0}, c[2] = {0, 0};
+    const bool v0 = lowband_mode(lb, j, r[0], c[0]);
+    const bool v1 = lowband_mode(lb, j + SUR_LOWBAND_THREADS, r[1], c[1]);
+    if (!v0 && !v1) return;
+    if (!v0) {
+        r[0] = r[1];
+        c[0] = c[1];
+    } else if (!v1) {
+        r[1] = r[0];
+        c[1] = c[0];
+    }
+    float2 p[2], q[2];
     if (g.iso)
-        ricc_rc_value<true>(g, lb.lv32, lb.ax, lb.ay, r, c, p, q);
+        ricc_rc_pair<true>(g, (const float *)s_lv, lb.ax, lb.ay, r, c, p, q);
     else
-        ricc_rc_value<false>(g, lb.lv32, lb.ax, lb.ay, r, c, p, q);
-    const size_t o = spec_idx(g, 0, r, c), om = spec_idx(g, 0, index_of_freq(-ky, g.nly), index_of_freq(-kx, g.nlx));
-    lb.Xp[o] = p;
-    lb.Xq[o] = q;
-    lb.Xp[om] = make_float2(p.x, -p.y);
-    lb.Xq[om] = make_float2(q.x, -q.y);
+        ricc_rc_pair<false>(g, (const float *)s_lv, lb.ax, lb.ay, r, c, p, q);
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        if (!(l ? v1 : v0)) continue;
+        const int kx = freq_of_index(c[l], g.nlx), ky = freq_of_index(r[l], g.nly);
+        const size_t o = spec_idx(g, 0, r[l], c[l]);
+        const size_t om = spec_idx(g, 0, index_of_freq(-ky, g.nly), index_of_freq(-kx, g.nlx));
+        lb.Xp[o] = p[l];
+        lb.Xq[o] = q[l];
+        lb.Xp[om] = make_float2(p[l].x, -p[l].y);
+        lb.Xq[om] = make_float2(q[l].x, -q[l].y);
+    }
 }
 
 int sur_lowband_setup(LowBandCase &c, double exact_kz, double zm)
 {
-    c.bx = c.by = 0;
+    c.bx = c.by = c.count = 0;
     c.kmax2 = 0.f;
-    if (!(exact_kz > 0) || !(zm > 0) || !(c.ax > 0) || !(c.ay > 0)) return 0;
+    if (!(exact_kz > 0) || !(zm > 0) || !(c.ax > 0) || !(c.ay > 0) || c.g.nz < 2) return 0;
     const double km = exact_kz / zm;
     // the box stays inside the mode range (freq_max), so that every solved
     // mode of the band is a mirror pair's representative
     c.bx = (int)std::min<double>(floor(km / c.ax), (double)freq_max(c.g.nlx));
     c.by = (int)std::min<double>(floor(km / c.ay), (double)freq_max(c.g.nly));
     c.kmax2 = (float)std::min(km * km, 1e30);
-    return c.by + c.bx * (2 * c.by + 1);
+    c.count = c.by + c.bx * (2 * c.by + 1);
+    return (c.count + SUR_LOWBAND_MODES - 1) / SUR_LOWBAND_MODES;
 }
 
-cudaError_t launch_sur_lowband(const LowBandCase *cases, int n, int total, cudaStream_t st)
+cudaError_t launch_sur_lowband(const LowBandCase *cases, int n, int nblocks, int max_nz, cudaStream_t st)
 {
-    if (total <= 0) return cudaSuccess;
-    sur_lowband_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(cases, n, total);
+    if (nblocks <= 0) return cudaSuccess;
+    const size_t smem = (size_t)std::max(max_nz - 1, 1) * BLDFM_LV32 * sizeof(float);
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(sur_lowband_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    sur_lowband_kernel<<<(unsigned)nblocks, SUR_LOWBAND_THREADS, smem, st>>>(cases, n);
     return cudaGetLastError();
 }
 

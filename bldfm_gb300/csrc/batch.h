@@ -65,16 +65,23 @@ cudaError_t launch_fp32_check(const BatchCase *cases, int n, float4 *acc, cudaSt
 // Accuracy guard of a surrogate batch (batch.cu: sur_guard_kernel): exact
 // FP32 values of every stride-th solved mode against the served spectra,
 // per-case sums into acc[k] = (|dXp|^2, |Xp|^2, |dXq|^2, |Xq|^2); prefix:
-// n + 1 sample offsets, each case's count padded to a multiple of 32.
+// n + 1 sample offsets, each case's count padded to a multiple of
+// SUR_GUARD_CTA (a CTA's samples belong to one case); max_nz: the largest
+// level count (the level table is staged in shared memory).
 #define SUR_GUARD_BOX 12  // solved modes with |kx|, |ky| <= 2, sampled by the guard
+#define SUR_GUARD_THREADS 256
+#define SUR_GUARD_CTA (2 * SUR_GUARD_THREADS)  // samples per CTA, two per thread
 cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefix, int64_t nsamples, int stride,
-                             float4 *acc, cudaStream_t st);
+                             int max_nz, float4 *acc, cudaStream_t st);
 
 // Exact low band of a surrogate footprint (batch.cu: sur_lowband_kernel):
 // the solved modes with |k| < kmax are re-solved by the exact FP32 sweep and
 // written over the served spectra, mirrors included, before the output
-// transform.  One thread per mode of the half box kx in [0, bx], ky in
-// [-by, by] (kx = 0: ky in [1, by]); modes outside the disc return at once.
+// transform.  The band's modes are enumerated over the half box kx in
+// [0, bx], ky in [-by, by] (kx = 0: ky in [1, by]), two per thread, 512 per
+// CTA; modes outside the disc are skipped.
+#define SUR_LOWBAND_THREADS 256
+#define SUR_LOWBAND_MODES (2 * SUR_LOWBAND_THREADS)  // box positions per CTA
 struct __align__(16) LowBandCase {
     SolveGeom g;
     const float *lv32;  // the case's FP32 level table (layout of g.iso)
@@ -82,12 +89,15 @@ struct __align__(16) LowBandCase {
     float ax, ay;       // wavenumber scales (Lx = ax kx, Ly = ay ky)
     float kmax2;        // squared wavenumber bound (1/m^2)
     int bx, by;         // index half-widths of the band's box
-    int first;          // the case's first thread in the launch
+    int count;          // box positions by + bx (2 by + 1)
+    int block0;         // the case's first CTA in the launch
 };
-// Fill the band of a case for |k| z_m < exact_kz; returns its thread count
-// (0 when exact_kz <= 0).  g, lv32, Xp, Xq, ax, ay must be set.
+// Fill the band of a case for |k| z_m < exact_kz (count = 0 when exact_kz
+// <= 0) and return its CTA count; g, lv32, Xp, Xq, ax, ay must be set.
 int sur_lowband_setup(LowBandCase &c, double exact_kz, double zm);
-cudaError_t launch_sur_lowband(const LowBandCase *cases, int n, int total, cudaStream_t st);
+// nblocks: the CTAs of all cases; max_nz: the largest level count (the
+// level table is staged in shared memory)
+cudaError_t launch_sur_lowband(const LowBandCase *cases, int n, int nblocks, int max_nz, cudaStream_t st);
 
 // register-resident transform passes (xform.cu), for line lengths 512, 768,
 // 1024, 1536, 2048, 3072: config id of a length (-1 if unsupported), lines

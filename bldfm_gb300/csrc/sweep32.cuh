@@ -525,6 +525,78 @@ __device__ __forceinline__ void ricc_rc_value(const SolveGeom &g, const float *_
     q = fc_mul(q, sh);
 }
 
+// ricc_rc_value for two modes (r[l], c[l]), l = 0, 1, in the two lanes of
+// packed f32x2 operations (each lane rounds exactly as ricc_rc_value does),
+// the level table in shared or global memory.
+template <bool ISO>
+__device__ __forceinline__ void ricc_rc_pair(const SolveGeom &g, const float *__restrict__ lv, float ax, float ay,
+                                             const int (&r)[2], const int (&c)[2], float2 (&p)[2], float2 (&q)[2])
+{
+    const int L = g.nz - 1;
+    const int jmax = g.jmax;
+    StepCoef<ISO> sc[2];
+    float2 R0[2];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const float lx = ax * (float)freq_of_index(c[l], g.nlx), ly = ay * (float)freq_of_index(r[l], g.nly);
+        sc[l].init(lx, ly, g.ex, g.ey);
+        const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
+                                     fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+        const float2 eg = csqrt_f(w);
+        const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+        const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
+        R0[l] = make_float2(ke.x * inv, -ke.y * inv);
+    }
+    PStep<ISO> ps;
+    ps.init(sc[0], sc[1]);
+    PCplx R = {make_float2(R0[0].x, R0[1].x), make_float2(R0[0].y, R0[1].y)};
+    int i = L - 1;
+    for (; i >= jmax; --i) {
+        const float *row = lv + (size_t)i * BLDFM_LV32;
+        const float4 r0 = *(const float4 *)row, r1 = *(const float4 *)(row + 4), r2 = *(const float4 *)(row + 8);
+        PCplx a, b, cc;
+        ps.eval_row(r0, r1, r2, a, b, cc);
+        pricc_step(R, a, b, cc);
+    }
+    const PCplx Rj = R;
+    PCplx Q = {make_float2(1.f, 1.f), make_float2(0.f, 0.f)};
+    int E[2] = {0, 0};
+    int cnt = 0;
+    for (; i >= 0; --i) {
+        const float *row = lv + (size_t)i * BLDFM_LV32;
+        const float4 r0 = *(const float4 *)row, r1 = *(const float4 *)(row + 4), r2 = *(const float4 *)(row + 8);
+        PCplx a, b, cc;
+        ps.eval_row(r0, r1, r2, a, b, cc);
+        pricc_step(R, a, b, cc);
+        pflux_step(Q, R, a, cc);
+        if (++cnt == 8) {
+            cnt = 0;
+            float2 q0 = make_float2(Q.re.x, Q.im.x), q1 = make_float2(Q.re.y, Q.im.y);
+            renorm(q0, E[0]);
+            renorm(q1, E[1]);
+            Q.re = make_float2(q0.x, q1.x);
+            Q.im = make_float2(q0.y, q1.y);
+        }
+    }
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const float2 Ql = l ? make_float2(Q.re.y, Q.im.y) : make_float2(Q.re.x, Q.im.x);
+        const float2 Rjl = l ? make_float2(Rj.re.y, Rj.im.y) : make_float2(Rj.re.x, Rj.im.x);
+        const int kx = freq_of_index(c[l], g.nlx), ky = freq_of_index(r[l], g.nly);
+        float2 sh = make_float2(1.f, 0.f);
+        if (g.do_shift) {
+            const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
+            float sn, cs;
+            sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
+            sh = make_float2(cs, sn);
+        }
+        const float2 q0 = make_float2((float)g.q0dc_fp, 0.f);
+        q[l] = fc_mul(q0, make_float2(ldexpf(Ql.x, E[l]), ldexpf(Ql.y, E[l])));
+        p[l] = fc_mul(fc_mul(Rjl, q[l]), sh);
+        q[l] = fc_mul(q[l], sh);
+    }
+}
+
 // the same for solved mode m of the mode list; (r, c) receive its row and column
 template <bool ISO>
 __device__ __forceinline__ void ricc_mode_value(const SolveGeom &g, const float *__restrict__ lv,
