@@ -542,18 +542,38 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 //   j < by            kx = 0, ky = j + 1,
 //   otherwise         kx = 1 + (j - by) / (2 by + 1), ky = (j - by) % (2 by + 1) - by,
 // the solved representative of each mirror pair (kx > 0, or kx = 0 and
-// ky > 0; the band stays inside the mode range, so every mirror exists).
-__device__ __forceinline__ bool lowband_mode(const LowBandCase &lb, int j, int &r, int &c)
+// ky > 0; inside the mode range, so every mirror exists); then the unpaired
+// Nyquist modes (no mirror in the grid) the box reaches:
+//   column  kx = -nlx/2, ky in [-by, by]   (ncol = 2 by + 1 or 0),
+//   row     ky = -nly/2, kx in [-bx, bx]   (nrow = 2 bx + 1 or 0),
+//   corner  (-nlx/2, -nly/2)               (ncorner = 1 or 0).
+__device__ __forceinline__ bool lowband_mode(const LowBandCase &lb, int j, int &r, int &c, bool &mirror)
 {
     if (j >= lb.count) return false;
     int kx, ky;
-    if (j < lb.by) {
-        kx = 0;
-        ky = j + 1;
+    mirror = true;
+    if (j < lb.nbox) {
+        if (j < lb.by) {
+            kx = 0;
+            ky = j + 1;
+        } else {
+            const int t = j - lb.by, w = 2 * lb.by + 1;
+            kx = 1 + t / w;
+            ky = t - (kx - 1) * w - lb.by;
+        }
     } else {
-        const int t = j - lb.by, w = 2 * lb.by + 1;
-        kx = 1 + t / w;
-        ky = t - (kx - 1) * w - lb.by;
+        mirror = false;
+        j -= lb.nbox;
+        if (j < lb.ncol) {
+            kx = -(lb.g.nlx / 2);
+            ky = j - lb.by;
+        } else if ((j -= lb.ncol) < lb.nrow) {
+            ky = -(lb.g.nly / 2);
+            kx = j - lb.bx;
+        } else {
+            kx = -(lb.g.nlx / 2);
+            ky = -(lb.g.nly / 2);
+        }
     }
     const float lx = lb.ax * (float)kx, ly = lb.ay * (float)ky;
     if (!(fmaf(lx, lx, ly * ly) < lb.kmax2)) return false;
@@ -578,8 +598,9 @@ __global__ void __launch_bounds__(SUR_LOWBAND_THREADS) sur_lowband_kernel(const 
     __syncthreads();
     const int j = (b - lb.block0) * SUR_LOWBAND_MODES + threadIdx.x;
     int r[2] = {0, 0}, c[2] = {0, 0};
-    const bool v0 = lowband_mode(lb, j, r[0], c[0]);
-    const bool v1 = lowband_mode(lb, j + SUR_LOWBAND_THREADS, r[1], c[1]);
+    bool mir[2] = {true, true};
+    const bool v0 = lowband_mode(lb, j, r[0], c[0], mir[0]);
+    const bool v1 = lowband_mode(lb, j + SUR_LOWBAND_THREADS, r[1], c[1], mir[1]);
     if (!v0 && !v1) return;
     if (!v0) {
         r[0] = r[1];
@@ -596,28 +617,37 @@ __global__ void __launch_bounds__(SUR_LOWBAND_THREADS) sur_lowband_kernel(const 
 #pragma unroll
     for (int l = 0; l < 2; ++l) {
         if (!(l ? v1 : v0)) continue;
-        const int kx = freq_of_index(c[l], g.nlx), ky = freq_of_index(r[l], g.nly);
         const size_t o = spec_idx(g, 0, r[l], c[l]);
-        const size_t om = spec_idx(g, 0, index_of_freq(-ky, g.nly), index_of_freq(-kx, g.nlx));
         lb.Xp[o] = p[l];
         lb.Xq[o] = q[l];
-        lb.Xp[om] = make_float2(p[l].x, -p[l].y);
-        lb.Xq[om] = make_float2(q[l].x, -q[l].y);
+        if (mir[l]) {
+            const int kx = freq_of_index(c[l], g.nlx), ky = freq_of_index(r[l], g.nly);
+            const size_t om = spec_idx(g, 0, index_of_freq(-ky, g.nly), index_of_freq(-kx, g.nlx));
+            lb.Xp[om] = make_float2(p[l].x, -p[l].y);
+            lb.Xq[om] = make_float2(q[l].x, -q[l].y);
+        }
     }
 }
 
 int sur_lowband_setup(LowBandCase &c, double exact_kz, double zm)
 {
-    c.bx = c.by = c.count = 0;
+    c.bx = c.by = c.nbox = c.ncol = c.nrow = c.ncorner = c.count = 0;
     c.kmax2 = 0.f;
     if (!(exact_kz > 0) || !(zm > 0) || !(c.ax > 0) || !(c.ay > 0) || c.g.nz < 2) return 0;
     const double km = exact_kz / zm;
-    // the box stays inside the mode range (freq_max), so that every solved
-    // mode of the band is a mirror pair's representative
-    c.bx = (int)std::min<double>(floor(km / c.ax), (double)freq_max(c.g.nlx));
-    c.by = (int)std::min<double>(floor(km / c.ay), (double)freq_max(c.g.nly));
+    // the half box stays inside the mode range (freq_max), where every solved
+    // mode is a mirror pair's representative; the Nyquist frequency of an
+    // even mode count (-n/2, no mirror) is enumerated apart
+    const double fx = floor(km / c.ax), fy = floor(km / c.ay);
+    c.bx = (int)std::min<double>(fx, (double)freq_max(c.g.nlx));
+    c.by = (int)std::min<double>(fy, (double)freq_max(c.g.nly));
+    const bool nx = c.g.nlx % 2 == 0 && fx >= c.g.nlx / 2, ny = c.g.nly % 2 == 0 && fy >= c.g.nly / 2;
+    c.nbox = c.by + c.bx * (2 * c.by + 1);
+    c.ncol = nx ? 2 * c.by + 1 : 0;
+    c.nrow = ny ? 2 * c.bx + 1 : 0;
+    c.ncorner = nx && ny ? 1 : 0;
     c.kmax2 = (float)std::min(km * km, 1e30);
-    c.count = c.by + c.bx * (2 * c.by + 1);
+    c.count = c.nbox + c.ncol + c.nrow + c.ncorner;
     return (c.count + SUR_LOWBAND_MODES - 1) / SUR_LOWBAND_MODES;
 }
 

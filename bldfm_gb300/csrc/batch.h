@@ -78,7 +78,9 @@ cudaError_t launch_sur_guard(const BatchCase *cases, int n, const int64_t *prefi
 // the solved modes with |k| < kmax are re-solved by the exact FP32 sweep and
 // written over the served spectra, mirrors included, before the output
 // transform.  The band's modes are enumerated over the half box kx in
-// [0, bx], ky in [-by, by] (kx = 0: ky in [1, by]), two per thread, 512 per
+// [0, bx], ky in [-by, by] (kx = 0: ky in [1, by]), then, when the box
+// reaches an even mode count's Nyquist frequency, the unpaired modes of the
+// Nyquist column kx = -nlx/2 and row ky = -nly/2; two per thread, 512 per
 // CTA; modes outside the disc are skipped.
 #define SUR_LOWBAND_THREADS 256
 #define SUR_LOWBAND_MODES (2 * SUR_LOWBAND_THREADS)  // box positions per CTA
@@ -89,7 +91,8 @@ struct __align__(16) LowBandCase {
     float ax, ay;       // wavenumber scales (Lx = ax kx, Ly = ay ky)
     float kmax2;        // squared wavenumber bound (1/m^2)
     int bx, by;         // index half-widths of the band's box
-    int count;          // box positions by + bx (2 by + 1)
+    int nbox, ncol, nrow, ncorner;  // positions: half box, Nyquist column, row, corner
+    int count;          // nbox + ncol + nrow + ncorner
     int block0;         // the case's first CTA in the launch
 };
 // Fill the band of a case for |k| z_m < exact_kz (count = 0 when exact_kz

@@ -409,7 +409,7 @@ class Surrogate:
         km = mode_kmax(kw["srf_shape"], kw["domain"], kw.get("modes", (512, 512)), kw.get("halo"))
         return self.in_box(kw["n"], kw["zm"], s1, s2, km)
 
-    def serve(self, items, batch=16, keep=None):
+    def serve(self, items, batch=16, keep=None, return_errors=False):
         """Footprints of a met timeseries (keyword dicts of ``prepare``):
         in-box cases through the network in batched fused launches, every
         ``spot_every``-th footprint the network serves (the guard passed it)
@@ -422,8 +422,14 @@ class Surrogate:
         "fp32-guard", "fp64-spot", "fp64-box".  ``keep``: indices whose
         outputs are returned (default all); the others are computed, checked
         and dropped (outputs[k] = None), so a long timeseries does not hold
-        every footprint in memory."""
+        every footprint in memory.  ``return_errors``: also return each
+        step's error statement, the estimated relative L2 error against the
+        exact solution: the guard's estimate for a served footprint, the FP32
+        path's own statement for a guard re-solve, None for an FP64 result
+        (the FP64 solution itself, as the drop-in states it), and the measured
+        error for a served footprint that a spot check compared."""
         out, paths = [None] * len(items), [None] * len(items)
+        errs = [None] * len(items)
         kept = None if keep is None else set(keep)
         inbox = []
         for k, kw in enumerate(items):
@@ -444,10 +450,11 @@ class Surrogate:
                 self.stats["surrogate"] += 1
                 self.stats["guard"].append(float(e))
                 out[k], paths[k] = (c, f), "surrogate"
+                errs[k] = float(e)
                 if not e <= self.guard_tol:
                     self.stats["guard_fail"] += 1
-                    _, gc, gf = steady_state_transport_solver(**pr["kw"], mode=self.guard_mode)
-                    out[k], paths[k] = (gc, gf), "fp32-guard"
+                    res = steady_state_transport_solver(**pr["kw"], mode=self.guard_mode, return_error=True)
+                    out[k], paths[k], errs[k] = (res[1], res[2]), "fp32-guard", res[3]
                     continue
                 # spot checks count the footprints the network serves (those
                 # the guard passed): the re-solved ones are exact already
@@ -463,12 +470,14 @@ class Surrogate:
                         self.stats["spot_fail"] += 1
                         if self.fallback != self.spot_mode:
                             ref = steady_state_transport_solver(**pr["kw"], mode=self.fallback)
-                        out[k], paths[k] = (ref[1], ref[2]), "fp64-spot"
+                        out[k], paths[k], errs[k] = (ref[1], ref[2]), "fp64-spot", None
+                    else:
+                        errs[k] = err  # measured: the spot check's exact solve
             if kept is not None:
                 for k in ks:
                     if k not in kept:
                         out[k] = None
-        return out, paths
+        return (out, paths, errs) if return_errors else (out, paths)
 
     def footprint(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
                   ustar=None, z0=None, mol=1e9):

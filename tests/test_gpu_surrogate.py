@@ -128,9 +128,10 @@ def test_batched_serving_matches_single():
 
 def test_exact_low_band():
     """The footprint's lowest wavenumbers through the exact FP32 sweep in
-    place of the network: with the band over every mode (exact_kz huge; the
-    unpaired Nyquist modes stay with the network) the served footprint is the
-    FP32 solver's, in the single and the batched path; with the default band
+    place of the network: with the band over every mode (exact_kz huge,
+    mirror pairs and the unpaired Nyquist modes) the served footprint is the
+    FP32 solver's, in the single and the batched path, on square and
+    non-square grids; with the default band
     (|k| z_m < 4) the trained network's error against the exact solution drops
     at least threefold against the network alone."""
     from bldfm_gb300.solver import steady_state_transport_solver
@@ -140,7 +141,9 @@ def test_exact_low_band():
     items = [dict(n=128, zm=20.0, wind=(2.83, 2.83), srf_shape=(256, 256), domain=(500.0, 500.0), modes=(256, 256),
                   meas_pt=(250.0, 250.0), ustar=0.3, mol=-50.0),
              dict(n=128, zm=15.0, wind=(-3.0, 2.0), srf_shape=(256, 256), domain=(500.0, 500.0), modes=(256, 256),
-                  meas_pt=(200.0, 300.0), ustar=0.33, mol=-80.0)]
+                  meas_pt=(200.0, 300.0), ustar=0.33, mol=-80.0),
+             dict(n=128, zm=12.0, wind=(-3.0, 1.0), srf_shape=(128, 192), domain=(600.0, 900.0), modes=(128, 192),
+                  meas_pt=(300.0, 200.0), ustar=0.35, mol=-40.0)]
     full = Surrogate(net, spot_every=0, exact_kz=1e9)
     bouts = [(c.cpu().numpy(), f.cpu().numpy()) for c, f in full.solve_batch_prepared(full.prepare_batch(items))]
     assert full.status() == 0
@@ -343,7 +346,11 @@ def test_production_network_serves_the_production_footprint():
         if sur.classify(kw) != outside:
             items.append(kw)
     keep = [0, 3, 7, 9]
-    out, paths = sur.serve(items, batch=8, keep=keep)
+    out, paths, errs = sur.serve(items, batch=8, keep=keep, return_errors=True)
+    # every step states its error: the guard's estimate (served), the FP32
+    # path's statement (guard re-solve), None for the FP64 fallback
+    assert errs[9] is None
+    assert all(e is not None and 0 < e < 1e-3 for e in errs[:9]), errs
     assert paths[9] == "fp64-box" and all(p in ("surrogate", "fp32-guard") for p in paths[:9]), paths
     assert all((out[k] is None) == (k not in keep) for k in range(10))
     for k in keep:
