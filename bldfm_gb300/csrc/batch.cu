@@ -688,12 +688,13 @@ cudaError_t launch_sur_lowband(const LowBandCase *cases, int n, int nblocks, int
 // A_i = [[a, -b], [-c, a]], so lane l composes its run of levels
 // [lo_l, hi_l) into M_l = A_lo ... A_{hi-1}; a suffix scan over the lanes
 // gives S_l = M_l ... M_31, from which lane l takes the ratio at the top of
-// its run, R_{hi_l} = S_{l+1}(R_L); each lane then runs its own levels (ratio
-// and flux factors c_i R_i + a_i below the highest output level), and the
-// flux product at an output level is the product of the lower lanes' factors
-// and this lane's below it.  A serial float-float sweep took 0.32 ms per
-// 16-footprint batch (206 dependent steps per sample); the split one runs
-// about 7 levels per lane plus 5 scan steps.
+// its run, R_{hi_l} = S_{l+1}(R_L); the lane's flux factors below the
+// highest output level follow from the halves of its map without a division
+// per level (check_mode), and the flux product at an output level is the
+// product of the lower lanes' factors and this lane's below it.  A serial
+// float-float sweep took 0.32 ms per 16-footprint batch (206 dependent steps
+// per sample); the split one with a ratio-and-flux pass per lane (a complex
+// float-float division per level) 0.08 ms.
 #define CHECK_NS 32
 #define CHECK_BOX 2
 __device__ __forceinline__ ff ffrow(const float2 *row, int j) { return {row[j].x, row[j].y}; }
@@ -701,8 +702,8 @@ __device__ __forceinline__ ff ffrow(const float2 *row, int j) { return {row[j].x
 // a, b, c of level row i (generic layout {-Kx, -Ky, -u, -v, A, B0, B1, H, C1,
 // -2 C1}) for wavenumbers (lx, ly), lx2 = lx^2, ly2 = ly^2: T = Tr + i Ti,
 // a = 1 - A T, b = B0 - B1 T, c = H T - C1 T^2
-__device__ __forceinline__ void coef_ff(const float2 *row, const ff lx, const ff ly, const ff lx2, const ff ly2,
-                                        cff &a, cff &b, cff &c)
+__device__ __noinline__ void coef_ff(const float2 *row, const ff lx, const ff ly, const ff lx2, const ff ly2, cff &a,
+                                     cff &b, cff &c)
 {
     const ff one = ff_from(1.f);
     const ff Tr = ff_add(ff_mul(ffrow(row, 0), lx2), ff_mul(ffrow(row, 1), ly2));
@@ -719,7 +720,7 @@ __device__ __forceinline__ void coef_ff(const float2 *row, const ff lx, const ff
 struct mff {
     cff m11, m12, m21, m22;
 };
-__device__ __forceinline__ mff mff_mul(const mff &x, const mff &y)
+__device__ __noinline__ mff mff_mul(const mff &x, const mff &y)
 {
     return {cff_add(cff_mul(x.m11, y.m11), cff_mul(x.m12, y.m21)), cff_add(cff_mul(x.m11, y.m12), cff_mul(x.m12, y.m22)),
             cff_add(cff_mul(x.m21, y.m11), cff_mul(x.m22, y.m21)), cff_add(cff_mul(x.m21, y.m12), cff_mul(x.m22, y.m22))};
@@ -729,14 +730,22 @@ __device__ __forceinline__ cff cff_scale(cff a, float s)
     return {{a.re.hi * s, a.re.lo * s}, {a.im.hi * s, a.im.lo * s}};
 }
 __device__ __forceinline__ float cff_maxabs(cff a) { return fmaxf(fabsf(a.re.hi), fabsf(a.im.hi)); }
-// exact power-of-two rescaling (the map is unchanged)
-__device__ __forceinline__ void mff_norm(mff &x)
+// exact power-of-two rescaling (the map is unchanged); E receives the
+// exponent taken out (the matrix equals x * 2^E)
+__device__ __forceinline__ void mff_norm(mff &x, int &E)
 {
     const float m = fmaxf(fmaxf(cff_maxabs(x.m11), cff_maxabs(x.m12)), fmaxf(cff_maxabs(x.m21), cff_maxabs(x.m22)));
     if (m > 0.f && isfinite(m)) {
-        const float s = ldexpf(1.f, -ilogbf(m));
+        const int e = ilogbf(m);
+        const float s = ldexpf(1.f, -e);
         x = {cff_scale(x.m11, s), cff_scale(x.m12, s), cff_scale(x.m21, s), cff_scale(x.m22, s)};
+        E += e;
     }
+}
+__device__ __forceinline__ void mff_norm(mff &x)
+{
+    int e = 0;
+    mff_norm(x, e);
 }
 __device__ __forceinline__ cff cff_shfl_down(cff a, int d)
 {
@@ -768,6 +777,19 @@ __device__ __forceinline__ void cff_renorm(cff &Q, int &E)
     }
 }
 
+// the same for a homogeneous pair (N, D) with one exponent
+__device__ __forceinline__ void cff_renorm2(cff &N, cff &D, int &E)
+{
+    const float m = fmaxf(cff_maxabs(N), cff_maxabs(D));
+    if (m > 0.f && isfinite(m)) {
+        const int e = ilogbf(m);
+        const float s = ldexpf(1.f, -e);
+        N = cff_scale(N, s);
+        D = cff_scale(D, s);
+        E += e;
+    }
+}
+
 __device__ __forceinline__ cff cff_shfl_up(cff a, int d)
 {
     return {{__shfl_up_sync(0xffffffffu, a.re.hi, d), __shfl_up_sync(0xffffffffu, a.re.lo, d)},
@@ -777,10 +799,20 @@ __device__ __forceinline__ cff cff_shfl_up(cff a, int d)
 // exact (p, q) of mode (r, c) at every output level vs the FP32 spectra, the
 // whole warp together; every lane returns its part of
 // v = (sum |dXp|^2, sum |Xp|^2, sum |dXq|^2, sum |Xq|^2) over the output levels
-// in its run of levels.  The flux product at output level j is
-// Q(j) = prod_{i < j} f_i, f_i = c_i R_i + a_i: the product of the lower
-// lanes' factors (an exclusive prefix product over the lanes) times this
-// lane's factors below j.
+// in its run of levels.
+//
+// Homogeneous form: with v_i = A_i v_{i+1}, v = (N, D), the ratio is
+// R_i = N_i / D_i and the flux factor telescopes,
+//   f_i = c_i R_i + a_i = (c_i N_i + a_i D_i) / D_i = det A_i D_{i+1} / D_i,
+// det A_i = a_i^2 - b_i c_i, so a lane's factors below the highest output
+// level jm, over [lo, s) with s = clamp(jm, lo, hi), multiply to
+//   F = (prod det A_i) D_s / D_lo,  v_s = M_high (R_top, 1), v_lo = M_low v_s,
+// from the two halves M_low = A_lo ... A_{s-1}, M_high = A_s ... A_{hi-1} of
+// the lane's map: no division per level.  The flux product at an output
+// level j of the lane is Q(j) = P F_j, P the lower lanes' product (an
+// exclusive prefix product over the lanes) and F_j the factors of [lo, j):
+// F for j = s, else (det product over [lo, j)) D_j / D_lo from a second
+// pass down from s to the lane's lowest output level.
 __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, int lane, float4 &v)
 {
     const SolveGeom &g = bc.g;
@@ -797,17 +829,31 @@ __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, in
     const cff RL = cff_div(one, cff{ff_mul(kz, lam.re), ff_mul(kz, lam.im)});
     const int L = g.nz - 1, jm = g.jmax;
     const int lo = (int)(((int64_t)lane * L) / 32), hi = (int)(((int64_t)(lane + 1) * L) / 32);
-    // this lane's run of levels as one map
-    mff M = {one, zero, zero, one};
+    const int sp = jm < lo ? lo : (jm > hi ? hi : jm);  // split level s
+    // the lane's map in two halves (each times 2^E) and the det product of
+    // the lower half
+    mff Ml = {one, zero, zero, one}, Mh = {one, zero, zero, one};
+    int EMl = 0, EMh = 0, EDet = 0;
+    cff Det = one;
     for (int i = lo; i < hi; ++i) {
         cff a, b, cc;
         coef_ff(bc.lvff + (size_t)i * BLDFM_LV32, lx, ly, lx2, ly2, a, b, cc);
-        M = mff_mul(M, mff{a, cff{ff_neg(b.re), ff_neg(b.im)}, cff{ff_neg(cc.re), ff_neg(cc.im)}, a});
-        mff_norm(M);
+        const mff Ai = {a, cff{ff_neg(b.re), ff_neg(b.im)}, cff{ff_neg(cc.re), ff_neg(cc.im)}, a};
+        if (i < sp) {
+            Ml = mff_mul(Ml, Ai);
+            mff_norm(Ml, EMl);
+            Det = cff_mul(Det, cff_sub(cff_mul(a, a), cff_mul(b, cc)));
+            cff_renorm(Det, EDet);
+        } else {
+            Mh = mff_mul(Mh, Ai);
+            mff_norm(Mh, EMh);
+        }
     }
+    mff M = mff_mul(Ml, Mh);
+    mff_norm(M);
     // suffix scan: S = M_lane ... M_31
     mff S = M;
-#pragma unroll
+#pragma unroll 1
     for (int d = 1; d < 32; d <<= 1) {
         const mff T = mff_shfl_down(S, d);
         if (lane + d < 32) {
@@ -820,22 +866,21 @@ __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, in
     cff Rtop = RL;
     if (lane < 31)
         Rtop = cff_div(cff_add(cff_mul(Sn.m11, RL), Sn.m12), cff_add(cff_mul(Sn.m21, RL), Sn.m22));
-    // pass 1: this lane's flux factors below the highest output level
-    cff F = one, R = Rtop;
+    // v_s = M_high (R_top, 1) (times 2^EMh), v_lo = M_low v_s (times 2^(EMl + EMh))
+    const cff Ns = cff_add(cff_mul(Mh.m11, Rtop), Mh.m12), Ds = cff_add(cff_mul(Mh.m21, Rtop), Mh.m22);
+    const cff Dlo = cff_add(cff_mul(Ml.m21, Ns), cff_mul(Ml.m22, Ds));
+    // the lane's flux factors: F = Det Ds / Dlo (times 2^(EDet - EMl))
+    cff F = one;
     int EF = 0;
-    for (int i = hi - 1; i >= lo; --i) {
-        cff a, b, cc;
-        coef_ff(bc.lvff + (size_t)i * BLDFM_LV32, lx, ly, lx2, ly2, a, b, cc);
-        R = cff_div(cff_sub(cff_mul(a, R), b), cff_sub(a, cff_mul(cc, R)));
-        if (i < jm) {
-            F = cff_mul(F, cff_add(cff_mul(cc, R), a));
-            cff_renorm(F, EF);
-        }
+    if (sp > lo) {
+        F = cff_div(cff_mul(Det, Ds), Dlo);
+        EF = EDet - EMl;
+        cff_renorm(F, EF);
     }
     // exclusive prefix product over the lanes: P = F_0 ... F_{lane-1}
     cff P = F;
     int EP = EF;
-#pragma unroll
+#pragma unroll 1
     for (int d = 1; d < 32; d <<= 1) {
         const cff Po = cff_shfl_up(P, d);
         const int Eo = __shfl_up_sync(0xffffffffu, EP, d);
@@ -851,7 +896,7 @@ __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, in
         P = one;
         EP = 0;
     }
-    const cff PF = cff_mul(P, F);  // the flux product up to the top of this lane's run
+    const cff PF = cff_mul(P, F);  // the flux product up to level s of this lane
     const int EPF = EP + EF;
     // source spectrum and the FP32 sweep's phase factor (taken as exact)
     cff q0 = {ff_from_double(g.q0dc_fp), ff_from(0.f)};
@@ -889,26 +934,34 @@ __device__ __forceinline__ void check_mode(const BatchCase &bc, int r, int c, in
     };
     // the top level as an output level (no run contains it)
     if (lane == 31 && jm == L && bc.slot[L] >= 0) emit(L, PF, EPF, RL);
-    // pass 2: the ratio again; at output level j, Q(j) = P F / (factors of
-    // this run from j up to min(hi, jm)), kept in V
-    cff V = one;
-    int EV = 0;
-    R = Rtop;
-    for (int i = hi - 1; i >= lo; --i) {
+    // the highest output level in this lane's run (s = jm)
+    if (jm >= lo && jm < hi && bc.slot[jm] >= 0) emit(jm, PF, EPF, cff_div(Ns, Ds));
+    // output levels below s in this lane's run: down from s, v_i and the det
+    // product G over [i, s) (a footprint has none: its only level is jm)
+    int jlo = sp;
+    for (int i = lo; i < sp; ++i)
+        if (bc.slot[i] >= 0) {
+            jlo = i;
+            break;
+        }
+    cff N = Ns, D = Ds, G = one;
+    int ED = EMh, EG = 0;
+    for (int i = sp - 1; i >= jlo; --i) {
         cff a, b, cc;
         coef_ff(bc.lvff + (size_t)i * BLDFM_LV32, lx, ly, lx2, ly2, a, b, cc);
-        R = cff_div(cff_sub(cff_mul(a, R), b), cff_sub(a, cff_mul(cc, R)));
-        cff f = one;
-        if (i < jm) {
-            f = cff_add(cff_mul(cc, R), a);
-            V = cff_mul(V, f);
-            cff_renorm(V, EV);
-        }
-        if (i <= jm && bc.slot[i] >= 0) {
-            cff Qj = cff_div(PF, V);
-            int E = EPF - EV;
+        const cff Nn = cff_sub(cff_mul(a, N), cff_mul(b, D));
+        const cff Dn = cff_sub(cff_mul(a, D), cff_mul(cc, N));
+        N = Nn;
+        D = Dn;
+        cff_renorm2(N, D, ED);
+        G = cff_mul(G, cff_sub(cff_mul(a, a), cff_mul(b, cc)));
+        cff_renorm(G, EG);
+        if (bc.slot[i] >= 0) {
+            // Q(i) = P (Det / G) (D_i / D_lo)
+            cff Qj = cff_mul(P, cff_div(cff_mul(Det, D), cff_mul(G, Dlo)));
+            int E = EP + EDet - EG + ED - EMl - EMh;
             cff_renorm(Qj, E);
-            emit(i, Qj, E, R);
+            emit(i, Qj, E, cff_div(N, D));
         }
     }
 }

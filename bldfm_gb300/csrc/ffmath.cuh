@@ -84,8 +84,10 @@ __device__ __forceinline__ cff cff_mul(cff a, cff b)
     return {ff_sub(ff_mul(a.re, b.re), ff_mul(a.im, b.im)), ff_add(ff_mul(a.re, b.im), ff_mul(a.im, b.re))};
 }
 __device__ __forceinline__ ff cff_norm2(cff a) { return ff_add(ff_mul(a.re, a.re), ff_mul(a.im, a.im)); }
-// a / b as a conj(b) / |b|^2
-__device__ __forceinline__ cff cff_div(cff a, cff b)
+// a / b as a conj(b) / |b|^2 (out of line: the accuracy check calls it in
+// several places, and its code inlined at each pushed the check kernel out
+// of the instruction cache)
+__device__ __noinline__ cff cff_div(cff a, cff b)
 {
     const ff n = cff_norm2(b);
     const cff t = cff_mul(a, cff{b.re, ff_neg(b.im)});
