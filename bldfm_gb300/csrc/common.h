@@ -122,6 +122,11 @@ struct SolveGeom {
     int32_t iso;                // Kx == Ky and (u, v) along one direction at every level
     int32_t jmax;               // highest output level (slot level), -1 if none
     float ex, ey;               // wind direction unit vector (iso tables)
+    // the FP32 path's copies of kxk_top, kyk_top, uk_top, vk_top, kz_top and
+    // q0dc_fp, rounded once on the host: the per-mode setup of the FP32
+    // sweeps then needs no FP64 conversion (FP64 runs at 1/64 of the FP32
+    // rate on GB300)
+    float kxk_top_f, kyk_top_f, uk_top_f, vk_top_f, kz_top_f, q0dc_f;
 };
 
 // fftfreq ordering helpers: index <-> signed frequency.

@@ -101,6 +101,7 @@ int solve_geometry(const bldfm_desc *d, const double *z, const double *prof, con
     // numpy evaluates ones(complex128) / nxe / nye with Smith's reciprocal-scale
     // division, i.e. (1/nxe) * (1/nye) (solver.py:134)
     g.q0dc_fp = (1.0 / g.nxe) * (1.0 / g.nye);
+    g.q0dc_f = (float)g.q0dc_fp;
     if (d->footprint) {
         g.do_shift = 1;
         g.sx = d->meas_x + halo;
@@ -130,6 +131,11 @@ int solve_geometry(const bldfm_desc *d, const double *z, const double *prof, con
         g.kyk_top = Ky[nz - 1] * kzinv;
         g.uk_top = u[nz - 1] * kzinv;
         g.vk_top = v[nz - 1] * kzinv;
+        g.kz_top_f = (float)g.kz_top;
+        g.kxk_top_f = (float)g.kxk_top;
+        g.kyk_top_f = (float)g.kyk_top;
+        g.uk_top_f = (float)g.uk_top;
+        g.vk_top_f = (float)g.vk_top;
         double ex = 1.0, ey = 0.0;
         g.iso = hx_profiles_iso(nz, prof, &ex, &ey);
         g.ex = (float)ex;

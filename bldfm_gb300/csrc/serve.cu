@@ -71,7 +71,7 @@ __device__ __forceinline__ void emit_spectrum(const SolveGeom &g, uint32_t e, co
         Tq.y = -Tq.y;
         Rt.y = -Rt.y;
     }
-    const float q0 = (float)g.q0dc_fp;
+    const float q0 = g.q0dc_f;
     float2 q = make_float2(q0 * Tq.x, q0 * Tq.y);
     float2 p = sp_cmul(make_float2(Rt.x * inv_wind, Rt.y * inv_wind), q);
     if (g.do_shift) {

@@ -152,10 +152,10 @@ __device__ __forceinline__ void ricc_mode(const SolveGeom &g, const float *__res
     StepCoef<ISO> sc;
     sc.init(lx, ly, g.ex, g.ey);
     // top eigenvalue and radiation ratio R_L = 1 / (Kz_top eig)
-    const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
-                                 fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+    const float2 w = make_float2(fmaf(g.kxk_top_f, lx * lx, g.kyk_top_f * ly * ly),
+                                 fmaf(g.uk_top_f, lx, g.vk_top_f * ly));
     const float2 eg = csqrt_f(w);
-    const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+    const float2 ke = make_float2(g.kz_top_f * eg.x, g.kz_top_f * eg.y);
     const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
     float2 R = make_float2(ke.x * inv, -ke.y * inv);
     // above the highest output level: only the ratio
@@ -200,7 +200,7 @@ __device__ __forceinline__ void ricc_mode(const SolveGeom &g, const float *__res
             }
         }
     }
-    const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2((float)g.q0dc_fp, 0.f);
+    const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2(g.q0dc_f, 0.f);
     float2 sh = make_float2(1.f, 0.f);
     if (g.do_shift) {
         const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
@@ -363,10 +363,10 @@ __device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const floa
             unpack_mode(modes[u < nvalid ? m[u] : m[0]], r, c, paired);
             const float lx = ax * (float)freq_of_index(c, g.nlx), ly = ay * (float)freq_of_index(r, g.nly);
             sc[l].init(lx, ly, g.ex, g.ey);
-            const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
-                                         fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+            const float2 w = make_float2(fmaf(g.kxk_top_f, lx * lx, g.kyk_top_f * ly * ly),
+                                         fmaf(g.uk_top_f, lx, g.vk_top_f * ly));
             const float2 eg = csqrt_f(w);
-            const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+            const float2 ke = make_float2(g.kz_top_f * eg.x, g.kz_top_f * eg.y);
             const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
             R[l] = make_float2(ke.x * inv, -ke.y * inv);
         }
@@ -436,7 +436,7 @@ __device__ __forceinline__ void ricc_modes_packed(const SolveGeom &g, const floa
         bool paired;
         unpack_mode(modes[m[u]], r, c, paired);
         const int kx = freq_of_index(c, g.nlx), ky = freq_of_index(r, g.nly);
-        const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2((float)g.q0dc_fp, 0.f);
+        const float2 q0 = q0spec ? q0spec[(size_t)c * g.nly + r] : make_float2(g.q0dc_f, 0.f);
         float2 sh = make_float2(1.f, 0.f);
         if (g.do_shift) {
             const uint32_t turns = (uint32_t)kx * g.turn_x + (uint32_t)ky * g.turn_y;
@@ -487,10 +487,10 @@ __device__ __forceinline__ void ricc_rc_value(const SolveGeom &g, const float *_
     const float lx = ax * (float)kx, ly = ay * (float)ky;
     StepCoef<ISO> sc;
     sc.init(lx, ly, g.ex, g.ey);
-    const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
-                                 fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+    const float2 w = make_float2(fmaf(g.kxk_top_f, lx * lx, g.kyk_top_f * ly * ly),
+                                 fmaf(g.uk_top_f, lx, g.vk_top_f * ly));
     const float2 eg = csqrt_f(w);
-    const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+    const float2 ke = make_float2(g.kz_top_f * eg.x, g.kz_top_f * eg.y);
     const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
     float2 R = make_float2(ke.x * inv, -ke.y * inv);
     int i = L - 1;
@@ -519,7 +519,7 @@ __device__ __forceinline__ void ricc_rc_value(const SolveGeom &g, const float *_
         sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
         sh = make_float2(cs, sn);
     }
-    const float2 q0 = make_float2((float)g.q0dc_fp, 0.f);
+    const float2 q0 = make_float2(g.q0dc_f, 0.f);
     q = fc_mul(q0, make_float2(ldexpf(Q.x, E), ldexpf(Q.y, E)));
     p = fc_mul(fc_mul(Rj, q), sh);
     q = fc_mul(q, sh);
@@ -540,10 +540,10 @@ __device__ __forceinline__ void ricc_rc_pair(const SolveGeom &g, const float *__
     for (int l = 0; l < 2; ++l) {
         const float lx = ax * (float)freq_of_index(c[l], g.nlx), ly = ay * (float)freq_of_index(r[l], g.nly);
         sc[l].init(lx, ly, g.ex, g.ey);
-        const float2 w = make_float2(fmaf((float)g.kxk_top, lx * lx, (float)g.kyk_top * ly * ly),
-                                     fmaf((float)g.uk_top, lx, (float)g.vk_top * ly));
+        const float2 w = make_float2(fmaf(g.kxk_top_f, lx * lx, g.kyk_top_f * ly * ly),
+                                     fmaf(g.uk_top_f, lx, g.vk_top_f * ly));
         const float2 eg = csqrt_f(w);
-        const float2 ke = make_float2((float)g.kz_top * eg.x, (float)g.kz_top * eg.y);
+        const float2 ke = make_float2(g.kz_top_f * eg.x, g.kz_top_f * eg.y);
         const float inv = 1.0f / fmaf(ke.x, ke.x, ke.y * ke.y);
         R0[l] = make_float2(ke.x * inv, -ke.y * inv);
     }
@@ -590,7 +590,7 @@ __device__ __forceinline__ void ricc_rc_pair(const SolveGeom &g, const float *__
             sincospif((float)(int32_t)turns * 4.656612873077393e-10f, &sn, &cs);
             sh = make_float2(cs, sn);
         }
-        const float2 q0 = make_float2((float)g.q0dc_fp, 0.f);
+        const float2 q0 = make_float2(g.q0dc_f, 0.f);
         q[l] = fc_mul(q0, make_float2(ldexpf(Ql.x, E[l]), ldexpf(Ql.y, E[l])));
         p[l] = fc_mul(fc_mul(Rjl, q[l]), sh);
         q[l] = fc_mul(q[l], sh);
