@@ -489,7 +489,10 @@ using Z512 = rx::Shape<8, 8, 8>;
 // contiguous stores) issued 13% fewer instructions than rx2_rows_batch_kernel
 // but ran 7% slower (43.3 against 40.6 us per 16 footprints, ncu): its
 // staging round trip added shared-memory and barrier waits at the same two
-// CTAs per SM.
+// CTAs per SM.  The column pass stays one line per group: the same pass with
+// two band columns per group in FP32x2 lanes (zoom_line<S, C2>, four staged
+// columns per group, 128 registers, 2 CTAs per SM instead of 3) made both
+// passes 0.0978 against 0.0951 ms per 16 footprints (CUDA events).
 template <class S>
 size_t rz_smem_of()
 {
