@@ -586,11 +586,16 @@ struct BatchBuild {
     size_t sweep_smem = 0, col_smem = 0, row_smem = 0;
     // persistent one-line transforms (lines per CTA 1)
     int persist = 0, col_grid = 0, row_grid = 0, maxnfy = 0, maxnfx = 0, maxnly = 0;
-    // register-resident transform passes: config of the column / row line
-    // length shared by every case of the batch, or -1
+    // register-resident transform passes: rx_col >= 0 when they run, with
+    // one column and one row launch per group of cases sharing their line
+    // configs (xg); -1 for the shared-memory passes (one group)
     int rx_col = -1, rx_row = -1;
+    int nxg = 1;
+    XGroup xg[BATCH_MAX_XGROUPS] = {};
     int check = 1;  // run the accuracy check
-    std::vector<int64_t> tile0, col0, row0;
+    std::vector<int64_t> tile0, col0, row0;  // col0 / row0 from the case's group start
+    std::vector<int64_t> colbase, rowbase;   // the group start of each case
+    std::vector<int> cpck, rpck;             // lines per column / row CTA of each case
 };
 
 int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, DeviceCache *dc, BatchBuild &B,
@@ -607,6 +612,10 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.tile0.resize(n);
     B.col0.resize(n);
     B.row0.resize(n);
+    B.colbase.assign(n, 0);
+    B.rowbase.assign(n, 0);
+    B.cpck.assign(n, 1);
+    B.rpck.assign(n, 1);
     int maxL = 0, maxnz = 0, maxnfy = 0, maxnfx = 0;
     for (int k = 0; k < n; ++k) {
         const bldfm_case &c = cs[k];
@@ -629,25 +638,51 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.maxnfx = maxnfx;
     int xl = opts ? opts->xform_lines : 0;
     if (xl != 0 && xl != 1 && xl != 2 && xl != 4 && xl != 8 && xl != 16) return BLDFM_ERR_ARG;
-    // register-resident passes (xform_lines 0, 8 or 16) when every case shares
-    // a supported column and row line length; otherwise the shared-memory
-    // passes.  0 and 16 take the zoomed column pass wherever every case's
-    // band and kept window allow it (3 M lines, the default halo).
+    // register-resident passes (xform_lines 0, 8 or 16) when every case has
+    // supported column and row line lengths, one launch per group of cases
+    // sharing their configs (at most BATCH_MAX_XGROUPS groups); otherwise the
+    // shared-memory passes.  0 and 16 take the zoomed column pass for the
+    // cases whose band and kept window allow it (3 M lines, the default halo).
+    std::vector<int> grp(n, 0);
+    B.nxg = 1;
     if (xl == 0 || xl == 8 || xl == 16) {
-        B.rx_col = rx_config(B.hp[0].g.nfy);
-        B.rx_row = rx_config(B.hp[0].g.nfx);
-        for (int k = 1; k < n; ++k)
-            if (B.hp[k].g.nfy != B.hp[0].g.nfy || B.hp[k].g.nfx != B.hp[0].g.nfx) B.rx_col = -1;
-        if (B.rx_col < 0 || B.rx_row < 0) B.rx_col = B.rx_row = -1;
-        if (B.rx_col >= 0 && xl != 8) {
-            int zc = 0;
-            for (int k = 0; k < n && zc >= 0; ++k) {
-                const SolveGeom &g = B.hp[k].g;
+        std::vector<int> cc(n), rc(n);
+        bool ok = true;
+        for (int k = 0; k < n && ok; ++k) {
+            const SolveGeom &g = B.hp[k].g;
+            cc[k] = rx_config(g.nfy);
+            rc[k] = rx_config(g.nfx);
+            ok = cc[k] >= 0 && rc[k] >= 0;
+            if (ok && xl != 8) {
                 const int hy = std::max(-freq_min(g.nly), freq_max(g.nly));
-                const int c = rx_zoom_config(g.nfy, hy, g.out_ny);
-                zc = (c < 0 || (k > 0 && c != zc)) ? -1 : c;
+                const int z = rx_zoom_config(g.nfy, hy, g.out_ny);
+                if (z >= 0) cc[k] = z;
             }
-            if (zc >= 0) B.rx_col = zc;
+        }
+        int ng = 0;
+        for (int k = 0; k < n && ok; ++k) {
+            int gi = 0;
+            while (gi < ng && !(B.xg[gi].rx_col == cc[k] && B.xg[gi].rx_row == rc[k])) ++gi;
+            if (gi == ng) {
+                if (ng == BATCH_MAX_XGROUPS) {
+                    ok = false;
+                    break;
+                }
+                B.xg[ng].rx_col = cc[k];
+                B.xg[ng].rx_row = rc[k];
+                ++ng;
+            }
+            grp[k] = gi;
+            B.cpck[k] = rx_lines_per_cta(cc[k], true);
+            B.rpck[k] = rx_lines_per_cta(rc[k], false);
+        }
+        if (ok) {
+            B.nxg = ng;
+            B.rx_col = B.xg[0].rx_col;
+            B.rx_row = B.xg[0].rx_row;
+        } else {
+            B.rx_col = B.rx_row = -1;
+            std::fill(grp.begin(), grp.end(), 0);
         }
         xl = 0;
     }
@@ -657,16 +692,30 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     auto col_bytes = [&](int c) { return (2 * (size_t)c + 1) * maxnfy * 8; };
     B.cpc = xl > 0 ? xl : out_cols_per_cta(maxnfy, 8);
     while (B.cpc > 1 && col_bytes(B.cpc) > 190 * 1024) B.cpc >>= 1;
-    if (B.rx_col >= 0) {
-        B.cpc = rx_lines_per_cta(B.rx_col, true);
-        B.rpc = rx_lines_per_cta(B.rx_row, false);
+    if (B.rx_col < 0) {
+        B.nxg = 1;
+        for (int k = 0; k < n; ++k) {
+            B.cpck[k] = B.cpc;
+            B.rpck[k] = B.rpc;
+        }
     }
-    for (int k = 0; k < n; ++k) {
-        const SolveGeom &g = B.hp[k].g;
-        B.col0[k] = B.ncol;
-        B.ncol += g.nlvls * ((g.nbx + B.cpc - 1) / B.cpc);
-        B.row0[k] = B.nrow;
-        B.nrow += g.nlvls * ((g.out_ny + B.rpc - 1) / B.rpc);
+    B.ncol = B.nrow = 0;
+    for (int gi = 0; gi < B.nxg; ++gi) {
+        XGroup &x = B.xg[gi];
+        x.col_start = B.ncol;
+        x.row_start = B.nrow;
+        for (int k = 0; k < n; ++k) {
+            if (grp[k] != gi) continue;
+            const SolveGeom &g = B.hp[k].g;
+            B.colbase[k] = x.col_start;
+            B.rowbase[k] = x.row_start;
+            B.col0[k] = B.ncol - x.col_start;
+            B.row0[k] = B.nrow - x.row_start;
+            B.ncol += g.nlvls * ((g.nbx + B.cpck[k] - 1) / B.cpck[k]);
+            B.nrow += g.nlvls * ((g.out_ny + B.rpck[k] - 1) / B.rpck[k]);
+        }
+        x.col_ctas = B.ncol - x.col_start;
+        x.row_ctas = B.nrow - x.row_start;
     }
     B.off_tile_case = o;
     o = al(o + 4 * (size_t)std::max<int64_t>(B.ntiles, 1));
@@ -734,8 +783,11 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.row_smem = (2 * (size_t)B.rpc + 1) * maxnfx * 8;
     B.persist = B.cpc == 1 && B.rpc == 1;
     if (B.rx_col >= 0) {
-        B.col_smem = rx_smem(B.rx_col, true);
-        B.row_smem = rx_smem(B.rx_row, false);
+        B.col_smem = B.row_smem = 0;
+        for (int gi = 0; gi < B.nxg; ++gi) {
+            B.col_smem = std::max(B.col_smem, rx_smem(B.xg[gi].rx_col, true));
+            B.row_smem = std::max(B.row_smem, rx_smem(B.xg[gi].rx_row, false));
+        }
         B.persist = 0;
     }
     if (B.persist) {
@@ -821,8 +873,8 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
         x.tile0 = B.tile0[k];
         x.col0 = B.col0[k];
         x.row0 = B.row0[k];
-        x.rpc = B.rpc;
-        x.cpc = B.cpc;
+        x.rpc = B.rpck[k];
+        x.cpc = B.cpck[k];
         double *lv64 = (double *)(blob + B.off_lv64[k]);
         if (g.footprint)
             hx_level_dz_w(nz, c.z_host, c.prof_host, lv64);  // all the k = 0 values need (no trapezoid pass)
@@ -847,9 +899,10 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
             tile_case[B.tile0[k] + t] = k;
             tile_cost.push_back((double)std::max(nz - 1, 1));
         }
-        for (int64_t i = 0; i < (int64_t)g.nlvls * ((g.nbx + B.cpc - 1) / B.cpc); ++i) col_case[B.col0[k] + i] = k;
-        const int nblk = (g.out_ny + B.rpc - 1) / B.rpc;
-        for (int64_t i = 0; i < (int64_t)g.nlvls * nblk; ++i) row_case[B.row0[k] + i] = k;
+        const int64_t ncb = (g.nbx + B.cpck[k] - 1) / B.cpck[k];
+        for (int64_t i = 0; i < (int64_t)g.nlvls * ncb; ++i) col_case[B.colbase[k] + B.col0[k] + i] = k;
+        const int nblk = (g.out_ny + B.rpck[k] - 1) / B.rpck[k];
+        for (int64_t i = 0; i < (int64_t)g.nlvls * nblk; ++i) row_case[B.rowbase[k] + B.row0[k] + i] = k;
     }
     // cost-weighted contiguous partition of the tiles over G persistent CTAs
     double total = 0;
@@ -910,6 +963,8 @@ int batch_enqueue(const bldfm_case *cs, int n, BatchBuild &B, char *ws, const vo
     bl.maxn_row = B.maxnfx;
     bl.rx_col = B.rx_col;
     bl.rx_row = B.rx_row;
+    bl.nxg = B.nxg;
+    for (int i = 0; i < B.nxg; ++i) bl.xg[i] = B.xg[i];
     if (tdc) tmark(*tdc, st);  // 1: the sweep
     CK(launch_batch_kernels(bl, st, 0));
     // the accuracy check reads the spectra, as the transform passes do: it
@@ -949,6 +1004,16 @@ std::vector<int64_t> batch_key(const bldfm_case *cs, int n, const BatchBuild &B,
     k.push_back(B.persist);
     k.push_back(B.rx_col);
     k.push_back(B.rx_row);
+    k.push_back(B.nxg);
+    for (int i = 0; i < B.nxg; ++i) {
+        const XGroup &x = B.xg[i];
+        k.push_back(x.rx_col);
+        k.push_back(x.rx_row);
+        k.push_back(x.col_start);
+        k.push_back(x.col_ctas);
+        k.push_back(x.row_start);
+        k.push_back(x.row_ctas);
+    }
     k.push_back(B.check);
     k.push_back(B.col_grid);
     k.push_back(B.row_grid);
@@ -1297,6 +1362,8 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     bl.maxn_row = B.maxnfx;
     bl.rx_col = B.rx_col;
     bl.rx_row = B.rx_row;
+    bl.nxg = B.nxg;
+    for (int i = 0; i < B.nxg; ++i) bl.xg[i] = B.xg[i];
     CK(launch_batch_kernels(bl, st, 1));
     tmark(dc, st);  // 5: end
     return BLDFM_OK;

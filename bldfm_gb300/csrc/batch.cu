@@ -1063,9 +1063,18 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
                                                                                   bl.cta_tiles, bl.err);
     }
     if (part == 1 && bl.rx_col >= 0) {
-        cudaError_t e = launch_rx_pass(bl.rx_col, true, bl, bl.col_ctas, st);
-        if (e != cudaSuccess) return e;
-        return launch_rx_pass(bl.rx_row, false, bl, bl.row_ctas, st);
+        // every group's column pass, then every group's row pass
+        for (int pass = 0; pass < 2; ++pass)
+            for (int i = 0; i < bl.nxg; ++i) {
+                const XGroup &x = bl.xg[i];
+                BatchLaunch gl = bl;
+                gl.col_case = bl.col_case + x.col_start;
+                gl.row_case = bl.row_case + x.row_start;
+                const cudaError_t e = pass == 0 ? launch_rx_pass(x.rx_col, true, gl, x.col_ctas, st)
+                                                : launch_rx_pass(x.rx_row, false, gl, x.row_ctas, st);
+                if (e != cudaSuccess) return e;
+            }
+        return cudaGetLastError();
     }
     if (part == 1 && bl.persist) {
         if (bl.col_ctas > 0)

@@ -33,6 +33,16 @@ struct __align__(16) BatchCase {
     int32_t cpc;    // band columns per column-transform CTA
 };
 
+// A group of a batch's cases that share the register-resident transform
+// configs: one column-pass and one row-pass launch each, over its CTAs
+// [col_start, col_start + col_ctas) and [row_start, row_start + row_ctas) of
+// the CTA-to-case maps (each case's col0 / row0 counts from its group's start)
+#define BATCH_MAX_XGROUPS 8
+struct XGroup {
+    int rx_col, rx_row;
+    int col_start, col_ctas, row_start, row_ctas;
+};
+
 struct BatchLaunch {
     const BatchCase *cases;
     const int *tile_case;
@@ -49,9 +59,11 @@ struct BatchLaunch {
     // persistent one-line transforms (col_ctas / row_ctas count items, launched
     // on col_grid / row_grid CTAs); shared-memory sizes from the largest case
     int persist, col_grid, row_grid, maxn_col, maxnly, maxn_row;
-    // register-resident transform passes (xform.cu): line-length configs of
-    // the column and row passes, or -1 for the shared-memory passes
+    // register-resident transform passes (xform.cu): rx_col >= 0 when they
+    // run (one launch per group of xg), -1 for the shared-memory passes
     int rx_col, rx_row;
+    int nxg;
+    XGroup xg[BATCH_MAX_XGROUPS];
 };
 
 cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int part);

@@ -67,3 +67,21 @@ def test_register_passes_match_shared_memory_passes_and_oracle(shape, domain, mo
         err = max(G.rel_l2(variant[0][1], oc), G.rel_l2(variant[0][2], of))
         print(shape, modes, halo, footprint, "%s vs double-double %.2e" % (name, err))
         assert err <= 1e-3, err
+
+
+def test_mixed_line_lengths_one_launch_per_group():
+    """A batch whose cases have different column and row line lengths runs the
+    register-resident passes as one launch per group of cases sharing their
+    configs (here a zoomed 768 group, a zoomed 1536 group, an unzoomed 1024
+    group and a 1536 x 768 group, interleaved in the batch) and matches the
+    shared-memory passes, which take the whole batch in one launch."""
+    from bldfm_gb300.batch import BatchSolver, solve_batch
+
+    shapes = [SHAPES[1], SHAPES[3], SHAPES[2], SHAPES[6], SHAPES[1], SHAPES[3]]
+    kws = [_kw(*s, footprint=bool(i % 2), seed=10 + i) for i, s in enumerate(shapes)]
+    grouped = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=0))
+    shared = solve_batch(kws, solver=BatchSolver(use_graph=False, xform_lines=2))
+    for a, b in zip(grouped, shared):
+        assert a[1].shape == b[1].shape
+        assert G.rel_l2(a[1], b[1]) <= 1e-5 and G.rel_l2(a[2], b[2]) <= 1e-5, (G.rel_l2(a[1], b[1]),
+                                                                            G.rel_l2(a[2], b[2]))
