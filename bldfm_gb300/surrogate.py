@@ -480,16 +480,40 @@ class Surrogate:
         return (out, paths, errs) if return_errors else (out, paths)
 
     def footprint(self, n, zm, wind, srf_shape, domain, modes=(512, 512), meas_pt=(0.0, 0.0), halo=None,
-                  ustar=None, z0=None, mol=1e9):
+                  ustar=None, z0=None, mol=1e9, return_error=False):
         """One footprint at z_m: (grid, conc, flx) as the solver returns them,
-        and the path that produced it ("surrogate", "fp64-box", "fp64-spot")."""
+        and the path that produced it ("surrogate", "fp32-guard", "fp64-box",
+        "fp64-spot").  With the fused kernel (variant 0) the footprint goes
+        through the batched path as a batch of one, so it gets the exact low
+        band and the accuracy guard, and a footprint whose estimate exceeds
+        ``guard_tol`` is re-solved by ``guard_mode``.  ``return_error``: also
+        return its error statement (as ``serve`` states it: the guard's
+        estimate, the FP32 path's statement after a guard re-solve, the
+        measured error after a spot check, None for an FP64 result)."""
         p = self.prepare(n, zm, wind, srf_shape, domain, modes, meas_pt, halo, ustar, z0, mol)
         s1, s2, _ = p["s"]
         self.count += 1
+
+        def ret(res, path, err):
+            return (res, path, err) if return_error else (res, path)
+
         if not (self.variant == 1 or self.in_box(n, zm, s1, s2, mode_kmax(srf_shape, domain, modes, halo))):
             self.stats["out_of_box"] += 1
-            return steady_state_transport_solver(**p["kw"], mode=self.fallback), "fp64-box"
-        conc_d, flx_d = self.solve_prepared(p)
+            return ret(steady_state_transport_solver(**p["kw"], mode=self.fallback), "fp64-box", None)
+        stated = None
+        if self.variant == 0 and self.net is not None:
+            kw = dict(n=n, zm=zm, wind=wind, srf_shape=srf_shape, domain=domain, modes=modes, meas_pt=meas_pt,
+                      halo=halo, ustar=ustar, z0=z0, mol=mol)
+            b = self.prepare_batch([kw])
+            (conc_d, flx_d), = self.solve_batch_prepared(b)
+            stated = float(self.guard_estimates(b)[0])
+            self.stats["guard"].append(stated)
+            if not stated <= self.guard_tol:
+                self.stats["guard_fail"] += 1
+                res = steady_state_transport_solver(**p["kw"], mode=self.guard_mode, return_error=True)
+                return ret(tuple(res[:3]), "fp32-guard", res[3])
+        else:
+            conc_d, flx_d = self.solve_prepared(p)
         conc, flx = conc_d.cpu().numpy(), flx_d.cpu().numpy()
         grid = _grid(p["z"], n, srf_shape, domain)
         self.stats["surrogate"] += 1
@@ -502,8 +526,9 @@ class Surrogate:
                 self.stats["spot_fail"] += 1
                 if self.fallback != self.spot_mode:
                     ref = steady_state_transport_solver(**p["kw"], mode=self.fallback)
-                return ref, "fp64-spot"
-        return (grid, conc, flx), "surrogate"
+                return ret(ref, "fp64-spot", None)
+            stated = err
+        return ret((grid, conc, flx), "surrogate", stated)
 
 
 def _grid(z, level, shape, domain):

@@ -78,6 +78,29 @@ def test_exact_transfer_serving_matches_solver(wdir, mol):
     assert abs(flx.sum() - f64.sum()) / abs(f64.sum()) < 1e-5
 
 
+def test_single_footprint_states_its_error():
+    """Surrogate.footprint with the fused kernel runs as a batch of one: the
+    same footprint as serve(), with the guard's estimate as its error
+    statement (here within a factor of 3 of the true error)."""
+    from bldfm_gb300.solver import steady_state_transport_solver
+    from bldfm_gb300.surrogate import Surrogate, load
+
+    net, box, meta = load()
+    kw = dict(n=128, zm=20.0, wind=(2.83, 2.83), srf_shape=(256, 256), domain=(500.0, 500.0), modes=(256, 256),
+              meas_pt=(250.0, 250.0), ustar=0.3, mol=-50.0)
+    sur = Surrogate(net, spot_every=0, tol=1e-3)
+    (grid, conc, flx), path, stated = sur.footprint(**kw, return_error=True)
+    assert path == "surrogate" and stated is not None
+    out, paths = Surrogate(net, spot_every=0, tol=1e-3).serve([kw])
+    assert paths == ["surrogate"]
+    assert _rel(conc, out[0][0].cpu().numpy()) < 1e-12 and _rel(flx, out[0][1].cpu().numpy()) < 1e-12
+    p = sur.prepare(**kw)
+    _, cr, fr = steady_state_transport_solver(**p["kw"], mode="fp64r")
+    true = max(_rel(conc, cr), _rel(flx, fr))
+    print("stated %.2e true %.2e" % (stated, true))
+    assert true / 3 <= stated <= 3 * true
+
+
 def test_fused_serving_matches_layerwise():
     """The fused features -> MLP -> spectra kernel computes what the
     layer-by-layer tensor-core MLP and the spectra kernel compute."""
