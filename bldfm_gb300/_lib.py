@@ -163,6 +163,7 @@ _SIGS = {
     ),
     "bldfm_set_stage_timing": (ctypes.c_int, [ctypes.c_int]),
     "bldfm_stage_times": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "bldfm_memcpy_async": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P]),
     "bldfm_sweep32_flops": (ctypes.c_int, [ctypes.c_int32, _P, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
     "bldfm_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double), _P]),
     "bldfm_batch_plan": (

@@ -120,9 +120,21 @@ def error_estimates(sums):
 class BatchResults(list):
     """A list of ``(grid, conc, flx)`` results with ``error_estimates``: per
     case, the estimated relative L2 error against the exact FP64 solution
-    (None when the solver ran without the accuracy check)."""
+    (None when the solver ran without the accuracy check), computed from the
+    device check's sums when first read."""
 
-    error_estimates = None
+    _sums = None
+    _est = None
+
+    @property
+    def error_estimates(self):
+        if self._est is None and self._sums is not None:
+            self._est = error_estimates(self._sums)
+        return self._est
+
+    @error_estimates.setter
+    def error_estimates(self, v):
+        self._est = v
 
 
 class BatchSolver:
@@ -293,14 +305,22 @@ _grid = output_grid
 
 
 def _enqueue_batch(solver, cases):
-    """Enqueue a batch and the copy of its outputs into a fresh pinned host
-    buffer on the solver's stream; returns the pending state."""
+    """Enqueue a batch and the copy of its outputs and of the workspace head
+    (status word, the check's sums) into one fresh pinned host buffer on the
+    solver's stream; returns the pending state."""
     shapes = solver.solve_prepared(solver.prepare(cases, views=False))
-    host = torch.empty(solver.out_elems, dtype=torch.float64, pin_memory=True)
-    head = torch.empty(64 + 16 * len(cases), dtype=torch.uint8, pin_memory=True)  # status word, check sums
-    with torch.cuda.stream(solver.stream):
-        host.copy_(solver._out_buf[: solver.out_elems], non_blocking=True)
-        head.copy_(solver._ws[: head.numel()], non_blocking=True)
+    nout = 8 * solver.out_elems
+    nhead = 64 + 16 * len(cases)
+    block = torch.empty(nout + nhead, dtype=torch.uint8, pin_memory=True)
+    host = block[:nout].view(torch.float64)
+    head = block[nout:]
+    lib = _lib.load()
+    s = ctypes.c_void_p(solver.stream.cuda_stream)
+    base = block.data_ptr()
+    _lib.check(lib.bldfm_memcpy_async(ctypes.c_void_p(base), ctypes.c_void_p(solver._out_buf.data_ptr()), nout, s),
+               "solve_batch")
+    _lib.check(lib.bldfm_memcpy_async(ctypes.c_void_p(base + nout), ctypes.c_void_p(solver._ws.data_ptr()), nhead,
+                                      s), "solve_batch")
     return (solver, cases, shapes, solver._keep, host, head)
 
 
@@ -308,14 +328,15 @@ def _finish_batch(pending):
     """Wait for an enqueued batch and build its (grid, conc, flx) results."""
     solver, cases, shapes, keep, host, head = pending
     solver.stream.synchronize()
-    st = int(head[:4].view(torch.int32)[0])
+    hd = head.numpy()
+    st = int(hd[:4].view(np.int32)[0])
     if st != 0:
         _lib.check(st, "solve_batch")
     hn = host.numpy()
     results = BatchResults()
     n = len(cases)
     if getattr(solver, "check", True):
-        results.error_estimates = error_estimates(head[64:].view(torch.float32).numpy())
+        results._sums = hd[64 : 64 + 16 * n].view(np.float32).reshape(n, 4).copy()
     if n and all(sh == shapes[0] for sh in shapes):  # one geometry: views of one reshaped array
         sq = tuple(v for v in shapes[0] if v != 1)
         hv = hn[: 2 * n * _count(shapes[0])].reshape((n, 2) + sq)

@@ -5,9 +5,14 @@
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -36,7 +41,7 @@ struct HostPlan {
     SolveGeom g;
     FftPlan plx_fwd, ply_fwd, plx_out, ply_out;
     std::vector<int> slot;  // nz entries
-    std::vector<int4> xband;
+    std::shared_ptr<const std::vector<int4>> xband;  // output band columns (memoised per size)
     bool shape_ok;          // truncated source spectrum matches modes
 };
 
@@ -92,19 +97,18 @@ int make_plan(const bldfm_desc *d, const double *z, const double *prof, const in
     // output band columns and the transform plans depend on sizes only and
     // are memoised
     static std::mutex memo_mutex;
-    static std::map<std::pair<int, int>, std::vector<int4>> xband_memo;
+    static std::map<std::pair<int, int>, std::shared_ptr<const std::vector<int4>>> xband_memo;
     static std::map<int, FftPlan> plan_memo;
     std::lock_guard<std::mutex> memo_lock(memo_mutex);
-    auto xm = xband_memo.find(std::make_pair(g.nlx, g.nfx));
-    if (xm != xband_memo.end()) {
-        hp.xband = xm->second;
-    } else {
+    auto &xb = xband_memo[std::make_pair(g.nlx, g.nfx)];
+    if (!xb) {
         const int f0 = freq_min(g.nlx), f1 = freq_max(g.nlx);
-        hp.xband.resize(2 * std::max(-f0, f1) + 1);
-        hp.xband.resize(band_columns(g.nlx, g.nfx, hp.xband.data()));
-        xband_memo[std::make_pair(g.nlx, g.nfx)] = hp.xband;
+        auto v = std::make_shared<std::vector<int4>>(2 * std::max(-f0, f1) + 1);
+        v->resize(band_columns(g.nlx, g.nfx, v->data()));
+        xb = v;
     }
-    g.nbx = (int)hp.xband.size();
+    hp.xband = xb;
+    g.nbx = (int)hp.xband->size();
     auto plan_of = [&](int n, FftPlan &p) {
         auto it = plan_memo.find(n);
         if (it != plan_memo.end()) {
@@ -322,10 +326,11 @@ int get_xband(DeviceCache &dc, const HostPlan &hp, int4 **out)
         return BLDFM_OK;
     }
     int4 *d = nullptr;
-    const size_t bytes = std::max<size_t>(hp.xband.size(), 1) * sizeof(int4);
+    const std::vector<int4> &xband = *hp.xband;
+    const size_t bytes = std::max<size_t>(xband.size(), 1) * sizeof(int4);
     if (cudaMalloc(&d, bytes) != cudaSuccess) return BLDFM_ERR_CUDA;
-    if (!hp.xband.empty() &&
-        cudaMemcpy(d, hp.xband.data(), hp.xband.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (!xband.empty() &&
+        cudaMemcpy(d, xband.data(), xband.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
         return BLDFM_ERR_CUDA;
     dc.xband[key] = d;
     *out = d;
@@ -373,6 +378,113 @@ inline void timers_begin(DeviceCache &dc)
     dc.tpending++;
     dc.cur->used = 0;
 }
+
+// Persistent host threads for the per-case work of a batch call (level
+// tables, k = 0 values, plans, descriptor and CTA-map fills): fn(i) for
+// i < n.  A call is a job whose items the calling thread and the workers
+// claim through an atomic counter; the caller starts at once and spins only
+// until the items have finished and the workers that took the job have left
+// it (a worker that wakes after the job has finished finds none), so a call
+// never waits for sleeping threads.  One call at a time: every entry point
+// that uses it holds g_mutex.  The workers start on first use and are joined
+// when the library unloads; a forked child (which has none of them) runs the
+// items itself.
+class HostPool {
+  public:
+    static HostPool &get()
+    {
+        static HostPool p;
+        return p;
+    }
+    void run(int n, const std::function<void(int)> &fn)
+    {
+        // a few items: waking workers costs more than they save
+        if (n < 4 || th_.empty() || getpid() != pid_) {
+            for (int i = 0; i < n; ++i) fn(i);
+            return;
+        }
+        Job job;
+        job.fn = &fn;
+        job.n = n;
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = &job;
+            ++gen_;
+        }
+        // wake as many workers as there are items besides the caller's first
+        const int wake = std::min<int>(n - 1, (int)th_.size());
+        if (wake == (int)th_.size())
+            cv_.notify_all();
+        else
+            for (int i = 0; i < wake; ++i) cv_.notify_one();
+        work(job);
+        while (job.done.load(std::memory_order_acquire) < n) std::this_thread::yield();
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = nullptr;  // workers that wake from now on find no job
+        }
+        while (job.refs.load(std::memory_order_acquire) > 0) std::this_thread::yield();
+    }
+    ~HostPool()
+    {
+        if (getpid() != pid_) {  // a forked child: the threads are not its own
+            for (auto &t : th_) t.detach();
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+
+  private:
+    struct Job {
+        const std::function<void(int)> *fn = nullptr;
+        int n = 0;
+        std::atomic<int> next{0}, done{0};
+        std::atomic<int> refs{0};  // workers inside the job (taken under m_)
+    };
+    HostPool() : pid_(getpid())
+    {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nt = (int)std::min(7u, hw > 1 ? hw - 1 : 0u);
+        for (int i = 0; i < nt; ++i) th_.emplace_back([this] { loop(); });
+    }
+    static void work(Job &j)
+    {
+        for (int i = j.next.fetch_add(1); i < j.n; i = j.next.fetch_add(1)) {
+            (*j.fn)(i);
+            j.done.fetch_add(1, std::memory_order_release);
+        }
+    }
+    void loop()
+    {
+        uint64_t seen = 0;
+        for (;;) {
+            Job *j = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                j = job_;
+                if (!j) continue;
+                j->refs.fetch_add(1);
+            }
+            work(*j);
+            j->refs.fetch_sub(1, std::memory_order_release);
+        }
+    }
+    pid_t pid_;
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_;
+    Job *job_ = nullptr;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
 
 void eigval_parallel(const ModeList &ml, const SolveGeom &g, const double *prof, int nz, double *eig)
 {
@@ -617,13 +729,22 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     B.cpck.assign(n, 1);
     B.rpck.assign(n, 1);
     int maxL = 0, maxnz = 0, maxnfy = 0, maxnfx = 0;
-    for (int k = 0; k < n; ++k) {
+    // every case's checks and plan on the host pool; the first failing case
+    // (lowest index) gives the status
+    std::vector<int> status(n, BLDFM_OK);
+    HostPool::get().run(n, [&](int k) {
         const bldfm_case &c = cs[k];
-        if (c.desc.mode != BLDFM_MODE_FP32 || c.desc.analytic) return BLDFM_ERR_UNSUPPORTED;
-        if (!c.z_host || !c.prof_host || !c.levels_host || !c.conc_dev || !c.flx_dev) return BLDFM_ERR_ARG;
-        if (!c.desc.footprint && !c.srf_flx_dev) return BLDFM_ERR_ARG;
-        int rc = make_plan(&c.desc, c.z_host, c.prof_host, c.levels_host, c.nlvls, B.hp[k]);
-        if (rc != BLDFM_OK) return rc;
+        if (c.desc.mode != BLDFM_MODE_FP32 || c.desc.analytic)
+            status[k] = BLDFM_ERR_UNSUPPORTED;
+        else if (!c.z_host || !c.prof_host || !c.levels_host || !c.conc_dev || !c.flx_dev ||
+                 (!c.desc.footprint && !c.srf_flx_dev))
+            status[k] = BLDFM_ERR_ARG;
+        else
+            status[k] = make_plan(&c.desc, c.z_host, c.prof_host, c.levels_host, c.nlvls, B.hp[k]);
+    });
+    for (int k = 0; k < n; ++k)
+        if (status[k] != BLDFM_OK) return status[k];
+    for (int k = 0; k < n; ++k) {
         const SolveGeom &g = B.hp[k].g;
         B.tile0[k] = B.ntiles;
         const int64_t tm = (int64_t)B.threads * BATCH_MODES_PER_THREAD;
@@ -841,9 +962,10 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
     int *col_case = (int *)(blob + B.off_col_case);
     int *row_case = (int *)(blob + B.off_row_case);
     char *wb = ws + B.blob_at;  // device address of the blob
-    std::vector<double> tile_cost;
-    tile_cost.reserve((size_t)B.ntiles);
-    for (int k = 0; k < n; ++k) {
+    // every case writes its own regions of the blob: the cases run on the
+    // host pool (a 16-footprint step's tables and maps took ~0.1 ms on one
+    // core of the Arm host, a fifth of the step)
+    auto one_case = [&](int k) {
         const HostPlan &hp = B.hp[k];
         const SolveGeom &g = hp.g;
         const bldfm_case &c = cs[k];
@@ -895,16 +1017,22 @@ void batch_fill_blob(const bldfm_case *cs, int n, BatchBuild &B, char *ws, char 
                          g.precision == BLDFM_PREC_SINGLE, g.nlvls, 0, (double *)(blob + B.off_dc[k]));
         const int64_t tm = (int64_t)B.threads * BATCH_MODES_PER_THREAD;
         const int64_t nt = (g.nsolved + tm - 1) / tm;
-        for (int64_t t = 0; t < nt; ++t) {
-            tile_case[B.tile0[k] + t] = k;
-            tile_cost.push_back((double)std::max(nz - 1, 1));
-        }
+        for (int64_t t = 0; t < nt; ++t) tile_case[B.tile0[k] + t] = k;
         const int64_t ncb = (g.nbx + B.cpck[k] - 1) / B.cpck[k];
         for (int64_t i = 0; i < (int64_t)g.nlvls * ncb; ++i) col_case[B.colbase[k] + B.col0[k] + i] = k;
         const int nblk = (g.out_ny + B.rpck[k] - 1) / B.rpck[k];
         for (int64_t i = 0; i < (int64_t)g.nlvls * nblk; ++i) row_case[B.rowbase[k] + B.row0[k] + i] = k;
-    }
+    };
+    HostPool::get().run(n, one_case);
     // cost-weighted contiguous partition of the tiles over G persistent CTAs
+    std::vector<double> tile_cost;
+    tile_cost.reserve((size_t)B.ntiles);
+    for (int k = 0; k < n; ++k) {
+        const SolveGeom &g = B.hp[k].g;
+        const int64_t tm = (int64_t)B.threads * BATCH_MODES_PER_THREAD;
+        const int64_t nt = (g.nsolved + tm - 1) / tm;
+        for (int64_t t = 0; t < nt; ++t) tile_cost.push_back((double)std::max(g.nz - 1, 1));
+    }
     double total = 0;
     for (double c : tile_cost) total += c;
     int64_t t = 0;
@@ -1408,6 +1536,14 @@ int bldfm_set_stage_timing(int enable)
     dc.tpending = 0;
     dc.tnext = 0;
     return BLDFM_OK;
+}
+
+int bldfm_memcpy_async(void *dst, const void *src, size_t bytes, void *stream)
+{
+    if (bytes == 0) return BLDFM_OK;
+    if (!dst || !src) return BLDFM_ERR_ARG;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, (cudaStream_t)stream) == cudaSuccess ? BLDFM_OK
+                                                                                                 : BLDFM_ERR_CUDA;
 }
 
 int bldfm_stage_times(float *ms, int n)

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../../include/bldfm_gb300.h"
@@ -1092,14 +1093,31 @@ cudaError_t launch_batch_kernels(const BatchLaunch &bl, cudaStream_t st, int par
     return cudaGetLastError();
 }
 
+// resident CTAs per SM of the persistent sweep, memoised per (device, shape,
+// shared memory): the first query sets every batch kernel's attributes
 int batch_sweep_occupancy(int threads, size_t smem)
 {
+    static std::mutex m;
+    static std::map<std::tuple<int, int, size_t>, int> memo;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    const auto key = std::make_tuple(dev, threads, smem);
+    {
+        std::lock_guard<std::mutex> lk(m);
+        const auto it = memo.find(key);
+        if (it != memo.end()) return it->second;
+    }
     prepare_batch_attributes();
     int nb = 0;
     const cudaError_t e =
         threads == 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, riccati32_batch_kernel<128>, 128, smem)
                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, riccati32_batch_kernel<256>, 256, smem);
-    return e == cudaSuccess && nb > 0 ? nb : 1;
+    const int r = e == cudaSuccess && nb > 0 ? nb : 1;
+    if (e == cudaSuccess) {
+        std::lock_guard<std::mutex> lk(m);
+        memo[key] = r;
+    }
+    return r;
 }
 
 // resident CTAs per SM of the persistent column (col != 0) or row transform

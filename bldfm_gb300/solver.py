@@ -45,10 +45,12 @@ def output_grid(z, levels, shape, domain):
     reference's, as read-only arrays shared between calls with the same
     levels, shape and domain (building three fresh (ny, nx) arrays costs
     more host time than an FP32 solve)."""
-    zl = np.asarray(z)[levels]
-    key = (zl.tobytes(), tuple(shape), tuple(domain))
+    # one level (an integer): its height is the key, without indexing z
+    zk = float(z[levels]) if isinstance(levels, (int, np.integer)) else np.asarray(z)[levels].tobytes()
+    key = (zk, tuple(shape), tuple(domain))
     g = _GRID_CACHE.get(key)
     if g is None:
+        zl = np.asarray(z)[levels]
         ny, nx = shape
         x = np.linspace(0, domain[0], nx, endpoint=False)
         y = np.linspace(0, domain[1], ny, endpoint=False)

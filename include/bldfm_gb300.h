@@ -156,9 +156,18 @@ int bldfm_vertical_profiles_batch(int32_t ncases, const bldfm_profile_params *pa
  * [1] sweep, [2] k=0 mode / combination, [3] output transform.  It returns the
  * number of stages written and restarts the average.  Batches
  * (bldfm_solve_batch without a graph) record [0] upload and per-case forward
- * transforms, [1] the sweep, [2] the output transform. */
+ * transforms, [1] the sweep, [2] the output transform, [3] the accuracy
+ * check; surrogate batches [0] upload, [1] the serving kernel, [2] the exact
+ * low band, [3] the accuracy guard, [4] the output transform. */
 int bldfm_set_stage_timing(int enable);
 int bldfm_stage_times(float *ms, int n);
+
+/* Asynchronous copy of `bytes` between any two addresses the CUDA runtime
+ * knows (cudaMemcpyDefault: device, pinned host) on `stream`.  No reference
+ * counterpart: a convenience for hosts without a CUDA runtime binding (the
+ * Python layer copies each batch's results and status into one pinned host
+ * buffer with it). */
+int bldfm_memcpy_async(void *dst, const void *src, size_t bytes, void *stream);
 
 /* Algorithmic flops of the FP32 Riccati sweep for one solved mode (an FMA
  * counted as 2, MUL/ADD/RCP as 1) on the nz-level table of prof_host with
