@@ -144,3 +144,38 @@ def test_status_strings_name_every_code():
     codes = [getattr(_lib, n) for n in dir(_lib) if n.startswith("ERR_")]
     names = {lib.bldfm_status_str(c).decode() for c in codes}
     assert "unknown status" not in names and len(names) == len(codes)
+
+
+def test_batch_plan_reports_the_first_failing_case():
+    """A batch of eight cases is planned on the library's host threads; the
+    status is the first failing case's (lowest index), whichever thread
+    planned it, and a valid batch plans to the same workspace every time."""
+    lib = _lib.load()
+    z, prof = _good()
+    lv = np.array([len(z) - 1], dtype=np.int64)
+    out = np.zeros(1)
+    bad = prof.copy()
+    bad[4, 3] = -1.0  # Kz < 0: BLDFM_ERR_PROFILE
+
+    def batch(faults):
+        arr = (_lib.Case * 8)()
+        keep = []
+        for k in range(8):
+            modes = (63, 48) if faults.get(k) == "odd" else (64, 48)
+            p = bad if faults.get(k) == "profile" else prof
+            d = make_desc((48, 64), len(z), (128.0, 96.0), modes, (40.0, 50.0), 0.0, True, False, None, "double",
+                          "fp32")
+            c = arr[k]
+            c.desc = d
+            c.z_host, c.prof_host, c.levels_host = z.ctypes.data, p.ctypes.data, lv.ctypes.data
+            c.nlvls = 1
+            c.conc_dev = c.flx_dev = out.ctypes.data  # planning never dereferences the outputs
+            keep.append(d)
+        nb = ctypes.c_int64(0)
+        st = lib.bldfm_batch_plan(arr, 8, ctypes.byref(_lib.BatchOpts(0, 0, 0, 0, 0)), ctypes.byref(nb))
+        return st, nb.value
+
+    assert batch({3: "profile", 6: "odd"})[0] == _lib.ERR_PROFILE
+    assert batch({2: "odd", 5: "profile"})[0] == _lib.ERR_ODD_MODES
+    sizes = {batch({}) for _ in range(20)}
+    assert len(sizes) == 1 and next(iter(sizes))[0] == 0 and next(iter(sizes))[1] > 0
