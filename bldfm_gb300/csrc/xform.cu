@@ -282,7 +282,10 @@ __global__ void __launch_bounds__(kThreads, min_ctas<S>()) rx_rows_batch_kernel(
 }
 
 // Paired row pass: each group transforms output rows 2 grp and 2 grp + 1 of
-// the CTA's block together.
+// the CTA's block together.  Its inputs are read from global memory (the
+// column pass's output, in L2): staging the pair's two adjacent rows by one
+// bulk copy, as the column pass stages its spectrum columns, measured no
+// faster (0.0963 against 0.0955 ms for both passes per 16 footprints).
 template <class S>
 __global__ void __launch_bounds__(kThreads, 2) rx2_rows_batch_kernel(const BatchCase *__restrict__ cases,
                                                                     const int *__restrict__ cta_case, int *err)
