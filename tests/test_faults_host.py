@@ -179,3 +179,50 @@ def test_batch_plan_reports_the_first_failing_case():
     assert batch({2: "odd", 5: "profile"})[0] == _lib.ERR_ODD_MODES
     sizes = {batch({}) for _ in range(20)}
     assert len(sizes) == 1 and next(iter(sizes))[0] == 0 and next(iter(sizes))[1] > 0
+
+
+def test_batch_plan_from_many_threads():
+    """Host threads calling the library at once (each call holds the
+    library's lock and reuses its pool of host threads) plan their batches
+    exactly as one thread does."""
+    import threading
+
+    lib = _lib.load()
+    z, prof = _good()
+    lv = np.array([len(z) - 1], dtype=np.int64)
+    out = np.zeros(1)
+    arrs = []
+    for n in (4, 6, 8, 12):
+        arr = (_lib.Case * n)()
+        for k in range(n):
+            c = arr[k]
+            c.desc = make_desc((48, 64), len(z), (128.0, 96.0), (64, 48), (40.0, 50.0), 0.0, True, False, None,
+                               "double", "fp32")
+            c.z_host, c.prof_host, c.levels_host = z.ctypes.data, prof.ctypes.data, lv.ctypes.data
+            c.nlvls = 1
+            c.conc_dev = c.flx_dev = out.ctypes.data
+        arrs.append((arr, n))
+
+    def plan(arr, n):
+        nb = ctypes.c_int64(0)
+        st = lib.bldfm_batch_plan(arr, n, ctypes.byref(_lib.BatchOpts(0, 0, 0, 0, 0)), ctypes.byref(nb))
+        return st, nb.value
+
+    want = [plan(a, n) for a, n in arrs]
+    got, errs = [], []
+
+    def worker(i):
+        try:
+            for _ in range(50):
+                a, n = arrs[i % len(arrs)]
+                got.append((i % len(arrs), plan(a, n)))
+        except Exception as e:  # surfaced below
+            errs.append(e)
+
+    th = [threading.Thread(target=worker, args=(i,)) for i in range(8)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errs
+    assert len(got) == 400 and all(r == want[i] for i, r in got)
