@@ -24,11 +24,13 @@ from .batch import BatchSolver
 # of another stream, which the pipelined timing below can reward.
 CANDIDATES = [(256, 0), (256, 6), (128, 0), (128, 12), (128, 18), (256, 3), (128, 7)]
 # transform passes: 16 = register-resident lines, the column pass zoomed
-# where every case's band and kept window allow it, 8 = register-resident lines (batches whose
-# cases share a supported line length; others fall back to the default),
-# 4 / 2 / 1 = shared-memory passes with that many lines per CTA
+# for the cases whose band and kept window allow it, 8 = register-resident
+# lines unzoomed (both one launch per group of cases sharing their line
+# configs; a batch with an unsupported line length falls back to the
+# shared-memory passes), 4 / 2 / 1 = shared-memory passes with that many
+# lines per CTA
 XFORM_LINES = [16, 8, 4, 2, 1]
-SIGNATURE_VERSION = 3  # bumped when the candidate set changes: older cached winners are ignored
+SIGNATURE_VERSION = 4  # bumped when the candidates or the kernels behind them change: older winners are ignored
 
 
 def _cache_path():
