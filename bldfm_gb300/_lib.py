@@ -24,6 +24,7 @@ ERR_CUDA = -8
 ERR_TIMEOUT = -9
 ERR_NONFINITE = -10
 ERR_PROFILE = -11
+ERR_HOST = -12
 
 PREC_SINGLE = 0
 PREC_DOUBLE = 1
@@ -265,6 +266,8 @@ def check(status, what="bldfm"):
         raise ValueError("%s: %s" % (what, msg))
     if status == ERR_NONFINITE:
         raise FloatingPointError("%s: %s" % (what, msg))
+    if status == ERR_HOST:
+        raise MemoryError("%s: %s" % (what, msg))
     raise RuntimeError("%s: %s (status %d)" % (what, msg, status))
 
 

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <exception>
 #include <functional>
 #include <map>
 #include <memory>
@@ -421,9 +422,11 @@ class HostPool {
         while (job.done.load(std::memory_order_acquire) < n) std::this_thread::yield();
         {
             std::lock_guard<std::mutex> lk(m_);
-            job_ = nullptr;  // workers that wake from now on find no job
+            if (job_ == &job) job_ = nullptr;  // workers that wake from now on find no job
         }
         while (job.refs.load(std::memory_order_acquire) > 0) std::this_thread::yield();
+        // an item that threw (std::bad_alloc in planning) rethrows in the caller
+        if (job.failed.load(std::memory_order_acquire)) std::rethrow_exception(job.error);
     }
     ~HostPool()
     {
@@ -445,6 +448,8 @@ class HostPool {
         int n = 0;
         std::atomic<int> next{0}, done{0};
         std::atomic<int> refs{0};  // workers inside the job (taken under m_)
+        std::atomic<bool> claim{false}, failed{false};
+        std::exception_ptr error;  // the first item's exception, set before failed
     };
     HostPool() : pid_(getpid())
     {
@@ -455,7 +460,15 @@ class HostPool {
     static void work(Job &j)
     {
         for (int i = j.next.fetch_add(1); i < j.n; i = j.next.fetch_add(1)) {
-            (*j.fn)(i);
+            try {
+                (*j.fn)(i);
+            } catch (...) {
+                bool expect = false;
+                if (j.claim.compare_exchange_strong(expect, true)) {
+                    j.error = std::current_exception();
+                    j.failed.store(true, std::memory_order_release);
+                }
+            }
             j.done.fetch_add(1, std::memory_order_release);
         }
     }
@@ -1502,6 +1515,18 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
 // ---------------------------------------------------------------------------
 // exported entry points
 // ---------------------------------------------------------------------------
+// A C++ exception of the host side (std::bad_alloc while planning, a thread
+// that cannot be started) ends at the C boundary as a status.
+template <class F>
+static int guarded(F &&f)
+{
+    try {
+        return f();
+    } catch (...) {
+        return BLDFM_ERR_HOST;
+    }
+}
+
 extern "C" {
 
 const char *bldfm_status_str(int s)
@@ -1520,6 +1545,7 @@ const char *bldfm_status_str(int s)
     case BLDFM_ERR_NONFINITE: return "non-finite values in the output";
     case BLDFM_ERR_PROFILE:
         return "z must be strictly increasing and the profiles finite with Kz > 0 and Kx, Ky >= 0";
+    case BLDFM_ERR_HOST: return "host-side failure (memory allocation or thread start)";
     default: return "unknown status";
     }
 }
@@ -1610,221 +1636,239 @@ int bldfm_fma_peak(int kind, double *flops_per_s, void *stream)
 
 int bldfm_plan(const bldfm_desc *d, int nlvls, bldfm_plan_info *out)
 {
-    if (!out) return BLDFM_ERR_ARG;
-    HostPlan hp;
-    int rc = make_plan(d, nullptr, nullptr, nullptr, nlvls, hp);
-    if (rc != BLDFM_OK) return rc;
-    // without levels the snapshot count is bounded by nlvls
-    hp.g.nsnap = std::min(nlvls, hp.g.nz);
-    const SolveGeom &g = hp.g;
-    out->nxe = g.nxe;
-    out->nye = g.nye;
-    out->nlx = g.nlx;
-    out->nly = g.nly;
-    out->px = g.px;
-    out->py = g.py;
-    out->nfx = g.nfx;
-    out->nfy = g.nfy;
-    out->out_nx = g.out_nx;
-    out->out_ny = g.out_ny;
-    out->nsolved = g.nsolved;
-    out->workspace_bytes = (int64_t)layout_for(g).total;
-    return BLDFM_OK;
+    return guarded([&]() -> int {
+        if (!out) return BLDFM_ERR_ARG;
+        HostPlan hp;
+        int rc = make_plan(d, nullptr, nullptr, nullptr, nlvls, hp);
+        if (rc != BLDFM_OK) return rc;
+        // without levels the snapshot count is bounded by nlvls
+        hp.g.nsnap = std::min(nlvls, hp.g.nz);
+        const SolveGeom &g = hp.g;
+        out->nxe = g.nxe;
+        out->nye = g.nye;
+        out->nlx = g.nlx;
+        out->nly = g.nly;
+        out->px = g.px;
+        out->py = g.py;
+        out->nfx = g.nfx;
+        out->nfy = g.nfy;
+        out->out_nx = g.out_nx;
+        out->out_ny = g.out_ny;
+        out->nsolved = g.nsolved;
+        out->workspace_bytes = (int64_t)layout_for(g).total;
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_solve(const bldfm_desc *d, const double *srf_flx_dev, const double *z_host, const double *prof_host,
                 const int64_t *levels_host, int32_t nlvls, double *conc_dev, double *flx_dev, void *workspace_dev,
                 size_t workspace_bytes, void *stream)
 {
-    std::lock_guard<std::mutex> lk(g_mutex);
-    return solve_impl(d, srf_flx_dev, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
-                      workspace_bytes, (cudaStream_t)stream);
+    return guarded([&]() -> int {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        return solve_impl(d, srf_flx_dev, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
+                          workspace_bytes, (cudaStream_t)stream);
+    });
 }
 
 int bldfm_solve_host(const bldfm_desc *d, const double *srf_flx_host, const double *z_host, const double *prof_host,
                      const int64_t *levels_host, int32_t nlvls, double *conc_host, double *flx_host)
 {
-    std::lock_guard<std::mutex> lk(g_mutex);
-    if (!d || !conc_host || !flx_host) return BLDFM_ERR_ARG;
-    bldfm_plan_info pi;
-    int rc;
-    {
-        HostPlan hp;
-        rc = make_plan(d, z_host, prof_host, levels_host, nlvls, hp);
-        if (rc != BLDFM_OK) return rc;
-        pi.out_nx = hp.g.out_nx;
-        pi.out_ny = hp.g.out_ny;
-        pi.workspace_bytes = (int64_t)layout_for(hp.g).total;
-    }
-    int status = BLDFM_OK;
-    DeviceCache &dc = cache_for_current(&status);
-    if (status != BLDFM_OK) return status;
-    HostBuffers &hb = dc.hb;
-    if (!hb.stream) CK(cudaStreamCreateWithFlags(&hb.stream, cudaStreamNonBlocking));
-    if ((size_t)pi.workspace_bytes > hb.ws_bytes) {
-        if (hb.ws) cudaFree(hb.ws);
-        hb.ws = nullptr;
-        CK(cudaMalloc(&hb.ws, (size_t)pi.workspace_bytes));
-        hb.ws_bytes = (size_t)pi.workspace_bytes;
-    }
-    const size_t outb = (size_t)nlvls * pi.out_ny * pi.out_nx * sizeof(double);
-    if (outb > hb.out_bytes) {
-        if (hb.conc) cudaFree(hb.conc);
-        if (hb.flx) cudaFree(hb.flx);
-        hb.conc = hb.flx = nullptr;
-        CK(cudaMalloc(&hb.conc, std::max<size_t>(outb, 8)));
-        CK(cudaMalloc(&hb.flx, std::max<size_t>(outb, 8)));
-        hb.out_bytes = outb;
-    }
-    const double *srf_dev = nullptr;
-    if (!d->footprint) {
-        if (!srf_flx_host) return BLDFM_ERR_ARG;
-        const size_t sb = (size_t)d->nx * d->ny * sizeof(double);
-        if (sb > hb.srf_bytes) {
-            if (hb.srf) cudaFree(hb.srf);
-            hb.srf = nullptr;
-            CK(cudaMalloc(&hb.srf, sb));
-            hb.srf_bytes = sb;
+    return guarded([&]() -> int {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        if (!d || !conc_host || !flx_host) return BLDFM_ERR_ARG;
+        bldfm_plan_info pi;
+        int rc;
+        {
+            HostPlan hp;
+            rc = make_plan(d, z_host, prof_host, levels_host, nlvls, hp);
+            if (rc != BLDFM_OK) return rc;
+            pi.out_nx = hp.g.out_nx;
+            pi.out_ny = hp.g.out_ny;
+            pi.workspace_bytes = (int64_t)layout_for(hp.g).total;
         }
-        CK(cudaMemcpyAsync(hb.srf, srf_flx_host, sb, cudaMemcpyHostToDevice, hb.stream));
-        srf_dev = hb.srf;
-    }
-    rc = solve_impl(d, srf_dev, z_host, prof_host, levels_host, nlvls, hb.conc, hb.flx, hb.ws, hb.ws_bytes,
-                    hb.stream);
-    if (rc != BLDFM_OK) return rc;
-    if (outb) {
-        CK(cudaMemcpyAsync(conc_host, hb.conc, outb, cudaMemcpyDeviceToHost, hb.stream));
-        CK(cudaMemcpyAsync(flx_host, hb.flx, outb, cudaMemcpyDeviceToHost, hb.stream));
-    }
-    int err = 0;
-    CK(cudaMemcpyAsync(&err, hb.ws, sizeof(int), cudaMemcpyDeviceToHost, hb.stream));
-    CK(cudaStreamSynchronize(hb.stream));
-    if (err != 0) return err == BLDFM_ERR_NONFINITE ? BLDFM_ERR_NONFINITE : BLDFM_ERR_TIMEOUT;
-    return BLDFM_OK;
+        int status = BLDFM_OK;
+        DeviceCache &dc = cache_for_current(&status);
+        if (status != BLDFM_OK) return status;
+        HostBuffers &hb = dc.hb;
+        if (!hb.stream) CK(cudaStreamCreateWithFlags(&hb.stream, cudaStreamNonBlocking));
+        if ((size_t)pi.workspace_bytes > hb.ws_bytes) {
+            if (hb.ws) cudaFree(hb.ws);
+            hb.ws = nullptr;
+            CK(cudaMalloc(&hb.ws, (size_t)pi.workspace_bytes));
+            hb.ws_bytes = (size_t)pi.workspace_bytes;
+        }
+        const size_t outb = (size_t)nlvls * pi.out_ny * pi.out_nx * sizeof(double);
+        if (outb > hb.out_bytes) {
+            if (hb.conc) cudaFree(hb.conc);
+            if (hb.flx) cudaFree(hb.flx);
+            hb.conc = hb.flx = nullptr;
+            CK(cudaMalloc(&hb.conc, std::max<size_t>(outb, 8)));
+            CK(cudaMalloc(&hb.flx, std::max<size_t>(outb, 8)));
+            hb.out_bytes = outb;
+        }
+        const double *srf_dev = nullptr;
+        if (!d->footprint) {
+            if (!srf_flx_host) return BLDFM_ERR_ARG;
+            const size_t sb = (size_t)d->nx * d->ny * sizeof(double);
+            if (sb > hb.srf_bytes) {
+                if (hb.srf) cudaFree(hb.srf);
+                hb.srf = nullptr;
+                CK(cudaMalloc(&hb.srf, sb));
+                hb.srf_bytes = sb;
+            }
+            CK(cudaMemcpyAsync(hb.srf, srf_flx_host, sb, cudaMemcpyHostToDevice, hb.stream));
+            srf_dev = hb.srf;
+        }
+        rc = solve_impl(d, srf_dev, z_host, prof_host, levels_host, nlvls, hb.conc, hb.flx, hb.ws, hb.ws_bytes,
+                        hb.stream);
+        if (rc != BLDFM_OK) return rc;
+        if (outb) {
+            CK(cudaMemcpyAsync(conc_host, hb.conc, outb, cudaMemcpyDeviceToHost, hb.stream));
+            CK(cudaMemcpyAsync(flx_host, hb.flx, outb, cudaMemcpyDeviceToHost, hb.stream));
+        }
+        int err = 0;
+        CK(cudaMemcpyAsync(&err, hb.ws, sizeof(int), cudaMemcpyDeviceToHost, hb.stream));
+        CK(cudaStreamSynchronize(hb.stream));
+        if (err != 0) return err == BLDFM_ERR_NONFINITE ? BLDFM_ERR_NONFINITE : BLDFM_ERR_TIMEOUT;
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases, const bldfm_batch_opts *opts, int64_t *workspace_bytes)
 {
-    std::lock_guard<std::mutex> lk(g_mutex);
-    if (!workspace_bytes) return BLDFM_ERR_ARG;
-    BatchBuild B;
-    int rc = batch_build(cases, ncases, opts, nullptr, B);
-    if (rc != BLDFM_OK) return rc;
-    *workspace_bytes = (int64_t)B.total;
-    return BLDFM_OK;
+    return guarded([&]() -> int {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        if (!workspace_bytes) return BLDFM_ERR_ARG;
+        BatchBuild B;
+        int rc = batch_build(cases, ncases, opts, nullptr, B);
+        if (rc != BLDFM_OK) return rc;
+        *workspace_bytes = (int64_t)B.total;
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch_opts *opts, void *workspace,
                       size_t workspace_bytes, void *stream)
 {
-    std::lock_guard<std::mutex> lk(g_mutex);
-    if (!workspace) return BLDFM_ERR_ARG;
-    if (((uintptr_t)workspace & 255) != 0) return BLDFM_ERR_ARG;
-    int status = BLDFM_OK;
-    DeviceCache &dc = cache_for_current(&status);
-    if (status != BLDFM_OK) return status;
-    BatchBuild B;
-    int rc = batch_build(cases, ncases, opts, &dc, B);
-    if (rc != BLDFM_OK) return rc;
-    if (workspace_bytes < B.total) return BLDFM_ERR_WORKSPACE;
-    cudaStream_t st = (cudaStream_t)stream;
-    char *ws = (char *)workspace;
-    const bool graph = opts && opts->use_graph && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
-    DeviceCache::Aux *aux = nullptr;
-    if ((rc = get_aux(dc, st, &aux)) != BLDFM_OK) return rc;
-    if (!graph) {
-        StageSlot *slt = nullptr;
-        if ((rc = acquire_stage(dc, B.blob_bytes + 256, &slt)) != BLDFM_OK) return rc;
-        batch_fill_blob(cases, ncases, B, ws, (char *)slt->buf);
-        timers_begin(dc);
-        if ((rc = batch_enqueue(cases, ncases, B, ws, slt->buf, st, dc.timing ? &dc : nullptr, aux)) != BLDFM_OK)
-            return rc;
-        CK(cudaEventRecord(slt->ev, st));
-        return BLDFM_OK;
-    }
-    // graph path: an instance whose previous replay has finished, else a new
-    // capture (up to two instances per topology), else wait for the oldest
-    std::vector<int64_t> key = batch_key(cases, ncases, B, ws);
-    auto &insts = dc.graphs[key];
-    DeviceCache::GraphInst *gi = nullptr;
-    for (auto &x : insts)
-        if (cudaEventQuery(x.done) == cudaSuccess) {
-            gi = &x;
-            break;
+    return guarded([&]() -> int {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        if (!workspace) return BLDFM_ERR_ARG;
+        if (((uintptr_t)workspace & 255) != 0) return BLDFM_ERR_ARG;
+        int status = BLDFM_OK;
+        DeviceCache &dc = cache_for_current(&status);
+        if (status != BLDFM_OK) return status;
+        BatchBuild B;
+        int rc = batch_build(cases, ncases, opts, &dc, B);
+        if (rc != BLDFM_OK) return rc;
+        if (workspace_bytes < B.total) return BLDFM_ERR_WORKSPACE;
+        cudaStream_t st = (cudaStream_t)stream;
+        char *ws = (char *)workspace;
+        const bool graph = opts && opts->use_graph && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+        DeviceCache::Aux *aux = nullptr;
+        if ((rc = get_aux(dc, st, &aux)) != BLDFM_OK) return rc;
+        if (!graph) {
+            StageSlot *slt = nullptr;
+            if ((rc = acquire_stage(dc, B.blob_bytes + 256, &slt)) != BLDFM_OK) return rc;
+            batch_fill_blob(cases, ncases, B, ws, (char *)slt->buf);
+            timers_begin(dc);
+            if ((rc = batch_enqueue(cases, ncases, B, ws, slt->buf, st, dc.timing ? &dc : nullptr, aux)) != BLDFM_OK)
+                return rc;
+            CK(cudaEventRecord(slt->ev, st));
+            return BLDFM_OK;
         }
-    if (!gi && insts.size() < 2) {
-        DeviceCache::GraphInst x;
-        if (cudaHostAlloc(&x.pinned, B.blob_bytes, cudaHostAllocDefault) != cudaSuccess) return BLDFM_ERR_CUDA;
-        x.bytes = B.blob_bytes;
-        CK(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
-        batch_fill_blob(cases, ncases, B, ws, (char *)x.pinned);
-        // capture the whole batch once; a failure leaves the stream usable
-        cudaGraph_t graph_h = nullptr;
-        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        rc = batch_enqueue(cases, ncases, B, ws, x.pinned, st, nullptr, aux);
-        cudaError_t ce = cudaStreamEndCapture(st, &graph_h);
-        if (rc != BLDFM_OK || ce != cudaSuccess) {
-            if (graph_h) cudaGraphDestroy(graph_h);
-            return rc != BLDFM_OK ? rc : BLDFM_ERR_CUDA;
+        // graph path: an instance whose previous replay has finished, else a new
+        // capture (up to two instances per topology), else wait for the oldest
+        std::vector<int64_t> key = batch_key(cases, ncases, B, ws);
+        auto &insts = dc.graphs[key];
+        DeviceCache::GraphInst *gi = nullptr;
+        for (auto &x : insts)
+            if (cudaEventQuery(x.done) == cudaSuccess) {
+                gi = &x;
+                break;
+            }
+        if (!gi && insts.size() < 2) {
+            DeviceCache::GraphInst x;
+            if (cudaHostAlloc(&x.pinned, B.blob_bytes, cudaHostAllocDefault) != cudaSuccess) return BLDFM_ERR_CUDA;
+            x.bytes = B.blob_bytes;
+            CK(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+            batch_fill_blob(cases, ncases, B, ws, (char *)x.pinned);
+            // capture the whole batch once; a failure leaves the stream usable
+            cudaGraph_t graph_h = nullptr;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            rc = batch_enqueue(cases, ncases, B, ws, x.pinned, st, nullptr, aux);
+            cudaError_t ce = cudaStreamEndCapture(st, &graph_h);
+            if (rc != BLDFM_OK || ce != cudaSuccess) {
+                if (graph_h) cudaGraphDestroy(graph_h);
+                return rc != BLDFM_OK ? rc : BLDFM_ERR_CUDA;
+            }
+            ce = cudaGraphInstantiate(&x.exec, graph_h, 0);
+            cudaGraphDestroy(graph_h);
+            if (ce != cudaSuccess) return BLDFM_ERR_CUDA;
+            CK(cudaGraphLaunch(x.exec, st));
+            CK(cudaEventRecord(x.done, st));
+            insts.push_back(x);
+            return BLDFM_OK;
         }
-        ce = cudaGraphInstantiate(&x.exec, graph_h, 0);
-        cudaGraphDestroy(graph_h);
-        if (ce != cudaSuccess) return BLDFM_ERR_CUDA;
-        CK(cudaGraphLaunch(x.exec, st));
-        CK(cudaEventRecord(x.done, st));
-        insts.push_back(x);
+        if (!gi) {
+            gi = &insts[0];
+            CK(cudaEventSynchronize(gi->done));
+        }
+        batch_fill_blob(cases, ncases, B, ws, (char *)gi->pinned);
+        CK(cudaGraphLaunch(gi->exec, st));
+        CK(cudaEventRecord(gi->done, st));
         return BLDFM_OK;
-    }
-    if (!gi) {
-        gi = &insts[0];
-        CK(cudaEventSynchronize(gi->done));
-    }
-    batch_fill_blob(cases, ncases, B, ws, (char *)gi->pinned);
-    CK(cudaGraphLaunch(gi->exec, st));
-    CK(cudaEventRecord(gi->done, st));
-    return BLDFM_OK;
+    });
 }
 
 int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls, int64_t *workspace_bytes)
 {
-    if (!workspace_bytes) return BLDFM_ERR_ARG;
-    int rc = sur_check_desc(d, nlvls);
-    if (rc != BLDFM_OK) return rc;
-    std::lock_guard<std::mutex> lk(g_mutex);
-    HostPlan hp;
-    if ((rc = make_plan(d, nullptr, nullptr, nullptr, nlvls, hp)) != BLDFM_OK) return rc;
-    *workspace_bytes = (int64_t)sur_layout(hp.g).total;
-    return BLDFM_OK;
+    return guarded([&]() -> int {
+        if (!workspace_bytes) return BLDFM_ERR_ARG;
+        int rc = sur_check_desc(d, nlvls);
+        if (rc != BLDFM_OK) return rc;
+        std::lock_guard<std::mutex> lk(g_mutex);
+        HostPlan hp;
+        if ((rc = make_plan(d, nullptr, nullptr, nullptr, nlvls, hp)) != BLDFM_OK) return rc;
+        *workspace_bytes = (int64_t)sur_layout(hp.g).total;
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_surrogate_solve(void *net, const bldfm_desc *d, const bldfm_surrogate_case *met, const double *z_host,
                           const double *prof_host, const int64_t *levels_host, int32_t nlvls, double *conc_dev,
                           double *flx_dev, void *workspace_dev, size_t workspace_bytes, void *stream)
 {
-    std::lock_guard<std::mutex> lk(g_mutex);
-    return sur_solve_impl(net, d, met, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
-                          workspace_bytes, (cudaStream_t)stream);
+    return guarded([&]() -> int {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        return sur_solve_impl(net, d, met, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
+                              workspace_bytes, (cudaStream_t)stream);
+    });
 }
 
 int bldfm_surrogate_batch_plan(const bldfm_case *cases, const bldfm_surrogate_case *mets, int32_t ncases,
                                int64_t *workspace_bytes)
 {
-    if (!workspace_bytes) return BLDFM_ERR_ARG;
-    int rc = sur_batch_check(cases, mets, ncases);
-    if (rc != BLDFM_OK) return rc;
-    std::lock_guard<std::mutex> lk(g_mutex);
-    BatchBuild B;
-    bldfm_batch_opts opts = {256, 0, 0, 0, 1};
-    if ((rc = batch_build(cases, ncases, &opts, nullptr, B, sur_extra_bytes(ncases))) != BLDFM_OK) return rc;
-    *workspace_bytes = (int64_t)(B.total + sur_guard_bytes(ncases));
-    return BLDFM_OK;
+    return guarded([&]() -> int {
+        if (!workspace_bytes) return BLDFM_ERR_ARG;
+        int rc = sur_batch_check(cases, mets, ncases);
+        if (rc != BLDFM_OK) return rc;
+        std::lock_guard<std::mutex> lk(g_mutex);
+        BatchBuild B;
+        bldfm_batch_opts opts = {256, 0, 0, 0, 1};
+        if ((rc = batch_build(cases, ncases, &opts, nullptr, B, sur_extra_bytes(ncases))) != BLDFM_OK) return rc;
+        *workspace_bytes = (int64_t)(B.total + sur_guard_bytes(ncases));
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_surrogate_solve_batch(void *net, const bldfm_case *cases, const bldfm_surrogate_case *mets,
                                 int32_t ncases, void *workspace, size_t workspace_bytes, void *stream)
 {
-    std::lock_guard<std::mutex> lk(g_mutex);
-    return sur_solve_batch_impl(net, cases, mets, ncases, workspace, workspace_bytes, (cudaStream_t)stream);
+    return guarded([&]() -> int {
+        std::lock_guard<std::mutex> lk(g_mutex);
+        return sur_solve_batch_impl(net, cases, mets, ncases, workspace, workspace_bytes, (cudaStream_t)stream);
+    });
 }
 
 }  // extern "C"

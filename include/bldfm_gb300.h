@@ -44,6 +44,8 @@ extern "C" {
 #define BLDFM_ERR_NONFINITE -10      /* non-finite values detected in the output */
 #define BLDFM_ERR_PROFILE -11        /* z not strictly increasing, a non-finite z or profile value,
                                         Kz <= 0 or Kx, Ky < 0 (checked on the host before any work) */
+#define BLDFM_ERR_HOST -12           /* host-side failure: memory allocation or thread start (a C++
+                                        exception inside the library, caught at the entry point) */
 
 /* ---- descriptor -------------------------------------------------------- */
 #define BLDFM_PREC_SINGLE 0 /* reference precision="single": spectra stored as complex64 */

@@ -144,6 +144,9 @@ def test_status_strings_name_every_code():
     codes = [getattr(_lib, n) for n in dir(_lib) if n.startswith("ERR_")]
     names = {lib.bldfm_status_str(c).decode() for c in codes}
     assert "unknown status" not in names and len(names) == len(codes)
+    # a C++ exception inside the library (host allocation) arrives as a status
+    with pytest.raises(MemoryError, match="host-side failure"):
+        _lib.check(_lib.ERR_HOST)
 
 
 def test_batch_plan_reports_the_first_failing_case():
