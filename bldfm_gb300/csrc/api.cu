@@ -22,6 +22,7 @@
 #include "batch.h"
 #include "common.h"
 #include "geometry.h"
+#include "guard.h"
 #include "host_exact.h"
 #include "kernels.h"
 #include "serve.h"
@@ -943,7 +944,8 @@ int batch_build(const bldfm_case *cs, int n, const bldfm_batch_opts *opts, Devic
     if (!dc) return BLDFM_OK;
     // persistent sweep grid
     int per_sm = (opts && opts->ctas_per_sm > 0) ? opts->ctas_per_sm : batch_sweep_occupancy(B.threads, B.sweep_smem);
-    B.G = (int)std::min<int64_t>(std::min<int64_t>((int64_t)dc->nsm * per_sm, BATCH_MAX_CTAS), std::max<int64_t>(B.ntiles, 1));
+    B.G = (int)std::min<int64_t>(std::min<int64_t>((int64_t)dc->nsm * per_sm, BATCH_MAX_CTAS),
+                                 std::max<int64_t>(B.ntiles, 1));
     B.ml.resize(n);
     B.twxo.resize(n);
     B.twyo.resize(n);
@@ -1479,8 +1481,9 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
     tmark(dc, st);  // 3: the accuracy guard
     float4 *acc = (float4 *)(w + B.total);
     CK(cudaMemsetAsync(acc, 0, 16 * (size_t)n, st));
-    CK(launch_sur_guard((const BatchCase *)(wb + B.off_cases), n, (const int64_t *)(wb + B.extra_off + sur_prefix_off(n)),
-                        prefix[n], SUR_GUARD_STRIDE, lb_maxnz, acc, st));
+    CK(launch_sur_guard((const BatchCase *)(wb + B.off_cases), n,
+                        (const int64_t *)(wb + B.extra_off + sur_prefix_off(n)), prefix[n], SUR_GUARD_STRIDE, lb_maxnz,
+                        acc, st));
     tmark(dc, st);  // 4: the output transform
     BatchLaunch bl;
     memset(&bl, 0, sizeof(bl));
@@ -1515,18 +1518,6 @@ int sur_solve_batch_impl(void *net, const bldfm_case *cs, const bldfm_surrogate_
 // ---------------------------------------------------------------------------
 // exported entry points
 // ---------------------------------------------------------------------------
-// A C++ exception of the host side (std::bad_alloc while planning, a thread
-// that cannot be started) ends at the C boundary as a status.
-template <class F>
-static int guarded(F &&f)
-{
-    try {
-        return f();
-    } catch (...) {
-        return BLDFM_ERR_HOST;
-    }
-}
-
 extern "C" {
 
 const char *bldfm_status_str(int s)
@@ -1636,7 +1627,7 @@ int bldfm_fma_peak(int kind, double *flops_per_s, void *stream)
 
 int bldfm_plan(const bldfm_desc *d, int nlvls, bldfm_plan_info *out)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         if (!out) return BLDFM_ERR_ARG;
         HostPlan hp;
         int rc = make_plan(d, nullptr, nullptr, nullptr, nlvls, hp);
@@ -1664,7 +1655,7 @@ int bldfm_solve(const bldfm_desc *d, const double *srf_flx_dev, const double *z_
                 const int64_t *levels_host, int32_t nlvls, double *conc_dev, double *flx_dev, void *workspace_dev,
                 size_t workspace_bytes, void *stream)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         std::lock_guard<std::mutex> lk(g_mutex);
         return solve_impl(d, srf_flx_dev, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
                           workspace_bytes, (cudaStream_t)stream);
@@ -1674,7 +1665,7 @@ int bldfm_solve(const bldfm_desc *d, const double *srf_flx_dev, const double *z_
 int bldfm_solve_host(const bldfm_desc *d, const double *srf_flx_host, const double *z_host, const double *prof_host,
                      const int64_t *levels_host, int32_t nlvls, double *conc_host, double *flx_host)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         std::lock_guard<std::mutex> lk(g_mutex);
         if (!d || !conc_host || !flx_host) return BLDFM_ERR_ARG;
         bldfm_plan_info pi;
@@ -1737,7 +1728,7 @@ int bldfm_solve_host(const bldfm_desc *d, const double *srf_flx_host, const doub
 
 int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases, const bldfm_batch_opts *opts, int64_t *workspace_bytes)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         std::lock_guard<std::mutex> lk(g_mutex);
         if (!workspace_bytes) return BLDFM_ERR_ARG;
         BatchBuild B;
@@ -1751,7 +1742,7 @@ int bldfm_batch_plan(const bldfm_case *cases, int32_t ncases, const bldfm_batch_
 int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch_opts *opts, void *workspace,
                       size_t workspace_bytes, void *stream)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         std::lock_guard<std::mutex> lk(g_mutex);
         if (!workspace) return BLDFM_ERR_ARG;
         if (((uintptr_t)workspace & 255) != 0) return BLDFM_ERR_ARG;
@@ -1764,7 +1755,8 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch
         if (workspace_bytes < B.total) return BLDFM_ERR_WORKSPACE;
         cudaStream_t st = (cudaStream_t)stream;
         char *ws = (char *)workspace;
-        const bool graph = opts && opts->use_graph && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+        const bool graph =
+            opts && opts->use_graph && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
         DeviceCache::Aux *aux = nullptr;
         if ((rc = get_aux(dc, st, &aux)) != BLDFM_OK) return rc;
         if (!graph) {
@@ -1823,7 +1815,7 @@ int bldfm_solve_batch(const bldfm_case *cases, int32_t ncases, const bldfm_batch
 
 int bldfm_surrogate_plan(const bldfm_desc *d, int32_t nlvls, int64_t *workspace_bytes)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         if (!workspace_bytes) return BLDFM_ERR_ARG;
         int rc = sur_check_desc(d, nlvls);
         if (rc != BLDFM_OK) return rc;
@@ -1839,7 +1831,7 @@ int bldfm_surrogate_solve(void *net, const bldfm_desc *d, const bldfm_surrogate_
                           const double *prof_host, const int64_t *levels_host, int32_t nlvls, double *conc_dev,
                           double *flx_dev, void *workspace_dev, size_t workspace_bytes, void *stream)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         std::lock_guard<std::mutex> lk(g_mutex);
         return sur_solve_impl(net, d, met, z_host, prof_host, levels_host, nlvls, conc_dev, flx_dev, workspace_dev,
                               workspace_bytes, (cudaStream_t)stream);
@@ -1849,7 +1841,7 @@ int bldfm_surrogate_solve(void *net, const bldfm_desc *d, const bldfm_surrogate_
 int bldfm_surrogate_batch_plan(const bldfm_case *cases, const bldfm_surrogate_case *mets, int32_t ncases,
                                int64_t *workspace_bytes)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         if (!workspace_bytes) return BLDFM_ERR_ARG;
         int rc = sur_batch_check(cases, mets, ncases);
         if (rc != BLDFM_OK) return rc;
@@ -1865,7 +1857,7 @@ int bldfm_surrogate_batch_plan(const bldfm_case *cases, const bldfm_surrogate_ca
 int bldfm_surrogate_solve_batch(void *net, const bldfm_case *cases, const bldfm_surrogate_case *mets,
                                 int32_t ncases, void *workspace, size_t workspace_bytes, void *stream)
 {
-    return guarded([&]() -> int {
+    return bldfm_guarded([&]() -> int {
         std::lock_guard<std::mutex> lk(g_mutex);
         return sur_solve_batch_impl(net, cases, mets, ncases, workspace, workspace_bytes, (cudaStream_t)stream);
     });

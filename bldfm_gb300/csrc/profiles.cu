@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/bldfm_gb300.h"
+#include "guard.h"
 #include "profiles.h"
 
 namespace {
@@ -164,34 +165,36 @@ extern "C" int bldfm_vertical_profiles_batch(int32_t ncases, const bldfm_profile
                                              int64_t *zoff_out, size_t *ws_bytes_out, double *z_dev,
                                              double *prof_dev, void *ws_dev, size_t ws_bytes, void *stream)
 {
-    if (ncases < 1 || !params || !nz_out || !zoff_out) return BLDFM_ERR_ARG;
-    std::vector<ProfileCase> pcs((size_t)ncases);
-    std::vector<int64_t> zoff((size_t)ncases);
-    int64_t total = 0;
-    for (int k = 0; k < ncases; ++k) {
-        const bldfm_profile_params &a = params[k];
-        const int rc = profile_scalars(a.n, a.meas_height, a.um, a.vm, a.ustar, a.z0, a.mol, a.prsc, a.closure,
-                                       a.domain_height, a.stretch, a.tke, &pcs[(size_t)k]);
-        if (rc != BLDFM_OK) return rc;
-        nz_out[k] = pcs[(size_t)k].nz;
-        zoff[(size_t)k] = zoff_out[k] = total;
-        total += pcs[(size_t)k].nz;
-    }
-    const size_t table = ((sizeof(ProfileCase) * (size_t)ncases + 255) & ~(size_t)255);
-    const size_t need = table + sizeof(int64_t) * (size_t)ncases;
-    if (ws_bytes_out) *ws_bytes_out = need;
-    if (!z_dev) return BLDFM_OK;
-    if (!prof_dev || !ws_dev || ws_bytes < need || ((uintptr_t)ws_dev & 15)) return BLDFM_ERR_ARG;
-    cudaStream_t st = (cudaStream_t)stream;
-    char *w = (char *)ws_dev;
-    // pageable sources: the copies have read them when the calls return
-    if (cudaMemcpyAsync(w, pcs.data(), sizeof(ProfileCase) * (size_t)ncases, cudaMemcpyHostToDevice, st) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(w + table, zoff.data(), sizeof(int64_t) * (size_t)ncases, cudaMemcpyHostToDevice, st) !=
+    return bldfm_guarded([&]() -> int {
+        if (ncases < 1 || !params || !nz_out || !zoff_out) return BLDFM_ERR_ARG;
+        std::vector<ProfileCase> pcs((size_t)ncases);
+        std::vector<int64_t> zoff((size_t)ncases);
+        int64_t total = 0;
+        for (int k = 0; k < ncases; ++k) {
+            const bldfm_profile_params &a = params[k];
+            const int rc = profile_scalars(a.n, a.meas_height, a.um, a.vm, a.ustar, a.z0, a.mol, a.prsc, a.closure,
+                                           a.domain_height, a.stretch, a.tke, &pcs[(size_t)k]);
+            if (rc != BLDFM_OK) return rc;
+            nz_out[k] = pcs[(size_t)k].nz;
+            zoff[(size_t)k] = zoff_out[k] = total;
+            total += pcs[(size_t)k].nz;
+        }
+        const size_t table = ((sizeof(ProfileCase) * (size_t)ncases + 255) & ~(size_t)255);
+        const size_t need = table + sizeof(int64_t) * (size_t)ncases;
+        if (ws_bytes_out) *ws_bytes_out = need;
+        if (!z_dev) return BLDFM_OK;
+        if (!prof_dev || !ws_dev || ws_bytes < need || ((uintptr_t)ws_dev & 15)) return BLDFM_ERR_ARG;
+        cudaStream_t st = (cudaStream_t)stream;
+        char *w = (char *)ws_dev;
+        // pageable sources: the copies have read them when the calls return
+        if (cudaMemcpyAsync(w, pcs.data(), sizeof(ProfileCase) * (size_t)ncases, cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(w + table, zoff.data(), sizeof(int64_t) * (size_t)ncases, cudaMemcpyHostToDevice, st) !=
+                cudaSuccess)
+            return BLDFM_ERR_CUDA;
+        if (launch_profiles_batch((const ProfileCase *)w, (const int64_t *)(w + table), ncases, z_dev, prof_dev, st) !=
             cudaSuccess)
-        return BLDFM_ERR_CUDA;
-    if (launch_profiles_batch((const ProfileCase *)w, (const int64_t *)(w + table), ncases, z_dev, prof_dev, st) !=
-        cudaSuccess)
-        return BLDFM_ERR_CUDA;
-    return BLDFM_OK;
+            return BLDFM_ERR_CUDA;
+        return BLDFM_OK;
+    });
 }

@@ -7,10 +7,12 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <vector>
 
 #include "../../include/bldfm_gb300.h"
 #include "common.h"
+#include "guard.h"
 #include "mlp_common.cuh"
 #include "profiles.h"
 #include "surrogate_phys.cuh"
@@ -51,38 +53,41 @@ struct StoreF32 {
 // core path against a reference GEMM; allocates its own device buffers.
 extern "C" int bldfm_tc_gemm_check(const uint16_t *A, const uint16_t *B, float *D, int32_t M, int32_t K)
 {
-    if (!A || !B || !D || M <= 0 || K <= 0 || M % 128 != 0 || K % 16 != 0) return BLDFM_ERR_ARG;
-    int KC = K <= 256 ? K : 256;
-    if (K % KC != 0) return BLDFM_ERR_ARG;
-    std::vector<uint16_t> Ab, Bb;
-    host_block(A, M, K, 128, KC, Ab);
-    host_block(B, 256, K, 256, KC, Bb);
-    uint16_t *dA = nullptr, *dB = nullptr;
-    float *dD = nullptr;
-    int *derr = nullptr;
-    int rc = BLDFM_OK;
-    if (cudaMalloc(&dA, Ab.size() * 2) != cudaSuccess || cudaMalloc(&dB, Bb.size() * 2) != cudaSuccess ||
-        cudaMalloc(&dD, (size_t)M * 256 * 4) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess)
-        rc = BLDFM_ERR_CUDA;
-    if (rc == BLDFM_OK) {
-        cudaMemcpy(dA, Ab.data(), Ab.size() * 2, cudaMemcpyHostToDevice);
-        cudaMemcpy(dB, Bb.data(), Bb.size() * 2, cudaMemcpyHostToDevice);
-        cudaMemset(derr, 0, 4);
-        const size_t smem = tc_gemm_smem(KC);
-        cudaFuncSetAttribute(tc_gemm_kernel<StoreF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        StoreF32 epi{dD, 256};
-        tc_gemm_kernel<StoreF32><<<M / 128, 128, smem>>>(dA, dB, K, KC, epi, derr);
-        int herr = 0;
-        if (cudaDeviceSynchronize() != cudaSuccess) rc = BLDFM_ERR_CUDA;
-        if (rc == BLDFM_OK && cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = BLDFM_ERR_CUDA;
-        if (rc == BLDFM_OK && herr != 0) rc = BLDFM_ERR_TIMEOUT;
-        if (rc == BLDFM_OK) cudaMemcpy(D, dD, (size_t)M * 256 * 4, cudaMemcpyDeviceToHost);
-    }
-    cudaFree(dA);
-    cudaFree(dB);
-    cudaFree(dD);
-    cudaFree(derr);
-    return rc;
+    return bldfm_guarded([&]() -> int {
+        if (!A || !B || !D || M <= 0 || K <= 0 || M % 128 != 0 || K % 16 != 0) return BLDFM_ERR_ARG;
+        int KC = K <= 256 ? K : 256;
+        if (K % KC != 0) return BLDFM_ERR_ARG;
+        std::vector<uint16_t> Ab, Bb;
+        host_block(A, M, K, 128, KC, Ab);
+        host_block(B, 256, K, 256, KC, Bb);
+        uint16_t *dA = nullptr, *dB = nullptr;
+        float *dD = nullptr;
+        int *derr = nullptr;
+        int rc = BLDFM_OK;
+        if (cudaMalloc(&dA, Ab.size() * 2) != cudaSuccess || cudaMalloc(&dB, Bb.size() * 2) != cudaSuccess ||
+            cudaMalloc(&dD, (size_t)M * 256 * 4) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess)
+            rc = BLDFM_ERR_CUDA;
+        if (rc == BLDFM_OK) {
+            cudaMemcpy(dA, Ab.data(), Ab.size() * 2, cudaMemcpyHostToDevice);
+            cudaMemcpy(dB, Bb.data(), Bb.size() * 2, cudaMemcpyHostToDevice);
+            cudaMemset(derr, 0, 4);
+            const size_t smem = tc_gemm_smem(KC);
+            cudaFuncSetAttribute(tc_gemm_kernel<StoreF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            StoreF32 epi{dD, 256};
+            tc_gemm_kernel<StoreF32><<<M / 128, 128, smem>>>(dA, dB, K, KC, epi, derr);
+            int herr = 0;
+            if (cudaDeviceSynchronize() != cudaSuccess) rc = BLDFM_ERR_CUDA;
+            if (rc == BLDFM_OK && cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = BLDFM_ERR_CUDA;
+            if (rc == BLDFM_OK && herr != 0) rc = BLDFM_ERR_TIMEOUT;
+            if (rc == BLDFM_OK) cudaMemcpy(D, dD, (size_t)M * 256 * 4, cudaMemcpyDeviceToHost);
+        }
+        cudaFree(dA);
+        cudaFree(dB);
+        cudaFree(dD);
+        cudaFree(derr);
+        return rc;
+    });
 }
 
 // ===========================================================================
@@ -458,16 +463,22 @@ struct Mlp {
     uint16_t *dZrows[3] = {}, *dZT[3] = {};  // index j-2 for dZ_j, j = 2..4
     float *dZ1 = nullptr, *Y = nullptr, *loss = nullptr;
     int *err = nullptr;
-    std::vector<void *> allocs;
+    std::vector<void *> allocs;  // every device allocation, freed with the object
+    Mlp() = default;
+    Mlp(const Mlp &) = delete;
+    Mlp &operator=(const Mlp &) = delete;
+    ~Mlp()
+    {
+        for (void *p : allocs) cudaFree(p);
+    }
 };
 
 template <typename T>
 bool mlp_alloc(Mlp &M, T **p, size_t count)
 {
-    void *q = nullptr;
-    if (cudaMalloc(&q, count * sizeof(T)) != cudaSuccess) return false;
-    M.allocs.push_back(q);
-    *p = (T *)q;
+    M.allocs.push_back(nullptr);  // may throw: nothing is held yet
+    if (cudaMalloc(&M.allocs.back(), count * sizeof(T)) != cudaSuccess) return false;
+    *p = (T *)M.allocs.back();
     return true;
 }
 
@@ -482,11 +493,7 @@ WBlocks mlp_blocks(const Mlp &M)
     return b;
 }
 
-void mlp_free(Mlp *M)
-{
-    for (void *p : M->allocs) cudaFree(p);
-    delete M;
-}
+void mlp_free(Mlp *M) { delete M; }
 
 template <class Epi>
 cudaError_t gemm(const uint16_t *A, const uint16_t *Bop, int tiles, int K, int splits, Epi epi, int *err,
@@ -534,48 +541,45 @@ extern "C" {
 
 int bldfm_surrogate_create(int32_t batch, uint64_t seed, void **handle)
 {
-    if (!handle || batch < 256 || batch % 256 != 0) return BLDFM_ERR_ARG;
-    Mlp *M = new Mlp();
-    M->B = batch;
-    const size_t B = (size_t)batch;
-    bool ok = mlp_alloc(*M, &M->P, MLP_NPARAM) && mlp_alloc(*M, &M->G, MLP_NPARAM) &&
-              mlp_alloc(*M, &M->m, MLP_NPARAM) && mlp_alloc(*M, &M->v, MLP_NPARAM) &&
-              mlp_alloc(*M, &M->H4, B * MLP_H) && mlp_alloc(*M, &M->dZ1, B * MLP_H) &&
-              mlp_alloc(*M, &M->Y, B * MLP_OUT) && mlp_alloc(*M, &M->loss, 1) && mlp_alloc(*M, &M->err, 1);
-    for (int j = 0; j < 3 && ok; ++j)
-        ok = mlp_alloc(*M, &M->Wt[j], (size_t)MLP_H * MLP_H) && mlp_alloc(*M, &M->W[j], (size_t)MLP_H * MLP_H) &&
-             mlp_alloc(*M, &M->Wq[j], (size_t)MLP_H * MLP_H) &&
-             mlp_alloc(*M, &M->Hrows[j], B * MLP_H) && mlp_alloc(*M, &M->HT[j], B * MLP_H) &&
-             mlp_alloc(*M, &M->dZrows[j], B * MLP_H) && mlp_alloc(*M, &M->dZT[j], B * MLP_H);
-    for (int j = 0; j < 4 && ok; ++j) ok = mlp_alloc(*M, &M->Gz[j], B * MLP_H);
-    if (!ok) {
-        mlp_free(M);
-        return BLDFM_ERR_CUDA;
-    }
-    // He-scaled normal weights (Box-Muller on a 64-bit LCG), zero biases
-    std::vector<float> p(MLP_NPARAM, 0.f);
-    uint64_t s = seed * 6364136223846793005ULL + 1442695040888963407ULL;
-    auto unif = [&]() {
-        s = s * 6364136223846793005ULL + 1442695040888963407ULL;
-        return ((s >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-    };
-    auto normal = [&]() { return sqrt(-2.0 * log(unif())) * cos(6.283185307179586 * unif()); };
-    for (int i = 0; i < MLP_IN * MLP_H; ++i) p[MLP_OFF_W0 + i] = (float)(normal() * sqrt(2.0 / MLP_IN));
-    for (int j = 1; j <= 3; ++j)
-        for (int i = 0; i < MLP_H * MLP_H; ++i) p[MLP_OFF_WT(j) + i] = (float)(normal() * sqrt(2.0 / MLP_H));
-    for (int i = 0; i < MLP_H * MLP_OUT; ++i) p[MLP_OFF_W4 + i] = (float)(normal() * sqrt(1.0 / MLP_H));
-    cudaMemcpy(M->P, p.data(), MLP_NPARAM * 4, cudaMemcpyHostToDevice);
-    cudaMemset(M->m, 0, MLP_NPARAM * 4);
-    cudaMemset(M->v, 0, MLP_NPARAM * 4);
-    cudaMemset(M->G, 0, MLP_NPARAM * 4);
-    cudaMemset(M->err, 0, 4);
-    weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, mlp_blocks(*M));
-    if (cudaDeviceSynchronize() != cudaSuccess) {
-        mlp_free(M);
-        return BLDFM_ERR_CUDA;
-    }
-    *handle = M;
-    return BLDFM_OK;
+    return bldfm_guarded([&]() -> int {
+        if (!handle || batch < 256 || batch % 256 != 0) return BLDFM_ERR_ARG;
+        std::unique_ptr<Mlp> own(new Mlp());  // freed on every early return
+        Mlp *M = own.get();
+        M->B = batch;
+        const size_t B = (size_t)batch;
+        bool ok = mlp_alloc(*M, &M->P, MLP_NPARAM) && mlp_alloc(*M, &M->G, MLP_NPARAM) &&
+                  mlp_alloc(*M, &M->m, MLP_NPARAM) && mlp_alloc(*M, &M->v, MLP_NPARAM) &&
+                  mlp_alloc(*M, &M->H4, B * MLP_H) && mlp_alloc(*M, &M->dZ1, B * MLP_H) &&
+                  mlp_alloc(*M, &M->Y, B * MLP_OUT) && mlp_alloc(*M, &M->loss, 1) && mlp_alloc(*M, &M->err, 1);
+        for (int j = 0; j < 3 && ok; ++j)
+            ok = mlp_alloc(*M, &M->Wt[j], (size_t)MLP_H * MLP_H) && mlp_alloc(*M, &M->W[j], (size_t)MLP_H * MLP_H) &&
+                 mlp_alloc(*M, &M->Wq[j], (size_t)MLP_H * MLP_H) &&
+                 mlp_alloc(*M, &M->Hrows[j], B * MLP_H) && mlp_alloc(*M, &M->HT[j], B * MLP_H) &&
+                 mlp_alloc(*M, &M->dZrows[j], B * MLP_H) && mlp_alloc(*M, &M->dZT[j], B * MLP_H);
+        for (int j = 0; j < 4 && ok; ++j) ok = mlp_alloc(*M, &M->Gz[j], B * MLP_H);
+        if (!ok) return BLDFM_ERR_CUDA;
+        // He-scaled normal weights (Box-Muller on a 64-bit LCG), zero biases
+        std::vector<float> p(MLP_NPARAM, 0.f);
+        uint64_t s = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+        auto unif = [&]() {
+            s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+            return ((s >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        };
+        auto normal = [&]() { return sqrt(-2.0 * log(unif())) * cos(6.283185307179586 * unif()); };
+        for (int i = 0; i < MLP_IN * MLP_H; ++i) p[MLP_OFF_W0 + i] = (float)(normal() * sqrt(2.0 / MLP_IN));
+        for (int j = 1; j <= 3; ++j)
+            for (int i = 0; i < MLP_H * MLP_H; ++i) p[MLP_OFF_WT(j) + i] = (float)(normal() * sqrt(2.0 / MLP_H));
+        for (int i = 0; i < MLP_H * MLP_OUT; ++i) p[MLP_OFF_W4 + i] = (float)(normal() * sqrt(1.0 / MLP_H));
+        cudaMemcpy(M->P, p.data(), MLP_NPARAM * 4, cudaMemcpyHostToDevice);
+        cudaMemset(M->m, 0, MLP_NPARAM * 4);
+        cudaMemset(M->v, 0, MLP_NPARAM * 4);
+        cudaMemset(M->G, 0, MLP_NPARAM * 4);
+        cudaMemset(M->err, 0, 4);
+        weights_to_blocks_kernel<<<dim3(MLP_H * MLP_H / 256, 3), 256>>>(M->P, mlp_blocks(*M));
+        if (cudaDeviceSynchronize() != cudaSuccess) return BLDFM_ERR_CUDA;
+        *handle = own.release();
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_surrogate_destroy(void *handle)
@@ -699,6 +703,14 @@ struct TransferPool {
     TransferCase *cases = nullptr;  // device
     float4 *steps = nullptr;        // device [case][lmax]: (h~, K~, U~, 0) of step i
     std::vector<TransferCase> host_cases;
+    TransferPool() = default;
+    TransferPool(const TransferPool &) = delete;
+    TransferPool &operator=(const TransferPool &) = delete;
+    ~TransferPool()
+    {
+        cudaFree(cases);
+        cudaFree(steps);
+    }
 };
 
 // counter-based uniform in (0, 1): splitmix64 of (seed, index, stream)
@@ -795,54 +807,47 @@ extern "C" {
 
 int bldfm_transfer_pool_create(const double *s1, const double *s2, int32_t ncases, int32_t n, void **pool)
 {
-    if (!s1 || !s2 || ncases < 1 || n < 2 || !pool) return BLDFM_ERR_ARG;
-    TransferPool *P = new TransferPool();
-    P->ncases = ncases;
-    P->n = n;
-    std::vector<std::vector<float4>> st(ncases);
-    P->host_cases.resize(ncases);
-    for (int c = 0; c < ncases; ++c) {
-        // z_m = 1 and unit wind at z_m: z0 = exp(-s2), L = 1 / s1, u* from the log-law
-        const double mol = fabs(s1[c]) < 1e-12 ? 1e12 : 1.0 / s1[c];
-        ProfileCase pc;
-        const int rc = profile_scalars(n, 1.0, 1.0, 0.0, -1.0, exp(-s2[c]), mol, 1.0, 0, -1.0, -1.0, -1.0, &pc);
-        if (rc != BLDFM_OK || pc.nz > BLDFM_MAX_NZ) {
-            delete P;
-            return rc != BLDFM_OK ? rc : BLDFM_ERR_UNSUPPORTED;
+    return bldfm_guarded([&]() -> int {
+        if (!s1 || !s2 || ncases < 1 || n < 2 || !pool) return BLDFM_ERR_ARG;
+        std::unique_ptr<TransferPool> own(new TransferPool());  // freed on every early return
+        TransferPool *P = own.get();
+        P->ncases = ncases;
+        P->n = n;
+        std::vector<std::vector<float4>> st(ncases);
+        P->host_cases.resize(ncases);
+        for (int c = 0; c < ncases; ++c) {
+            // z_m = 1 and unit wind at z_m: z0 = exp(-s2), L = 1 / s1, u* from the log-law
+            const double mol = fabs(s1[c]) < 1e-12 ? 1e12 : 1.0 / s1[c];
+            ProfileCase pc;
+            const int rc = profile_scalars(n, 1.0, 1.0, 0.0, -1.0, exp(-s2[c]), mol, 1.0, 0, -1.0, -1.0, -1.0, &pc);
+            if (rc != BLDFM_OK || pc.nz > BLDFM_MAX_NZ) return rc != BLDFM_OK ? rc : BLDFM_ERR_UNSUPPORTED;
+            std::vector<double> z(pc.nz), prof(5 * (size_t)pc.nz);
+            profile_levels_host(pc, z.data(), prof.data());
+            TransferCase &tc = P->host_cases[c];
+            tc.nz = pc.nz;
+            tc.jm = n;
+            tc.ktop = (float)prof[4 * (size_t)pc.nz + pc.nz - 1];
+            tc.utop = (float)prof[pc.nz - 1];
+            tc.s1 = (float)s1[c];
+            tc.s2 = (float)s2[c];
+            tc.s3 = (float)pc.ustar;
+            tc.pad = 0;
+            st[c].resize(pc.nz - 1);
+            surrogate_steps_from_profiles(pc.nz, z.data(), prof.data(), 1.0, 1.0, 1.0, 0.0, st[c].data());
+            P->lmax = std::max(P->lmax, pc.nz - 1);
         }
-        std::vector<double> z(pc.nz), prof(5 * (size_t)pc.nz);
-        profile_levels_host(pc, z.data(), prof.data());
-        TransferCase &tc = P->host_cases[c];
-        tc.nz = pc.nz;
-        tc.jm = n;
-        tc.ktop = (float)prof[4 * (size_t)pc.nz + pc.nz - 1];
-        tc.utop = (float)prof[pc.nz - 1];
-        tc.s1 = (float)s1[c];
-        tc.s2 = (float)s2[c];
-        tc.s3 = (float)pc.ustar;
-        tc.pad = 0;
-        st[c].resize(pc.nz - 1);
-        surrogate_steps_from_profiles(pc.nz, z.data(), prof.data(), 1.0, 1.0, 1.0, 0.0, st[c].data());
-        P->lmax = std::max(P->lmax, pc.nz - 1);
-    }
-    std::vector<float4> flat((size_t)ncases * P->lmax, make_float4(0.f, 1.f, 0.f, 0.f));
-    for (int c = 0; c < ncases; ++c) std::copy(st[c].begin(), st[c].end(), flat.begin() + (size_t)c * P->lmax);
-    if (cudaMalloc(&P->cases, sizeof(TransferCase) * ncases) != cudaSuccess ||
-        cudaMalloc(&P->steps, sizeof(float4) * flat.size()) != cudaSuccess) {
-        cudaFree(P->cases);
-        delete P;
-        return BLDFM_ERR_CUDA;
-    }
-    if (cudaMemcpy(P->cases, P->host_cases.data(), sizeof(TransferCase) * ncases, cudaMemcpyHostToDevice) !=
-            cudaSuccess ||
-        cudaMemcpy(P->steps, flat.data(), sizeof(float4) * flat.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaFree(P->cases);
-        cudaFree(P->steps);
-        delete P;
-        return BLDFM_ERR_CUDA;
-    }
-    *pool = P;
-    return BLDFM_OK;
+        std::vector<float4> flat((size_t)ncases * P->lmax, make_float4(0.f, 1.f, 0.f, 0.f));
+        for (int c = 0; c < ncases; ++c) std::copy(st[c].begin(), st[c].end(), flat.begin() + (size_t)c * P->lmax);
+        if (cudaMalloc(&P->cases, sizeof(TransferCase) * ncases) != cudaSuccess ||
+            cudaMalloc(&P->steps, sizeof(float4) * flat.size()) != cudaSuccess)
+            return BLDFM_ERR_CUDA;
+        if (cudaMemcpy(P->cases, P->host_cases.data(), sizeof(TransferCase) * ncases, cudaMemcpyHostToDevice) !=
+                cudaSuccess ||
+            cudaMemcpy(P->steps, flat.data(), sizeof(float4) * flat.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return BLDFM_ERR_CUDA;
+        *pool = own.release();
+        return BLDFM_OK;
+    });
 }
 
 int bldfm_transfer_pool_destroy(void *pool)
@@ -850,8 +855,6 @@ int bldfm_transfer_pool_destroy(void *pool)
     TransferPool *P = (TransferPool *)pool;
     if (!P) return BLDFM_ERR_ARG;
     cudaDeviceSynchronize();
-    cudaFree(P->cases);
-    cudaFree(P->steps);
     delete P;
     return BLDFM_OK;
 }
