@@ -495,7 +495,11 @@ using Z512 = rx::Shape<8, 8, 8>;
 // CTAs per SM.  The column pass stays one line per group: the same pass with
 // two band columns per group in FP32x2 lanes (zoom_line<S, C2>, four staged
 // columns per group, 128 registers, 2 CTAs per SM instead of 3) made both
-// passes 0.0978 against 0.0951 ms per 16 footprints (CUDA events).
+// passes 0.0978 against 0.0951 ms per 16 footprints (CUDA events).  The three
+// twisted transforms run side by side: one after another through a third of
+// the exchange buffer (64 registers, 4 CTAs per SM, three times the named
+// barriers, kept rows written as they form) measured 5.94 against 5.98 us per
+// footprint for both passes, within noise.
 template <class S>
 size_t rz_smem_of()
 {
