@@ -804,7 +804,7 @@ def main():
     # oracle checks and the long sections, so that it sees the process state
     # a user's process has (the CPU checks and the 10k-step serving run leave
     # busy host threads and a large heap behind); the median of three passes ---
-    from bldfm_gb300.batch import solve_stream
+    from bldfm_gb300.batch import solve_stream, stream_depth
 
     esolver = BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
     e2e_steps = max(2, min(args.steps, 300))
@@ -814,12 +814,14 @@ def main():
     for i in range(e2e_steps):
         solve_batch(kwb[i % NB], solver=esolver)
     e2e_sync = world * B * e2e_steps / (time.perf_counter() - t)
-    # the pipelined timeseries API over the same steps (four solvers take the steps in turn)
+    # the pipelined timeseries API over the same steps: its default number of
+    # solvers (batches in flight) take the steps in turn
+    depth = stream_depth(kwb[0])
     ssolvers = tuple(BatchSolver(threads=threads, ctas_per_sm=per_sm, use_graph=True, xform_lines=xlines)
-                     for _ in range(4))
-    # warm: graphs of both solvers and the pinned host blocks a consumer that
+                     for _ in range(depth))
+    # warm: graphs of every solver and the pinned host blocks a consumer that
     # holds one result while the next is produced keeps alive
-    warm = list(solve_stream([kwb[i % NB] for i in range(8)], solvers=ssolvers))
+    warm = list(solve_stream([kwb[i % NB] for i in range(2 * depth)], solvers=ssolvers))
     del warm
     e2e_passes = []
     for _ in range(3):
@@ -978,8 +980,8 @@ def main():
                      "frac": (achieved64 / (peak64.value / 1e12)) if achieved64 else None},
             "e2e": {"value": e2e_fps, "unit": "footprints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "api": "bldfm_gb300.batch.solve_stream over the timed steps (numpy in, numpy out, "
-                           "pinned copies inside, each step's arrays fresh; four solvers in turn); median of "
-                           "three passes of %d steps" % e2e_steps,
+                           "pinned copies inside, each step's arrays fresh; its default %d solvers in turn, "
+                           "so %d steps in flight); median of three passes of %d steps" % (depth, depth, e2e_steps),
                     "passes": e2e_passes,
                     "solve_batch_synchronous": e2e_sync,
                     "single_case_dropin": e2e_single},

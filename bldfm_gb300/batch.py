@@ -359,11 +359,34 @@ def _finish_batch(pending):
     return results
 
 
+STREAM_BYTES = 1 << 30  # output bytes in flight solve_stream's default depth allows
+STREAM_DEPTH = 8  # most batches in flight by default
+
+
+def stream_depth(cases):
+    """Default number of solvers (batches in flight) of ``solve_stream`` for
+    batches like ``cases``: eight, fewer when eight batches' FP64 outputs
+    (conc and flux, device and pinned host copies) would exceed ~1 GiB, at
+    least two.  Measured on the 16-footprint 512^2 batch, end to end: 29.9k
+    footprints/s with four batches in flight, 30.9k with six and 31.2k with
+    eight (the device-resident rate is 31.4k): the copy back and the host
+    work of the oldest batches need more than three batches of kernels
+    queued behind them to stay hidden."""
+    per = 0
+    for kw in cases:
+        ny, nx = np.shape(kw["srf_flx"])[-2:]
+        lv = kw.get("levels", 0)
+        nl = 1 if np.ndim(lv) == 0 else max(1, int(np.size(lv)))
+        per += 16 * int(ny) * int(nx) * nl
+    return int(max(2, min(STREAM_DEPTH, STREAM_BYTES // max(per, 1))))
+
+
 def solve_stream(batches, *, solvers=None, **opts):
     """Solve an iterable of batches (each a list of keyword-argument dicts of
     ``steady_state_transport_solver``) in FP32, yielding each batch's list of
-    ``(grid, conc, flx)`` in order.  The solvers (default four; each with its
-    own stream, workspace and outputs) take the batches in turn: batch i is
+    ``(grid, conc, flx)`` in order.  The solvers (each with its own stream,
+    workspace and outputs; by default ``stream_depth`` of the first batch,
+    created as they are first needed) take the batches in turn: batch i is
     prepared and enqueued before batch i - len(solvers) + 1 is waited for, so
     the host work, the kernels and the copies back of up to len(solvers)
     batches overlap (with two, the copy back and the host work of a batch sit
@@ -371,10 +394,14 @@ def solve_stream(batches, *, solvers=None, **opts):
     BatchSolvers."""
     from collections import deque
 
-    solvers = solvers or tuple(BatchSolver(**opts) for _ in range(4))
-    ns = len(solvers)
+    solvers = list(solvers) if solvers else None
     pending = deque()
     for i, cases in enumerate(batches):
+        if solvers is None:
+            solvers = [None] * stream_depth(cases)
+        ns = len(solvers)
+        if solvers[i % ns] is None:
+            solvers[i % ns] = BatchSolver(**opts)
         pending.append(_enqueue_batch(solvers[i % ns], cases))
         if len(pending) == ns:
             yield _finish_batch(pending.popleft())

@@ -93,3 +93,17 @@ def test_fp64_mode_and_parallel_strategies(stubbed):
     assert list(out) == ["T0"] and len(out["T0"]) == 2
     with pytest.raises(ValueError, match="Unknown parallel_over"):
         interface.run_bldfm_parallel(cfg, parallel_over="cells")
+
+
+def test_stream_depth_bounds_the_outputs_in_flight():
+    """solve_stream keeps eight batches in flight for the benchmark's
+    16-footprint 512^2 steps and fewer when eight batches' FP64 outputs would
+    pass ~1 GiB, never fewer than two."""
+    from bldfm_gb300.batch import STREAM_BYTES, stream_depth
+
+    small = [dict(srf_flx=np.zeros((512, 512)), levels=128)] * 16
+    assert stream_depth(small) == 8
+    big = [dict(srf_flx=np.zeros((1024, 1024)), levels=np.arange(3))] * 64
+    assert stream_depth(big) == 2
+    mid = [dict(srf_flx=np.zeros((1024, 1024)), levels=5)] * 16  # 256 MiB of outputs per batch
+    assert stream_depth(mid) == 4 and 4 * 16 * 16 * 1024 * 1024 <= STREAM_BYTES
