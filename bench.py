@@ -429,7 +429,7 @@ def serving_cases(nsteps, seed=7):
 def serving_section(args, dev, nsteps=10000):
     """Surrogate serving with fallback on the production footprint as a
     10k-step met timeseries: wall time of Surrogate.serve (batched fused
-    launches of the n = 256 network, FP64 fallback for the out-of-box steps,
+    launches of the n = 256 network, accurate-FP64 fallback for the out-of-box steps,
     the per-case accuracy guard with FP32 re-solves, accurate-FP64 spot
     checks of every 64th served step), the path counts, and the relL2
     distribution of 16 served steps (sampled before the run) against the exact
@@ -446,7 +446,9 @@ def serving_section(args, dev, nsteps=10000):
     sur = S.Surrogate(net, box=box, spot_every=64, tol=1e-3)
     sur.serve(items[:16])  # warm (plans, twiddles, fallback path)
     sur = S.Surrogate(net, box=box, spot_every=64, tol=1e-3)
-    sampled = list(range(5, nsteps, max(1, nsteps // 16)))[:16]
+    # 12 in-box steps and 4 out-of-box ones (every 10th step, index 9 mod 10)
+    sampled = sorted(set(list(range(5, nsteps, max(1, nsteps // 12)))[:12] +
+                         list(range(9, nsteps, max(10, (nsteps // 40) * 10)))[:4]))
     torch.cuda.synchronize()
     t = time.perf_counter()
     out, paths = sur.serve(items, keep=sampled)
