@@ -54,9 +54,9 @@ MODES = (512, 512)
 MEAS = (500.0, 500.0)
 # DRAM traffic per launch of the batched FP32 sweep (16 footprints of the
 # workload), dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture:
-# 0.81 MB read + 10.07 MB written (a compute kernel; most of the spectra
+# 0.81 MB read + 9.01 MB written (a compute kernel; most of the spectra
 # stay in L2 for the transforms)
-RICC_BATCH_DRAM_BYTES = 10.88e6
+RICC_BATCH_DRAM_BYTES = 9.82e6
 
 # algorithmic flops per (mode, sweep step), FMA counted as 2; the FP32 sweep's
 # count per mode comes from bldfm_sweep32_flops (it depends on the output level)
