@@ -339,13 +339,33 @@ __device__ __forceinline__ double2 dc_mul(double2 a, double2 b)
     return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 
+// 1/x for a positive normal x: the approximate hardware reciprocal refined by
+// two Newton-Raphson steps for f(y) = 1/y - x (y <- y + y (1 - x y)), each of
+// which doubles the number of correct bits, to within an ulp or two of the
+// rounded quotient.  Faster than the IEEE division, whose exact rounding the
+// accurate FP64 mode does not need.
+__device__ __forceinline__ double rcp_newton(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+// Per-level products of the accurate FP64 sweep's step coefficients
+// (A = S1 H2, B1 = S2 H3, C1 = S4 H3), formed once per CTA in shared memory
+#define RICC64_K 3
+#define RICC64_SMEM (200 * 1024)  // dynamic shared memory the kernel is set up for
+
 template <bool SINGLE>
 __global__ void __launch_bounds__(128) riccati64_kernel(SolveGeom g, const double *__restrict__ lvtab,
                                                         const int *__restrict__ slot_of_step,
                                                         const uint32_t *__restrict__ modes,
                                                         const double2 *__restrict__ q0spec,
                                                         double *__restrict__ scratch, double2 *__restrict__ Xp,
-                                                        double2 *__restrict__ Xq, int *err)
+                                                        double2 *__restrict__ Xq, int *err, bool kprod)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint64_t bar;
@@ -357,6 +377,16 @@ __global__ void __launch_bounds__(128) riccati64_kernel(SolveGeom g, const doubl
             return;
     }
     for (int i = threadIdx.x; i < g.nz; i += blockDim.x) s_slot[i] = slot_of_step[i];
+    // after the slot map, 8-byte aligned
+    double *s_k = (double *)(smem_raw + ((((size_t)L * BLDFM_LV64 * sizeof(double) + (size_t)g.nz * sizeof(int)) + 7) &
+                                         ~(size_t)7));
+    __syncthreads();
+    for (int i = threadIdx.x; kprod && i < L; i += blockDim.x) {
+        const double *lv = s_lv + (size_t)i * BLDFM_LV64;
+        s_k[RICC64_K * i] = lv[LV_S1] * lv[LV_H2];
+        s_k[RICC64_K * i + 1] = lv[LV_S2] * lv[LV_H3];
+        s_k[RICC64_K * i + 2] = lv[LV_S4] * lv[LV_H3];
+    }
     __syncthreads();
     const int jmax = g.jmax;
     const int64_t ns = g.nsolved;
@@ -377,7 +407,17 @@ __global__ void __launch_bounds__(128) riccati64_kernel(SolveGeom g, const doubl
             const double *lv = s_lv + (size_t)i * BLDFM_LV64;
             const double Tr = -fma(lv[LV_KX], lx2, lv[LV_KY] * ly2);
             const double Ti = -fma(lv[LV_U], lx, lv[LV_V] * ly);
-            const double A = lv[LV_S1] * lv[LV_H2], B1 = lv[LV_S2] * lv[LV_H3], C1 = lv[LV_S4] * lv[LV_H3];
+            double A, B1, C1;
+            if (kprod) {  // the same for every thread of the launch
+                const double *k = s_k + RICC64_K * i;
+                A = k[0];
+                B1 = k[1];
+                C1 = k[2];
+            } else {
+                A = lv[LV_S1] * lv[LV_H2];
+                B1 = lv[LV_S2] * lv[LV_H3];
+                C1 = lv[LV_S4] * lv[LV_H3];
+            }
             a = make_double2(fma(-A, Tr, 1.0), -A * Ti);
             b = make_double2(fma(-B1, Tr, lv[LV_S3]), -B1 * Ti);
             const double t2r = fma(Tr, Tr, -Ti * Ti), t2i = 2.0 * Tr * Ti;
@@ -387,7 +427,7 @@ __global__ void __launch_bounds__(128) riccati64_kernel(SolveGeom g, const doubl
             const double2 cR = dc_mul(cc, R);
             const double2 D = make_double2(a.x - cR.x, a.y - cR.y);
             const double2 N = make_double2(fma(a.x, R.x, fma(-a.y, R.y, -b.x)), fma(a.x, R.y, fma(a.y, R.x, -b.y)));
-            const double dinv = 1.0 / fma(D.x, D.x, D.y * D.y);
+            const double dinv = rcp_newton(fma(D.x, D.x, D.y * D.y));
             R = make_double2(fma(N.x, D.x, N.y * D.y) * dinv, fma(N.y, D.x, -N.x * D.y) * dinv);
         };
         int i = L - 1;
@@ -481,16 +521,23 @@ cudaError_t launch_riccati64(const SolveGeom &g, const double *lvtab, const int 
                              cudaStream_t st)
 {
     if (g.nsnap < 1 || g.nsolved == 0) return cudaSuccess;
-    const size_t smem = (size_t)(g.nz - 1) * BLDFM_LV64 * sizeof(double) + (size_t)g.nz * sizeof(int) + 16;
+    // level table, slot map, then (8-byte aligned) the per-level products
+    // when they fit in the shared memory the kernel is set up for
+    const size_t base = (((size_t)(g.nz - 1) * BLDFM_LV64 * sizeof(double) + (size_t)g.nz * sizeof(int) + 7) &
+                         ~(size_t)7) +
+                        16;
+    const size_t withk = base + (size_t)(g.nz - 1) * RICC64_K * sizeof(double);
+    const bool kprod = withk <= RICC64_SMEM;
+    const size_t smem = kprod ? withk : base;
     const int threads = 128;
     int64_t blocks = (g.nsolved + threads - 1) / threads;
     if (blocks > 64LL * nsm) blocks = 64LL * nsm;
     if (g.nsnap == 1)
         riccati64_kernel<true><<<(unsigned)blocks, threads, smem, st>>>(g, lvtab, slot, modes, q0spec, scratch, Xp,
-                                                                        Xq, err);
+                                                                        Xq, err, kprod);
     else
         riccati64_kernel<false><<<(unsigned)blocks, threads, smem, st>>>(g, lvtab, slot, modes, q0spec, scratch, Xp,
-                                                                         Xq, err);
+                                                                         Xq, err, kprod);
     return LAUNCH_CHECK();
 }
 
@@ -932,8 +979,8 @@ void prepare_kernel_attributes()
     set_fft_smem_attr<double>();
     set_fft_smem_attr<float>();
     cudaFuncSetAttribute(sweep64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(riccati64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(riccati64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(riccati64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RICC64_SMEM);
+    cudaFuncSetAttribute(riccati64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RICC64_SMEM);
     cudaFuncSetAttribute(riccati32_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(riccati32_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(riccati32_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
